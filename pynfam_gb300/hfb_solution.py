@@ -1,0 +1,467 @@
+"""HFB ground state for pnFAM, rebuilt from an HFBTHO ``.hel`` file.
+
+This is the input side of the solver (it runs once per nucleus, on the host).
+It reproduces what the reference obtains by re-running HFBTHO for zero
+iterations (pnfam: hfbtho_interface.f90:20-226 -> HFBTHO_DFT_SOLVER) and then
+reshaping the result for the FAM (pnfam: hfbtho_solution.f90:137-459):
+
+1. harmonic-oscillator basis functions on the Gauss-Hermite x Gauss-Laguerre
+   mesh, with the square roots of the quadrature weights mixed in
+   (hfbtho_solver.f90:3463-3671 ``gaupol``, :4237-4314 ``optHFBTHO``,
+   :1215-1240 ``coordinateLST``);
+2. the HFB matrix (h, Delta) of each Omega block from the mean and pairing
+   fields stored in the file (hfbtho_solver.f90:5145-5366 ``gamdel``);
+3. block diagonalisation of [[h-lambda, Delta], [Delta, -h+lambda]] inside the
+   particle-number loop that re-adjusts the Fermi energy (hfbtho_solver.f90:
+   1441-1972 ``hfbdiag``, :1977-2075 ``ALambda``), including the quasiparticle
+   pairing window;
+4. the local density rho(r) of the final solution (hfbtho_solver.f90:4318-4734
+   ``DENSIT``), used for the density-dependent couplings;
+5. explicit time-reversed partners (doubling of blocks, states, U, V, E), the
+   spin-up-first ordering inside each block and the zeroing of quasiparticles
+   above the pairing window (hfbtho_solution.f90:137-459).
+
+All arrays are float64.  Mesh index ``ihil = ih + il*ngh`` (Hermite/z fastest),
+as in HFBTHO.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .hel import HelData, read_hel
+
+CUTOFF_TOL = 1.0e-6  # hfbtho_variables.f90:253
+
+
+class HFBReconstructionError(RuntimeError):
+    pass
+
+
+# ----------------------------------------------------------------------------
+# 1. Basis functions on the mesh
+# ----------------------------------------------------------------------------
+def _hermite_functions(xh, wh, nzm):
+    """qh[n, ih], qh1[n, ih] (gaupol, hfbtho_solver.f90:3489-3503)."""
+    ngh = len(xh)
+    qh = np.zeros((max(nzm, 1) + 1, ngh))
+    qh1 = np.zeros_like(qh)
+    w0 = np.pi ** (-0.25) * np.exp(-0.5 * xh * xh) * np.sqrt(wh)
+    s2 = math.sqrt(2.0)
+    qh[0] = w0
+    qh[1] = s2 * w0 * xh
+    qh1[0] = -w0 * xh
+    qh1[1] = s2 * w0 * (1.0 - xh * xh)
+    for n in range(2, nzm + 1):
+        qh[n] = (s2 * xh * qh[n - 1] - math.sqrt(n - 1) * qh[n - 2]) / math.sqrt(n)
+        qh1[n] = math.sqrt(2 * n) * qh[n - 1] - xh * qh[n]
+    return qh, qh1
+
+
+def _laguerre_functions(xl, wl, nrm, nlm):
+    """ql[n, l, il], ql1[n, l, il] (gaupol, hfbtho_solver.f90:3510-3546)."""
+    ngl = len(xl)
+    nn = max(nrm, 1) + 1
+    ql = np.zeros((nn, nlm + 1, ngl))
+    ql1 = np.zeros_like(ql)
+    wfi = [1.0 / math.sqrt(math.factorial(k)) for k in range(nlm + 3)]
+    w00 = math.sqrt(2.0) * np.exp(-0.5 * xl)
+    for l in range(nlm + 1):
+        w0 = w00 * np.sqrt(0.5 * wl * xl ** l)
+        ql[0, l] = wfi[l] * w0
+        ql[1, l] = (l + 1 - xl) * wfi[l + 1] * w0
+        ql1[0, l] = (l - xl) * wfi[l] * w0
+        ql1[1, l] = (float(l * l + l) - xl * float(l + l + 3) + xl * xl) * wfi[l + 1] * w0
+        for n in range(2, nrm + 1):
+            dsq = math.sqrt(n) * math.sqrt(n + l)
+            d1 = float(n + n + l - 1) - xl
+            d2 = math.sqrt(n - 1) * math.sqrt(n - 1 + l)
+            d3 = float(n + n + l) - xl
+            d4 = 2.0 * dsq
+            ql[n, l] = (d1 * ql[n - 1, l] - d2 * ql[n - 2, l]) / dsq
+            ql1[n, l] = d3 * ql[n, l] - d4 * ql[n - 1, l]
+    return ql, ql1
+
+
+@dataclass
+class MeshBasis:
+    """HO basis (HFBTHO order, Omega>0 half) evaluated on the mesh."""
+    qhla: np.ndarray   # [nt, nghl] wave function * sqrt(weight)
+    fi1r: np.ndarray   # d/dr
+    fi1z: np.ndarray   # d/dz
+    fi2d: np.ndarray   # Laplacian (r,z part)
+    y: np.ndarray      # 1/r on the mesh [nghl]
+    z: np.ndarray      # z on the mesh [nghl]
+    wdcori: np.ndarray # inverse of (quadrature weight x Jacobian)
+    xlam: np.ndarray   # per block: Lambda of spin-up states (Omega-1/2)
+    xlap: np.ndarray   # per block: Lambda of spin-down states (Omega+1/2)
+
+
+def build_mesh_basis(h: HelData) -> MeshBasis:
+    ngh, ngl = h.ngh, h.ngl
+    nzm, nrm, nlm = int(h.nz.max()), int(h.nr.max()), int(h.nl.max())
+    qh, qh1 = _hermite_functions(h.xh, h.wh, nzm)
+    ql, ql1 = _laguerre_functions(h.xl, h.wl, nrm, nlm)
+    bz, bp = h.bz, h.bp
+    xh = np.tile(h.xh, ngl)          # ihil = ih + il*ngh
+    xl = np.repeat(h.xl, ngh)
+    wh = np.tile(h.wh, ngl)
+    wl = np.repeat(h.wl, ngh)
+    ih = np.tile(np.arange(ngh), ngl)
+    il = np.repeat(np.arange(ngl), ngh)
+    v2 = 0.5 / xl
+    v4 = v2 * v2
+    y = 1.0 / (np.sqrt(xl) * bp)
+    nt = len(h.nr)
+    qhla = np.empty((nt, ngh * ngl)); fi1r = np.empty_like(qhla)
+    fi1z = np.empty_like(qhla); fi2d = np.empty_like(qhla)
+    for ja in range(nt):
+        nza, nra, nla = int(h.nz[ja]), int(h.nr[ja]), int(h.nl[ja])
+        qha = qh[nza, ih]; qla = ql[nra, nla, il]
+        q = qha * qla
+        qhl1a = qha * ql1[nra, nla, il] * v2
+        qh1la = qh1[nza, ih] * qla
+        qhla[ja] = q
+        fi1r[ja] = (2.0 * np.sqrt(xl) / bp) * qhl1a
+        fi1z[ja] = qh1la / bz
+        cnzaa = nza + nza + 1
+        cnraa = nra + nra + nla + 1
+        fi2d[ja] = ((xh * xh - cnzaa) / (bz * bz)
+                    + 4.0 * (0.25 - cnraa * v2 + nla * nla * v4) * xl / (bp * bp)) * q
+    wdcor = np.pi * wh * wl * bz * bp * bp
+    # Lambda of the spin-up / spin-down members of each block, from Omega
+    nb = len(h.ID)
+    xlam = np.zeros(nb); xlap = np.zeros(nb)
+    start = 0
+    for ib in range(nb):
+        two_omega = int(2 * h.nl[start] + h.ns[start])
+        xlap[ib] = (two_omega + 1) // 2
+        xlam[ib] = xlap[ib] - 1
+        start += int(h.ID[ib])
+    return MeshBasis(qhla, fi1r, fi1z, fi2d, y, bz * xh, 1.0 / wdcor, xlam, xlap)
+
+
+# ----------------------------------------------------------------------------
+# 2. HFB matrix from the fields (gamdel)
+# ----------------------------------------------------------------------------
+def hfb_matrices(h: HelData, mb: MeshBasis):
+    """Per block: dict it -> (h_block, delta_block), full symmetric matrices.
+
+    Restates gamdel (hfbtho_solver.f90:5190-5302) for one block at a time with
+    the mesh sum vectorised; h/Delta for neutrons ('n') and protons ('p').
+    """
+    out = {"n": [], "p": []}
+    start = 0
+    y = mb.y
+    for ib, nd in enumerate(h.ID):
+        nd = int(nd)
+        sl = slice(start, start + nd)
+        ns = h.ns[sl]
+        up = (ns > 0).astype(float)[:, None]
+        dn = (ns < 0).astype(float)[:, None]
+        q = mb.qhla[sl]; r1 = mb.fi1r[sl]; z1 = mb.fi1z[sl]; d2 = mb.fi2d[sl]
+        xlam, xlap = mb.xlam[ib], mb.xlap[ib]
+        xlamy = xlam * y; xlapy = xlap * y; xlampy = xlamy + xlapy
+        xlamy2 = xlam * xlam * y * y; xlapy2 = xlap * xlap * y * y
+        FU, FUR, FUZ, FUD2 = q * up, r1 * up, z1 * up, (d2 - xlamy2 * q) * up
+        FD, FDR, FDZ, FDD2 = q * dn, r1 * dn, z1 * dn, (d2 - xlapy2 * q) * dn
+        for t in ("n", "p"):
+            f = h.fields[t]
+            hm = np.zeros((nd, nd)); dm = np.zeros((nd, nd))
+            # spin up-up
+            vh = FU[:, None, :] * FU[None, :, :]
+            hbh = vh * xlamy2 + FUR[:, None] * FUR[None, :] + FUZ[:, None] * FUZ[None, :]
+            vdh = 2 * hbh + FU[:, None] * FUD2[None, :] + FU[None, :] * FUD2[:, None]
+            snr = FUR[:, None] * FU[None, :] + FUR[None, :] * FU[:, None]
+            snz = FUZ[:, None] * FU[None, :] + FUZ[None, :] * FU[:, None]
+            vsh = snr * xlamy
+            sfiz = 2 * vh * xlamy
+            # spin down-down
+            vhd = FD[:, None, :] * FD[None, :, :]
+            hbhd = vhd * xlapy2 + FDR[:, None] * FDR[None, :] + FDZ[:, None] * FDZ[None, :]
+            vdhd = 2 * hbhd + FD[:, None] * FDD2[None, :] + FD[None, :] * FDD2[:, None]
+            snrd = FDR[:, None] * FD[None, :] + FDR[None, :] * FD[:, None]
+            snzd = FDZ[:, None] * FD[None, :] + FDZ[None, :] * FD[:, None]
+            vshd = -snrd * xlapy
+            sfizd = -2 * vhd * xlapy
+            vh = vh + vhd; hbh = hbh + hbhd; vdh = vdh + vdhd
+            snr = snr + snrd; snz = snz + snzd; vsh = vsh + vshd; sfiz = sfiz + sfizd
+            hm += (sfiz * f["vSFIZ"] + vh * f["v"] + snr * f["vr"] + snz * f["vz"]
+                   + vdh * f["vd"] + vsh * f["vs"] + hbh * f["vhb"]).sum(-1)
+            dm += (vh * f["dv"]).sum(-1)
+            # spin-flip: (a=n1 down, b=n2 up) and (a=n1 up, b=n2 down); the
+            # reference fills only n2<=n1, mirrored here to the full matrix.
+            # a down, b up
+            fitw3 = -FDZ[:, None] * FU[None, :]
+            fitw4 = FUZ[None, :] * FD[:, None]
+            vshx = -FDR[:, None] * FUZ[None, :] + FUR[None, :] * FDZ[:, None] + fitw3 * xlamy - fitw4 * xlapy
+            srfi = -FDR[:, None] * FU[None, :] + FUR[None, :] * FD[:, None]
+            sfir = FD[:, None] * FU[None, :] * xlampy
+            szfi = fitw3 + fitw4
+            du = (vshx * f["vs"] + f["vSRFI"] * srfi + f["vSFIR"] * sfir + f["vSZFI"] * szfi).sum(-1)
+            # a up, b down
+            fitw3 = -FDZ[None, :] * FU[:, None]
+            fitw4 = FUZ[:, None] * FD[None, :]
+            vshx = FUR[:, None] * FDZ[None, :] - FDR[None, :] * FUZ[:, None] - fitw4 * xlapy + fitw3 * xlamy
+            srfi = FUR[:, None] * FD[None, :] - FDR[None, :] * FU[:, None]
+            sfir = FU[:, None] * FD[None, :] * xlampy
+            szfi = fitw3 + fitw4
+            ud = (vshx * f["vs"] + f["vSRFI"] * srfi + f["vSFIR"] * sfir + f["vSZFI"] * szfi).sum(-1)
+            nsab = ns[:, None] + ns[None, :]
+            flip = (nsab == 0)
+            a_dn_b_up = flip & (ns[None, :] > 0)
+            a_up_b_dn = flip & (ns[None, :] < 0)
+            hm = np.where(a_dn_b_up, du, hm)
+            hm = np.where(a_up_b_dn, ud, hm)
+            # the reference computes element (n1, n2<=n1) and uses it for both
+            lo = np.tril(hm)
+            hm = lo + np.tril(hm, -1).T
+            lo = np.tril(dm)
+            dm = lo + np.tril(dm, -1).T
+            out[t].append((hm, dm))
+        start += nd
+    return out
+
+
+# ----------------------------------------------------------------------------
+# 3. Diagonalisation with the particle-number loop (hfbdiag + ALambda)
+# ----------------------------------------------------------------------------
+def _alambda(al, erhfb, drhfb, tz, cpv0_zero):
+    """Fermi energy from the BCS-like particle number (hfbtho_solver.f90:1977-2075)."""
+    if cpv0_zero:
+        ntz = int(tz + 0.1) // 2
+        d = np.sort(erhfb)
+        if ntz < len(d):
+            return 0.5 * (d[ntz - 1] + d[ntz])
+        return d[ntz - 1] + 0.001
+    xinf, xsup = -1000.0, 1000.0
+    for lit in range(1, 501):
+        y = erhfb - al
+        a = y * y + drhfb ** 2
+        b = np.sqrt(a)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            vh = np.where(b > 0, 0.5 * (1.0 - y / b), 0.0)
+            dvh = np.where(b > 0, 0.5 * drhfb ** 2 / (a * b), 0.0)
+        vh = np.where(vh < 1e-12, 0.0, vh)
+        vh = np.where((vh - 1.0) > 1e-12, 1.0, vh)
+        sn = float(np.sum(2.0 * vh))
+        dez = float(np.sum(2.0 * dvh))
+        ez = sn - tz
+        absez = abs(ez) / tz
+        if ez < 0:
+            xinf = max(xinf, al)
+        else:
+            xsup = min(xsup, al)
+        if lit == 1:
+            al = al - ez if absez <= 0.10 else al - 0.10 * math.copysign(1.0, ez)
+        else:
+            al = al - ez / (dez + 1e-20)
+        if al < xinf or al > xsup:
+            al = 0.5 * (xinf + xsup)
+        if absez <= 1e-10:
+            return al
+    return al
+
+
+@dataclass
+class QPSolution:
+    """Quasiparticles of one isospin, Omega>0 half, HFBTHO block order."""
+    E: list        # per block: [nd] quasiparticle energies
+    U: list        # per block: [nd, nd] (row = basis state, col = qp)
+    V: list
+    active: list   # per block: [nd] bool, below the pairing window
+    ala: float
+
+
+def diagonalise(h: HelData, hd, it: str, tz: float) -> QPSolution:
+    """hfbdiag(it, icanon) restricted to what pnFAM reads (no blocking, T=0)."""
+    k = 0 if it == "n" else 1
+    ala = float(h.ala[k])
+    pwi = h.pwi
+    cpv0_zero = (h.CpV0[k] == 0.0)
+    sitest = min(0.10, h.si * 0.010)
+    blocks = hd[it]
+    eig = None
+    norm_to_improve = True
+    inner = -1
+    sumnz = 1.0
+    while norm_to_improve:
+        inner += 1
+        if abs(sumnz) < sitest or inner == 20:
+            norm_to_improve = False
+        al = ala
+        erhfb, drhfb = [], []
+        eig = []
+        nsum = 0.0
+        for (hm, dm) in blocks:
+            nd = hm.shape[0]
+            M = np.empty((2 * nd, 2 * nd))
+            M[:nd, :nd] = hm - al * np.eye(nd)
+            M[nd:, nd:] = -hm + al * np.eye(nd)
+            M[nd:, :nd] = dm
+            M[:nd, nd:] = dm
+            w, vec = np.linalg.eigh(M)
+            Eq = w[nd:]
+            Ub = vec[:nd, nd:]
+            Vb = vec[nd:, nd:]
+            pn = np.sum(Vb * Vb, axis=0)
+            ela = Eq * (1.0 - 2.0 * pn)
+            enb = ela + al
+            ekb = np.sqrt(np.abs(Eq * Eq - ela * ela))
+            arg = 100.0 * (enb - pwi)
+            with np.errstate(over="ignore"):
+                expo = np.where(np.abs(arg) < math.log(np.finfo(float).max), np.exp(np.minimum(arg, 700.0)), np.inf)
+            act = (enb <= pwi) | (np.abs(1.0 / (1.0 + expo)) > CUTOFF_TOL)
+            erhfb.append(enb[act]); drhfb.append(ekb[act])
+            nsum += float(np.sum(2.0 * pn[act]))
+            eig.append((Eq, Ub, Vb, act))
+        erhfb = np.concatenate(erhfb); drhfb = np.concatenate(drhfb)
+        if len(erhfb) == 0:
+            raise HFBReconstructionError("no states below the pairing window")
+        sumnz = nsum - tz
+        al = _alambda(al, erhfb, drhfb, tz, cpv0_zero)
+        final_ala = ala
+        ala = al
+    return QPSolution([e[0] for e in eig], [e[1] for e in eig], [e[2] for e in eig],
+                      [e[3] for e in eig], final_ala)
+
+
+def local_density(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float) -> np.ndarray:
+    """rho(r) of one isospin from the final quasiparticles (DENSIT, T=0)."""
+    tro = np.zeros(h.ngh * h.ngl)
+    start = 0
+    for ib, nd in enumerate(h.ID):
+        nd = int(nd)
+        ns = h.ns[start:start + nd]
+        q = mb.qhla[start:start + nd]
+        V = qp.V[ib][:, qp.active[ib]]
+        fu = V[ns > 0].T @ q[ns > 0]
+        fd = V[ns < 0].T @ q[ns < 0]
+        tro += np.sum(fu * fu + fd * fd, axis=0)
+        start += nd
+    s = 2.0 * tro.sum()
+    return tro * mb.wdcori * (2.0 * tz / s)
+
+
+# ----------------------------------------------------------------------------
+# 5. pnFAM view of the solution (TR doubling, spin sort, pairing window)
+# ----------------------------------------------------------------------------
+@dataclass
+class HFBSolution:
+    """The ground state in the layout the FAM kernels consume.
+
+    Doubled basis of ``dqp`` states in ``nb`` blocks (blocks nb/2.. are the
+    time-reversed partners of blocks 0..nb/2-1), spin-up states first inside
+    every block.  U is block diagonal; V maps block i to its partner
+    (i +- nb/2).  Block matrices are stored block by block, column-major inside
+    a block (Fortran order), in block-row order.
+    """
+    Z: int
+    N: int
+    n00: int
+    nb: int
+    db: np.ndarray          # [nb]
+    isstart: np.ndarray     # [nb] first state of each block (0-based)
+    nr: np.ndarray
+    nz: np.ndarray
+    nl: np.ndarray
+    ns: np.ndarray
+    npar: np.ndarray
+    num_spin_up: np.ndarray # [nb]
+    nghl: int
+    wf: np.ndarray          # [dqp, nghl]
+    wfdr: np.ndarray
+    wfdz: np.ndarray
+    wfdp: np.ndarray        # y*nl*wf
+    wfd2_all: np.ndarray    # wfd2 - y*nl*wfdp
+    y: np.ndarray
+    z: np.ndarray
+    wdcori: np.ndarray
+    Ep: np.ndarray          # [dqp]
+    En: np.ndarray
+    Up: list                # per block row: [db, db] (block-diagonal)
+    Vp: list                # per block row i: [db_i, db_partner]
+    Un: list
+    Vn: list
+    rho_n: np.ndarray       # [nghl] local densities (for couplings)
+    rho_p: np.ndarray
+    hel: HelData
+
+    @property
+    def dqp(self) -> int:
+        return int(self.db.sum())
+
+    def partner(self, ib: int) -> int:
+        half = self.nb // 2
+        return ib + half if ib < half else ib - half
+
+
+def load_hfb_solution(path: str) -> HFBSolution:
+    """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file."""
+    h = read_hel(path)
+    mb = build_mesh_basis(h)
+    hd = hfb_matrices(h, mb)
+    qpn = diagonalise(h, hd, "n", float(h.N))
+    qpp = diagonalise(h, hd, "p", float(h.Z))
+    rho_n = local_density(h, mb, qpn, float(h.N))
+    rho_p = local_density(h, mb, qpp, float(h.Z))
+
+    nbh = len(h.ID)
+    nb = 2 * nbh
+    db = np.concatenate([h.ID, h.ID]).astype(np.int64)
+    nt = len(h.nr)
+    nr = np.concatenate([h.nr, h.nr]); nz = np.concatenate([h.nz, h.nz])
+    nl = np.concatenate([h.nl, -h.nl]); ns = np.concatenate([h.ns, -h.ns])
+    npar = 1 + (h.nz + h.nl) % 2
+    npar = np.concatenate([npar, npar])
+    sign = np.where(h.ns < 0, -1.0, 1.0)[:, None]
+    wf = np.concatenate([mb.qhla, sign * mb.qhla])
+    wfdr = np.concatenate([mb.fi1r, sign * mb.fi1r])
+    wfdz = np.concatenate([mb.fi1z, sign * mb.fi1z])
+    wfd2 = np.concatenate([mb.fi2d, sign * mb.fi2d])
+
+    isstart = np.concatenate([[0], np.cumsum(db)[:-1]]).astype(np.int64)
+    # spin sort inside each (doubled) block
+    new_order = np.empty(2 * nt, dtype=np.int64)
+    num_up = np.zeros(nb, dtype=np.int64)
+    for ib in range(nb):
+        s0, d = isstart[ib], db[ib]
+        idx = np.arange(s0, s0 + d)
+        upi = idx[ns[idx] > 0]; dni = idx[ns[idx] < 0]
+        num_up[ib] = len(upi)
+        new_order[s0:s0 + d] = np.concatenate([upi, dni])
+    nr, nz, nl, ns, npar = nr[new_order], nz[new_order], nl[new_order], ns[new_order], npar[new_order]
+    wf, wfdr, wfdz, wfd2 = wf[new_order], wfdr[new_order], wfdz[new_order], wfd2[new_order]
+    y = mb.y
+    wfdp = y[None, :] * nl[:, None] * wf
+    wfd2_all = wfd2 - y[None, :] * nl[:, None] * wfdp
+
+    def doubled(qp: QPSolution):
+        E = np.concatenate(qp.E + qp.E)
+        act = np.concatenate(qp.active + qp.active)
+        U = [u.copy() for u in qp.U] + [u.copy() for u in qp.U]
+        V = [-v for v in qp.V] + [v.copy() for v in qp.V]
+        # rows of U, V follow the spin sort of their block row
+        for ib in range(nb):
+            s0, d = isstart[ib], db[ib]
+            perm = new_order[s0:s0 + d] - s0
+            U[ib] = U[ib][perm]
+            V[ib] = V[ib][perm]
+        # erase quasiparticles above the pairing window (columns); the QP
+        # columns of block row i live in block i for U and partner(i) for V
+        for ib in range(nb):
+            s0, d = isstart[ib], db[ib]
+            a = act[s0:s0 + d]
+            U[ib][:, ~a] = 0.0
+            pr = ib + nbh if ib < nbh else ib - nbh
+            V[pr][:, ~a] = 0.0
+        E = np.where(act, E, 0.0)
+        return E, U, V
+
+    Ep, Up, Vp = doubled(qpp)
+    En, Un, Vn = doubled(qpn)
+    return HFBSolution(h.Z, h.N, h.n00, nb, db, isstart, nr, nz, nl, ns, npar, num_up,
+                       h.ngh * h.ngl, wf, wfdr, wfdz, wfdp, wfd2_all, y, mb.z, mb.wdcori,
+                       Ep, En, Up, Vp, Un, Vn, rho_n, rho_p, h)
