@@ -1,0 +1,152 @@
+/*
+ * pnfam_gpu.h -- C ABI of the GB300 pnFAM solver library (libpnfam_gb300.so).
+ *
+ * The reference runs the finite-amplitude-method (FAM) iteration of one
+ * (operator, K, omega) point per pnfam_main.x process on the CPU
+ * (pnfam_solver.f90:32-221).  This library keeps the ground state and the
+ * operator resident on one GPU and solves a batch of omega points at once.
+ *
+ * Conventions
+ *  - All arrays are caller-owned host memory, copied in/out; float64.
+ *  - Block matrices: "one non-zero block per block row" layout of the
+ *    reference blockmatrix type (pnfam_type_blockmatrix.f90:22-26): blocks in
+ *    increasing block-row order, each block column-major (Fortran order).
+ *  - The basis is the doubled (explicit time-reversed) basis of
+ *    hfbtho_solution.f90:164-353, spin-up states first inside every block.
+ *  - Return value 0 = success; otherwise one of PNFAM_E* below, with a
+ *    message available from pnfam_gpu_last_error().  Contexts are not
+ *    thread-safe: one context per host thread.
+ */
+#ifndef PNFAM_GPU_H
+#define PNFAM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PNFAM_OK = 0,
+  PNFAM_EINVAL = 1,      /* bad shape / argument */
+  PNFAM_ENOMEM = 2,      /* device allocation failed */
+  PNFAM_ECUDA = 3,       /* CUDA runtime error, or no usable GPU */
+  PNFAM_ENONFINITE = 4,  /* non-finite value produced by the iteration */
+  PNFAM_ESTATE = 5       /* call out of order (e.g. solve before set_operator) */
+};
+
+typedef struct pnfam_ctx pnfam_ctx_t;
+
+/* Basis description (doubled basis). */
+typedef struct {
+  int nb;                 /* number of blocks (even; block i+nb/2 is the TR partner of i) */
+  const int* db;          /* [nb] block sizes */
+  const int* num_spin_up; /* [nb] spin-up states at the start of each block */
+  const int* ns;          /* [dqp] 2*spin projection, +1 / -1 */
+  int nghl;               /* mesh points */
+} pnfam_basis_t;
+
+/* Residual-interaction couplings (pnfam_interaction.f90:246-258). */
+typedef struct {
+  const double* crho;     /* [nghl] C^rho(r)  */
+  const double* cs;       /* [nghl] C^s(r)    */
+  const double* cpair;    /* [nghl] C^pair(r) */
+  const double* cspair;   /* [nghl] C^spair(r)*/
+  double scalars[12];     /* cdrho, ctau, ctj0, ctj1, ctj2, crdj, cds, ct, cj, cgs, cf, csdj */
+} pnfam_coupl_t;
+
+/* Solver options (namelist &solver, pnfam_setup.f90:102-103; mixing factor
+ * of pnfam_broyden.f90:20). */
+typedef struct {
+  int max_iter;               /* iterations before giving up (iter_conv = -1) */
+  int broyden_history_size;   /* M; 0 = linear mixing; <0 = no mixing */
+  double convergence_epsilon;
+  double alpha_mix;           /* 0.7 in the reference */
+  double quench_residual_int; /* scales the residual interaction; 0 skips it */
+  int precision;              /* 0 = FP64 everywhere (the drop-in form) */
+  int reserved[7];
+} pnfam_solver_opts_t;
+
+/*
+ * Create a context on the current CUDA device and upload the ground state.
+ * Replaces the reference's per-process set-up of the HFB solution
+ * (pnfam_setup.f90:285-382 setup_hfb_solution) and of the residual
+ * interaction (pnfam_setup.f90:389-400 setup_hamiltonian).
+ *   Ep, En        [dqp] quasiparticle energies (zero above the pairing window)
+ *   Up, Un        block diagonal, block i: db[i] x db[i]
+ *   Vp, Vn        block i: db[i] x db[partner(i)] (rows of block i)
+ *   phi           [5][dqp][nghl]: wf, d/dr wf, y*nl*wf, d/dz wf, Laplacian
+ *                 (hfbtho_solution.f90:114-121 wf, wfdr, wfdp, wfdz, wfd2_all)
+ *   wdcori        [nghl] inverse quadrature weights
+ */
+int pnfam_gpu_init(const pnfam_basis_t* basis,
+                   const double* Ep, const double* En,
+                   const double* Up, const double* Vp,
+                   const double* Un, const double* Vn,
+                   const double* phi, const double* wdcori,
+                   const pnfam_coupl_t* coupl,
+                   pnfam_ctx_t** out);
+
+/*
+ * Set the external field (operator O_K) and its cross terms.
+ * Replaces the operator half of init_pnfam_solver (pnfam_solver.f90:226-381:
+ * Fqp = W^T Fsp W and the block structures that follow from F).
+ *   beta_minus    1 for beta-, 0 for beta+
+ *   fcols         [nb] block column of F for each block row, -1 if empty
+ *                 (init_fam_mapping, pnfam_extfield.f90:763-841)
+ *   Fsp           F_sp elements in the fcols structure
+ *   n_xterms, Gsp cross-term operators with the same structure (may be 0/NULL)
+ */
+int pnfam_gpu_set_operator(pnfam_ctx_t* ctx, int beta_minus, const int* fcols,
+                           const double* Fsp, int n_xterms, const double* const* Gsp);
+
+/*
+ * Solve npts omega points (ifam, pnfam_solver.f90:93-221) as one batch.
+ *   re_w, im_w    [npts] complex energies
+ *   re_S, im_S    [npts*(1+n_xterms)] strength and cross terms (-1/pi contraction)
+ *   iters         [npts] iteration at convergence, -1 if max_iter was reached
+ *   si_out        [npts] final Broyden residual si
+ *   hist          optional, NULL or [npts*(max_iter+1)*3]: per iteration
+ *                 (si, Re S, Im S) as printed in the reference's iteration table
+ */
+int pnfam_gpu_solve(pnfam_ctx_t* ctx, int npts, const double* re_w, const double* im_w,
+                    const pnfam_solver_opts_t* opts,
+                    double* re_S, double* im_S, int* iters, double* si_out, double* hist);
+
+/*
+ * The reference's in-process plugin seam: calc_hamiltonian
+ * (pnfam_setup.f90:74-89 calc_dHsp_interface; pnfam_hamiltonian_blas.f90:51-74).
+ * Given the perturbed single-particle densities (rho_pn in the F structure,
+ * kappa(+) in the transpose of the X structure, rho_np in the F structure,
+ * kappa(-) in the transpose of the Y structure; each as Re and Im arrays of
+ * nxy elements) return the perturbed fields h_pn (F), Delta(+) (X),
+ * h_np (F), Delta(-) (Y).  Requires pnfam_gpu_set_operator.
+ */
+int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* ctx,
+                               const double* re_rho_pn, const double* im_rho_pn,
+                               const double* re_kp, const double* im_kp,
+                               const double* re_rho_np, const double* im_rho_np,
+                               const double* re_km, const double* im_km,
+                               double* re_h_pn, double* im_h_pn,
+                               double* re_dp, double* im_dp,
+                               double* re_h_np, double* im_h_np,
+                               double* re_dm, double* im_dm);
+
+/* Number of non-trivial FAM matrix elements nxy (valid after set_operator). */
+long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
+
+/* Timing of the last solve: per stage accumulated device ms (order:
+ * k1_blockgemm, density, meanfield, field_projection, k2_blockgemm, green,
+ * broyden, strength; filled only when opts.reserved[0] != 0), then, if
+ * nstage > 8, the whole solve's device time (CUDA events on the solver's
+ * stream), and the number of kernel launches. */
+int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
+                           long long* launches);
+
+void pnfam_gpu_free(pnfam_ctx_t* ctx);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* pnfam_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PNFAM_GPU_H */

@@ -605,7 +605,8 @@ def _bm(m: BlockMatrix, sgn=1.0):
 class FAMOracle:
     """pnfam_solve for one (operator, omega) on a prepared HFB solution."""
 
-    def __init__(self, hfb, couplings, F, G=(), quench=1.0, alpha_mix=0.7):
+    def __init__(self, hfb, couplings, F, G=(), quench=1.0, alpha_mix=float(np.float32(0.7))):
+        # alpha_mix: pnfam_broyden.f90:20 sets 0.7 from a single-precision literal
         self.hfb, self.cp, self.quench, self.alpha = hfb, couplings, quench, alpha_mix
         nb, db = hfb.nb, hfb.db
         self.nb, self.db = nb, db

@@ -1,0 +1,92 @@
+"""ctypes binding of the C ABI declared in include/pnfam_gpu.h.
+
+The library is loaded from the package directory (in-tree build).  There is
+no fallback: if the library is missing or no GPU is usable, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libpnfam_gb300.so")
+
+EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam_gpu_calc_hamiltonian",
+           "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error")
+
+ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENONFINITE", 5: "ESTATE"}
+
+
+class PnfamGPUError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Basis(C.Structure):
+    _fields_ = [("nb", C.c_int), ("db", C.POINTER(C.c_int)), ("num_spin_up", C.POINTER(C.c_int)),
+                ("ns", C.POINTER(C.c_int)), ("nghl", C.c_int)]
+
+
+class Coupl(C.Structure):
+    _fields_ = [("crho", C.POINTER(C.c_double)), ("cs", C.POINTER(C.c_double)),
+                ("cpair", C.POINTER(C.c_double)), ("cspair", C.POINTER(C.c_double)),
+                ("scalars", C.c_double * 12)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [("max_iter", C.c_int), ("broyden_history_size", C.c_int),
+                ("convergence_epsilon", C.c_double), ("alpha_mix", C.c_double),
+                ("quench_residual_int", C.c_double), ("precision", C.c_int),
+                ("reserved", C.c_int * 7)]
+
+
+_lib = None
+
+
+def load(path: str = LIBPATH):
+    """Load the library (raises OSError if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with `python -m pynfam_gb300.build`")
+    lib = C.CDLL(path)
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    lib.pnfam_gpu_init.argtypes = [C.POINTER(Basis), dp, dp, dp, dp, dp, dp, dp, dp, C.POINTER(Coupl), C.POINTER(C.c_void_p)]
+    lib.pnfam_gpu_init.restype = C.c_int
+    lib.pnfam_gpu_set_operator.argtypes = [C.c_void_p, C.c_int, ip, dp, C.c_int, C.POINTER(dp)]
+    lib.pnfam_gpu_set_operator.restype = C.c_int
+    lib.pnfam_gpu_solve.argtypes = [C.c_void_p, C.c_int, dp, dp, C.POINTER(SolverOpts), dp, dp, ip, dp, dp]
+    lib.pnfam_gpu_solve.restype = C.c_int
+    lib.pnfam_gpu_calc_hamiltonian.argtypes = [C.c_void_p] + [dp] * 16
+    lib.pnfam_gpu_calc_hamiltonian.restype = C.c_int
+    lib.pnfam_gpu_nxy.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_nxy.restype = C.c_longlong
+    lib.pnfam_gpu_last_profile.argtypes = [C.c_void_p, dp, C.c_int, C.POINTER(C.c_longlong)]
+    lib.pnfam_gpu_last_profile.restype = C.c_int
+    lib.pnfam_gpu_free.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_free.restype = None
+    lib.pnfam_gpu_last_error.argtypes = []
+    lib.pnfam_gpu_last_error.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != 0:
+        msg = _lib.pnfam_gpu_last_error().decode(errors="replace") if _lib else ""
+        raise PnfamGPUError(rc, msg)
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_int))

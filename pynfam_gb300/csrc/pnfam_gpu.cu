@@ -1,0 +1,802 @@
+// pnfam_gpu.cu -- C ABI + host orchestration of the GB300 pnFAM solver.
+//
+// The ground state (U, V, E, basis functions on the mesh, couplings) is
+// uploaded once per nucleus; an operator is set once per (O, K, beta); a
+// batch of omega points is then iterated in lock step, each point keeping
+// its own Broyden history and stopping at its own convergence, exactly as
+// the reference's per-process ifam loop (pnfam_solver.f90:114-209) does.
+#include "../../include/pnfam_gpu.h"
+#include "pnfam_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace pnfam;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                             \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      return fail(e_ == cudaErrorMemoryAllocation ? PNFAM_ENOMEM : PNFAM_ECUDA,              \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    }                                                                                        \
+  } while (0)
+
+namespace {
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <class T>
+static cudaError_t dalloc(DBuf<T>& b, size_t n) {
+  if (b.n >= n && b.p) return cudaSuccess;
+  b.release();
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&b.p, n * sizeof(T));
+  if (e == cudaSuccess) b.n = n;
+  return e;
+}
+
+template <class T>
+static cudaError_t upload(DBuf<T>& b, const T* h, size_t n) {
+  cudaError_t e = dalloc(b, n);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+struct MatRef {      // op(stored block)
+  int buf;
+  long long off;
+  int rows, cols;    // stored shape
+  int trans;
+  int orows() const { return trans ? cols : rows; }
+  int ocols() const { return trans ? rows : cols; }
+};
+
+struct Term2 {       // s * A * T
+  double alpha[2];
+  MatRef A, T;
+};
+
+struct TaskList {
+  std::vector<GemmTask> tasks;
+  std::vector<int> tile2task;
+  DBuf<GemmTask> d_tasks;
+  DBuf<int> d_tile2task;
+  int ntiles = 0;
+
+  void add(int M, int N, int K, const std::vector<GemmTerm>& terms, int cbuf, long long coff, int ldc) {
+    if (M <= 0 || N <= 0) return;
+    GemmTask t;
+    memset(&t, 0, sizeof(t));
+    t.M = M; t.N = N; t.K = K; t.nterm = (int)terms.size();
+    for (size_t i = 0; i < terms.size(); ++i) t.t[i] = terms[i];
+    t.cbuf = cbuf; t.coff = coff; t.ldc = ldc;
+    const int ntm = (M + GT - 1) / GT, ntn = (N + GT - 1) / GT;
+    t.tile0 = ntiles; t.ntn = ntn;
+    for (int k = 0; k < ntm * ntn; ++k) tile2task.push_back((int)tasks.size());
+    ntiles += ntm * ntn;
+    tasks.push_back(t);
+  }
+  cudaError_t finalize() {
+    cudaError_t e = upload(d_tasks, tasks.data(), tasks.size());
+    if (e != cudaSuccess) return e;
+    return upload(d_tile2task, tile2task.data(), tile2task.size());
+  }
+  void clear() {
+    tasks.clear(); tile2task.clear(); ntiles = 0;
+  }
+};
+
+static GemmTerm mkterm(const MatRef& A, const MatRef& B, double a_re, double a_im) {
+  GemmTerm g;
+  memset(&g, 0, sizeof(g));
+  g.abuf = A.buf; g.aoff = A.off; g.lda = A.rows; g.tA = A.trans;
+  g.bbuf = B.buf; g.boff = B.off; g.ldb = B.rows; g.tB = B.trans;
+  g.alpha[0] = a_re; g.alpha[1] = a_im;
+  return g;
+}
+
+}  // namespace
+
+struct pnfam_ctx {
+  int dev = 0;
+  // basis (host)
+  int nb = 0, dqp = 0, nghl = 0;
+  std::vector<int> db, st, nup, tr;
+  std::vector<long long> uoff;
+  std::vector<signed char> ns;
+  // device ground state
+  DBuf<int> d_db, d_st, d_nup;
+  DBuf<signed char> d_ns;
+  DBuf<double> d_up, d_vp, d_un, d_vn, d_ep, d_en, d_phi, d_wd, d_crho, d_cs, d_cpair, d_cspair;
+  double sc[12] = {0};
+  // operator
+  bool have_op = false;
+  int beta_minus = 1;
+  long long nxy = 0;
+  int nops = 1;
+  std::vector<int> fc, xc, yc, xtc, ytc;
+  std::vector<long long> foff, xoff, yoff, xtoff, ytoff;
+  DBuf<int> d_fc, d_xtc, d_ytc, d_erow, d_ecol;
+  DBuf<long long> d_foff, d_xtoff, d_ytoff;
+  DBuf<double> d_fops;   // [nops][2*nxy] operator and cross terms in the QP basis
+  TaskList k1a, k1b, k2a, k2b;
+  std::vector<HTask> htasks;
+  DBuf<HTask> d_htasks;
+  // per-solve buffers
+  int cap_P = 0, cap_M = 0;
+  DBuf<double> d_state, d_vout, d_T, d_rsp, d_hsp, d_hqp, d_dpart, d_mf;
+  DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
+  DBuf<int> d_active;
+  DBuf<BufDesc> d_bufs;
+  int G = 1;
+  int nchunk_bro = 1, nchunk_c = 1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t evt[2] = {nullptr, nullptr};   // whole-solve device time
+  double stage_ms[8] = {0};
+  double total_ms = 0.0;
+  long long launches = 0;
+
+  ~pnfam_ctx() {
+    DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active};
+    for (auto* b : ib) b->release();
+    d_ns.release();
+    DBuf<double>* dbs[] = {&d_up, &d_vp, &d_un, &d_vn, &d_ep, &d_en, &d_phi, &d_wd, &d_crho, &d_cs,
+                           &d_cpair, &d_cspair, &d_fops, &d_state, &d_vout, &d_T, &d_rsp, &d_hsp,
+                           &d_hqp, &d_dpart, &d_mf, &d_df, &d_dv, &d_bpart, &d_si, &d_norm,
+                           &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim};
+    for (auto* b : dbs) b->release();
+    d_foff.release(); d_xtoff.release(); d_ytoff.release();
+    d_htasks.release(); d_bufs.release();
+    k1a.d_tasks.release(); k1a.d_tile2task.release();
+    k1b.d_tasks.release(); k1b.d_tile2task.release();
+    k2a.d_tasks.release(); k2a.d_tile2task.release();
+    k2b.d_tasks.release(); k2b.d_tile2task.release();
+    if (ev[0]) cudaEventDestroy(ev[0]);
+    if (ev[1]) cudaEventDestroy(ev[1]);
+    if (evt[0]) cudaEventDestroy(evt[0]);
+    if (evt[1]) cudaEventDestroy(evt[1]);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  DevBasis devbasis() const {
+    DevBasis B;
+    B.nb = nb; B.dqp = dqp; B.nghl = nghl;
+    B.db = d_db.p; B.st = d_st.p; B.nup = d_nup.p; B.ns = d_ns.p;
+    B.phi = d_phi.p; B.wdcori = d_wd.p;
+    B.crho = d_crho.p; B.cs = d_cs.p; B.cpair = d_cpair.p; B.cspair = d_cspair.p;
+    for (int i = 0; i < 12; ++i) B.sc[i] = sc[i];
+    return B;
+  }
+  int left_u() const { return beta_minus ? B_UP : B_UN; }
+  int left_v() const { return beta_minus ? B_VP : B_VN; }
+  int right_u() const { return beta_minus ? B_UN : B_UP; }
+  int right_v() const { return beta_minus ? B_VN : B_VP; }
+  MatRef ublk(int buf, int i, int trans) const { return MatRef{buf, uoff[i], db[i], db[i], trans}; }
+  MatRef vblk(int buf, int i, int trans) const { return MatRef{buf, uoff[i], db[i], db[tr[i]], trans}; }
+};
+
+// ---------------------------------------------------------------------------
+// structures and task lists
+// ---------------------------------------------------------------------------
+static std::vector<long long> offsets(const std::vector<int>& cols, const std::vector<int>& db, long long* total) {
+  std::vector<long long> off(cols.size(), -1);
+  long long p = 0;
+  for (size_t i = 0; i < cols.size(); ++i)
+    if (cols[i] >= 0) { off[i] = p; p += (long long)db[i] * db[cols[i]]; }
+  *total = p;
+  return off;
+}
+
+// Stage-1/stage-2 split of sum_t s_t A_t (op(B_t) C_t'):
+// T_t = op(B_t) op(C_t) in scratch, then out = sum_t s_t op(A_t) T_t.
+struct TripleTerm {
+  double alpha[2];
+  MatRef A, B, C;
+};
+
+static void emit_triple(TaskList& s1, TaskList& s2, long long& toff, const std::vector<TripleTerm>& terms,
+                        int obuf, long long ooff, int orows, int ocols) {
+  std::vector<GemmTerm> st2;
+  for (const TripleTerm& t : terms) {
+    const int M = t.B.orows(), N = t.C.ocols(), K = t.B.ocols();
+    MatRef T{B_T, toff, M, N, 0};
+    s1.add(M, N, K, {mkterm(t.B, t.C, 1.0, 1.0)}, B_T, toff, M);
+    toff += (long long)M * N;
+    st2.push_back(mkterm(t.A, T, t.alpha[0], t.alpha[1]));
+  }
+  s2.add(orows, ocols, terms[0].A.ocols(), st2, obuf, ooff, orows);
+}
+
+static void build_tasks(pnfam_ctx* c) {
+  const int nb = c->nb;
+  const long long nxy = c->nxy;
+  const int UL = c->left_u(), VL = c->left_v(), UR = c->right_u(), VR = c->right_v();
+  auto X = [&](int i, int tr_) { return MatRef{B_STATE, c->xoff[i], c->db[i], c->db[c->xc[i]], tr_}; };
+  auto Y = [&](int i, int tr_) { return MatRef{B_STATE, nxy + c->yoff[i], c->db[i], c->db[c->yc[i]], tr_}; };
+  c->k1a.clear(); c->k1b.clear(); c->k2a.clear(); c->k2b.clear();
+  long long toff = 0;
+  // ---- K1: dR_sp = W1 dR_qp W2^T (pnfam_solver.f90:144-150) ----
+  for (int i = 0; i < nb; ++i) {
+    if (c->fc[i] < 0) continue;
+    const int j = c->fc[i], x = c->xc[i], t = c->tr[i];
+    // rho_pn = UL_i X_i VR_j^T - VL_i Y_t UR_j^T      (F structure, row i)
+    emit_triple(c->k1a, c->k1b, toff,
+                {{{1.0, 1.0}, c->ublk(UL, i, 0), X(i, 0), c->vblk(VR, j, 1)},
+                 {{-1.0, -1.0}, c->vblk(VL, i, 0), Y(t, 0), c->ublk(UR, j, 1)}},
+                B_RSP, 0 * nxy + c->foff[i], c->db[i], c->db[j]);
+    // kappa(+) stored = -UR_x X_i^T UL_i^T + VR_x Y_t^T VL_i^T   (XT structure, row x)
+    emit_triple(c->k1a, c->k1b, toff,
+                {{{-1.0, -1.0}, c->ublk(UR, x, 0), X(i, 1), c->ublk(UL, i, 1)},
+                 {{1.0, 1.0}, c->vblk(VR, x, 0), Y(t, 1), c->vblk(VL, i, 1)}},
+                B_RSP, 1 * nxy + c->xtoff[x], c->db[x], c->db[i]);
+  }
+  for (int i = 0; i < nb; ++i) {
+    if (c->yc[i] < 0) continue;
+    const int y = c->yc[i], t = c->tr[i];
+    // kappa(-) stored = s (VR_y X_t^T VL_i^T - UR_y Y_i^T UL_i^T), s = +1 Re, -1 Im  (YT, row y)
+    emit_triple(c->k1a, c->k1b, toff,
+                {{{1.0, -1.0}, c->vblk(VR, y, 0), X(t, 1), c->vblk(VL, i, 1)},
+                 {{-1.0, 1.0}, c->ublk(UR, y, 0), Y(i, 1), c->ublk(UL, i, 1)}},
+                B_RSP, 2 * nxy + c->ytoff[y], c->db[y], c->db[i]);
+  }
+  for (int j = 0; j < nb; ++j) {
+    if (c->fc[j] < 0) continue;
+    const int i = c->fc[j], t = c->tr[i];
+    // rho_np stored = -UR_j X_t^T VL_i^T + VR_j Y_i^T UL_i^T      (F structure, row j)
+    emit_triple(c->k1a, c->k1b, toff,
+                {{{-1.0, -1.0}, c->ublk(UR, j, 0), X(t, 1), c->vblk(VL, i, 1)},
+                 {{1.0, 1.0}, c->vblk(VR, j, 0), Y(i, 1), c->ublk(UL, i, 1)}},
+                B_RSP, 3 * nxy + c->foff[j], c->db[j], c->db[i]);
+  }
+  // ---- K2: dH_qp = W1^T dH_sp W2 (pnfam_solver.f90:160-166) ----
+  auto H = [&](int q, int row, const std::vector<long long>& off, const std::vector<int>& cols, int tr_) {
+    return MatRef{B_HSP, q * nxy + off[row], c->db[row], c->db[cols[row]], tr_};
+  };
+  toff = 0;
+  for (int i = 0; i < nb; ++i) {
+    if (c->fc[i] < 0) continue;
+    const int j = c->fc[i], x = c->xc[i], t = c->tr[i];
+    // H20_i = UL_i^T h11_i VR_j + UL_i^T h12_i UR_x + s VL_t^T m21_t VR_j - VL_t^T m22_x^T UR_x
+    emit_triple(c->k2a, c->k2b, toff,
+                {{{1.0, 1.0}, c->ublk(UL, i, 1), H(0, i, c->foff, c->fc, 0), c->vblk(VR, j, 0)},
+                 {{1.0, 1.0}, c->ublk(UL, i, 1), H(1, i, c->xoff, c->xc, 0), c->ublk(UR, x, 0)},
+                 {{-1.0, 1.0}, c->vblk(VL, t, 1), H(2, t, c->yoff, c->yc, 0), c->vblk(VR, j, 0)},
+                 {{-1.0, -1.0}, c->vblk(VL, t, 1), H(3, x, c->foff, c->fc, 1), c->ublk(UR, x, 0)}},
+                B_HQP, c->xoff[i], c->db[i], c->db[x]);
+  }
+  for (int i = 0; i < nb; ++i) {
+    if (c->yc[i] < 0) continue;
+    const int y = c->yc[i], t = c->tr[i], j = c->xc[t];
+    // H02s_i = -VL_t^T h11_t UR_y - s UL_i^T m21_i UR_y - VL_t^T h12_t VR_j + UL_i^T m22_j^T VR_j
+    emit_triple(c->k2a, c->k2b, toff,
+                {{{-1.0, -1.0}, c->vblk(VL, t, 1), H(0, t, c->foff, c->fc, 0), c->ublk(UR, y, 0)},
+                 {{1.0, -1.0}, c->ublk(UL, i, 1), H(2, i, c->yoff, c->yc, 0), c->ublk(UR, y, 0)},
+                 {{-1.0, -1.0}, c->vblk(VL, t, 1), H(1, t, c->xoff, c->xc, 0), c->vblk(VR, j, 0)},
+                 {{1.0, 1.0}, c->ublk(UL, i, 1), H(3, j, c->foff, c->fc, 1), c->vblk(VR, j, 0)}},
+                B_HQP, nxy + c->yoff[i], c->db[i], c->db[y]);
+  }
+  // ---- field projection tasks (spin-uniform row tiles) ----
+  c->htasks.clear();
+  auto add_h = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
+    const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
+    const int seg[3] = {0, nu, d};
+    for (int s = 0; s < 2; ++s)
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += 32)
+        for (int b0 = 0; b0 < dc; b0 += 32) {
+          HTask h;
+          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = std::min(32, seg[s + 1] - a0);
+          h.b0 = b0; h.nbc = std::min(32, dc - b0); h.sa = s == 0 ? 1 : -1;
+          h.mode = mode; h.call = call; h.outq = outq; h.ooff = ooff;
+          c->htasks.push_back(h);
+        }
+  };
+  for (int i = 0; i < nb; ++i) {
+    if (c->fc[i] >= 0) { add_h(i, c->fc[i], 0, 0, 0, c->foff[i]); add_h(i, c->fc[i], 0, 1, 3, c->foff[i]); }
+    if (c->xc[i] >= 0) add_h(i, c->xc[i], 1, 0, 1, c->xoff[i]);
+    if (c->yc[i] >= 0) add_h(i, c->yc[i], 1, 1, 2, c->yoff[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// buffers for a batch of P points
+// ---------------------------------------------------------------------------
+static int ensure_buffers(pnfam_ctx* c, int P, int M) {
+  const long long nxy = c->nxy;
+  CK(dalloc(c->d_state, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_vout, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_T, (size_t)P * 16 * nxy));
+  CK(dalloc(c->d_rsp, (size_t)P * 8 * nxy));
+  CK(dalloc(c->d_hsp, (size_t)P * 8 * nxy));
+  CK(dalloc(c->d_hqp, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_dpart, (size_t)P * 2 * c->G * 2 * ND * c->nghl));
+  CK(dalloc(c->d_mf, (size_t)P * 2 * NMF * 2 * c->nghl));
+  const int Mh = std::max(M, 1);
+  CK(dalloc(c->d_df, (size_t)P * Mh * 4 * nxy));
+  CK(dalloc(c->d_dv, (size_t)P * Mh * 4 * nxy));
+  CK(dalloc(c->d_bpart, (size_t)P * c->nchunk_bro * BRO_NPART));
+  CK(dalloc(c->d_si, (size_t)P));
+  CK(dalloc(c->d_norm, (size_t)P));
+  CK(dalloc(c->d_beta, (size_t)P * Mh * Mh));
+  CK(dalloc(c->d_gamma, (size_t)P * 64));
+  CK(dalloc(c->d_cpart, (size_t)P * c->nchunk_c * 2 * c->nops));
+  CK(dalloc(c->d_wre, (size_t)P));
+  CK(dalloc(c->d_wim, (size_t)P));
+  CK(dalloc(c->d_active, (size_t)P));
+  BufDesc bd[NBUF];
+  bd[B_UP] = {c->d_up.p, 0, 0};
+  bd[B_VP] = {c->d_vp.p, 0, 0};
+  bd[B_UN] = {c->d_un.p, 0, 0};
+  bd[B_VN] = {c->d_vn.p, 0, 0};
+  bd[B_STATE] = {c->d_state.p, 4 * nxy, 2 * nxy};
+  bd[B_T] = {c->d_T.p, 16 * nxy, 8 * nxy};
+  bd[B_RSP] = {c->d_rsp.p, 8 * nxy, 4 * nxy};
+  bd[B_HSP] = {c->d_hsp.p, 8 * nxy, 4 * nxy};
+  bd[B_HQP] = {c->d_hqp.p, 4 * nxy, 2 * nxy};
+  CK(upload(c->d_bufs, bd, NBUF));
+  return PNFAM_OK;
+}
+
+static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
+  if (tl.ntiles == 0) return PNFAM_OK;
+  dim3 grid(tl.ntiles, 2 * P);
+  k_gemm<<<grid, 256, 0, c->stream>>>(tl.d_tasks.p, tl.d_tile2task.p, c->d_bufs.p, active);
+  c->launches++;
+  CK(cudaGetLastError());
+  return PNFAM_OK;
+}
+
+// residual interaction: state (X, Y) -> hqp (H20, H02 stored)
+static int residual(pnfam_ctx* c, int P, bool timed) {
+  const int* act = c->d_active.p;
+  auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
+  auto toc = [&](int k) {
+    if (!timed) return;
+    cudaEventRecord(c->ev[1], c->stream);
+    cudaEventSynchronize(c->ev[1]);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    c->stage_ms[k] += ms;
+  };
+  int rc;
+  tic();
+  if ((rc = launch_gemm(c, c->k1a, P, act))) return rc;
+  if ((rc = launch_gemm(c, c->k1b, P, act))) return rc;
+  toc(0);
+  const long long nxy = c->nxy;
+  DensCall d0, d1;
+  d0.rho = c->d_rsp.p + 0 * nxy; d0.rho_sp = 8 * nxy; d0.rho_spl = 4 * nxy;
+  d0.rcols = c->d_fc.p; d0.roffs = c->d_foff.p;
+  d0.kap = c->d_rsp.p + 1 * nxy; d0.kap_sp = 8 * nxy; d0.kap_spl = 4 * nxy;
+  d0.kcols = c->d_xtc.p; d0.koffs = c->d_xtoff.p;
+  d1.rho = c->d_rsp.p + 3 * nxy; d1.rho_sp = 8 * nxy; d1.rho_spl = 4 * nxy;
+  d1.rcols = c->d_fc.p; d1.roffs = c->d_foff.p;
+  d1.kap = c->d_rsp.p + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
+  d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
+  const DevBasis B = c->devbasis();
+  tic();
+  {
+    dim3 grid((c->nghl + DRT - 1) / DRT, c->G, 2 * P);
+    k_density<<<grid, 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p, act);
+    c->launches++;
+    CK(cudaGetLastError());
+  }
+  toc(1);
+  tic();
+  {
+    dim3 grid((c->nghl + 127) / 128, 2 * P);
+    k_meanfield<<<grid, 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
+    c->launches++;
+    CK(cudaGetLastError());
+  }
+  toc(2);
+  tic();
+  {
+    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+    dim3 grid((unsigned)c->htasks.size(), P);
+    k_hproj<<<grid, 256, smem, c->stream>>>(B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
+    c->launches++;
+    CK(cudaGetLastError());
+  }
+  toc(3);
+  tic();
+  if ((rc = launch_gemm(c, c->k2a, P, act))) return rc;
+  if ((rc = launch_gemm(c, c->k2b, P, act))) return rc;
+  toc(4);
+  return PNFAM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, const double* En,
+                              const double* Up, const double* Vp, const double* Un, const double* Vn,
+                              const double* phi, const double* wdcori, const pnfam_coupl_t* coupl,
+                              pnfam_ctx_t** out) {
+  g_err.clear();
+  if (!basis || !Ep || !En || !Up || !Vp || !Un || !Vn || !phi || !wdcori || !coupl || !out)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_init: NULL argument");
+  *out = nullptr;
+  if (basis->nb <= 0 || basis->nb % 2 || basis->nghl <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_init: nb must be positive and even, nghl positive");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(PNFAM_ECUDA, "pnfam_gpu_init: no CUDA device available");
+  pnfam_ctx* c = new pnfam_ctx();
+  cudaGetDevice(&c->dev);
+  c->nb = basis->nb;
+  c->nghl = basis->nghl;
+  c->db.assign(basis->db, basis->db + c->nb);
+  c->nup.assign(basis->num_spin_up, basis->num_spin_up + c->nb);
+  c->st.resize(c->nb);
+  c->tr.resize(c->nb);
+  c->uoff.resize(c->nb);
+  long long mo = 0;
+  int s = 0;
+  for (int i = 0; i < c->nb; ++i) {
+    if (c->db[i] < 0 || c->nup[i] < 0 || c->nup[i] > c->db[i]) {
+      delete c;
+      return fail(PNFAM_EINVAL, "pnfam_gpu_init: bad block size or spin count");
+    }
+    c->st[i] = s; s += c->db[i];
+    c->uoff[i] = mo; mo += (long long)c->db[i] * c->db[i];
+    c->tr[i] = i < c->nb / 2 ? i + c->nb / 2 : i - c->nb / 2;
+  }
+  for (int i = 0; i < c->nb; ++i)
+    if (c->db[i] != c->db[c->tr[i]]) { delete c; return fail(PNFAM_EINVAL, "pnfam_gpu_init: TR partner blocks differ in size"); }
+  c->dqp = s;
+  c->ns.resize(s);
+  for (int k = 0; k < s; ++k) {
+    if (basis->ns[k] != 1 && basis->ns[k] != -1) { delete c; return fail(PNFAM_EINVAL, "pnfam_gpu_init: ns must be +-1"); }
+    c->ns[k] = (signed char)basis->ns[k];
+  }
+  for (int i = 0; i < 12; ++i) c->sc[i] = coupl->scalars[i];
+  auto up = [&](auto& buf, const auto* h, size_t n) -> int { CK(upload(buf, h, n)); return 0; };
+  int rc = 0;
+  const size_t nphi = (size_t)5 * s * c->nghl;
+  if ((rc = up(c->d_db, c->db.data(), c->nb)) || (rc = up(c->d_st, c->st.data(), c->nb)) ||
+      (rc = up(c->d_nup, c->nup.data(), c->nb)) || (rc = up(c->d_ns, c->ns.data(), (size_t)s)) ||
+      (rc = up(c->d_up, Up, (size_t)mo)) || (rc = up(c->d_vp, Vp, (size_t)mo)) ||
+      (rc = up(c->d_un, Un, (size_t)mo)) || (rc = up(c->d_vn, Vn, (size_t)mo)) ||
+      (rc = up(c->d_ep, Ep, (size_t)s)) || (rc = up(c->d_en, En, (size_t)s)) ||
+      (rc = up(c->d_phi, phi, nphi)) || (rc = up(c->d_wd, wdcori, (size_t)c->nghl)) ||
+      (rc = up(c->d_crho, coupl->crho, (size_t)c->nghl)) || (rc = up(c->d_cs, coupl->cs, (size_t)c->nghl)) ||
+      (rc = up(c->d_cpair, coupl->cpair, (size_t)c->nghl)) || (rc = up(c->d_cspair, coupl->cspair, (size_t)c->nghl))) {
+    delete c;
+    return rc;
+  }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
+      cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess) {
+    delete c;
+    return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
+  }
+  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+  if (cudaFuncSetAttribute(k_hproj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    delete c;
+    return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
+  }
+  *out = c;
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int* fcols, const double* Fsp,
+                                      int n_xterms, const double* const* Gsp) {
+  g_err.clear();
+  if (!c || !fcols || !Fsp || n_xterms < 0 || (n_xterms > 0 && !Gsp))
+    return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: bad argument");
+  const int nb = c->nb;
+  c->beta_minus = beta_minus ? 1 : 0;
+  c->fc.assign(fcols, fcols + nb);
+  for (int i = 0; i < nb; ++i)
+    if (c->fc[i] < -1 || c->fc[i] >= nb) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: fcols out of range");
+  c->xc.assign(nb, -1); c->yc.assign(nb, -1); c->xtc.assign(nb, -1); c->ytc.assign(nb, -1);
+  for (int i = 0; i < nb; ++i) {
+    if (c->fc[i] >= 0) c->xc[i] = c->tr[c->fc[i]];
+    c->yc[i] = c->fc[c->tr[i]];
+  }
+  for (int i = 0; i < nb; ++i) {
+    if (c->xc[i] >= 0) { if (c->xtc[c->xc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: F is not one block per column"); c->xtc[c->xc[i]] = i; }
+    if (c->yc[i] >= 0) { if (c->ytc[c->yc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: F is not one block per column"); c->ytc[c->yc[i]] = i; }
+  }
+  long long nf, nx, ny, nxt, nyt;
+  c->foff = offsets(c->fc, c->db, &nf);
+  c->xoff = offsets(c->xc, c->db, &nx);
+  c->yoff = offsets(c->yc, c->db, &ny);
+  c->xtoff = offsets(c->xtc, c->db, &nxt);
+  c->ytoff = offsets(c->ytc, c->db, &nyt);
+  if (nf != nx || nf != ny || nf != nxt || nf != nyt || nf == 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: inconsistent block structure");
+  c->nxy = nf;
+  c->nops = 1 + n_xterms;
+  CK(upload(c->d_fc, c->fc.data(), nb));
+  CK(upload(c->d_xtc, c->xtc.data(), nb));
+  CK(upload(c->d_ytc, c->ytc.data(), nb));
+  CK(upload(c->d_foff, c->foff.data(), nb));
+  CK(upload(c->d_xtoff, c->xtoff.data(), nb));
+  CK(upload(c->d_ytoff, c->ytoff.data(), nb));
+  // element -> (row state, column state) for the X|Y layout (Green's function)
+  std::vector<int> erow(2 * nf), ecol(2 * nf);
+  const std::vector<double>* dummy = nullptr; (void)dummy;
+  for (int part = 0; part < 2; ++part) {
+    const std::vector<int>& cols = part == 0 ? c->xc : c->yc;
+    const std::vector<long long>& off = part == 0 ? c->xoff : c->yoff;
+    for (int i = 0; i < nb; ++i) {
+      if (cols[i] < 0) continue;
+      const int d = c->db[i], dc = c->db[cols[i]];
+      for (int b = 0; b < dc; ++b)
+        for (int a = 0; a < d; ++a) {
+          const long long e = part * nf + off[i] + a + (long long)b * d;
+          erow[e] = c->st[i] + a;
+          ecol[e] = c->st[cols[i]] + b;
+        }
+    }
+  }
+  CK(upload(c->d_erow, erow.data(), erow.size()));
+  CK(upload(c->d_ecol, ecol.data(), ecol.size()));
+  // partition of the density work
+  {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+    const int ntr = (c->nghl + DRT - 1) / DRT;
+    int nrows = 0;
+    for (int i = 0; i < nb; ++i) nrows += c->fc[i] >= 0;
+    c->G = std::max(1, std::min(nrows, (2 * std::max(nsm, 1) + ntr - 1) / ntr));
+  }
+  c->nchunk_bro = (int)std::min<long long>(64, std::max<long long>(1, (4 * nf) / 4096));
+  c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (2 * nf) / 4096));
+  build_tasks(c);
+  CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
+  CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
+  c->have_op = true;
+  int rc = ensure_buffers(c, std::max(1, c->cap_P), std::max(1, c->cap_M));
+  if (rc) return rc;
+  c->cap_P = std::max(1, c->cap_P); c->cap_M = std::max(1, c->cap_M);
+  // F_qp and cross terms: K2 applied to dH_sp = (F, 0, 0, 0) (pnfam_solver.f90:368-381)
+  CK(dalloc(c->d_fops, (size_t)c->nops * 2 * nf));
+  std::vector<int> one = {1};
+  CK(upload(c->d_active, one.data(), 1));
+  for (int k = 0; k < c->nops; ++k) {
+    const double* src = k == 0 ? Fsp : Gsp[k - 1];
+    CK(cudaMemsetAsync(c->d_hsp.p, 0, sizeof(double) * 8 * nf, c->stream));
+    CK(cudaMemcpyAsync(c->d_hsp.p, src, sizeof(double) * nf, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = launch_gemm(c, c->k2a, 1, c->d_active.p))) return rc;
+    if ((rc = launch_gemm(c, c->k2b, 1, c->d_active.p))) return rc;
+    CK(cudaMemcpyAsync(c->d_fops.p + (long long)k * 2 * nf, c->d_hqp.p, sizeof(double) * 2 * nf,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
+                               const pnfam_solver_opts_t* o, double* re_S, double* im_S, int* iters,
+                               double* si_out, double* hist) {
+  g_err.clear();
+  if (!c || !o || !re_w || !im_w || !re_S || !im_S || !iters || !si_out || P <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_solve: bad argument");
+  if (!c->have_op) return fail(PNFAM_ESTATE, "pnfam_gpu_solve: call pnfam_gpu_set_operator first");
+  if (o->max_iter < 0) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: max_iter < 0");
+  if (o->precision != 0) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: only precision 0 (FP64) is available");
+  const bool no_res = std::fabs(o->quench_residual_int) < 1e-10;
+  int M = no_res ? -1 : o->broyden_history_size;
+  if (M > 64) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: broyden_history_size > 64 is not supported");
+  const long long nxy = c->nxy;
+  const int N = (int)(4 * nxy);
+  int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(M, 1), c->cap_M));
+  if (rc) return rc;
+  c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(M, 1), c->cap_M);
+  for (int k = 0; k < 8; ++k) c->stage_ms[k] = 0.0;
+  c->launches = 0;
+  const bool timed = o->reserved[0] != 0;
+  CK(cudaEventRecord(c->evt[0], c->stream));
+  CK(cudaMemsetAsync(c->d_state.p, 0, sizeof(double) * (size_t)P * N, c->stream));
+  CK(cudaMemcpyAsync(c->d_wre.p, re_w, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_wim.p, im_w, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+  const int nops = c->nops;
+  std::vector<double> si(P, 1.0), sre((size_t)P * nops, 0.0), sim((size_t)P * nops, 0.0);
+  std::vector<int> active(P, 1), conv(P, -1);
+  std::vector<double> hsi(P), cpart((size_t)P * c->nchunk_c * 2 * nops);
+  const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
+  const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
+  BroState S;
+  S.N = N; S.M = std::max(M, 1); S.alpha = o->alpha_mix;
+  S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
+  S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
+  const double w0 = 0.01;
+  const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
+  auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
+  auto toc = [&](int k) {
+    if (!timed) return;
+    cudaEventRecord(c->ev[1], c->stream);
+    cudaEventSynchronize(c->ev[1]);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    c->stage_ms[k] += ms;
+  };
+  for (int it = 0; it <= o->max_iter; ++it) {
+    int nact = 0;
+    for (int p = 0; p < P; ++p) {
+      if (!active[p]) continue;
+      if (hist) {
+        double* h = hist + ((size_t)p * (o->max_iter + 1) + it) * 3;
+        h[0] = si[p]; h[1] = sre[(size_t)p * nops]; h[2] = sim[(size_t)p * nops];
+      }
+      if (si[p] < o->convergence_epsilon) { conv[p] = it; active[p] = 0; continue; }
+      if (it == o->max_iter) { conv[p] = -1; active[p] = 0; continue; }
+      ++nact;
+    }
+    if (nact == 0) break;
+    CK(cudaMemcpyAsync(c->d_active.p, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+    const int* act = c->d_active.p;
+    if (!no_res) {
+      if ((rc = residual(c, P, timed))) return rc;
+    }
+    tic();
+    {
+      dim3 grid(gx, P);
+      k_green<<<grid, 256, 0, c->stream>>>(nxy, P, no_res ? nullptr : c->d_hqp.p, c->d_fops.p, c->d_erow.p,
+                                           c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p, o->quench_residual_int,
+                                           c->d_vout.p, act);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
+    toc(5);
+    // ---- Broyden (pnfam_broyden.f90:117-216) ----
+    tic();
+    int mode;
+    S.it = it;
+    if (M < 0) mode = 2;
+    else if (M == 0 || it == 0) mode = 1;
+    else mode = 0;
+    const bool upd = (mode == 0 && it >= 2);
+    if (mode == 0) {
+      auto fdiv = [](int a, int b) { return a / b; };  // C++ truncates like Fortran
+      S.iter_used = std::min(it - 1, M);
+      S.ipos = it - 1 - fdiv(it - 2, M) * M - 1;
+      S.inext = it - fdiv(it - 1, M) * M - 1;
+    } else {
+      S.iter_used = 0; S.ipos = 0; S.inext = 0;
+    }
+    {
+      dim3 grid(c->nchunk_bro, P);
+      k_bro_diff<<<grid, 256, 0, c->stream>>>(S, upd ? 1 : 0, act);
+      k_bro_solve<<<P, 32, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+      c->launches += 2;
+      if (mode == 0) {
+        k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, upd ? 1 : 0, act);
+        k_bro_solve<<<P, 32, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+        c->launches += 2;
+      }
+      dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
+      k_bro_update<<<ug, 256, 0, c->stream>>>(S, mode, c->d_gamma.p, act);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
+    toc(6);
+    tic();
+    {
+      dim3 grid(c->nchunk_c, P);
+      k_contract<<<grid, 256, 0, c->stream>>>(nxy, nops, c->d_fops.p, c->d_state.p, c->nchunk_c, c->d_cpart.p, act);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(hsi.data(), c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(cpart.data(), c->d_cpart.p, sizeof(double) * cpart.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    toc(7);
+    const double pi = 3.141592653589793238462643;
+    for (int p = 0; p < P; ++p) {
+      if (!active[p]) continue;
+      si[p] = hsi[p];
+      if (!std::isfinite(si[p])) return fail(PNFAM_ENONFINITE, "pnfam_gpu_solve: non-finite residual");
+      for (int k = 0; k < nops; ++k) {
+        double a = 0.0, b = 0.0;
+        for (int ch = 0; ch < c->nchunk_c; ++ch) {
+          a += cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k];
+          b += cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k + 1];
+        }
+        sre[(size_t)p * nops + k] = -a / pi;
+        sim[(size_t)p * nops + k] = -b / pi;
+      }
+    }
+  }
+  CK(cudaEventRecord(c->evt[1], c->stream));
+  CK(cudaEventSynchronize(c->evt[1]));
+  {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->evt[0], c->evt[1]);
+    c->total_ms = ms;
+  }
+  for (int p = 0; p < P; ++p) {
+    iters[p] = conv[p];
+    si_out[p] = si[p];
+    for (int k = 0; k < nops; ++k) {
+      re_S[(size_t)p * nops + k] = sre[(size_t)p * nops + k];
+      im_S[(size_t)p * nops + k] = sim[(size_t)p * nops + k];
+    }
+  }
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* c, const double* re_rho_pn, const double* im_rho_pn,
+                                          const double* re_kp, const double* im_kp, const double* re_rho_np,
+                                          const double* im_rho_np, const double* re_km, const double* im_km,
+                                          double* re_h_pn, double* im_h_pn, double* re_dp, double* im_dp,
+                                          double* re_h_np, double* im_h_np, double* re_dm, double* im_dm) {
+  g_err.clear();
+  if (!c) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian: NULL context");
+  if (!c->have_op) return fail(PNFAM_ESTATE, "pnfam_gpu_calc_hamiltonian: call pnfam_gpu_set_operator first");
+  const void* in[8] = {re_rho_pn, im_rho_pn, re_kp, im_kp, re_rho_np, im_rho_np, re_km, im_km};
+  void* outp[8] = {re_h_pn, im_h_pn, re_dp, im_dp, re_h_np, im_h_np, re_dm, im_dm};
+  for (int k = 0; k < 8; ++k)
+    if (!in[k] || !outp[k]) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian: NULL array");
+  int rc = ensure_buffers(c, std::max(1, c->cap_P), std::max(1, c->cap_M));
+  if (rc) return rc;
+  const long long nxy = c->nxy;
+  const size_t nb = sizeof(double) * nxy;
+  // RSP quadrant q, plane pl at pl*4nxy + q*nxy (point 0): 0 rho_pn, 1 kappa+, 2 kappa-, 3 rho_np
+  const int qin[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(c->d_rsp.p + (k & 1) * 4 * nxy + qin[k] * nxy, in[k], nb, cudaMemcpyHostToDevice, c->stream));
+  std::vector<int> one = {1};
+  CK(cudaMemcpyAsync(c->d_active.p, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  DensCall d0, d1;
+  d0.rho = c->d_rsp.p + 0 * nxy; d0.rho_sp = 8 * nxy; d0.rho_spl = 4 * nxy;
+  d0.rcols = c->d_fc.p; d0.roffs = c->d_foff.p;
+  d0.kap = c->d_rsp.p + 1 * nxy; d0.kap_sp = 8 * nxy; d0.kap_spl = 4 * nxy;
+  d0.kcols = c->d_xtc.p; d0.koffs = c->d_xtoff.p;
+  d1.rho = c->d_rsp.p + 3 * nxy; d1.rho_sp = 8 * nxy; d1.rho_spl = 4 * nxy;
+  d1.rcols = c->d_fc.p; d1.roffs = c->d_foff.p;
+  d1.kap = c->d_rsp.p + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
+  d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
+  const DevBasis B = c->devbasis();
+  const int* act = c->d_active.p;
+  k_density<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p, act);
+  k_meanfield<<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
+  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+  k_hproj<<<dim3((unsigned)c->htasks.size(), 1), 256, smem, c->stream>>>(B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
+  CK(cudaGetLastError());
+  const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(outp[k], c->d_hsp.p + (k & 1) * 4 * nxy + qout[k] * nxy, nb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return PNFAM_OK;
+}
+
+extern "C" long long pnfam_gpu_nxy(const pnfam_ctx_t* c) { return c && c->have_op ? c->nxy : 0; }
+
+extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, int nstage, long long* launches) {
+  if (!c) return fail(PNFAM_EINVAL, "pnfam_gpu_last_profile: NULL context");
+  for (int k = 0; k < nstage && k < 8; ++k) stage_ms[k] = c->stage_ms[k];
+  if (nstage > 8) stage_ms[8] = c->total_ms;
+  if (launches) *launches = c->launches;
+  return PNFAM_OK;
+}
+
+extern "C" void pnfam_gpu_free(pnfam_ctx_t* c) { delete c; }
+
+extern "C" const char* pnfam_gpu_last_error(void) { return g_err.c_str(); }

@@ -398,9 +398,10 @@ class HFBSolution:
         return ib + half if ib < half else ib - half
 
 
-def load_hfb_solution(path: str) -> HFBSolution:
-    """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file."""
-    h = read_hel(path)
+def load_hfb_solution(path) -> HFBSolution:
+    """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file
+    (a path, or an already decoded :class:`HelData`)."""
+    h = path if isinstance(path, HelData) else read_hel(path)
     mb = build_mesh_basis(h)
     hd = hfb_matrices(h, mb)
     qpn = diagonalise(h, hd, "n", float(h.N))

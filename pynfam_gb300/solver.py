@@ -1,0 +1,135 @@
+"""Host-side mirror of the reference solver interface, on top of the C ABI.
+
+``GPUSolver`` owns one device context per nucleus (pnfam_gpu_init), one
+operator at a time (pnfam_gpu_set_operator) and solves batches of omega points
+(pnfam_gpu_solve).  It mirrors the reference's pnfam_solve / init_pnfam_solver
+/ ifam split (pnfam_solver.f90:32-221) with the per-process set-up hoisted out
+of the per-point loop.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .blockmatrix import BlockMatrix
+
+
+@dataclass
+class SolveResult:
+    re_S: np.ndarray      # [P, 1 + n_xterms]
+    im_S: np.ndarray
+    iters: np.ndarray     # [P] iteration at convergence, -1 if interrupted
+    si: np.ndarray        # [P]
+    hist: np.ndarray = None  # [P, max_iter + 1, 3] (si, Re S, Im S), NaN after convergence
+    seconds: float = 0.0
+
+
+def _flat_blocks(blocks) -> np.ndarray:
+    parts = [np.asarray(b, dtype=np.float64).reshape(-1, order="F") for b in blocks]
+    return np.ascontiguousarray(np.concatenate(parts)) if parts else np.zeros(0)
+
+
+class GPUSolver:
+    """One nucleus resident on the current CUDA device."""
+
+    def __init__(self, hfb, couplings):
+        self.lib = _lib.load()
+        self.hfb = hfb
+        self.nb = int(hfb.nb)
+        self._keep = []
+        db = np.ascontiguousarray(hfb.db, dtype=np.int32)
+        nup = np.ascontiguousarray(hfb.num_spin_up, dtype=np.int32)
+        ns = np.ascontiguousarray(hfb.ns, dtype=np.int32)
+        self._keep += [db, nup, ns]
+        basis = _lib.Basis(self.nb, _lib.iptr(db), _lib.iptr(nup), _lib.iptr(ns), int(hfb.nghl))
+        phi = np.ascontiguousarray(np.stack([hfb.wf, hfb.wfdr, hfb.wfdp, hfb.wfdz, hfb.wfd2_all]))
+        Up, Vp, Un, Vn = (_flat_blocks(x) for x in (hfb.Up, hfb.Vp, hfb.Un, hfb.Vn))
+        Ep = np.ascontiguousarray(hfb.Ep, dtype=np.float64)
+        En = np.ascontiguousarray(hfb.En, dtype=np.float64)
+        wd = np.ascontiguousarray(hfb.wdcori, dtype=np.float64)
+        cpl = [np.ascontiguousarray(a, dtype=np.float64) for a in (couplings.crho, couplings.cs, couplings.cpair, couplings.cspair)]
+        self._keep += [phi, Up, Vp, Un, Vn, Ep, En, wd] + cpl
+        cp = _lib.Coupl(_lib.dptr(cpl[0]), _lib.dptr(cpl[1]), _lib.dptr(cpl[2]), _lib.dptr(cpl[3]),
+                        (C.c_double * 12)(*couplings.scalars()))
+        ctx = C.c_void_p()
+        _lib.check(self.lib.pnfam_gpu_init(C.byref(basis), _lib.dptr(Ep), _lib.dptr(En), _lib.dptr(Up),
+                                           _lib.dptr(Vp), _lib.dptr(Un), _lib.dptr(Vn), _lib.dptr(phi),
+                                           _lib.dptr(wd), C.byref(cp), C.byref(ctx)))
+        self.ctx = ctx
+        self.nops = 1
+        self.F = None
+
+    def set_operator(self, F, G=()):
+        """F: ExternalField (or BlockMatrix + beta flag via F.beta_minus)."""
+        mat = F.mat if hasattr(F, "mat") else F
+        fcols = np.ascontiguousarray(mat.cols, dtype=np.int32)
+        fsp = np.ascontiguousarray(mat.flatten(), dtype=np.float64)
+        gs = [np.ascontiguousarray(g.mat.flatten(), dtype=np.float64) for g in G]
+        arr = (C.POINTER(C.c_double) * max(1, len(gs)))(*[_lib.dptr(g) for g in gs]) if gs else None
+        _lib.check(self.lib.pnfam_gpu_set_operator(self.ctx, 1 if F.beta_minus else 0, _lib.iptr(fcols),
+                                                   _lib.dptr(fsp), len(gs), arr))
+        self.nops = 1 + len(gs)
+        self.F = F
+        self.fcols = fcols
+
+    @property
+    def nxy(self) -> int:
+        return int(self.lib.pnfam_gpu_nxy(self.ctx))
+
+    def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
+              history=False, timed=False) -> SolveResult:
+        import time
+        if alpha_mix is None:
+            from .pnfam_setup import ALPHA_MIX as alpha_mix
+        w = np.atleast_1d(np.asarray(omegas, dtype=complex))
+        P = len(w)
+        wre = np.ascontiguousarray(w.real); wim = np.ascontiguousarray(w.imag)
+        reS = np.zeros(P * self.nops); imS = np.zeros(P * self.nops)
+        iters = np.zeros(P, dtype=np.int32); si = np.zeros(P)
+        hist = np.full(P * (max_iter + 1) * 3, np.nan) if history else None
+        o = _lib.SolverOpts()
+        o.max_iter = int(max_iter); o.broyden_history_size = int(broyden_m)
+        o.convergence_epsilon = float(eps); o.alpha_mix = float(alpha_mix)
+        o.quench_residual_int = float(quench); o.precision = 0
+        o.reserved[0] = 1 if timed else 0
+        t0 = time.perf_counter()
+        _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
+                                            _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
+                                            _lib.dptr(hist) if hist is not None else None))
+        dt = time.perf_counter() - t0
+        return SolveResult(reS.reshape(P, self.nops), imS.reshape(P, self.nops), iters, si,
+                           hist.reshape(P, max_iter + 1, 3) if hist is not None else None, dt)
+
+    def last_profile(self):
+        ms = np.zeros(9); n = C.c_longlong()
+        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 9, C.byref(n)))
+        names = ("k1_blockgemm", "density", "meanfield", "field_projection", "k2_blockgemm", "green", "broyden",
+                 "strength", "total")
+        return dict(zip(names, ms.tolist())), int(n.value)
+
+    def calc_hamiltonian(self, rho_pn, kp, rho_np, km):
+        """Plugin seam: complex flat arrays (nxy) in the structures documented in
+        include/pnfam_gpu.h; returns (h_pn, Delta+, h_np, Delta-) complex."""
+        n = self.nxy
+        ins = []
+        for a in (rho_pn, kp, rho_np, km):
+            a = np.asarray(a, dtype=complex)
+            ins += [np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)]
+        outs = [np.zeros(n) for _ in range(8)]
+        _lib.check(self.lib.pnfam_gpu_calc_hamiltonian(self.ctx, *[_lib.dptr(x) for x in ins],
+                                                       *[_lib.dptr(x) for x in outs]))
+        return tuple(outs[2 * k] + 1j * outs[2 * k + 1] for k in range(4))
+
+    def close(self):
+        if getattr(self, "ctx", None) is not None and self.ctx.value:
+            self.lib.pnfam_gpu_free(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

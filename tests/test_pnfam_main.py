@@ -1,0 +1,95 @@
+"""The pnfam_main drop-in: namelist + hfbtho_output.hel in, <name>.dat out,
+parsed the way pynfam's pnfamParser reads it (pynfam/outputs/pnfam_parser.py)."""
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+from golden_cases import GOLDEN, golden
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EXE = os.path.join(ROOT, "pynfam_gb300", "bin", "pnfam_main.x")
+
+
+def write_in(path, pt, interaction, name):
+    n = pt["namelist"]
+    txt = f"""&general
+    fam_output_filename = '{name}'
+    print_stdout = .false.
+    use_fam_storage = 0
+    real_eqrpa = {n['real_eqrpa']!r}
+    imag_eqrpa = {n['imag_eqrpa']!r}
+/
+
+&ext_field
+    beta_type = '{n['beta_type']}'
+    operator_name = '{n['operator_name']}'
+    operator_k = {n['operator_k']}
+    compute_crossterms = {'.true.' if n['compute_crossterms'] else '.false.'}
+    two_body_current_mode = 0
+    two_body_current_usep = .false.
+    two_body_current_lecs = -3.1962, 3.1962, 0
+/
+
+{interaction}
+&solver
+    max_iter = {n['max_iter']}
+    convergence_epsilon = {n['convergence_epsilon']!r}
+    broyden_history_size = {n['broyden_history_size']}
+    energy_shift_prot = 0.0
+    energy_shift_neut = 0.0
+    quench_residual_int = {n['quench_residual_int']!r}
+/
+"""
+    open(path, "w").write(txt)
+
+
+def parse_dat(path):
+    """What pnfamParser extracts: version, convergence, time and the table."""
+    lines = open(path).read().splitlines()
+    version = [l for l in lines if "Version:" in l][0].split()[-1]
+    conv = "Yes" if any("iteration converged" in l for l in lines) else \
+        ("No" if any("iteration interrupted" in l for l in lines) else None)
+    time_line = [l for l in lines if "Total CPU time" in l][0]
+    t = float(time_line.split()[-2])
+    table = [l.split() for l in lines if l.strip() and not l.startswith("#")]
+    assert table[0] == ["Real", "Imag"]
+    rows = {r[0]: (float(r[1]), float(r[2])) for r in table[1:]}
+    return version, conv, t, rows
+
+
+def test_cli_reports_missing_ground_state(tmp_path):
+    g = golden("S40")
+    write_in(tmp_path / "GT-K0.in", g["operators"]["GT-K0"][0], g["interaction"], "GT-K0")
+    env = dict(os.environ, PNFAM_GB300_CACHE="off")
+    p = subprocess.run([sys.executable, EXE, "GT-K0.in"], cwd=tmp_path, capture_output=True, text=True, env=env)
+    assert p.returncode == 1
+    assert "hfbtho_output.hel" in p.stderr
+    out = open(tmp_path / "GT-K0.dat").read()
+    assert "ERROR" in out and "Strength" not in out
+
+
+def test_cli_rejects_two_arguments(tmp_path):
+    p = subprocess.run([sys.executable, EXE, "a", "b"], cwd=tmp_path, capture_output=True, text=True)
+    assert p.returncode == 1 and "More than one" in p.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op,idx", [("GT-K0", 0), ("P-K1", 4)])
+def test_cli_point_matches_recorded(tmp_path, op, idx):
+    g = golden("S40")
+    pt = g["operators"][op][idx]
+    write_in(tmp_path / f"{op}.in", pt, g["interaction"], op)
+    shutil.copyfile(os.path.join(GOLDEN, "S40.hel"), tmp_path / "hfbtho_output.hel")
+    env = dict(os.environ, PNFAM_GB300_CACHE=str(tmp_path / "cache"))
+    p = subprocess.run([sys.executable, EXE, f"{op}.in"], cwd=tmp_path, capture_output=True, text=True, env=env)
+    assert p.returncode == 0 and p.stderr.strip() == "", p.stderr
+    version, conv, t, rows = parse_dat(tmp_path / f"{op}.dat")
+    assert conv == "Yes" and t >= 0.0 and version
+    for lab, (re_, im_) in pt["result"].items():
+        got = rows[lab]
+        assert abs(got[0] - re_) <= 1e-6 * abs(re_) + 1e-15, (lab, got, re_)
+        assert abs(got[1] - im_) <= 1e-6 * abs(im_) + 1e-15, (lab, got, im_)
