@@ -130,6 +130,42 @@ int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* ctx,
                                double* re_h_np, double* im_h_np,
                                double* re_dm, double* im_dm);
 
+/*
+ * Allocation-free field evaluation.  No counterpart in the reference: the
+ * reference evaluates the field only inside its own process.
+ *
+ * For callers that cannot allocate device memory themselves through CUDA (a
+ * host program that owns every device buffer through its own memory pool or
+ * through mapped host memory, or code running where device allocation is not
+ * allowed): the same computation as pnfam_gpu_calc_hamiltonian, with every
+ * input and output given as a DEVICE pointer by the caller and all
+ * intermediates kept in one fixed device array inside the library (about
+ * 12.5 MB, held on every GPU that loads the library until the process exits).
+ * This entry point calls no cudaMalloc/cudaFree and no allocating library
+ * routine.
+ *
+ *   basis         host struct with host arrays (as for pnfam_gpu_init)
+ *   d_phi         device [5][dqp][nghl] basis functions
+ *   d_wdcori      device [nghl]
+ *   d_coupl       couplings: the four arrays are DEVICE pointers [nghl]
+ *   fcols         host [nb] block map of the operator (as for set_operator)
+ *   d_in[8]       device: Re/Im rho_pn, Re/Im kappa(+), Re/Im rho_np, Re/Im kappa(-)
+ *   d_out[8]      device: Re/Im h_pn, Re/Im Delta(+), Re/Im h_np, Re/Im Delta(-)
+ *                 (structures as for pnfam_gpu_calc_hamiltonian)
+ *   stream        cudaStream_t to run on (NULL: the default stream); the call
+ *                 returns after the stream has finished the work
+ * Limits: nxy <= 32768, nghl <= 1600, dqp <= 1024, nb <= 64 (every operator
+ * up to N_sh = 12 on a 40 x 40 mesh); larger sizes return PNFAM_EINVAL.
+ * The first call on a device looks up the array's device address and sets a
+ * kernel attribute; make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (from several threads
+ * or streams) race and must be serialised by the caller.
+ */
+int pnfam_gpu_calc_hamiltonian_noalloc(const pnfam_basis_t* basis, const double* d_phi,
+                                       const double* d_wdcori, const pnfam_coupl_t* d_coupl,
+                                       const int* fcols, const double* const* d_in,
+                                       double* const* d_out, void* stream);
+
 /* Number of non-trivial FAM matrix elements nxy (valid after set_operator). */
 long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
 

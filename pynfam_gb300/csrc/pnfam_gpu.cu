@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -800,3 +801,200 @@ extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, in
 extern "C" void pnfam_gpu_free(pnfam_ctx_t* c) { delete c; }
 
 extern "C" const char* pnfam_gpu_last_error(void) { return g_err.c_str(); }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of pnfam_gpu_calc_hamiltonian
+//
+// For callers that cannot call cudaMalloc (a host code that owns all device
+// memory through its own pool or mapped memory, or code running where device
+// allocation is not allowed): the caller passes device pointers for every
+// input and output, and all intermediates live in one file-scope device array
+// of fixed size.  Every GPU that loads this library holds that array (about
+// 12.5 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr long long NA_MAX_NXY = 32768;   // FAM matrix elements (N_sh <= 12)
+constexpr int NA_MAX_NGHL = 1600;         // mesh points (40 x 40)
+constexpr int NA_MAX_DQP = 1024;          // basis states incl. time-reversed partners
+constexpr int NA_MAX_NB = 64;             // blocks incl. time-reversed partners
+constexpr int NA_MAX_HTASKS = 4096;       // field-projection tiles
+constexpr int NA_G = 2;                   // block-row groups of the density kernel
+
+constexpr size_t na_align(size_t n) { return (n + 255) / 256 * 256; }
+constexpr size_t NA_RSP = na_align(sizeof(double) * 8 * NA_MAX_NXY);
+constexpr size_t NA_HSP = na_align(sizeof(double) * 8 * NA_MAX_NXY);
+constexpr size_t NA_DPART = na_align(sizeof(double) * 2 * NA_G * 2 * ND * NA_MAX_NGHL);
+constexpr size_t NA_MF = na_align(sizeof(double) * 2 * NMF * 2 * NA_MAX_NGHL);
+constexpr size_t NA_INTS = na_align(sizeof(int) * (6 * NA_MAX_NB + 1));
+constexpr size_t NA_LONGS = na_align(sizeof(long long) * 3 * NA_MAX_NB);
+constexpr size_t NA_NS = na_align(NA_MAX_DQP);
+constexpr size_t NA_TASKS = na_align(sizeof(HTask) * NA_MAX_HTASKS);
+constexpr size_t NA_BYTES = NA_RSP + NA_HSP + NA_DPART + NA_MF + NA_INTS + NA_LONGS + NA_NS + NA_TASKS;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+namespace {
+struct NaDevice {
+  bool ready = false;
+  unsigned char* ptr = nullptr;
+};
+NaDevice g_na_dev[64];
+std::mutex g_na_mu;
+
+// Once per device, with that device current: the device address of the
+// scratch array (the host-side name is only a stand-in) and the kernel
+// attribute the field projection needs.
+int noalloc_setup(unsigned char** out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(PNFAM_ECUDA, "pnfam_gpu_calc_hamiltonian_noalloc: device index >= 64");
+  std::lock_guard<std::mutex> lock(g_na_mu);
+  NaDevice& d = g_na_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaGetSymbolAddress: ") +
+                                   cudaGetErrorString(e));
+    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+    e = cudaFuncSetAttribute(k_hproj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+      return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaFuncSetAttribute: ") +
+                                   cudaGetErrorString(e));
+    d.ptr = static_cast<unsigned char*>(p);
+    d.ready = true;
+  }
+  *out = d.ptr;
+  return PNFAM_OK;
+}
+}  // namespace
+
+extern "C" int pnfam_gpu_calc_hamiltonian_noalloc(
+    const pnfam_basis_t* basis, const double* d_phi, const double* d_wdcori, const pnfam_coupl_t* d_coupl,
+    const int* fcols, const double* const* d_in, double* const* d_out, void* stream) {
+  g_err.clear();
+  if (!basis || !basis->db || !basis->num_spin_up || !basis->ns || !d_phi || !d_wdcori || !d_coupl || !fcols ||
+      !d_in || !d_out)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: NULL argument");
+  for (int k = 0; k < 8; ++k)
+    if (!d_in[k] || !d_out[k]) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: NULL array");
+  if (!d_coupl->crho || !d_coupl->cs || !d_coupl->cpair || !d_coupl->cspair)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: NULL coupling array");
+  const int nb = basis->nb, nghl = basis->nghl;
+  if (nb <= 0 || nb % 2 || nghl <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: nb must be positive and even, nghl positive");
+  if (nb > NA_MAX_NB || nghl > NA_MAX_NGHL)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: nb <= 64 and nghl <= 1600 are the limits");
+  // host-side description (no device memory): reuse the solver's structure code
+  pnfam_ctx c;
+  c.nb = nb; c.nghl = nghl;
+  c.db.assign(basis->db, basis->db + nb);
+  c.nup.assign(basis->num_spin_up, basis->num_spin_up + nb);
+  c.st.resize(nb); c.tr.resize(nb); c.uoff.resize(nb);
+  int s = 0;
+  long long mo = 0;
+  for (int i = 0; i < nb; ++i) {
+    if (c.db[i] < 0 || c.nup[i] < 0 || c.nup[i] > c.db[i])
+      return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: bad block size or spin count");
+    c.st[i] = s; s += c.db[i];
+    c.uoff[i] = mo; mo += (long long)c.db[i] * c.db[i];
+    c.tr[i] = i < nb / 2 ? i + nb / 2 : i - nb / 2;
+  }
+  if (s > NA_MAX_DQP) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: dqp <= 1024 is the limit");
+  c.dqp = s;
+  std::vector<signed char> ns(s);
+  for (int k = 0; k < s; ++k) {
+    if (basis->ns[k] != 1 && basis->ns[k] != -1)
+      return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: ns must be +-1");
+    ns[k] = (signed char)basis->ns[k];
+  }
+  c.fc.assign(fcols, fcols + nb);
+  for (int i = 0; i < nb; ++i)
+    if (c.fc[i] < -1 || c.fc[i] >= nb) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: fcols out of range");
+  c.xc.assign(nb, -1); c.yc.assign(nb, -1); c.xtc.assign(nb, -1); c.ytc.assign(nb, -1);
+  for (int i = 0; i < nb; ++i) {
+    if (c.fc[i] >= 0) c.xc[i] = c.tr[c.fc[i]];
+    c.yc[i] = c.fc[c.tr[i]];
+  }
+  for (int i = 0; i < nb; ++i) {
+    if (c.xc[i] >= 0) { if (c.xtc[c.xc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: F is not one block per column"); c.xtc[c.xc[i]] = i; }
+    if (c.yc[i] >= 0) { if (c.ytc[c.yc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: F is not one block per column"); c.ytc[c.yc[i]] = i; }
+  }
+  long long nf, nx, ny, nxt, nyt;
+  c.foff = offsets(c.fc, c.db, &nf);
+  c.xoff = offsets(c.xc, c.db, &nx);
+  c.yoff = offsets(c.yc, c.db, &ny);
+  c.xtoff = offsets(c.xtc, c.db, &nxt);
+  c.ytoff = offsets(c.ytc, c.db, &nyt);
+  if (nf != nx || nf != ny || nf != nxt || nf != nyt || nf == 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: inconsistent block structure");
+  if (nf > NA_MAX_NXY) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: nxy <= 32768 is the limit");
+  c.nxy = nf;
+  build_tasks(&c);
+  if ((int)c.htasks.size() > NA_MAX_HTASKS)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_noalloc: more than 4096 field-projection tiles");
+  unsigned char* base = nullptr;
+  int rc = noalloc_setup(&base);
+  if (rc) return rc;
+  // carve the scratch array
+  double* rsp = reinterpret_cast<double*>(base);
+  double* hsp = reinterpret_cast<double*>(base + NA_RSP);
+  double* dpart = reinterpret_cast<double*>(base + NA_RSP + NA_HSP);
+  double* mf = reinterpret_cast<double*>(base + NA_RSP + NA_HSP + NA_DPART);
+  int* ints = reinterpret_cast<int*>(base + NA_RSP + NA_HSP + NA_DPART + NA_MF);
+  long long* longs = reinterpret_cast<long long*>(base + NA_RSP + NA_HSP + NA_DPART + NA_MF + NA_INTS);
+  signed char* dns = reinterpret_cast<signed char*>(base + NA_RSP + NA_HSP + NA_DPART + NA_MF + NA_INTS + NA_LONGS);
+  HTask* dtasks = reinterpret_cast<HTask*>(base + NA_RSP + NA_HSP + NA_DPART + NA_MF + NA_INTS + NA_LONGS + NA_NS);
+  std::vector<int> hints(6 * NA_MAX_NB + 1, 0);
+  std::vector<long long> hlongs(3 * NA_MAX_NB, 0);
+  for (int i = 0; i < nb; ++i) {
+    hints[0 * NA_MAX_NB + i] = c.db[i];
+    hints[1 * NA_MAX_NB + i] = c.st[i];
+    hints[2 * NA_MAX_NB + i] = c.nup[i];
+    hints[3 * NA_MAX_NB + i] = c.fc[i];
+    hints[4 * NA_MAX_NB + i] = c.xtc[i];
+    hints[5 * NA_MAX_NB + i] = c.ytc[i];
+    hlongs[0 * NA_MAX_NB + i] = c.foff[i];
+    hlongs[1 * NA_MAX_NB + i] = c.xtoff[i];
+    hlongs[2 * NA_MAX_NB + i] = c.ytoff[i];
+  }
+  hints[6 * NA_MAX_NB] = 1;  // active flag of the single point
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t nbytes = sizeof(double) * nf;
+  CK(cudaMemcpyAsync(ints, hints.data(), sizeof(int) * hints.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(longs, hlongs.data(), sizeof(long long) * hlongs.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dns, ns.data(), (size_t)s, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dtasks, c.htasks.data(), sizeof(HTask) * c.htasks.size(), cudaMemcpyHostToDevice, st));
+  // inputs in the solver's quadrant layout: plane pl at pl*4nxy, quadrant q at q*nxy
+  // (0 rho_pn, 1 kappa+, 2 kappa-, 3 rho_np)
+  const int qin[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(rsp + (k & 1) * 4 * nf + qin[k] * nf, d_in[k], nbytes, cudaMemcpyDeviceToDevice, st));
+  DevBasis B;
+  B.nb = nb; B.dqp = s; B.nghl = nghl;
+  B.db = ints; B.st = ints + NA_MAX_NB; B.nup = ints + 2 * NA_MAX_NB; B.ns = dns;
+  B.phi = d_phi; B.wdcori = d_wdcori;
+  B.crho = d_coupl->crho; B.cs = d_coupl->cs; B.cpair = d_coupl->cpair; B.cspair = d_coupl->cspair;
+  for (int i = 0; i < 12; ++i) B.sc[i] = d_coupl->scalars[i];
+  const int* act = ints + 6 * NA_MAX_NB;
+  DensCall d0, d1;
+  d0.rho = rsp + 0 * nf; d0.rho_sp = 8 * nf; d0.rho_spl = 4 * nf;
+  d0.rcols = ints + 3 * NA_MAX_NB; d0.roffs = longs;
+  d0.kap = rsp + 1 * nf; d0.kap_sp = 8 * nf; d0.kap_spl = 4 * nf;
+  d0.kcols = ints + 4 * NA_MAX_NB; d0.koffs = longs + NA_MAX_NB;
+  d1.rho = rsp + 3 * nf; d1.rho_sp = 8 * nf; d1.rho_spl = 4 * nf;
+  d1.rcols = ints + 3 * NA_MAX_NB; d1.roffs = longs;
+  d1.kap = rsp + 2 * nf; d1.kap_sp = 8 * nf; d1.kap_spl = 4 * nf;
+  d1.kcols = ints + 5 * NA_MAX_NB; d1.koffs = longs + 2 * NA_MAX_NB;
+  k_density<<<dim3((nghl + DRT - 1) / DRT, NA_G, 2), 256, 0, st>>>(B, d0, d1, NA_G, dpart, act);
+  k_meanfield<<<dim3((nghl + 127) / 128, 2), 128, 0, st>>>(B, NA_G, dpart, mf, act);
+  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+  k_hproj<<<dim3((unsigned)c.htasks.size(), 1), 256, smem, st>>>(B, dtasks, mf, hsp, nf, act);
+  CK(cudaGetLastError());
+  const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(d_out[k], hsp + (k & 1) * 4 * nf + qout[k] * nf, nbytes, cudaMemcpyDeviceToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  return PNFAM_OK;
+}
