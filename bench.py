@@ -295,8 +295,8 @@ def run_solve_only(args):
     from pynfam_gb300.solver import GPUSolver
     case, omegas = workload(args.points)
     s = case.nml["solver"]
-    kw = dict(max_iter=s["max_iter"], eps=s["convergence_epsilon"], broyden_m=s["broyden_history_size"],
-              quench=case.quench)
+    kw = dict(max_iter=args.max_iter or s["max_iter"], eps=args.eps or s["convergence_epsilon"],
+              broyden_m=s["broyden_history_size"], quench=case.quench, precision=args.precision)
     gpu = GPUSolver(case.hfb, case.couplings)
     gpu.set_operator(case.F, case.G)
     for _ in range(args.warmup):
@@ -304,10 +304,13 @@ def run_solve_only(args):
     ms, its = [], None
     for _ in range(args.steps):
         r = gpu.solve(omegas, **kw)
-        ms.append(gpu.last_profile()[0]["total"])
+        prof = gpu.last_profile()[0]
+        ms.append(prof["total"])
         its = r.iters.tolist()
     gpu.close()
-    print(json.dumps({"solve_only": True, "points": len(omegas), "ms": ms, "iters": its,
+    print(json.dumps({"solve_only": True, "precision": args.precision, "points": len(omegas), "ms": ms,
+                      "iters": its, "pit64": prof["point_iterations_fp64"], "pit32": prof["point_iterations_fp32"],
+                      "S": [[float(a), float(b)] for a, b in zip(r.re_S[:, 0], r.im_S[:, 0])],
                       "omegas": [[float(w.real), float(w.imag)] for w in omegas]}), flush=True)
 
 
@@ -318,6 +321,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--points", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--precision", type=int, default=0, choices=(0, 1),
+                    help="0: FP64 throughout; 1: FP32 field evaluation with FP64 finish")
+    ap.add_argument("--eps", type=float, default=None, help="solve-only: convergence epsilon override")
+    ap.add_argument("--max-iter", type=int, default=None, help="solve-only: max_iter override")
     ap.add_argument("--solve-only", action="store_true",
                     help="warm-up and timed solves only (no e2e/CPU/DGEMM legs); used for kernel profiling")
     args = ap.parse_args()

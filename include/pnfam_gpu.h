@@ -61,8 +61,19 @@ typedef struct {
   double convergence_epsilon;
   double alpha_mix;           /* 0.7 in the reference */
   double quench_residual_int; /* scales the residual interaction; 0 skips it */
-  int precision;              /* 0 = FP64 everywhere (the drop-in form) */
-  int reserved[7];
+  int precision;              /* 0 = FP64 everywhere (the drop-in form);
+                                 1 = mixed form (defect correction): the residual interaction
+                                 (block GEMMs, densities, fields) is evaluated in FP32 on the
+                                 increment X - X_a from an anchor X_a whose image g(X_a) is
+                                 held in FP64.  While max|X - X_a| <= 1000*epsilon the FP32
+                                 error is far below epsilon and convergence (si < epsilon) is
+                                 accepted on an increment evaluation; farther out a point
+                                 takes an FP64 anchor evaluation when si < 10^-reserved[1]
+                                 (default 100*epsilon) or si stops falling, and convergence
+                                 is accepted only on that anchor.  Every evaluation counts
+                                 against max_iter.  Broyden, Green's function and strength
+                                 are FP64 in both modes. */
+  int reserved[7];            /* [0]: per-stage event timing on/off; [1]: see precision */
 } pnfam_solver_opts_t;
 
 /*
@@ -173,7 +184,8 @@ long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
  * k1_blockgemm, density, meanfield, field_projection, k2_blockgemm, green,
  * broyden, strength; filled only when opts.reserved[0] != 0), then, if
  * nstage > 8, the whole solve's device time (CUDA events on the solver's
- * stream), and the number of kernel launches. */
+ * stream), if nstage > 10 the FP64 and FP32 point-iterations of the solve,
+ * and the number of kernel launches. */
 int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
                            long long* launches);
 

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <mutex>
 #include <cmath>
 #include <cstdio>
@@ -150,8 +151,17 @@ struct pnfam_ctx {
   int cap_P = 0, cap_M = 0;
   DBuf<double> d_state, d_vout, d_T, d_rsp, d_hsp, d_hqp, d_dpart, d_mf;
   DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
-  DBuf<int> d_active;
+  DBuf<int> d_active, d_act32, d_act64;
+  DBuf<int> d_pint;      // [4][P]: Broyden iteration, Broyden mode, increment step, anchor step
   DBuf<BufDesc> d_bufs;
+  // mixed precision: FP32 copies of the ground state and FP32 scratch
+  bool have32 = false;
+  DBuf<float> d_up32, d_vp32, d_un32, d_vn32, d_phi32;
+  DBuf<float> d_state32, d_T32, d_rsp32, d_hsp32, d_hqp32, d_dpart32, d_mf32;
+  DBuf<BufDescT<float>> d_bufs32;
+  DBuf<double> d_xsave, d_radd;   // [P][4nxy] mixed form: anchor X_a and its FP64 image g(X_a)
+  DBuf<unsigned long long> d_dmax;  // [P] max|X - X_a| of the last increment evaluation
+  long long pit64 = 0, pit32 = 0;   // point-iterations per precision in the last solve
   int G = 1;
   int nchunk_bro = 1, nchunk_c = 1;
   cudaStream_t stream = nullptr;
@@ -162,7 +172,13 @@ struct pnfam_ctx {
   long long launches = 0;
 
   ~pnfam_ctx() {
-    DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active};
+    DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active, &d_act32, &d_act64,
+                      &d_pint};
+    DBuf<float>* fb[] = {&d_up32, &d_vp32, &d_un32, &d_vn32, &d_phi32, &d_state32, &d_T32, &d_rsp32, &d_hsp32,
+                         &d_hqp32, &d_dpart32, &d_mf32};
+    for (auto* b : fb) b->release();
+    d_bufs32.release();
+    d_xsave.release(); d_radd.release(); d_dmax.release();
     for (auto* b : ib) b->release();
     d_ns.release();
     DBuf<double>* dbs[] = {&d_up, &d_vp, &d_un, &d_vn, &d_ep, &d_en, &d_phi, &d_wd, &d_crho, &d_cs,
@@ -183,15 +199,17 @@ struct pnfam_ctx {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  DevBasis devbasis() const {
-    DevBasis B;
+  template <class T>
+  DevBasisT<T> devbasis() const {
+    DevBasisT<T> B;
     B.nb = nb; B.dqp = dqp; B.nghl = nghl;
     B.db = d_db.p; B.st = d_st.p; B.nup = d_nup.p; B.ns = d_ns.p;
-    B.phi = d_phi.p; B.wdcori = d_wd.p;
+    B.phi = phi_ptr<T>(); B.wdcori = d_wd.p;
     B.crho = d_crho.p; B.cs = d_cs.p; B.cpair = d_cpair.p; B.cspair = d_cspair.p;
     for (int i = 0; i < 12; ++i) B.sc[i] = sc[i];
     return B;
   }
+  template <class T> const T* phi_ptr() const;
   int left_u() const { return beta_minus ? B_UP : B_UN; }
   int left_v() const { return beta_minus ? B_VP : B_VN; }
   int right_u() const { return beta_minus ? B_UN : B_UP; }
@@ -199,6 +217,9 @@ struct pnfam_ctx {
   MatRef ublk(int buf, int i, int trans) const { return MatRef{buf, uoff[i], db[i], db[i], trans}; }
   MatRef vblk(int buf, int i, int trans) const { return MatRef{buf, uoff[i], db[i], db[tr[i]], trans}; }
 };
+
+template <> const double* pnfam_ctx::phi_ptr<double>() const { return d_phi.p; }
+template <> const float* pnfam_ctx::phi_ptr<float>() const { return d_phi32.p; }
 
 // ---------------------------------------------------------------------------
 // structures and task lists
@@ -347,6 +368,7 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   CK(dalloc(c->d_wre, (size_t)P));
   CK(dalloc(c->d_wim, (size_t)P));
   CK(dalloc(c->d_active, (size_t)P));
+  CK(dalloc(c->d_pint, (size_t)4 * P));
   BufDesc bd[NBUF];
   bd[B_UP] = {c->d_up.p, 0, 0};
   bd[B_VP] = {c->d_vp.p, 0, 0};
@@ -361,18 +383,25 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   return PNFAM_OK;
 }
 
-static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
+template <class T>
+static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, const BufDescT<T>* bufs) {
   if (tl.ntiles == 0) return PNFAM_OK;
   dim3 grid(tl.ntiles, 2 * P);
-  k_gemm<<<grid, 256, 0, c->stream>>>(tl.d_tasks.p, tl.d_tile2task.p, c->d_bufs.p, active);
+  k_gemm<T><<<grid, 256, 0, c->stream>>>(tl.d_tasks.p, tl.d_tile2task.p, bufs, active);
   c->launches++;
   CK(cudaGetLastError());
   return PNFAM_OK;
 }
 
-// residual interaction: state (X, Y) -> hqp (H20, H02 stored)
-static int residual(pnfam_ctx* c, int P, bool timed) {
-  const int* act = c->d_active.p;
+static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
+  return launch_gemm<double>(c, tl, P, active, c->d_bufs.p);
+}
+
+// residual interaction of the points flagged in `act`: state (X, Y) -> hqp
+// (H20, H02 stored), computed in precision T (the FP32 form reads the FP32
+// copy of the state and writes the FP32 hqp)
+template <class T>
+static int residual_t(pnfam_ctx* c, int P, const int* act, bool timed) {
   auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
   auto toc = [&](int k) {
     if (!timed) return;
@@ -382,26 +411,34 @@ static int residual(pnfam_ctx* c, int P, bool timed) {
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
     c->stage_ms[k] += ms;
   };
+  constexpr bool f32 = std::is_same<T, float>::value;
+  const BufDescT<T>* bufs;
+  T *rsp, *hsp, *dpart, *mf;
+  if constexpr (f32) {
+    bufs = c->d_bufs32.p; rsp = c->d_rsp32.p; hsp = c->d_hsp32.p; dpart = c->d_dpart32.p; mf = c->d_mf32.p;
+  } else {
+    bufs = c->d_bufs.p; rsp = c->d_rsp.p; hsp = c->d_hsp.p; dpart = c->d_dpart.p; mf = c->d_mf.p;
+  }
   int rc;
   tic();
-  if ((rc = launch_gemm(c, c->k1a, P, act))) return rc;
-  if ((rc = launch_gemm(c, c->k1b, P, act))) return rc;
+  if ((rc = launch_gemm<T>(c, c->k1a, P, act, bufs))) return rc;
+  if ((rc = launch_gemm<T>(c, c->k1b, P, act, bufs))) return rc;
   toc(0);
   const long long nxy = c->nxy;
-  DensCall d0, d1;
-  d0.rho = c->d_rsp.p + 0 * nxy; d0.rho_sp = 8 * nxy; d0.rho_spl = 4 * nxy;
+  DensCallT<T> d0, d1;
+  d0.rho = rsp + 0 * nxy; d0.rho_sp = 8 * nxy; d0.rho_spl = 4 * nxy;
   d0.rcols = c->d_fc.p; d0.roffs = c->d_foff.p;
-  d0.kap = c->d_rsp.p + 1 * nxy; d0.kap_sp = 8 * nxy; d0.kap_spl = 4 * nxy;
+  d0.kap = rsp + 1 * nxy; d0.kap_sp = 8 * nxy; d0.kap_spl = 4 * nxy;
   d0.kcols = c->d_xtc.p; d0.koffs = c->d_xtoff.p;
-  d1.rho = c->d_rsp.p + 3 * nxy; d1.rho_sp = 8 * nxy; d1.rho_spl = 4 * nxy;
+  d1.rho = rsp + 3 * nxy; d1.rho_sp = 8 * nxy; d1.rho_spl = 4 * nxy;
   d1.rcols = c->d_fc.p; d1.roffs = c->d_foff.p;
-  d1.kap = c->d_rsp.p + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
+  d1.kap = rsp + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
-  const DevBasis B = c->devbasis();
+  const DevBasisT<T> B = c->devbasis<T>();
   tic();
   {
     dim3 grid((c->nghl + DRT - 1) / DRT, c->G, 2 * P);
-    k_density<<<grid, 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p, act);
+    k_density<T><<<grid, 256, 0, c->stream>>>(B, d0, d1, c->G, dpart, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -409,24 +446,68 @@ static int residual(pnfam_ctx* c, int P, bool timed) {
   tic();
   {
     dim3 grid((c->nghl + 127) / 128, 2 * P);
-    k_meanfield<<<grid, 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
+    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, c->G, dpart, mf, act);
     c->launches++;
     CK(cudaGetLastError());
   }
   toc(2);
   tic();
   {
-    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(T);
     dim3 grid((unsigned)c->htasks.size(), P);
-    k_hproj<<<grid, 256, smem, c->stream>>>(B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
+    k_hproj<T><<<grid, 256, smem, c->stream>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
     c->launches++;
     CK(cudaGetLastError());
   }
   toc(3);
   tic();
-  if ((rc = launch_gemm(c, c->k2a, P, act))) return rc;
-  if ((rc = launch_gemm(c, c->k2b, P, act))) return rc;
+  if ((rc = launch_gemm<T>(c, c->k2a, P, act, bufs))) return rc;
+  if ((rc = launch_gemm<T>(c, c->k2b, P, act, bufs))) return rc;
   toc(4);
+  return PNFAM_OK;
+}
+
+static int residual(pnfam_ctx* c, int P, bool timed) { return residual_t<double>(c, P, c->d_active.p, timed); }
+
+// FP32 copies of the ground state and FP32 scratch for P points
+static int ensure_buffers32(pnfam_ctx* c, int P) {
+  const long long nxy = c->nxy;
+  const size_t mo = (size_t)(c->uoff.back() + (long long)c->db.back() * c->db.back());
+  if (!c->have32) {
+    CK(dalloc(c->d_up32, mo)); CK(dalloc(c->d_vp32, mo)); CK(dalloc(c->d_un32, mo)); CK(dalloc(c->d_vn32, mo));
+    CK(dalloc(c->d_phi32, (size_t)5 * c->dqp * c->nghl));
+    const double* src[5] = {c->d_up.p, c->d_vp.p, c->d_un.p, c->d_vn.p, c->d_phi.p};
+    float* dst[5] = {c->d_up32.p, c->d_vp32.p, c->d_un32.p, c->d_vn32.p, c->d_phi32.p};
+    const long long n[5] = {(long long)mo, (long long)mo, (long long)mo, (long long)mo, 5LL * c->dqp * c->nghl};
+    for (int k = 0; k < 5; ++k) {
+      k_to_f32<<<1024, 256, 0, c->stream>>>(src[k], dst[k], n[k], 1, 0, nullptr);
+      CK(cudaGetLastError());
+    }
+    c->have32 = true;
+  }
+  CK(dalloc(c->d_state32, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_T32, (size_t)P * 16 * nxy));
+  CK(dalloc(c->d_rsp32, (size_t)P * 8 * nxy));
+  CK(dalloc(c->d_hsp32, (size_t)P * 8 * nxy));
+  CK(dalloc(c->d_hqp32, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_dpart32, (size_t)P * 2 * c->G * 2 * ND * c->nghl));
+  CK(dalloc(c->d_mf32, (size_t)P * 2 * NMF * 2 * c->nghl));
+  CK(dalloc(c->d_act32, (size_t)P));
+  CK(dalloc(c->d_act64, (size_t)P));
+  CK(dalloc(c->d_xsave, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_radd, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_dmax, (size_t)P));
+  BufDescT<float> bd[NBUF];
+  bd[B_UP] = {c->d_up32.p, 0, 0};
+  bd[B_VP] = {c->d_vp32.p, 0, 0};
+  bd[B_UN] = {c->d_un32.p, 0, 0};
+  bd[B_VN] = {c->d_vn32.p, 0, 0};
+  bd[B_STATE] = {c->d_state32.p, 4 * nxy, 2 * nxy};
+  bd[B_T] = {c->d_T32.p, 16 * nxy, 8 * nxy};
+  bd[B_RSP] = {c->d_rsp32.p, 8 * nxy, 4 * nxy};
+  bd[B_HSP] = {c->d_hsp32.p, 8 * nxy, 4 * nxy};
+  bd[B_HQP] = {c->d_hqp32.p, 4 * nxy, 2 * nxy};
+  CK(upload(c->d_bufs32, bd, NBUF));
   return PNFAM_OK;
 }
 
@@ -496,7 +577,8 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
   }
   const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-  if (cudaFuncSetAttribute(k_hproj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_hproj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2)) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
   }
@@ -601,7 +683,8 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
     return fail(PNFAM_EINVAL, "pnfam_gpu_solve: bad argument");
   if (!c->have_op) return fail(PNFAM_ESTATE, "pnfam_gpu_solve: call pnfam_gpu_set_operator first");
   if (o->max_iter < 0) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: max_iter < 0");
-  if (o->precision != 0) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: only precision 0 (FP64) is available");
+  if (o->precision != 0 && o->precision != 1)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_solve: precision must be 0 (FP64) or 1 (FP32 field, FP64 finish)");
   const bool no_res = std::fabs(o->quench_residual_int) < 1e-10;
   int M = no_res ? -1 : o->broyden_history_size;
   if (M > 64) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: broyden_history_size > 64 is not supported");
@@ -610,7 +693,24 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
   int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(M, 1), c->cap_M));
   if (rc) return rc;
   c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(M, 1), c->cap_M);
+  const bool mixed = o->precision == 1 && !no_res;
+  if (mixed && (rc = ensure_buffers32(c, c->cap_P))) return rc;
+  // Mixed form (precision 1): one Broyden iteration per evaluation, as in the FP64
+  // form, but the residual interaction is evaluated in FP32 on the increment
+  // d = X - X_a from an anchor X_a whose image g(X_a) is known in FP64:
+  //   g(X) = g(X_a) + G o (q H(d))    (H is linear; increment evaluation, FP32)
+  // The FP32 error of an increment evaluation scales with |d|, not |X|.  An anchor
+  // evaluation computes g(X) entirely in FP64 and makes X the new anchor.
+  // Iteration 0 is the anchor X_a = 0, g(0) = G o F, exact without a field
+  // evaluation.  A point is "near" its anchor while max|d| <= NEAR*epsilon, where
+  // the FP32 error is far below epsilon.  Convergence (si < epsilon) is accepted on
+  // an anchor or on a near increment evaluation; a far point takes an FP64 anchor
+  // when si < 10^-reserved[1] (default 100*epsilon) or si stops falling (the FP32
+  // noise floor).  Every evaluation counts against max_iter.
+  const double NEAR = 1000.0;
+  const double switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
   for (int k = 0; k < 8; ++k) c->stage_ms[k] = 0.0;
+  c->pit64 = 0; c->pit32 = 0;
   c->launches = 0;
   const bool timed = o->reserved[0] != 0;
   CK(cudaEventRecord(c->evt[0], c->stream));
@@ -619,16 +719,28 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
   CK(cudaMemcpyAsync(c->d_wim.p, im_w, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
   const int nops = c->nops;
   std::vector<double> si(P, 1.0), sre((size_t)P * nops, 0.0), sim((size_t)P * nops, 0.0);
-  std::vector<int> active(P, 1), conv(P, -1);
+  std::vector<int> active(P, 1), conv(P, -1), anchor(P, 1);
+  // host copy of the per-point integer block: [0] Broyden iteration, [1] Broyden mode,
+  // [2] increment evaluation, [3] anchor evaluation
+  std::vector<int> pint((size_t)4 * P, 0), act32(P, 0), act64(P, 0);
+  std::vector<double> best(P, 1e300);
+  std::vector<int> since_best(P, 0), nstall(P, 0);
   std::vector<double> hsi(P), cpart((size_t)P * c->nchunk_c * 2 * nops);
+  std::vector<unsigned long long> hdmax(P, 0);
   const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
   const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
+  int* d_itp = c->d_pint.p;
+  int* d_mode = c->d_pint.p + P;
+  int* d_incr = c->d_pint.p + 2 * P;
+  int* d_anch = c->d_pint.p + 3 * P;
   BroState S;
   S.N = N; S.M = std::max(M, 1); S.alpha = o->alpha_mix;
   S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
   S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
+  S.itp = d_itp; S.modep = d_mode;
   const double w0 = 0.01;
   const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
+  const dim3 vgrid((unsigned)std::min<long long>(2048, (N + 255) / 256), P);
   auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
   auto toc = [&](int k) {
     if (!timed) return;
@@ -638,6 +750,7 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
     c->stage_ms[k] += ms;
   };
+  const int bmode = M < 0 ? BRO_NOMIX : M == 0 ? BRO_LINEAR : BRO_BROYDEN;
   for (int it = 0; it <= o->max_iter; ++it) {
     int nact = 0;
     for (int p = 0; p < P; ++p) {
@@ -646,54 +759,92 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
         double* h = hist + ((size_t)p * (o->max_iter + 1) + it) * 3;
         h[0] = si[p]; h[1] = sre[(size_t)p * nops]; h[2] = sim[(size_t)p * nops];
       }
-      if (si[p] < o->convergence_epsilon) { conv[p] = it; active[p] = 0; continue; }
+      if (it > 0) {
+        // si[p] is the residual of the evaluation made at it - 1
+        if (!mixed || anchor[p]) {
+          if (si[p] < o->convergence_epsilon) { conv[p] = it; active[p] = 0; continue; }
+          if (mixed) { anchor[p] = 0; best[p] = si[p]; since_best[p] = 0; }
+        } else {
+          double dm;
+          std::memcpy(&dm, &hdmax[p], sizeof dm);
+          const bool near = dm <= NEAR * o->convergence_epsilon;
+          if (si[p] < o->convergence_epsilon && near) { conv[p] = it; active[p] = 0; continue; }
+          if (si[p] < best[p] * 0.5) { best[p] = si[p]; since_best[p] = 0; } else { ++since_best[p]; }
+          // the stagnation window doubles with every anchor it has triggered
+          const bool stalled = since_best[p] >= (5 << std::min(nstall[p], 4));
+          if (!near && (si[p] < switch_si || stalled)) { anchor[p] = 1; nstall[p] += stalled; }
+        }
+      }
       if (it == o->max_iter) { conv[p] = -1; active[p] = 0; continue; }
       ++nact;
     }
     if (nact == 0) break;
+    int n32 = 0, n64 = 0, nanch = 0;
+    for (int p = 0; p < P; ++p) {
+      const bool lo = mixed && !anchor[p];
+      act32[p] = active[p] && lo && it > 0;
+      act64[p] = active[p] && !lo && it > 0;
+      n32 += act32[p]; n64 += act64[p];
+      pint[p] = it;
+      pint[P + p] = it == 0 && bmode == BRO_BROYDEN ? BRO_LINEAR : bmode;
+      pint[2 * P + p] = act32[p];
+      pint[3 * P + p] = active[p] && mixed && anchor[p];
+      nanch += pint[3 * P + p];
+    }
+    c->pit32 += n32; c->pit64 += n64;
     CK(cudaMemcpyAsync(c->d_active.p, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_pint.p, pint.data(), sizeof(int) * 4 * P, cudaMemcpyHostToDevice, c->stream));
     const int* act = c->d_active.p;
-    if (!no_res) {
-      if ((rc = residual(c, P, timed))) return rc;
+    // the residual interaction of X = 0 vanishes: iteration 0 needs no field evaluation
+    if (!no_res && it > 0) {
+      if (!mixed) {
+        if ((rc = residual(c, P, timed))) return rc;
+      } else {
+        CK(cudaMemcpyAsync(c->d_act32.p, act32.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_act64.p, act64.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+        if (n64 && (rc = residual_t<double>(c, P, c->d_act64.p, timed))) return rc;
+        if (n32) {
+          CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
+          k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
+                                                 c->d_dmax.p);
+          if ((rc = residual_t<float>(c, P, c->d_act32.p, timed))) return rc;
+          k_to_f64<<<vgrid, 256, 0, c->stream>>>(c->d_hqp32.p, c->d_hqp.p, N, N, c->d_act32.p);
+          c->launches += 2;
+          CK(cudaGetLastError());
+        }
+      }
     }
     tic();
     {
       dim3 grid(gx, P);
-      k_green<<<grid, 256, 0, c->stream>>>(nxy, P, no_res ? nullptr : c->d_hqp.p, c->d_fops.p, c->d_erow.p,
-                                           c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p, o->quench_residual_int,
-                                           c->d_vout.p, act);
+      k_green<<<grid, 256, 0, c->stream>>>(nxy, P, no_res || it == 0 ? nullptr : c->d_hqp.p, c->d_fops.p,
+                                           c->d_erow.p, c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
+                                           o->quench_residual_int, c->d_vout.p, act, mixed ? d_incr : nullptr,
+                                           c->d_radd.p);
       c->launches++;
+      if (nanch) {  // new anchors: X_a = X, g(X_a) = vout
+        k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_xsave.p, c->d_state.p, N, d_anch);
+        k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_radd.p, c->d_vout.p, N, d_anch);
+        c->launches += 2;
+      }
       CK(cudaGetLastError());
     }
     toc(5);
-    // ---- Broyden (pnfam_broyden.f90:117-216) ----
+    // ---- Broyden (pnfam_broyden.f90:117-216), each point at its own iteration ----
     tic();
-    int mode;
-    S.it = it;
-    if (M < 0) mode = 2;
-    else if (M == 0 || it == 0) mode = 1;
-    else mode = 0;
-    const bool upd = (mode == 0 && it >= 2);
-    if (mode == 0) {
-      auto fdiv = [](int a, int b) { return a / b; };  // C++ truncates like Fortran
-      S.iter_used = std::min(it - 1, M);
-      S.ipos = it - 1 - fdiv(it - 2, M) * M - 1;
-      S.inext = it - fdiv(it - 1, M) * M - 1;
-    } else {
-      S.iter_used = 0; S.ipos = 0; S.inext = 0;
-    }
     {
+      const bool any_broyden = bmode == BRO_BROYDEN && it > 0;
       dim3 grid(c->nchunk_bro, P);
-      k_bro_diff<<<grid, 256, 0, c->stream>>>(S, upd ? 1 : 0, act);
+      k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
       k_bro_solve<<<P, 32, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
       c->launches += 2;
-      if (mode == 0) {
-        k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, upd ? 1 : 0, act);
+      if (any_broyden) {
+        k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
         k_bro_solve<<<P, 32, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
         c->launches += 2;
       }
       dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
-      k_bro_update<<<ug, 256, 0, c->stream>>>(S, mode, c->d_gamma.p, act);
+      k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
       c->launches++;
       CK(cudaGetLastError());
     }
@@ -706,6 +857,8 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
       CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(hsi.data(), c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    if (mixed)
+      CK(cudaMemcpyAsync(hdmax.data(), c->d_dmax.p, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(cpart.data(), c->d_cpart.p, sizeof(double) * cpart.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     toc(7);
@@ -774,7 +927,7 @@ extern "C" int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* c, const double* re_rho_p
   d1.rcols = c->d_fc.p; d1.roffs = c->d_foff.p;
   d1.kap = c->d_rsp.p + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
-  const DevBasis B = c->devbasis();
+  const DevBasis B = c->devbasis<double>();
   const int* act = c->d_active.p;
   k_density<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p, act);
   k_meanfield<<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
@@ -794,6 +947,7 @@ extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, in
   if (!c) return fail(PNFAM_EINVAL, "pnfam_gpu_last_profile: NULL context");
   for (int k = 0; k < nstage && k < 8; ++k) stage_ms[k] = c->stage_ms[k];
   if (nstage > 8) stage_ms[8] = c->total_ms;
+  if (nstage > 10) { stage_ms[9] = (double)c->pit64; stage_ms[10] = (double)c->pit32; }
   if (launches) *launches = c->launches;
   return PNFAM_OK;
 }
@@ -858,7 +1012,7 @@ int noalloc_setup(unsigned char** out) {
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaGetSymbolAddress: ") +
                                    cudaGetErrorString(e));
     const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-    e = cudaFuncSetAttribute(k_hproj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaFuncSetAttribute: ") +
                                    cudaGetErrorString(e));

@@ -24,11 +24,13 @@ namespace pnfam {
 // ---------------------------------------------------------------------------
 enum BufId { B_UP = 0, B_VP, B_UN, B_VN, B_STATE, B_T, B_RSP, B_HSP, B_HQP, NBUF };
 
-struct BufDesc {
-  double* base;
+template <class T>
+struct BufDescT {
+  T* base;
   long long sp;   // stride between points
   long long spl;  // stride between the Re and Im planes
 };
+using BufDesc = BufDescT<double>;
 
 struct GemmTerm {
   long long aoff, boff;
@@ -50,72 +52,75 @@ struct GemmTask {
 #define GT 32
 #define GK 16
 
-__device__ __forceinline__ const double* bufptr(const BufDesc* b, int id, int p, int plane, long long off) {
-  const BufDesc d = b[id];
+template <class T>
+__device__ __forceinline__ const T* bufptr(const BufDescT<T>* b, int id, int p, int plane, long long off) {
+  const BufDescT<T> d = b[id];
   return d.base + (long long)p * d.sp + (long long)plane * d.spl + off;
 }
 
-// C = sum_t alpha_t op(A_t) op(B_t); blockIdx.y = point*2 + plane
+// C = sum_t alpha_t op(A_t) op(B_t); blockIdx.y = point*2 + plane; T = compute type
+template <class T>
 __global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks, const int* __restrict__ tile2task,
-                                              const BufDesc* __restrict__ bufs, const int* __restrict__ active) {
+                                              const BufDescT<T>* __restrict__ bufs, const int* __restrict__ active) {
   const int z = blockIdx.y;
   const int p = z >> 1, plane = z & 1;
   if (active && !active[p]) return;
   const int tile = blockIdx.x;
-  const GemmTask& T = tasks[tile2task[tile]];
-  const int lt = tile - T.tile0;
-  const int m0 = (lt / T.ntn) * GT, n0 = (lt % T.ntn) * GT;
-  __shared__ double As[GK][GT + 1];
-  __shared__ double Bs[GK][GT + 1];
+  const GemmTask& Tk = tasks[tile2task[tile]];
+  const int lt = tile - Tk.tile0;
+  const int m0 = (lt / Tk.ntn) * GT, n0 = (lt % Tk.ntn) * GT;
+  __shared__ T As[GK][GT + 1];
+  __shared__ T Bs[GK][GT + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
-  const int M = T.M, N = T.N, K = T.K;
-  for (int it = 0; it < T.nterm; ++it) {
-    const GemmTerm& tm = T.t[it];
-    const double* A = bufptr(bufs, tm.abuf, p, plane, tm.aoff);
-    const double* B = bufptr(bufs, tm.bbuf, p, plane, tm.boff);
-    const double alpha = tm.alpha[plane];
+  T acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
+  const int M = Tk.M, N = Tk.N, K = Tk.K;
+  for (int it = 0; it < Tk.nterm; ++it) {
+    const GemmTerm& tm = Tk.t[it];
+    const T* A = bufptr(bufs, tm.abuf, p, plane, tm.aoff);
+    const T* B = bufptr(bufs, tm.bbuf, p, plane, tm.boff);
+    const T alpha = (T)tm.alpha[plane];
     for (int k0 = 0; k0 < K; k0 += GK) {
       for (int e = threadIdx.x; e < GK * GT; e += 256) {
         const int kk = e / GT, mm = e % GT;
         const int gm = m0 + mm, gk = k0 + kk;
-        double v = 0.0;
+        T v = 0;
         if (gm < M && gk < K) v = tm.tA ? A[gk + (long long)gm * tm.lda] : A[gm + (long long)gk * tm.lda];
         As[kk][mm] = alpha * v;
         const int gn = n0 + mm;
-        double w = 0.0;
+        T w = 0;
         if (gn < N && gk < K) w = tm.tB ? B[gn + (long long)gk * tm.ldb] : B[gk + (long long)gn * tm.ldb];
         Bs[kk][mm] = w;
       }
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < GK; ++kk) {
-        const double a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
-        const double b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
+        const T a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
+        const T b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
         acc00 = fma(a0, b0, acc00); acc01 = fma(a0, b1, acc01);
         acc10 = fma(a1, b0, acc10); acc11 = fma(a1, b1, acc11);
       }
       __syncthreads();
     }
   }
-  double* C = const_cast<double*>(bufptr(bufs, T.cbuf, p, plane, T.coff));
+  T* C = const_cast<T*>(bufptr(bufs, Tk.cbuf, p, plane, Tk.coff));
   const int r0 = m0 + ty * 2, c0 = n0 + tx * 2;
-  if (r0 < M && c0 < N) C[r0 + (long long)c0 * T.ldc] = acc00;
-  if (r0 < M && c0 + 1 < N) C[r0 + (long long)(c0 + 1) * T.ldc] = acc01;
-  if (r0 + 1 < M && c0 < N) C[r0 + 1 + (long long)c0 * T.ldc] = acc10;
-  if (r0 + 1 < M && c0 + 1 < N) C[r0 + 1 + (long long)(c0 + 1) * T.ldc] = acc11;
+  if (r0 < M && c0 < N) C[r0 + (long long)c0 * Tk.ldc] = acc00;
+  if (r0 < M && c0 + 1 < N) C[r0 + (long long)(c0 + 1) * Tk.ldc] = acc01;
+  if (r0 + 1 < M && c0 < N) C[r0 + 1 + (long long)c0 * Tk.ldc] = acc10;
+  if (r0 + 1 < M && c0 + 1 < N) C[r0 + 1 + (long long)(c0 + 1) * Tk.ldc] = acc11;
 }
 
 // ---------------------------------------------------------------------------
 // basis on device
 // ---------------------------------------------------------------------------
-struct DevBasis {
+template <class T>
+struct DevBasisT {
   int nb, dqp, nghl;
   const int* db;
   const int* st;
   const int* nup;
   const signed char* ns;
-  const double* phi;     // [5][dqp][nghl]
+  const T* phi;          // [5][dqp][nghl]
   const double* wdcori;
   const double* crho;
   const double* cs;
@@ -123,6 +128,7 @@ struct DevBasis {
   const double* cspair;
   double sc[12];         // cdrho, ctau, ctj0, ctj1, ctj2, crdj, cds, ct, cj, cgs, cf, csdj
 };
+using DevBasis = DevBasisT<double>;
 
 enum { ND = 28 };  // complex local densities
 // 0 rho 1 tau 2 tjrr 3 tjpr 4 tjzr 5 tjrp 6 tjpp 7 tjzp 8 tjrz 9 tjpz 10 tjzz
@@ -134,18 +140,21 @@ enum { D_RHO = 0, D_TAU, D_TJRR, D_TJPR, D_TJZR, D_TJRP, D_TJPP, D_TJZP, D_TJRZ,
 
 // One density call: rho in structure (rcols, roffs), kappa in (kcols, koffs), both
 // [P][2 planes][plane stride] at the given base/offset.
-struct DensCall {
-  const double* rho; long long rho_sp, rho_spl;
+template <class T>
+struct DensCallT {
+  const T* rho; long long rho_sp, rho_spl;
   const int* rcols; const long long* roffs;
-  const double* kap; long long kap_sp, kap_spl;
+  const T* kap; long long kap_sp, kap_spl;
   const int* kcols; const long long* koffs;
 };
+using DensCall = DensCallT<double>;
 
 #define DRT 32   // mesh points per CTA
 #define DBC 8    // b columns per chunk
 #define DAK 16   // a rows per chunk
 
-__device__ __forceinline__ double red8(double v) {
+template <class T>
+__device__ __forceinline__ T red8(T v) {
   v += __shfl_xor_sync(0xffffffffu, v, 4);
   v += __shfl_xor_sync(0xffffffffu, v, 2);
   v += __shfl_xor_sync(0xffffffffu, v, 1);
@@ -154,27 +163,29 @@ __device__ __forceinline__ double red8(double v) {
 
 // grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT r x DBC b
 // dpart: [P][2][G][2*ND][nghl]
-__global__ void __launch_bounds__(256) k_density(DevBasis B, DensCall c0, DensCall c1, int G,
-                                                 double* __restrict__ dpart, const int* __restrict__ active) {
+template <class T>
+__global__ void __launch_bounds__(256) k_density(DevBasisT<T> B, DensCallT<T> c0, DensCallT<T> c1, int G,
+                                                 T* __restrict__ dpart, const int* __restrict__ active) {
   const int p = blockIdx.z >> 1, call = blockIdx.z & 1;
   if (!active[p]) return;
-  const DensCall& C = call ? c1 : c0;
+  const DensCallT<T>& C = call ? c1 : c0;
   const int g = blockIdx.y;
   const int r0 = blockIdx.x * DRT;
   const int rl = threadIdx.x >> 3, bl = threadIdx.x & 7;
   const int nghl = B.nghl;
   const int r = r0 + rl;
   const bool rok = r < nghl;
-  __shared__ double acc[2 * ND][DRT];
-  __shared__ double sphi[4][DAK][DRT];
-  __shared__ double srho[2][DAK][DBC];
-  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) (&acc[0][0])[e] = 0.0;
+  __shared__ T acc[2 * ND][DRT];
+  __shared__ T sphi[4][DAK][DRT];
+  __shared__ T srho[2][DAK][DBC];
+  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) (&acc[0][0])[e] = 0;
   __syncthreads();
   const long long ps = (long long)B.dqp * nghl;
+  const T h5 = (T)0.5, two = (T)2;
 
 #define ACC(k, re, im)                                   \
   {                                                      \
-    const double vr_ = red8(re), vi_ = red8(im);         \
+    const T vr_ = red8<T>(re), vi_ = red8<T>(im);       \
     if (bl == 0) { acc[2 * (k)][rl] += vr_; acc[2 * (k) + 1][rl] += vi_; } \
   }
 
@@ -184,25 +195,25 @@ __global__ void __launch_bounds__(256) k_density(DevBasis B, DensCall c0, DensCa
     if (iy < 0) continue;
     const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
     const int sa = B.st[ix], sb = B.st[iy];
-    const double* rho = C.rho + (long long)p * C.rho_sp + C.roffs[ix];
+    const T* rho = C.rho + (long long)p * C.rho_sp + C.roffs[ix];
     for (int b0 = 0; b0 < dc; b0 += DBC) {
       const int b = b0 + bl;
-      double w[2][4][2];
+      T w[2][4][2];
 #pragma unroll
       for (int s = 0; s < 2; ++s)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { w[s][q][0] = 0.0; w[s][q][1] = 0.0; }
+        for (int q = 0; q < 4; ++q) { w[s][q][0] = 0; w[s][q][1] = 0; }
       for (int a0 = 0; a0 < d; a0 += DAK) {
         const int na = min(DAK, d - a0);
         for (int e = threadIdx.x; e < 4 * DAK * DRT; e += 256) {
           const int q = e / (DAK * DRT), rem = e % (DAK * DRT), aa = rem / DRT, rr = rem % DRT;
-          double v = 0.0;
+          T v = 0;
           if (aa < na && r0 + rr < nghl) v = B.phi[q * ps + (long long)(sa + a0 + aa) * nghl + r0 + rr];
           sphi[q][aa][rr] = v;
         }
         for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
           const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
-          double v = 0.0;
+          T v = 0;
           if (aa < na && b0 + bb < dc) v = rho[(long long)pl * C.rho_spl + (a0 + aa) + (long long)(b0 + bb) * d];
           srho[pl][aa][bb] = v;
         }
@@ -210,25 +221,25 @@ __global__ void __launch_bounds__(256) k_density(DevBasis B, DensCall c0, DensCa
         // spin-up rows first: split the chunk at the spin boundary
         const int nup_here = max(0, min(na, nu - a0));
         for (int aa = 0; aa < nup_here; ++aa) {
-          const double re = srho[0][aa][bl], im = srho[1][aa][bl];
+          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const double f = sphi[q][aa][rl];
+            const T f = sphi[q][aa][rl];
             w[0][q][0] = fma(f, re, w[0][q][0]); w[0][q][1] = fma(f, im, w[0][q][1]);
           }
         }
         for (int aa = nup_here; aa < na; ++aa) {
-          const double re = srho[0][aa][bl], im = srho[1][aa][bl];
+          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const double f = sphi[q][aa][rl];
+            const T f = sphi[q][aa][rl];
             w[1][q][0] = fma(f, re, w[1][q][0]); w[1][q][1] = fma(f, im, w[1][q][1]);
           }
         }
         __syncthreads();
       }
       // epilogue: contributions of column b at mesh point r
-      double P0 = 0, P1 = 0, P2 = 0, P3 = 0, sg = 0;
+      T P0 = 0, P1 = 0, P2 = 0, P3 = 0, sg = 0;
       const bool ok = rok && b < dc;
       if (ok) {
         const int jb = sb + b;
@@ -236,74 +247,74 @@ __global__ void __launch_bounds__(256) k_density(DevBasis B, DensCall c0, DensCa
         P1 = B.phi[1 * ps + (long long)jb * nghl + r];
         P2 = B.phi[2 * ps + (long long)jb * nghl + r];
         P3 = B.phi[3 * ps + (long long)jb * nghl + r];
-        sg = (double)B.ns[jb];
+        sg = (T)B.ns[jb];
       }
       const int si = (sg > 0) ? 0 : 1;  // same-spin set of wfa
       // select S (same spin as b) and O (opposite)
-      double Sr[4], Si[4], Or[4], Oi[4];
+      T Sr[4], Si[4], Or[4], Oi[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         Sr[q] = si == 0 ? w[0][q][0] : w[1][q][0]; Si[q] = si == 0 ? w[0][q][1] : w[1][q][1];
         Or[q] = si == 0 ? w[1][q][0] : w[0][q][0]; Oi[q] = si == 0 ? w[1][q][1] : w[0][q][1];
-        if (!ok) { Sr[q] = Si[q] = Or[q] = Oi[q] = 0.0; }
+        if (!ok) { Sr[q] = Si[q] = Or[q] = Oi[q] = 0; }
       }
-      const double sig = (sg < 0) ? 1.0 : -1.0;  // +1 if b is spin down
-      double xr, xi;
+      const T sig = (sg < 0) ? (T)1 : (T)-1;  // +1 if b is spin down
+      T xr, xi;
       // diagonal in spin
       xr = Sr[0] * P0; xi = Si[0] * P0;
       ACC(D_RHO, xr, xi);
       ACC(D_SZ, sg * xr, sg * xi);
-      xr = 0.5 * (Sr[0] * P2 + Sr[2] * P0); xi = 0.5 * (Si[0] * P2 + Si[2] * P0);
+      xr = h5 * (Sr[0] * P2 + Sr[2] * P0); xi = h5 * (Si[0] * P2 + Si[2] * P0);
       ACC(D_JP, xr, xi);
       ACC(D_TJPZ, sg * xr, sg * xi);
       xr = Sr[1] * P1 + Sr[2] * P2 + Sr[3] * P3; xi = Si[1] * P1 + Si[2] * P2 + Si[3] * P3;
       ACC(D_TAU, xr, xi);
       ACC(D_TZ, sg * xr, sg * xi);
-      xr = 0.5 * (Sr[0] * P1 - Sr[1] * P0); xi = 0.5 * (Si[0] * P1 - Si[1] * P0);
+      xr = h5 * (Sr[0] * P1 - Sr[1] * P0); xi = h5 * (Si[0] * P1 - Si[1] * P0);
       ACC(D_JR, -xi, xr);
       ACC(D_TJRZ, -sg * xi, sg * xr);
-      xr = 0.5 * (Sr[0] * P3 - Sr[3] * P0); xi = 0.5 * (Si[0] * P3 - Si[3] * P0);
+      xr = h5 * (Sr[0] * P3 - Sr[3] * P0); xi = h5 * (Si[0] * P3 - Si[3] * P0);
       ACC(D_JZ, -xi, xr);
       ACC(D_TJZZ, -sg * xi, sg * xr);
       // gs: diagonal part + off-diagonal parts
       {
-        double gr = sg * (Sr[0] * P3 + Sr[3] * P0), gi = sg * (Si[0] * P3 + Si[3] * P0);
+        T gr = sg * (Sr[0] * P3 + Sr[3] * P0), gi = sg * (Si[0] * P3 + Si[3] * P0);
         gr += sig * (Or[0] * P2 - Or[2] * P0) + (Or[0] * P1 + Or[1] * P0);
         gi += sig * (Oi[0] * P2 - Oi[2] * P0) + (Oi[0] * P1 + Oi[1] * P0);
         ACC(D_GS, gr, gi);
       }
       {
-        double fr = 0.5 * sg * (Sr[1] * P3 + Sr[3] * P1), fi = 0.5 * sg * (Si[1] * P3 + Si[3] * P1);
-        fr += Or[1] * P1 + sig * 0.5 * (Or[1] * P2 - Or[2] * P1);
-        fi += Oi[1] * P1 + sig * 0.5 * (Oi[1] * P2 - Oi[2] * P1);
+                T fr = h5 * sg * (Sr[1] * P3 + Sr[3] * P1), fi = h5 * sg * (Si[1] * P3 + Si[3] * P1);
+        fr += Or[1] * P1 + sig * h5 * (Or[1] * P2 - Or[2] * P1);
+        fi += Oi[1] * P1 + sig * h5 * (Oi[1] * P2 - Oi[2] * P1);
         ACC(D_FR, fr, fi);
       }
       {
         // fp += i*sg*(S2P3 - S3P2)/2 + i*(sig*O2P2 + (O2P1 - O1P2)/2)
-        const double ar = 0.5 * sg * (Sr[2] * P3 - Sr[3] * P2) + sig * Or[2] * P2 + 0.5 * (Or[2] * P1 - Or[1] * P2);
-        const double ai = 0.5 * sg * (Si[2] * P3 - Si[3] * P2) + sig * Oi[2] * P2 + 0.5 * (Oi[2] * P1 - Oi[1] * P2);
+                const T ar = h5 * sg * (Sr[2] * P3 - Sr[3] * P2) + sig * Or[2] * P2 + h5 * (Or[2] * P1 - Or[1] * P2);
+        const T ai = h5 * sg * (Si[2] * P3 - Si[3] * P2) + sig * Oi[2] * P2 + h5 * (Oi[2] * P1 - Oi[1] * P2);
         ACC(D_FP, -ai, ar);
       }
       {
-        double zr = sg * Sr[3] * P3, zi = sg * Si[3] * P3;
-        zr += 0.5 * (Or[3] * P1 + sig * Or[3] * P2 + Or[1] * P3 - sig * Or[2] * P3);
-        zi += 0.5 * (Oi[3] * P1 + sig * Oi[3] * P2 + Oi[1] * P3 - sig * Oi[2] * P3);
+                T zr = sg * Sr[3] * P3, zi = sg * Si[3] * P3;
+        zr += h5 * (Or[3] * P1 + sig * Or[3] * P2 + Or[1] * P3 - sig * Or[2] * P3);
+        zi += h5 * (Oi[3] * P1 + sig * Oi[3] * P2 + Oi[1] * P3 - sig * Oi[2] * P3);
         ACC(D_FZ, zr, zi);
       }
       // not diagonal in spin
       xr = Or[0] * P0; xi = Oi[0] * P0;
       ACC(D_SR, xr, xi);
       ACC(D_SP, -sig * xi, sig * xr);
-      xr = 0.5 * (Or[2] * P0 + Or[0] * P2); xi = 0.5 * (Oi[2] * P0 + Oi[0] * P2);
+      xr = h5 * (Or[2] * P0 + Or[0] * P2); xi = h5 * (Oi[2] * P0 + Oi[0] * P2);
       ACC(D_TJPR, xr, xi);
       ACC(D_TJPP, -sig * xi, sig * xr);
       xr = Or[1] * P1 + Or[2] * P2 + Or[3] * P3; xi = Oi[1] * P1 + Oi[2] * P2 + Oi[3] * P3;
       ACC(D_TR, xr, xi);
       ACC(D_TP, -sig * xi, sig * xr);
-      xr = 0.5 * (Or[0] * P1 - Or[1] * P0); xi = 0.5 * (Oi[0] * P1 - Oi[1] * P0);
+      xr = h5 * (Or[0] * P1 - Or[1] * P0); xi = h5 * (Oi[0] * P1 - Oi[1] * P0);
       ACC(D_TJRR, -xi, xr);
       ACC(D_TJRP, -sig * xr, -sig * xi);
-      xr = 0.5 * (Or[0] * P3 - Or[3] * P0); xi = 0.5 * (Oi[0] * P3 - Oi[3] * P0);
+      xr = h5 * (Or[0] * P3 - Or[3] * P0); xi = h5 * (Oi[0] * P3 - Oi[3] * P0);
       ACC(D_TJZR, -xi, xr);
       ACC(D_TJZP, -sig * xr, -sig * xi);
     }
@@ -314,59 +325,59 @@ __global__ void __launch_bounds__(256) k_density(DevBasis B, DensCall c0, DensCa
     if (iy < 0) continue;
     const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
     const int sa = B.st[ix], sb = B.st[iy];
-    const double* kap = C.kap + (long long)p * C.kap_sp + C.koffs[ix];
+    const T* kap = C.kap + (long long)p * C.kap_sp + C.koffs[ix];
     for (int b0 = 0; b0 < dc; b0 += DBC) {
       const int b = b0 + bl;
-      double w[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+      T w[2][2] = {{0, 0}, {0, 0}};
       for (int a0 = 0; a0 < d; a0 += DAK) {
         const int na = min(DAK, d - a0);
         for (int e = threadIdx.x; e < DAK * DRT; e += 256) {
           const int aa = e / DRT, rr = e % DRT;
-          double v = 0.0;
+          T v = 0;
           if (aa < na && r0 + rr < nghl) v = B.phi[(long long)(sa + a0 + aa) * nghl + r0 + rr];
           sphi[0][aa][rr] = v;
         }
         for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
           const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
-          double v = 0.0;
+          T v = 0;
           if (aa < na && b0 + bb < dc) v = kap[(long long)pl * C.kap_spl + (a0 + aa) + (long long)(b0 + bb) * d];
           srho[pl][aa][bb] = v;
         }
         __syncthreads();
         const int nup_here = max(0, min(na, nu - a0));
         for (int aa = 0; aa < nup_here; ++aa) {
-          const double f = sphi[0][aa][rl];
+          const T f = sphi[0][aa][rl];
           w[0][0] = fma(f, srho[0][aa][bl], w[0][0]); w[0][1] = fma(f, srho[1][aa][bl], w[0][1]);
         }
         for (int aa = nup_here; aa < na; ++aa) {
-          const double f = sphi[0][aa][rl];
+          const T f = sphi[0][aa][rl];
           w[1][0] = fma(f, srho[0][aa][bl], w[1][0]); w[1][1] = fma(f, srho[1][aa][bl], w[1][1]);
         }
         __syncthreads();
       }
-      double P0 = 0, sg = 0;
+      T P0 = 0, sg = 0;
       const bool ok = rok && b < dc;
       if (ok) {
         const int jb = sb + b;
         P0 = B.phi[(long long)jb * nghl + r];
-        sg = (double)B.ns[jb];
+        sg = (T)B.ns[jb];
       }
       const int si = (sg > 0) ? 0 : 1;
-      double Sr = si == 0 ? w[0][0] : w[1][0], Si = si == 0 ? w[0][1] : w[1][1];
-      double Or = si == 0 ? w[1][0] : w[0][0], Oi = si == 0 ? w[1][1] : w[0][1];
-      if (!ok) { Sr = Si = Or = Oi = 0.0; }
-      const double sig = (sg < 0) ? 1.0 : -1.0;
-      double xr = 2.0 * Or * P0, xi = 2.0 * Oi * P0;
+      T Sr = si == 0 ? w[0][0] : w[1][0], Si = si == 0 ? w[0][1] : w[1][1];
+      T Or = si == 0 ? w[1][0] : w[0][0], Oi = si == 0 ? w[1][1] : w[0][1];
+      if (!ok) { Sr = Si = Or = Oi = 0; }
+      const T sig = (sg < 0) ? (T)1 : (T)-1;
+      T xr = two * Or * P0, xi = two * Oi * P0;
       ACC(D_RB, -sg * xr, -sg * xi);
       ACC(D_SBZ, xr, xi);
-      xr = 2.0 * Sr * P0; xi = 2.0 * Si * P0;
+      xr = two * Sr * P0; xi = two * Si * P0;
       ACC(D_SBR, sig * xr, sig * xi);
       ACC(D_SBP, xi, -xr);
     }
   }
 #undef ACC
   __syncthreads();
-  double* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
+  T* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
   for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) {
     const int k = e / DRT, rr = e % DRT;
     if (r0 + rr < nghl) out[(long long)k * nghl + r0 + rr] = acc[k][rr];
@@ -388,21 +399,22 @@ __device__ __forceinline__ cplx cmk(double r, double i) { cplx c; c.r = r; c.i =
 __device__ __forceinline__ cplx cadd(cplx a, cplx b) { return cmk(a.r + b.r, a.i + b.i); }
 __device__ __forceinline__ cplx csc(double s, cplx a) { return cmk(s * a.r, s * a.i); }
 
-__global__ void __launch_bounds__(128) k_meanfield(DevBasis B, int G, const double* __restrict__ dpart,
-                                                   double* __restrict__ mfout, const int* __restrict__ active) {
+template <class T>
+__global__ void __launch_bounds__(128) k_meanfield(DevBasisT<T> B, int G, const T* __restrict__ dpart,
+                                                   T* __restrict__ mfout, const int* __restrict__ active) {
   const int p = blockIdx.y >> 1, call = blockIdx.y & 1;
   if (!active[p]) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int nghl = B.nghl;
   if (r >= nghl) return;
   cplx d[ND];
-  const double* dp = dpart + ((long long)p * 2 + call) * G * (2 * ND) * nghl;
+  const T* dp = dpart + ((long long)p * 2 + call) * G * (2 * ND) * nghl;
   const double wd = B.wdcori[r];
   for (int k = 0; k < ND; ++k) {
     double sr = 0.0, si = 0.0;
     for (int g = 0; g < G; ++g) {
-      sr += dp[((long long)g * 2 * ND + 2 * k) * nghl + r];
-      si += dp[((long long)g * 2 * ND + 2 * k + 1) * nghl + r];
+      sr += (double)dp[((long long)g * 2 * ND + 2 * k) * nghl + r];
+      si += (double)dp[((long long)g * 2 * ND + 2 * k + 1) * nghl + r];
     }
     d[k] = cmk(sr * wd, si * wd);
   }
@@ -596,10 +608,10 @@ __global__ void __launch_bounds__(128) k_meanfield(DevBasis B, int G, const doub
   mf[101] = cmk(cpair * rb.r - cspair * sbz.r, cpair * rb.i - cspair * sbz.i); // a+ b-
   mf[102] = cmk(-cpair * rb.r - cspair * sbz.r, -cpair * rb.i - cspair * sbz.i); // a- b+
   mf[103] = cmk(cspair * (-sbr.r + sbp.i), cspair * (-sbr.i - sbp.r));      // a- b-
-  double* out = mfout + ((long long)p * 2 + call) * NMF * 2 * nghl;
+  T* out = mfout + ((long long)p * 2 + call) * NMF * 2 * nghl;
   for (int k = 0; k < NMF; ++k) {
-    out[((long long)k * 2) * nghl + r] = mf[k].r;
-    out[((long long)k * 2 + 1) * nghl + r] = mf[k].i;
+    out[((long long)k * 2) * nghl + r] = (T)mf[k].r;
+    out[((long long)k * 2 + 1) * nghl + r] = (T)mf[k].i;
   }
 }
 
@@ -620,53 +632,54 @@ struct HTask {
 #define HRC 16   // mesh points per K chunk
 
 // grid (ntasks, P); 256 threads (16x16, 2x2 outputs each); dynamic smem
-__global__ void __launch_bounds__(256) k_hproj(DevBasis B, const HTask* __restrict__ tasks,
-                                               const double* __restrict__ mf, double* __restrict__ hsp,
+template <class T>
+__global__ void __launch_bounds__(256) k_hproj(DevBasisT<T> B, const HTask* __restrict__ tasks,
+                                               const T* __restrict__ mf, T* __restrict__ hsp,
                                                long long nxy, const int* __restrict__ active) {
   const int p = blockIdx.y;
   if (!active[p]) return;
-  const HTask T = tasks[blockIdx.x];
+  const HTask Th = tasks[blockIdx.x];
   const int nghl = B.nghl;
   const long long ps = (long long)B.dqp * nghl;
-  const int nc = T.mode == 0 ? 5 : 1;
-  extern __shared__ double sm[];
-  double* sA = sm;                          // [5][32][HRC]
-  double* sPb = sA + 5 * 32 * HRC;          // [5][32][HRC]
-  double* sMF = sPb + 5 * 32 * HRC;         // [25][2 sb][2 re/im][HRC]
-  double* sH = sMF + 25 * 2 * 2 * HRC;      // [5][32][2][HRC]
+  const int nc = Th.mode == 0 ? 5 : 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sA = reinterpret_cast<T*>(smraw);     // [5][32][HRC]
+  T* sPb = sA + 5 * 32 * HRC;               // [5][32][HRC]
+  T* sMF = sPb + 5 * 32 * HRC;              // [25][2 sb][2 re/im][HRC]
+  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][32][2][HRC]
   __shared__ signed char sns[32];
-  const int ja0 = B.st[T.ix] + T.a0, jb0 = B.st[T.iy] + T.b0;
-  if (threadIdx.x < 32) sns[threadIdx.x] = threadIdx.x < T.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
-  const double* mfp = mf + ((long long)p * 2 + T.call) * NMF * 2 * nghl;
+  const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
+  if (threadIdx.x < 32) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
+  const T* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * nghl;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
+  T ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
   for (int r0 = 0; r0 < nghl; r0 += HRC) {
     const int nr = min(HRC, nghl - r0);
     __syncthreads();
     for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
       const int q = e / (32 * HRC), rem = e % (32 * HRC), aa = rem / HRC, rr = rem % HRC;
-      double va = 0.0, vb = 0.0;
+      T va = 0, vb = 0;
       if (rr < nr) {
-        if (aa < T.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
-        if (aa < T.nbc) vb = B.phi[q * ps + (long long)(jb0 + aa) * nghl + r0 + rr];
+        if (aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
+        if (aa < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + aa) * nghl + r0 + rr];
       }
       sA[(q * 32 + aa) * HRC + rr] = va;
       sPb[(q * 32 + aa) * HRC + rr] = vb;
     }
-    if (T.mode == 0) {
+    if (Th.mode == 0) {
       for (int e = threadIdx.x; e < 25 * 2 * 2 * HRC; e += 256) {
         const int pair = e / (4 * HRC), rem = e % (4 * HRC), sb = rem / (2 * HRC), rem2 = rem % (2 * HRC);
         const int ri = rem2 / HRC, rr = rem2 % HRC;
         const int iy = pair / 5, iz = pair % 5;
-        double v = 0.0;
-        if (rr < nr) v = mfp[((long long)mfslot(iy, iz, T.sa, sb == 0 ? 1 : -1) * 2 + ri) * nghl + r0 + rr];
+        T v = 0;
+        if (rr < nr) v = mfp[((long long)mfslot(iy, iz, Th.sa, sb == 0 ? 1 : -1) * 2 + ri) * nghl + r0 + rr];
         sMF[e] = v;
       }
     } else {
       for (int e = threadIdx.x; e < 2 * 2 * HRC; e += 256) {
         const int sb = e / (2 * HRC), rem = e % (2 * HRC), ri = rem / HRC, rr = rem % HRC;
-        const int slot = 100 + (T.sa < 0 ? 2 : 0) + sb;
-        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : 0.0;
+        const int slot = 100 + (Th.sa < 0 ? 2 : 0) + sb;
+        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : (T)0;
       }
     }
     __syncthreads();
@@ -674,16 +687,16 @@ __global__ void __launch_bounds__(256) k_hproj(DevBasis B, const HTask* __restri
     for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
       const int iy = e / (32 * HRC), rem = e % (32 * HRC), bb = rem / HRC, rr = rem % HRC;
       const int sb = sns[bb] > 0 ? 0 : 1;
-      double hr = 0.0, hi = 0.0;
-      if (T.mode == 0) {
+      T hr = 0, hi = 0;
+      if (Th.mode == 0) {
 #pragma unroll
         for (int iz = 0; iz < 5; ++iz) {
-          const double f = sPb[(iz * 32 + bb) * HRC + rr];
-          const double* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
+          const T f = sPb[(iz * 32 + bb) * HRC + rr];
+          const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
           hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
         }
       } else {
-        const double f = sPb[bb * HRC + rr];
+        const T f = sPb[bb * HRC + rr];
         hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
       }
       sH[((iy * 32 + bb) * 2) * HRC + rr] = hr;
@@ -692,9 +705,9 @@ __global__ void __launch_bounds__(256) k_hproj(DevBasis B, const HTask* __restri
     __syncthreads();
     for (int q = 0; q < nc; ++q) {
       for (int rr = 0; rr < HRC; ++rr) {
-        const double a0 = sA[(q * 32 + ty * 2) * HRC + rr], a1 = sA[(q * 32 + ty * 2 + 1) * HRC + rr];
-        const double h0r = sH[((q * 32 + tx * 2) * 2) * HRC + rr], h0i = sH[((q * 32 + tx * 2) * 2 + 1) * HRC + rr];
-        const double h1r = sH[((q * 32 + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * 32 + tx * 2 + 1) * 2 + 1) * HRC + rr];
+        const T a0 = sA[(q * 32 + ty * 2) * HRC + rr], a1 = sA[(q * 32 + ty * 2 + 1) * HRC + rr];
+        const T h0r = sH[((q * 32 + tx * 2) * 2) * HRC + rr], h0i = sH[((q * 32 + tx * 2) * 2 + 1) * HRC + rr];
+        const T h1r = sH[((q * 32 + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * 32 + tx * 2 + 1) * 2 + 1) * HRC + rr];
         ar[0][0] = fma(a0, h0r, ar[0][0]); ai[0][0] = fma(a0, h0i, ai[0][0]);
         ar[0][1] = fma(a0, h1r, ar[0][1]); ai[0][1] = fma(a0, h1i, ai[0][1]);
         ar[1][0] = fma(a1, h0r, ar[1][0]); ai[1][0] = fma(a1, h0i, ai[1][0]);
@@ -702,18 +715,18 @@ __global__ void __launch_bounds__(256) k_hproj(DevBasis B, const HTask* __restri
       }
     }
   }
-  const int ld = B.db[T.ix];
-  double* ore = hsp + ((long long)p * 2 + 0) * 4 * nxy + (long long)T.outq * nxy + T.ooff;
-  double* oim = hsp + ((long long)p * 2 + 1) * 4 * nxy + (long long)T.outq * nxy + T.ooff;
+  const int ld = B.db[Th.ix];
+  T* ore = hsp + ((long long)p * 2 + 0) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
+  T* oim = hsp + ((long long)p * 2 + 1) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const int a = ty * 2 + i, b = tx * 2 + j;
-      if (a < T.na && b < T.nbc) {
-        const long long e = (T.a0 + a) + (long long)(T.b0 + b) * ld;
-        ore[e] = 2.0 * ar[i][j];
-        oim[e] = 2.0 * ai[i][j];
+      if (a < Th.na && b < Th.nbc) {
+        const long long e = (Th.a0 + a) + (long long)(Th.b0 + b) * ld;
+        ore[e] = (T)2 * ar[i][j];
+        oim[e] = (T)2 * ai[i][j];
       }
     }
 }
@@ -721,38 +734,44 @@ __global__ void __launch_bounds__(256) k_hproj(DevBasis B, const HTask* __restri
 // ---------------------------------------------------------------------------
 // Green's function update: vout = G o (q*H + F); layout [P][Re X|Y, Im X|Y]
 // ---------------------------------------------------------------------------
+// corr[p] != 0 (increment step of the mixed form, H evaluated from X - X_anchor):
+// vout = G o (q*H) + radd[p], radd = g(X_anchor) evaluated in FP64
 __global__ void k_green(long long nxy, int P, const double* __restrict__ hqp, const double* __restrict__ fqp,
                         const int* __restrict__ erow, const int* __restrict__ ecol,
                         const double* __restrict__ E1, const double* __restrict__ E2,
                         const double* __restrict__ wre, const double* __restrict__ wim, double quench,
-                        double* __restrict__ vout, const int* __restrict__ active) {
+                        double* __restrict__ vout, const int* __restrict__ active,
+                        const int* __restrict__ corr, const double* __restrict__ radd) {
   const int p = blockIdx.y;
   if (!active[p]) return;
   const long long n2 = 2 * nxy;
   const double wr = wre[p], wi = wim[p];
+  const bool cstep = corr && corr[p];
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n2; e += (long long)gridDim.x * blockDim.x) {
     double hr = 0.0, hi = 0.0;
     if (hqp) { hr = quench * hqp[(long long)p * 2 * n2 + e]; hi = quench * hqp[(long long)p * 2 * n2 + n2 + e]; }
-    hr += fqp[e];
+    if (!cstep) hr += fqp[e];
     // G = -1/(E1 + E2 -/+ w): X (e < nxy) uses -w, Y uses +w
     const double sgn = e < nxy ? -1.0 : 1.0;
     const double dr = E1[erow[e]] + E2[ecol[e]] + sgn * wr, di = sgn * wi;
     const double den = dr * dr + di * di;
     const double gr = -dr / den, gi = di / den;
-    vout[(long long)p * 2 * n2 + e] = gr * hr - gi * hi;
-    vout[(long long)p * 2 * n2 + n2 + e] = gr * hi + gi * hr;
+    double vr = gr * hr - gi * hi, vi = gr * hi + gi * hr;
+    if (cstep) { vr += radd[(long long)p * 2 * n2 + e]; vi += radd[(long long)p * 2 * n2 + n2 + e]; }
+    vout[(long long)p * 2 * n2 + e] = vr;
+    vout[(long long)p * 2 * n2 + n2 + e] = vi;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Broyden mixing on device (pnfam_broyden.f90:117-216)
+// Broyden mixing on device (pnfam_broyden.f90:117-216), one independent
+// history per point: itp[p] is the point's own Broyden iteration number and
+// modep[p] what the step does (BRO_* below)
 // ---------------------------------------------------------------------------
+enum { BRO_BROYDEN = 0, BRO_LINEAR = 1, BRO_NOMIX = 2 };
 struct BroState {
   int N;            // vector length (4*nxy)
   int M;            // history size
-  int it;           // iteration number
-  int ipos, inext;  // 0-based history slots
-  int iter_used;
   double alpha;
   double* vin;      // [P][N]
   double* vout;     // [P][N]
@@ -760,8 +779,19 @@ struct BroState {
   double* dv;       // [P][M][N]
   double* part;     // [P][nchunk][NPART] block partials
   int nchunk;
+  const int* itp;   // [P] Broyden iteration of each point
+  const int* modep; // [P] BRO_*
 };
 enum { BRO_NPART = 2 + 2 * 64 };  // 0: max|vout|, 1: |df_ipos|^2, 2..: dots
+
+// history slots of Broyden iteration `it` (Fortran integer division truncates
+// toward zero, as C++ does): iter_used columns in use, ipos the column updated
+// this step, inext the column written at the end (0-based)
+__host__ __device__ __forceinline__ void bro_slots(int it, int M, int& iter_used, int& ipos, int& inext) {
+  iter_used = it - 1 < M ? it - 1 : M;
+  ipos = it - 1 - ((it - 2) / M) * M - 1;
+  inext = it - ((it - 1) / M) * M - 1;
+}
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -785,14 +815,18 @@ __device__ __forceinline__ double block_max(double v, double* sh) {
 }
 
 // vout -= vin; max|vout|; history column ipos: df = vout - df, dv = vin - dv, |df|^2
-__global__ void __launch_bounds__(256) k_bro_diff(BroState S, int upd, const int* __restrict__ active) {
+__global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restrict__ active) {
   const int p = blockIdx.y;
   if (!active[p]) return;
   __shared__ double sh[32];
+  const int it = S.itp[p], mode = S.modep[p];
+  int iu, ipos, inext;
+  bro_slots(it, S.M, iu, ipos, inext);
+  const bool upd = mode == BRO_BROYDEN && it >= 2;
   double* vo = S.vout + (long long)p * S.N;
   const double* vi = S.vin + (long long)p * S.N;
-  double* df = upd ? S.df + ((long long)p * S.M + S.ipos) * S.N : nullptr;
-  double* dv = upd ? S.dv + ((long long)p * S.M + S.ipos) * S.N : nullptr;
+  double* df = upd ? S.df + ((long long)p * S.M + ipos) * S.N : nullptr;
+  double* dv = upd ? S.dv + ((long long)p * S.M + ipos) * S.N : nullptr;
   double mx = 0.0, nn = 0.0;
   const int chunk = (S.N + S.nchunk - 1) / S.nchunk;
   const int e0 = blockIdx.x * chunk, e1 = min(S.N, e0 + chunk);
@@ -815,31 +849,36 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, int upd, const int
   }
 }
 
-// normalise column ipos by 1/|df_ipos| (norm from k_bro_norm) and form the dots
+// normalise column ipos by 1/|df_ipos| and form the dots
 // dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used
 __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __restrict__ norm,
-                                                  int upd, const int* __restrict__ active) {
+                                                  const int* __restrict__ active) {
   const int p = blockIdx.y;
   if (!active[p]) return;
+  const int it = S.itp[p], mode = S.modep[p];
+  if (mode != BRO_BROYDEN || it < 1) return;
+  int iu, ipos, inext;
+  bro_slots(it, S.M, iu, ipos, inext);
+  const bool upd = it >= 2;
   __shared__ double sh[32];
   const double* vo = S.vout + (long long)p * S.N;
   const int chunk = (S.N + S.nchunk - 1) / S.nchunk;
   const int e0 = blockIdx.x * chunk, e1 = min(S.N, e0 + chunk);
-  const double sc = upd ? norm[p] : 1.0;
   double* dfp = S.df + (long long)p * S.M * S.N;
   double* dvp = S.dv + (long long)p * S.M * S.N;
   if (upd) {
+    const double sc = norm[p];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      dfp[(long long)S.ipos * S.N + e] *= sc;
-      dvp[(long long)S.ipos * S.N + e] *= sc;
+      dfp[(long long)ipos * S.N + e] *= sc;
+      dvp[(long long)ipos * S.N + e] *= sc;
     }
   }
   __syncthreads();
   double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
-  for (int k = 0; k < S.iter_used; ++k) {
+  for (int k = 0; k < iu; ++k) {
     double a = 0.0, b = 0.0;
     const double* fk = dfp + (long long)k * S.N;
-    const double* fi = dfp + (long long)S.ipos * S.N;
+    const double* fi = dfp + (long long)ipos * S.N;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
       a = fma(fk[e], fi[e], a);
       b = fma(fk[e], vo[e], b);
@@ -850,7 +889,8 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   }
 }
 
-// one CTA per point: reduce partials, maintain beta (M x M), solve beta*gamma = work
+// one CTA per point: reduce partials; stage 0: si and 1/|df_ipos|; stage 1:
+// maintain beta (M x M) and solve beta*gamma = work
 __global__ void k_bro_solve(BroState S, int stage, double w0, double* __restrict__ si, double* __restrict__ norm,
                             double* __restrict__ beta, double* __restrict__ gamma, const int* __restrict__ active) {
   const int p = blockIdx.x;
@@ -865,16 +905,19 @@ __global__ void k_bro_solve(BroState S, int stage, double w0, double* __restrict
     }
     return;
   }
+  const int it = S.itp[p], mode = S.modep[p];
+  if (mode != BRO_BROYDEN || it < 1) return;
+  int n, ipos, inext;
+  bro_slots(it, S.M, n, ipos, inext);
   __shared__ double A[64][65];
   __shared__ double x[64];
-  const int M = S.M, n = S.iter_used;
+  const int M = S.M;
   double* bp = beta + (long long)p * M * M;
   if (threadIdx.x == 0) {
-    // dots of the normalised new column with all used columns
     for (int k = 0; k < n; ++k) {
       double dd = 0.0, wk = 0.0;
       for (int c = 0; c < S.nchunk; ++c) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
-      if (k != S.ipos) { bp[k * M + S.ipos] = dd; bp[S.ipos * M + k] = dd; }
+      if (k != ipos) { bp[k * M + ipos] = dd; bp[ipos * M + k] = dd; }
       x[k] = wk;
     }
     for (int k = 0; k < n; ++k) bp[k * M + k] = w0 * w0 + 1.0;
@@ -903,30 +946,51 @@ __global__ void k_bro_solve(BroState S, int stage, double w0, double* __restrict
   }
 }
 
-// curv = alpha*vout - sum_i gamma_i (dv_i + alpha df_i); df[inext] = vout; dv[inext] = vin; vin += curv
-// mode 0: Broyden, 1: linear mixing (vin += alpha vout), 2: no mixing (vin += vout)
-__global__ void __launch_bounds__(256) k_bro_update(BroState S, int mode, const double* __restrict__ gamma,
+// BRO_BROYDEN: curv = alpha*vout - sum_i gamma_i (dv_i + alpha df_i);
+//              df[inext] = vout; dv[inext] = vin; vin += curv
+// BRO_LINEAR:  vin += alpha*vout;  BRO_NOMIX: vin += vout
+__global__ void __launch_bounds__(256) k_bro_update(BroState S, const double* __restrict__ gamma,
                                                     const int* __restrict__ active) {
   const int p = blockIdx.y;
   if (!active[p]) return;
+  const int it = S.itp[p], mode = S.modep[p];
+  int iu, ipos, inext;
+  bro_slots(it, S.M, iu, ipos, inext);
+  if (mode != BRO_BROYDEN) iu = 0;
   double* vi = S.vin + (long long)p * S.N;
   const double* vo = S.vout + (long long)p * S.N;
   __shared__ double g[64];
-  if (mode == 0 && threadIdx.x < S.iter_used) g[threadIdx.x] = gamma[(long long)p * 64 + threadIdx.x];
+  if (mode == BRO_BROYDEN && (int)threadIdx.x < iu) g[threadIdx.x] = gamma[(long long)p * 64 + threadIdx.x];
   __syncthreads();
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < S.N; e += (long long)gridDim.x * blockDim.x) {
     const double v = vo[e];
-    if (mode == 2) { vi[e] += v; continue; }
-    if (mode == 1) { vi[e] += S.alpha * v; continue; }
+    if (mode == BRO_NOMIX) { vi[e] += v; continue; }
+    if (mode == BRO_LINEAR) { vi[e] += S.alpha * v; continue; }
     double c = S.alpha * v;
     const double* dfp = S.df + (long long)p * S.M * S.N;
     const double* dvp = S.dv + (long long)p * S.M * S.N;
-    for (int k = 0; k < S.iter_used; ++k)
+    for (int k = 0; k < iu; ++k)
       c -= g[k] * (dvp[(long long)k * S.N + e] + S.alpha * dfp[(long long)k * S.N + e]);
     const double old = vi[e];
-    S.df[((long long)p * S.M + S.inext) * S.N + e] = v;
-    S.dv[((long long)p * S.M + S.inext) * S.N + e] = old;
+    S.df[((long long)p * S.M + inext) * S.N + e] = v;
+    S.dv[((long long)p * S.M + inext) * S.N + e] = old;
     vi[e] = old + c;
+  }
+}
+
+// per-point vector operations, [P][n] layout:
+// op 0: dst = src; op 1: dst += src; op 2: dst = 0; op 3: dst = a*src
+__global__ void k_vecop(int op, double a, double* __restrict__ dst, const double* __restrict__ src, long long n,
+                        const int* __restrict__ mask) {
+  const int p = blockIdx.y;
+  if (!mask[p]) return;
+  double* d = dst + (long long)p * n;
+  const double* s_ = src ? src + (long long)p * n : nullptr;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    if (op == 0) d[e] = s_[e];
+    else if (op == 1) d[e] += s_[e];
+    else if (op == 2) d[e] = 0.0;
+    else d[e] = a * s_[e];
   }
 }
 
@@ -958,4 +1022,35 @@ __global__ void __launch_bounds__(256) k_contract(long long nxy, int nops, const
   }
 }
 
+}  // namespace pnfam
+
+namespace pnfam {
+// per-point precision conversions: out[p*n + e] = in[p*n + e] for points with act[p]
+// (act == nullptr: all points)
+// out = (float)(in - sub), sub optional; with dmax, dmax[p] = max(dmax[p], max|in - sub|)
+// (dmax as the bit pattern of a non-negative double, which orders like the integer)
+__global__ void __launch_bounds__(256) k_to_f32(const double* __restrict__ in, float* __restrict__ out, long long n,
+                                                int P, long long ld, const int* __restrict__ act,
+                                                const double* __restrict__ sub = nullptr,
+                                                unsigned long long* __restrict__ dmax = nullptr) {
+  const int p = blockIdx.y;
+  if (act && !act[p]) return;
+  double m = 0.0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const double v = sub ? in[p * ld + e] - sub[p * ld + e] : in[p * ld + e];
+    m = fmax(m, fabs(v));
+    out[p * ld + e] = (float)v;
+  }
+  if (dmax) {
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(dmax + p, (unsigned long long)__double_as_longlong(m));
+  }
+}
+__global__ void k_to_f64(const float* __restrict__ in, double* __restrict__ out, long long n, long long ld,
+                         const int* __restrict__ act) {
+  const int p = blockIdx.y;
+  if (act && !act[p]) return;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    out[p * ld + e] = (double)in[p * ld + e];
+}
 }  // namespace pnfam

@@ -80,7 +80,13 @@ class GPUSolver:
         return int(self.lib.pnfam_gpu_nxy(self.ctx))
 
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
-              history=False, timed=False) -> SolveResult:
+              history=False, timed=False, precision=0, switch_exp=0) -> SolveResult:
+        """precision 0: FP64 throughout (the reference's arithmetic and iteration
+        trajectory).  precision 1: defect correction -- the field is evaluated in
+        FP32 on the increment from an FP64 anchor; within 1000*eps of the anchor
+        convergence is accepted on an FP32 increment evaluation, farther out an
+        FP64 anchor evaluation is taken when si < 10**-switch_exp (default
+        100*eps) or si stops falling."""
         import time
         if alpha_mix is None:
             from .pnfam_setup import ALPHA_MIX as alpha_mix
@@ -93,8 +99,9 @@ class GPUSolver:
         o = _lib.SolverOpts()
         o.max_iter = int(max_iter); o.broyden_history_size = int(broyden_m)
         o.convergence_epsilon = float(eps); o.alpha_mix = float(alpha_mix)
-        o.quench_residual_int = float(quench); o.precision = 0
+        o.quench_residual_int = float(quench); o.precision = int(precision)
         o.reserved[0] = 1 if timed else 0
+        o.reserved[1] = int(switch_exp)
         t0 = time.perf_counter()
         _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
                                             _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
@@ -104,10 +111,10 @@ class GPUSolver:
                            hist.reshape(P, max_iter + 1, 3) if hist is not None else None, dt)
 
     def last_profile(self):
-        ms = np.zeros(9); n = C.c_longlong()
-        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 9, C.byref(n)))
+        ms = np.zeros(11); n = C.c_longlong()
+        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 11, C.byref(n)))
         names = ("k1_blockgemm", "density", "meanfield", "field_projection", "k2_blockgemm", "green", "broyden",
-                 "strength", "total")
+                 "strength", "total", "point_iterations_fp64", "point_iterations_fp32")
         return dict(zip(names, ms.tolist())), int(n.value)
 
     def calc_hamiltonian(self, rho_pn, kp, rho_np, km):
