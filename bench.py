@@ -296,19 +296,21 @@ def run_solve_only(args):
     case, omegas = workload(args.points)
     s = case.nml["solver"]
     kw = dict(max_iter=args.max_iter or s["max_iter"], eps=args.eps or s["convergence_epsilon"],
-              broyden_m=s["broyden_history_size"], quench=case.quench, precision=args.precision)
+              broyden_m=s["broyden_history_size"] if args.broyden_m is None else args.broyden_m,
+              quench=case.quench, precision=args.precision)
     gpu = GPUSolver(case.hfb, case.couplings)
     gpu.set_operator(case.F, case.G)
     for _ in range(args.warmup):
         gpu.solve(omegas, **kw)
     ms, its = [], None
     for _ in range(args.steps):
-        r = gpu.solve(omegas, **kw)
+        r = gpu.solve(omegas, timed=args.timed, **kw)
         prof = gpu.last_profile()[0]
         ms.append(prof["total"])
         its = r.iters.tolist()
     gpu.close()
     print(json.dumps({"solve_only": True, "precision": args.precision, "points": len(omegas), "ms": ms,
+                      "stages_ms": {k: v for k, v in prof.items() if args.timed},
                       "iters": its, "pit64": prof["point_iterations_fp64"], "pit32": prof["point_iterations_fp32"],
                       "S": [[float(a), float(b)] for a, b in zip(r.re_S[:, 0], r.im_S[:, 0])],
                       "omegas": [[float(w.real), float(w.imag)] for w in omegas]}), flush=True)
@@ -325,6 +327,8 @@ def main():
                     help="0: FP64 throughout; 1: FP32 field evaluation with FP64 finish")
     ap.add_argument("--eps", type=float, default=None, help="solve-only: convergence epsilon override")
     ap.add_argument("--max-iter", type=int, default=None, help="solve-only: max_iter override")
+    ap.add_argument("--broyden-m", type=int, default=None, help="solve-only: Broyden history override")
+    ap.add_argument("--timed", action="store_true", help="solve-only: per-stage event timing")
     ap.add_argument("--solve-only", action="store_true",
                     help="warm-up and timed solves only (no e2e/CPU/DGEMM legs); used for kernel profiling")
     args = ap.parse_args()

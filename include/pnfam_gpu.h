@@ -123,6 +123,37 @@ int pnfam_gpu_solve(pnfam_ctx_t* ctx, int npts, const double* re_w, const double
                     double* re_S, double* im_S, int* iters, double* si_out, double* hist);
 
 /*
+ * Continuous batching.  No counterpart in the reference, which runs one point
+ * per process (pynfam's task farm): an engine keeps `slots` omega points of
+ * one (nucleus, operator) context on the device, each slot iterating on its
+ * own counter exactly as pnfam_gpu_solve iterates a point, and a slot whose
+ * point has converged (or reached max_iter) takes the next point while the
+ * others keep iterating.  Engines of different contexts run on their own
+ * streams and overlap on the GPU.  One engine per context at a time; the
+ * context's solve buffers belong to the engine until pnfam_gpu_engine_free.
+ *
+ *   create   slots and solver options (as for pnfam_gpu_solve)
+ *   admit    up to n points into free slots; returns the number admitted
+ *            (>= 0), or minus an error code; tags identify the points in the
+ *            results
+ *   launch   enqueue one iteration of every active slot (returns at once)
+ *   finish   wait for it, advance the slots, and copy out up to maxout
+ *            finished points: tag, strength [nops] per point, iters (-1: not
+ *            converged), si; *nout = number copied (the rest stay queued)
+ *   active   number of slots holding a point that is still iterating
+ */
+typedef struct pnfam_engine pnfam_engine_t;
+int pnfam_gpu_engine_create(pnfam_ctx_t* ctx, int slots, const pnfam_solver_opts_t* opts,
+                            pnfam_engine_t** engine);
+int pnfam_gpu_engine_admit(pnfam_engine_t* engine, int n, const double* re_w, const double* im_w,
+                           const long long* tags);
+int pnfam_gpu_engine_launch(pnfam_engine_t* engine);
+int pnfam_gpu_engine_finish(pnfam_engine_t* engine, int maxout, long long* tags, double* re_S,
+                            double* im_S, int* iters, double* si, int* nout);
+int pnfam_gpu_engine_active(const pnfam_engine_t* engine);
+void pnfam_gpu_engine_free(pnfam_engine_t* engine);
+
+/*
  * The reference's in-process plugin seam: calc_hamiltonian
  * (pnfam_setup.f90:74-89 calc_dHsp_interface; pnfam_hamiltonian_blas.f90:51-74).
  * Given the perturbed single-particle densities (rho_pn in the F structure,
@@ -140,6 +171,22 @@ int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* ctx,
                                double* re_dp, double* im_dp,
                                double* re_h_np, double* im_h_np,
                                double* re_dm, double* im_dm);
+
+/*
+ * The same field evaluation in the arithmetic of the mixed form's increment
+ * evaluations: densities and fields in FP32, the field projection on the
+ * tensor cores as 3xTF32 products (about FP32 accuracy).  No counterpart in
+ * the reference.  Inputs and outputs as for pnfam_gpu_calc_hamiltonian.
+ */
+int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* ctx,
+                                     const double* re_rho_pn, const double* im_rho_pn,
+                                     const double* re_kp, const double* im_kp,
+                                     const double* re_rho_np, const double* im_rho_np,
+                                     const double* re_km, const double* im_km,
+                                     double* re_h_pn, double* im_h_pn,
+                                     double* re_dp, double* im_dp,
+                                     double* re_h_np, double* im_h_np,
+                                     double* re_dm, double* im_dm);
 
 /*
  * Allocation-free field evaluation.  No counterpart in the reference: the

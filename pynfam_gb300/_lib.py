@@ -14,7 +14,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libpnfam_gb300.so")
 
 EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam_gpu_calc_hamiltonian",
-           "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error")
+           "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error",
+           "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
+           "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_free",
+           "pnfam_gpu_calc_hamiltonian_mixed")
 
 ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENONFINITE", 5: "ESTATE"}
 
@@ -64,6 +67,8 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_solve.restype = C.c_int
     lib.pnfam_gpu_calc_hamiltonian.argtypes = [C.c_void_p] + [dp] * 16
     lib.pnfam_gpu_calc_hamiltonian.restype = C.c_int
+    lib.pnfam_gpu_calc_hamiltonian_mixed.argtypes = [C.c_void_p] + [dp] * 16
+    lib.pnfam_gpu_calc_hamiltonian_mixed.restype = C.c_int
     lib.pnfam_gpu_nxy.argtypes = [C.c_void_p]
     lib.pnfam_gpu_nxy.restype = C.c_longlong
     lib.pnfam_gpu_last_profile.argtypes = [C.c_void_p, dp, C.c_int, C.POINTER(C.c_longlong)]
@@ -72,6 +77,19 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_free.restype = None
     lib.pnfam_gpu_last_error.argtypes = []
     lib.pnfam_gpu_last_error.restype = C.c_char_p
+    lp = C.POINTER(C.c_longlong)
+    lib.pnfam_gpu_engine_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(SolverOpts), C.POINTER(C.c_void_p)]
+    lib.pnfam_gpu_engine_create.restype = C.c_int
+    lib.pnfam_gpu_engine_admit.argtypes = [C.c_void_p, C.c_int, dp, dp, lp]
+    lib.pnfam_gpu_engine_admit.restype = C.c_int
+    lib.pnfam_gpu_engine_launch.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_engine_launch.restype = C.c_int
+    lib.pnfam_gpu_engine_finish.argtypes = [C.c_void_p, C.c_int, lp, dp, dp, ip, dp, ip]
+    lib.pnfam_gpu_engine_finish.restype = C.c_int
+    lib.pnfam_gpu_engine_active.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_engine_active.restype = C.c_int
+    lib.pnfam_gpu_engine_free.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_engine_free.restype = None
     _lib = lib
     return lib
 

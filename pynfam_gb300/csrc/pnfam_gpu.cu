@@ -122,6 +122,7 @@ static GemmTerm mkterm(const MatRef& A, const MatRef& B, double a_re, double a_i
 
 }  // namespace
 
+struct pnfam_engine;
 struct pnfam_ctx {
   int dev = 0;
   // basis (host)
@@ -147,12 +148,17 @@ struct pnfam_ctx {
   TaskList k1a, k1b, k2a, k2b;
   std::vector<HTask> htasks;
   DBuf<HTask> d_htasks;
+  std::vector<HTaskTC> htasks_tc;   // tensor-core field projection (FP32 data)
+  DBuf<HTaskTC> d_htasks_tc;
+  DBuf<int> d_actlist;   // [P] points of the current FP32 evaluation (tensor-core tiles)
+  DBuf<int> d_err;       // set by a tensor-core kernel whose wait gave up
   // per-solve buffers
   int cap_P = 0, cap_M = 0;
   DBuf<double> d_state, d_vout, d_T, d_rsp, d_hsp, d_hqp, d_dpart, d_mf;
   DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
   DBuf<int> d_active, d_act32, d_act64;
-  DBuf<int> d_pint;      // [4][P]: Broyden iteration, Broyden mode, increment step, anchor step
+  DBuf<int> d_pint;      // [6][P]: Broyden iteration, Broyden mode, increment step, anchor step,
+                         // zero field (first evaluation), newly admitted
   DBuf<BufDesc> d_bufs;
   // mixed precision: FP32 copies of the ground state and FP32 scratch
   bool have32 = false;
@@ -163,6 +169,7 @@ struct pnfam_ctx {
   DBuf<unsigned long long> d_dmax;  // [P] max|X - X_a| of the last increment evaluation
   long long pit64 = 0, pit32 = 0;   // point-iterations per precision in the last solve
   int G = 1;
+  int nsm = 1;
   int nchunk_bro = 1, nchunk_c = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -170,8 +177,11 @@ struct pnfam_ctx {
   double stage_ms[8] = {0};
   double total_ms = 0.0;
   long long launches = 0;
+  pnfam_engine* engine = nullptr;   // the engine using this context's solve buffers
+  void detach_engine();
 
   ~pnfam_ctx() {
+    detach_engine();
     DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active, &d_act32, &d_act64,
                       &d_pint};
     DBuf<float>* fb[] = {&d_up32, &d_vp32, &d_un32, &d_vn32, &d_phi32, &d_state32, &d_T32, &d_rsp32, &d_hsp32,
@@ -187,7 +197,7 @@ struct pnfam_ctx {
                            &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim};
     for (auto* b : dbs) b->release();
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
-    d_htasks.release(); d_bufs.release();
+    d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
     k1a.d_tasks.release(); k1a.d_tile2task.release();
     k1b.d_tasks.release(); k1b.d_tile2task.release();
     k2a.d_tasks.release(); k2a.d_tile2task.release();
@@ -321,25 +331,63 @@ static void build_tasks(pnfam_ctx* c) {
                  {{1.0, 1.0}, c->ublk(UL, i, 1), H(3, j, c->foff, c->fc, 1), c->vblk(VR, j, 0)}},
                 B_HQP, nxy + c->yoff[i], c->db[i], c->db[y]);
   }
-  // ---- field projection tasks (spin-uniform row tiles) ----
+  // ---- field projection tasks: spin-uniform row ranges, 4x4 outputs per thread,
+  // tiles sized to the blocks (at most 128 rows or columns, 256 threads) ----
   c->htasks.clear();
+  auto cdiv = [](int a, int b) { return (a + b - 1) / b; };
   auto add_h = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
     const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
     const int seg[3] = {0, nu, d};
-    for (int s = 0; s < 2; ++s)
-      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += 32)
-        for (int b0 = 0; b0 < dc; b0 += 32) {
+    for (int s = 0; s < 2; ++s) {
+      const int nseg = seg[s + 1] - seg[s];
+      if (nseg <= 0) continue;
+      const int wa = cdiv(nseg, cdiv(nseg, 4 * HP_MAXR));
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += wa) {
+        const int na = std::min(wa, seg[s + 1] - a0), rows = cdiv(na, 4);
+        const int cmax = std::min<int>(HP_MAXC, 256 / rows);
+        const int wb = cdiv(dc, cdiv(dc, 4 * cmax));
+        for (int b0 = 0; b0 < dc; b0 += wb) {
           HTask h;
-          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = std::min(32, seg[s + 1] - a0);
-          h.b0 = b0; h.nbc = std::min(32, dc - b0); h.sa = s == 0 ? 1 : -1;
+          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = na;
+          h.b0 = b0; h.nbc = std::min(wb, dc - b0); h.sa = s == 0 ? 1 : -1;
           h.mode = mode; h.call = call; h.outq = outq; h.ooff = ooff;
+          h.rows = rows; h.cols = cdiv(h.nbc, 4);
           c->htasks.push_back(h);
         }
+      }
+    }
+  };
+  // tensor-core tiles: rows of the output block (N <= 128, padded to 16) against up to
+  // 64 columns x pg points (M = 128 = Re and Im of 64 hpsi rows)
+  c->htasks_tc.clear();
+  auto add_tc = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
+    const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
+    const int seg[3] = {0, nu, d};
+    for (int s = 0; s < 2; ++s) {
+      const int nseg = seg[s + 1] - seg[s];
+      if (nseg <= 0) continue;
+      const int wa = cdiv(nseg, cdiv(nseg, (int)HTC_MAXN));
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += wa) {
+        const int na = std::min(wa, seg[s + 1] - a0);
+        const int wb = cdiv(dc, cdiv(dc, (int)HTC_MAXB));
+        for (int b0 = 0; b0 < dc; b0 += wb) {
+          HTaskTC h;
+          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = na; h.b0 = b0; h.nbc = std::min(wb, dc - b0);
+          h.sa = s == 0 ? 1 : -1; h.mode = mode; h.call = call; h.outq = outq; h.ooff = ooff;
+          h.np = std::max(16, cdiv(na, 16) * 16);
+          h.pg = std::max(1, std::min<int>(HTC_MAXPG, HTC_MAXB / h.nbc));
+          c->htasks_tc.push_back(h);
+        }
+      }
+    }
   };
   for (int i = 0; i < nb; ++i) {
     if (c->fc[i] >= 0) { add_h(i, c->fc[i], 0, 0, 0, c->foff[i]); add_h(i, c->fc[i], 0, 1, 3, c->foff[i]); }
     if (c->xc[i] >= 0) add_h(i, c->xc[i], 1, 0, 1, c->xoff[i]);
     if (c->yc[i] >= 0) add_h(i, c->yc[i], 1, 1, 2, c->yoff[i]);
+    if (c->fc[i] >= 0) { add_tc(i, c->fc[i], 0, 0, 0, c->foff[i]); add_tc(i, c->fc[i], 0, 1, 3, c->foff[i]); }
+    if (c->xc[i] >= 0) add_tc(i, c->xc[i], 1, 0, 1, c->xoff[i]);
+    if (c->yc[i] >= 0) add_tc(i, c->yc[i], 1, 1, 2, c->yoff[i]);
   }
 }
 
@@ -368,7 +416,14 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   CK(dalloc(c->d_wre, (size_t)P));
   CK(dalloc(c->d_wim, (size_t)P));
   CK(dalloc(c->d_active, (size_t)P));
-  CK(dalloc(c->d_pint, (size_t)4 * P));
+  CK(dalloc(c->d_pint, (size_t)6 * P));
+  CK(dalloc(c->d_actlist, (size_t)P));
+  if (!c->d_err.p) {
+    CK(dalloc(c->d_err, 1));
+    CK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream));
+  }
+  CK(dalloc(c->d_act32, (size_t)P));
+  CK(dalloc(c->d_act64, (size_t)P));
   BufDesc bd[NBUF];
   bd[B_UP] = {c->d_up.p, 0, 0};
   bd[B_VP] = {c->d_vp.p, 0, 0};
@@ -401,7 +456,8 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
 // (H20, H02 stored), computed in precision T (the FP32 form reads the FP32
 // copy of the state and writes the FP32 hqp)
 template <class T>
-static int residual_t(pnfam_ctx* c, int P, const int* act, bool timed) {
+// P: batch size (grid extent), nact: points active in this evaluation
+static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed) {
   auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
   auto toc = [&](int k) {
     if (!timed) return;
@@ -435,10 +491,14 @@ static int residual_t(pnfam_ctx* c, int P, const int* act, bool timed) {
   d1.kap = rsp + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasisT<T> B = c->devbasis<T>();
+  // block-row groups: enough CTAs to fill the GPU twice over for the active points
+  const int ntr = (c->nghl + DRT - 1) / DRT;
+  const int na = std::max(nact, 1);
+  const int G = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
   tic();
   {
-    dim3 grid((c->nghl + DRT - 1) / DRT, c->G, 2 * P);
-    k_density<T><<<grid, 256, 0, c->stream>>>(B, d0, d1, c->G, dpart, act);
+    dim3 grid(ntr, G, 2 * P);
+    k_density<T><<<grid, 256, density_smem_bytes<T>(), c->stream>>>(B, d0, d1, G, dpart, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -446,14 +506,21 @@ static int residual_t(pnfam_ctx* c, int P, const int* act, bool timed) {
   tic();
   {
     dim3 grid((c->nghl + 127) / 128, 2 * P);
-    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, c->G, dpart, mf, act);
+    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, G, dpart, mf, act);
     c->launches++;
     CK(cudaGetLastError());
   }
   toc(2);
   tic();
-  {
-    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(T);
+  if constexpr (f32) {
+    // tensor cores: c->d_actlist holds the nact points of this evaluation
+    dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
+    k_hproj_tc<<<grid, 256, hproj_tc_smem_bytes(), c->stream>>>(B, c->d_htasks_tc.p, c->d_actlist.p, nact, mf, hsp,
+                                                                 nxy, c->d_err.p);
+    c->launches++;
+    CK(cudaGetLastError());
+  } else {
+    const size_t smem = hproj_smem_bytes<T>();
     dim3 grid((unsigned)c->htasks.size(), P);
     k_hproj<T><<<grid, 256, smem, c->stream>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
     c->launches++;
@@ -467,7 +534,6 @@ static int residual_t(pnfam_ctx* c, int P, const int* act, bool timed) {
   return PNFAM_OK;
 }
 
-static int residual(pnfam_ctx* c, int P, bool timed) { return residual_t<double>(c, P, c->d_active.p, timed); }
 
 // FP32 copies of the ground state and FP32 scratch for P points
 static int ensure_buffers32(pnfam_ctx* c, int P) {
@@ -492,8 +558,6 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   CK(dalloc(c->d_hqp32, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_dpart32, (size_t)P * 2 * c->G * 2 * ND * c->nghl));
   CK(dalloc(c->d_mf32, (size_t)P * 2 * NMF * 2 * c->nghl));
-  CK(dalloc(c->d_act32, (size_t)P));
-  CK(dalloc(c->d_act64, (size_t)P));
   CK(dalloc(c->d_xsave, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_radd, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_dmax, (size_t)P));
@@ -576,9 +640,12 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
   }
-  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-  if (cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-      cudaFuncSetAttribute(k_hproj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2)) != cudaSuccess) {
+  if (cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)hproj_smem_bytes<double>()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_hproj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)hproj_smem_bytes<float>()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_hproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)hproj_tc_smem_bytes()) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
   }
@@ -623,7 +690,6 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   CK(upload(c->d_ytoff, c->ytoff.data(), nb));
   // element -> (row state, column state) for the X|Y layout (Green's function)
   std::vector<int> erow(2 * nf), ecol(2 * nf);
-  const std::vector<double>* dummy = nullptr; (void)dummy;
   for (int part = 0; part < 2; ++part) {
     const std::vector<int>& cols = part == 0 ? c->xc : c->yc;
     const std::vector<long long>& off = part == 0 ? c->xoff : c->yoff;
@@ -644,6 +710,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   {
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+    c->nsm = std::max(nsm, 1);
     const int ntr = (c->nghl + DRT - 1) / DRT;
     int nrows = 0;
     for (int i = 0; i < nb; ++i) nrows += c->fc[i] >= 0;
@@ -654,6 +721,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   build_tasks(c);
   CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
   CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
+  CK(upload(c->d_htasks_tc, c->htasks_tc.data(), c->htasks_tc.size()));
   c->have_op = true;
   int rc = ensure_buffers(c, std::max(1, c->cap_P), std::max(1, c->cap_M));
   if (rc) return rc;
@@ -675,26 +743,63 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   return PNFAM_OK;
 }
 
-extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
-                               const pnfam_solver_opts_t* o, double* re_S, double* im_S, int* iters,
-                               double* si_out, double* hist) {
-  g_err.clear();
-  if (!c || !o || !re_w || !im_w || !re_S || !im_S || !iters || !si_out || P <= 0)
-    return fail(PNFAM_EINVAL, "pnfam_gpu_solve: bad argument");
-  if (!c->have_op) return fail(PNFAM_ESTATE, "pnfam_gpu_solve: call pnfam_gpu_set_operator first");
-  if (o->max_iter < 0) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: max_iter < 0");
+// ---------------------------------------------------------------------------
+// Solve engine: P slots on one context, each slot one omega point with its own
+// iteration counter and Broyden history (pnfam_solver.f90:114-209 per slot).
+// A slot is admitted with a point, iterated one evaluation per launch/finish
+// pair, and retired when it converges or reaches max_iter; a retired slot can
+// take the next point while the others keep iterating (continuous batching).
+// ---------------------------------------------------------------------------
+struct pnfam_engine {
+  pnfam_ctx* c = nullptr;
+  pnfam_solver_opts_t o{};
+  int P = 0, M = 0, bmode = BRO_BROYDEN, N = 0, nops = 1;
+  long long nxy = 0;
+  bool no_res = false, mixed = false, timed = false;
+  double switch_si = 0.0;
+  static constexpr double NEAR = 1000.0;
+  // per slot (host)
+  std::vector<int> active, it, anchor, since_best, nstall, fresh;
+  std::vector<long long> tag;
+  std::vector<double> si, sre, sim, best, wre, wim;
+  std::vector<unsigned long long> hdmax;
+  std::vector<int> pint, act32, act64, actlist;
+  int herr = 0;
+  std::vector<double> hsi, cpart;
+  double* hist = nullptr;   // optional [P][max_iter+1][3] (batch solve only)
+  bool dirty_w = true;
+  int pending = 0;          // an evaluation is in flight
+  struct Done { long long tag; int slot, iters; double si; };
+  std::vector<Done> done;
+  std::vector<double> done_re, done_im;  // [ndone][nops]
+};
+
+// a context freed before its engine leaves the engine without a context
+void pnfam_ctx::detach_engine() {
+  if (engine) {
+    cudaStreamSynchronize(stream);
+    engine->c = nullptr;
+    engine->pending = 0;
+    engine = nullptr;
+  }
+}
+
+static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver_opts_t* o) {
+  if (!c->have_op) return fail(PNFAM_ESTATE, "call pnfam_gpu_set_operator first");
+  if (o->max_iter < 0) return fail(PNFAM_EINVAL, "max_iter < 0");
   if (o->precision != 0 && o->precision != 1)
-    return fail(PNFAM_EINVAL, "pnfam_gpu_solve: precision must be 0 (FP64) or 1 (FP32 field, FP64 finish)");
-  const bool no_res = std::fabs(o->quench_residual_int) < 1e-10;
-  int M = no_res ? -1 : o->broyden_history_size;
-  if (M > 64) return fail(PNFAM_EINVAL, "pnfam_gpu_solve: broyden_history_size > 64 is not supported");
-  const long long nxy = c->nxy;
-  const int N = (int)(4 * nxy);
-  int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(M, 1), c->cap_M));
+    return fail(PNFAM_EINVAL, "precision must be 0 (FP64) or 1 (mixed FP32/FP64)");
+  e->c = c; e->o = *o; e->P = P;
+  e->no_res = std::fabs(o->quench_residual_int) < 1e-10;
+  e->M = e->no_res ? -1 : o->broyden_history_size;
+  if (e->M > 64) return fail(PNFAM_EINVAL, "broyden_history_size > 64 is not supported");
+  e->bmode = e->M < 0 ? BRO_NOMIX : e->M == 0 ? BRO_LINEAR : BRO_BROYDEN;
+  e->nxy = c->nxy; e->N = (int)(4 * c->nxy); e->nops = c->nops;
+  int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(e->M, 1), c->cap_M));
   if (rc) return rc;
-  c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(M, 1), c->cap_M);
-  const bool mixed = o->precision == 1 && !no_res;
-  if (mixed && (rc = ensure_buffers32(c, c->cap_P))) return rc;
+  c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(e->M, 1), c->cap_M);
+  e->mixed = o->precision == 1 && !e->no_res;
+  if (e->mixed && (rc = ensure_buffers32(c, c->cap_P))) return rc;
   // Mixed form (precision 1): one Broyden iteration per evaluation, as in the FP64
   // form, but the residual interaction is evaluated in FP32 on the increment
   // d = X - X_a from an anchor X_a whose image g(X_a) is known in FP64:
@@ -707,40 +812,78 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
   // an anchor or on a near increment evaluation; a far point takes an FP64 anchor
   // when si < 10^-reserved[1] (default 100*epsilon) or si stops falling (the FP32
   // noise floor).  Every evaluation counts against max_iter.
-  const double NEAR = 1000.0;
-  const double switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
+  e->switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
+  e->timed = o->reserved[0] != 0;
+  const int nops = e->nops;
+  e->active.assign(P, 0); e->it.assign(P, 0); e->anchor.assign(P, 1); e->since_best.assign(P, 0);
+  e->nstall.assign(P, 0); e->fresh.assign(P, 0); e->tag.assign(P, -1);
+  e->si.assign(P, 1.0); e->sre.assign((size_t)P * nops, 0.0); e->sim.assign((size_t)P * nops, 0.0);
+  e->best.assign(P, 1e300); e->wre.assign(P, 0.0); e->wim.assign(P, 0.0); e->hdmax.assign(P, 0);
+  e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
+  e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
   for (int k = 0; k < 8; ++k) c->stage_ms[k] = 0.0;
-  c->pit64 = 0; c->pit32 = 0;
-  c->launches = 0;
-  const bool timed = o->reserved[0] != 0;
-  CK(cudaEventRecord(c->evt[0], c->stream));
-  CK(cudaMemsetAsync(c->d_state.p, 0, sizeof(double) * (size_t)P * N, c->stream));
-  CK(cudaMemcpyAsync(c->d_wre.p, re_w, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->d_wim.p, im_w, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
-  const int nops = c->nops;
-  std::vector<double> si(P, 1.0), sre((size_t)P * nops, 0.0), sim((size_t)P * nops, 0.0);
-  std::vector<int> active(P, 1), conv(P, -1), anchor(P, 1);
-  // host copy of the per-point integer block: [0] Broyden iteration, [1] Broyden mode,
-  // [2] increment evaluation, [3] anchor evaluation
-  std::vector<int> pint((size_t)4 * P, 0), act32(P, 0), act64(P, 0);
-  std::vector<double> best(P, 1e300);
-  std::vector<int> since_best(P, 0), nstall(P, 0);
-  std::vector<double> hsi(P), cpart((size_t)P * c->nchunk_c * 2 * nops);
-  std::vector<unsigned long long> hdmax(P, 0);
-  const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
-  const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
-  int* d_itp = c->d_pint.p;
-  int* d_mode = c->d_pint.p + P;
-  int* d_incr = c->d_pint.p + 2 * P;
-  int* d_anch = c->d_pint.p + 3 * P;
-  BroState S;
-  S.N = N; S.M = std::max(M, 1); S.alpha = o->alpha_mix;
-  S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
-  S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
-  S.itp = d_itp; S.modep = d_mode;
-  const double w0 = 0.01;
-  const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
-  const dim3 vgrid((unsigned)std::min<long long>(2048, (N + 255) / 256), P);
+  c->pit64 = 0; c->pit32 = 0; c->launches = 0;
+  return PNFAM_OK;
+}
+
+static void engine_retire(pnfam_engine* e, int p, int iters) {
+  e->done.push_back({e->tag[p], p, iters, e->si[p]});
+  for (int k = 0; k < e->nops; ++k) {
+    e->done_re.push_back(e->sre[(size_t)p * e->nops + k]);
+    e->done_im.push_back(e->sim[(size_t)p * e->nops + k]);
+  }
+  e->active[p] = 0;
+}
+
+static void engine_hist(pnfam_engine* e, int p) {
+  if (!e->hist) return;
+  double* h = e->hist + ((size_t)p * (e->o.max_iter + 1) + e->it[p]) * 3;
+  h[0] = e->si[p]; h[1] = e->sre[(size_t)p * e->nops]; h[2] = e->sim[(size_t)p * e->nops];
+}
+
+// admit up to n points into free slots; returns the number admitted
+static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double* im_w, const long long* tags) {
+  int k = 0;
+  for (int p = 0; p < e->P && k < n; ++p) {
+    if (e->active[p]) continue;
+    e->active[p] = 1; e->it[p] = 0; e->anchor[p] = 1; e->since_best[p] = 0; e->nstall[p] = 0;
+    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1;
+    for (int q = 0; q < e->nops; ++q) { e->sre[(size_t)p * e->nops + q] = 0.0; e->sim[(size_t)p * e->nops + q] = 0.0; }
+    e->wre[p] = re_w[k]; e->wim[p] = im_w[k];
+    e->tag[p] = tags ? tags[k] : k;
+    e->dirty_w = true;
+    engine_hist(e, p);
+    if (e->o.max_iter == 0) engine_retire(e, p, -1);
+    ++k;
+  }
+  return k;
+}
+
+// enqueue one evaluation (and Broyden step) for every active slot
+static int engine_launch(pnfam_engine* e) {
+  pnfam_ctx* c = e->c;
+  const int P = e->P, N = e->N;
+  const long long nxy = e->nxy;
+  int nact = 0, n32 = 0, n64 = 0, nanch = 0, nfresh = 0, any_bro = 0;
+  for (int p = 0; p < P; ++p) {
+    const bool a = e->active[p] != 0, first = a && e->it[p] == 0;
+    const bool lo = e->mixed && !e->anchor[p];
+    e->act32[p] = a && lo && !first;
+    e->act64[p] = a && !lo && !first;
+    nact += a; n32 += e->act32[p]; n64 += e->act64[p];
+    e->pint[p] = e->it[p];
+    e->pint[P + p] = first && e->bmode == BRO_BROYDEN ? BRO_LINEAR : e->bmode;
+    e->pint[2 * P + p] = e->act32[p];
+    e->pint[3 * P + p] = a && e->mixed && e->anchor[p];
+    e->pint[4 * P + p] = first;  // the field of X = 0 vanishes: no evaluation
+    e->pint[5 * P + p] = a && e->fresh[p];
+    nanch += e->pint[3 * P + p]; nfresh += e->pint[5 * P + p];
+    any_bro |= a && e->pint[P + p] == BRO_BROYDEN;
+    e->fresh[p] = 0;
+  }
+  if (nact == 0) return PNFAM_OK;
+  c->pit32 += n32; c->pit64 += n64;
+  const bool timed = e->timed;
   auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
   auto toc = [&](int k) {
     if (!timed) return;
@@ -750,132 +893,181 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
     c->stage_ms[k] += ms;
   };
-  const int bmode = M < 0 ? BRO_NOMIX : M == 0 ? BRO_LINEAR : BRO_BROYDEN;
-  for (int it = 0; it <= o->max_iter; ++it) {
-    int nact = 0;
-    for (int p = 0; p < P; ++p) {
-      if (!active[p]) continue;
-      if (hist) {
-        double* h = hist + ((size_t)p * (o->max_iter + 1) + it) * 3;
-        h[0] = si[p]; h[1] = sre[(size_t)p * nops]; h[2] = sim[(size_t)p * nops];
-      }
-      if (it > 0) {
-        // si[p] is the residual of the evaluation made at it - 1
-        if (!mixed || anchor[p]) {
-          if (si[p] < o->convergence_epsilon) { conv[p] = it; active[p] = 0; continue; }
-          if (mixed) { anchor[p] = 0; best[p] = si[p]; since_best[p] = 0; }
-        } else {
-          double dm;
-          std::memcpy(&dm, &hdmax[p], sizeof dm);
-          const bool near = dm <= NEAR * o->convergence_epsilon;
-          if (si[p] < o->convergence_epsilon && near) { conv[p] = it; active[p] = 0; continue; }
-          if (si[p] < best[p] * 0.5) { best[p] = si[p]; since_best[p] = 0; } else { ++since_best[p]; }
-          // the stagnation window doubles with every anchor it has triggered
-          const bool stalled = since_best[p] >= (5 << std::min(nstall[p], 4));
-          if (!near && (si[p] < switch_si || stalled)) { anchor[p] = 1; nstall[p] += stalled; }
-        }
-      }
-      if (it == o->max_iter) { conv[p] = -1; active[p] = 0; continue; }
-      ++nact;
-    }
-    if (nact == 0) break;
-    int n32 = 0, n64 = 0, nanch = 0;
-    for (int p = 0; p < P; ++p) {
-      const bool lo = mixed && !anchor[p];
-      act32[p] = active[p] && lo && it > 0;
-      act64[p] = active[p] && !lo && it > 0;
-      n32 += act32[p]; n64 += act64[p];
-      pint[p] = it;
-      pint[P + p] = it == 0 && bmode == BRO_BROYDEN ? BRO_LINEAR : bmode;
-      pint[2 * P + p] = act32[p];
-      pint[3 * P + p] = active[p] && mixed && anchor[p];
-      nanch += pint[3 * P + p];
-    }
-    c->pit32 += n32; c->pit64 += n64;
-    CK(cudaMemcpyAsync(c->d_active.p, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_pint.p, pint.data(), sizeof(int) * 4 * P, cudaMemcpyHostToDevice, c->stream));
-    const int* act = c->d_active.p;
-    // the residual interaction of X = 0 vanishes: iteration 0 needs no field evaluation
-    if (!no_res && it > 0) {
-      if (!mixed) {
-        if ((rc = residual(c, P, timed))) return rc;
-      } else {
-        CK(cudaMemcpyAsync(c->d_act32.p, act32.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync(c->d_act64.p, act64.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-        if (n64 && (rc = residual_t<double>(c, P, c->d_act64.p, timed))) return rc;
-        if (n32) {
-          CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
-          k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
-                                                 c->d_dmax.p);
-          if ((rc = residual_t<float>(c, P, c->d_act32.p, timed))) return rc;
-          k_to_f64<<<vgrid, 256, 0, c->stream>>>(c->d_hqp32.p, c->d_hqp.p, N, N, c->d_act32.p);
-          c->launches += 2;
-          CK(cudaGetLastError());
-        }
-      }
-    }
-    tic();
-    {
-      dim3 grid(gx, P);
-      k_green<<<grid, 256, 0, c->stream>>>(nxy, P, no_res || it == 0 ? nullptr : c->d_hqp.p, c->d_fops.p,
-                                           c->d_erow.p, c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
-                                           o->quench_residual_int, c->d_vout.p, act, mixed ? d_incr : nullptr,
-                                           c->d_radd.p);
-      c->launches++;
-      if (nanch) {  // new anchors: X_a = X, g(X_a) = vout
-        k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_xsave.p, c->d_state.p, N, d_anch);
-        k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_radd.p, c->d_vout.p, N, d_anch);
+  int* d_itp = c->d_pint.p;
+  int* d_mode = c->d_pint.p + P;
+  int* d_incr = c->d_pint.p + 2 * P;
+  int* d_anch = c->d_pint.p + 3 * P;
+  int* d_zero = c->d_pint.p + 4 * P;
+  int* d_fresh = c->d_pint.p + 5 * P;
+  const dim3 vgrid((unsigned)std::min<long long>(2048, (N + 255) / 256), P);
+  CK(cudaMemcpyAsync(c->d_active.p, e->active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_pint.p, e->pint.data(), sizeof(int) * 6 * P, cudaMemcpyHostToDevice, c->stream));
+  if (e->dirty_w) {
+    CK(cudaMemcpyAsync(c->d_wre.p, e->wre.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_wim.p, e->wim.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+    e->dirty_w = false;
+  }
+  if (nfresh) {  // newly admitted slots start from X = 0
+    k_vecop<<<vgrid, 256, 0, c->stream>>>(2, 0.0, c->d_state.p, nullptr, N, d_fresh);
+    c->launches++;
+  }
+  const int* act = c->d_active.p;
+  int rc;
+  if (!e->no_res) {
+    CK(cudaMemcpyAsync(c->d_act64.p, e->act64.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+    if (n64 && (rc = residual_t<double>(c, P, n64, c->d_act64.p, timed))) return rc;
+    if (e->mixed) {
+      CK(cudaMemcpyAsync(c->d_act32.p, e->act32.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+      if (n32) {
+        e->actlist.clear();
+        for (int p = 0; p < P; ++p)
+          if (e->act32[p]) e->actlist.push_back(p);
+        CK(cudaMemcpyAsync(c->d_actlist.p, e->actlist.data(), sizeof(int) * n32, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
+        k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
+                                               c->d_dmax.p);
+        if ((rc = residual_t<float>(c, P, n32, c->d_act32.p, timed))) return rc;
+        k_to_f64<<<vgrid, 256, 0, c->stream>>>(c->d_hqp32.p, c->d_hqp.p, N, N, c->d_act32.p);
         c->launches += 2;
+        CK(cudaGetLastError());
       }
-      CK(cudaGetLastError());
     }
-    toc(5);
-    // ---- Broyden (pnfam_broyden.f90:117-216), each point at its own iteration ----
-    tic();
-    {
-      const bool any_broyden = bmode == BRO_BROYDEN && it > 0;
-      dim3 grid(c->nchunk_bro, P);
-      k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
-      k_bro_solve<<<P, 32, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+  }
+  const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
+  const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
+  tic();
+  {
+    const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
+    k_green<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, P, e->no_res ? nullptr : c->d_hqp.p, c->d_fops.p, c->d_erow.p,
+                                                c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
+                                                e->o.quench_residual_int, c->d_vout.p, act,
+                                                e->mixed ? d_incr : nullptr, c->d_radd.p, d_zero);
+    c->launches++;
+    if (nanch) {  // new anchors: X_a = X, g(X_a) = vout
+      k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_xsave.p, c->d_state.p, N, d_anch);
+      k_vecop<<<vgrid, 256, 0, c->stream>>>(0, 0.0, c->d_radd.p, c->d_vout.p, N, d_anch);
       c->launches += 2;
-      if (any_broyden) {
-        k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
-        k_bro_solve<<<P, 32, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
-        c->launches += 2;
-      }
-      dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
-      k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
-      c->launches++;
-      CK(cudaGetLastError());
     }
-    toc(6);
-    tic();
-    {
-      dim3 grid(c->nchunk_c, P);
-      k_contract<<<grid, 256, 0, c->stream>>>(nxy, nops, c->d_fops.p, c->d_state.p, c->nchunk_c, c->d_cpart.p, act);
-      c->launches++;
-      CK(cudaGetLastError());
+    CK(cudaGetLastError());
+  }
+  toc(5);
+  // ---- Broyden (pnfam_broyden.f90:117-216), each slot at its own iteration ----
+  tic();
+  {
+    BroState S;
+    S.N = N; S.M = std::max(e->M, 1); S.alpha = e->o.alpha_mix;
+    S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
+    S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
+    S.itp = d_itp; S.modep = d_mode;
+    const double w0 = 0.01;
+    dim3 grid(c->nchunk_bro, P);
+    k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
+    k_bro_solve<<<P, 256, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+    c->launches += 2;
+    if (any_bro) {
+      k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
+      k_bro_solve<<<P, 256, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+      c->launches += 2;
     }
-    CK(cudaMemcpyAsync(hsi.data(), c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
-    if (mixed)
-      CK(cudaMemcpyAsync(hdmax.data(), c->d_dmax.p, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(cpart.data(), c->d_cpart.p, sizeof(double) * cpart.size(), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    toc(7);
-    const double pi = 3.141592653589793238462643;
-    for (int p = 0; p < P; ++p) {
-      if (!active[p]) continue;
-      si[p] = hsi[p];
-      if (!std::isfinite(si[p])) return fail(PNFAM_ENONFINITE, "pnfam_gpu_solve: non-finite residual");
-      for (int k = 0; k < nops; ++k) {
-        double a = 0.0, b = 0.0;
-        for (int ch = 0; ch < c->nchunk_c; ++ch) {
-          a += cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k];
-          b += cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k + 1];
-        }
-        sre[(size_t)p * nops + k] = -a / pi;
-        sim[(size_t)p * nops + k] = -b / pi;
+    dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
+    k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
+    c->launches++;
+    CK(cudaGetLastError());
+  }
+  toc(6);
+  tic();
+  {
+    dim3 grid(c->nchunk_c, P);
+    k_contract<<<grid, 256, 0, c->stream>>>(nxy, e->nops, c->d_fops.p, c->d_state.p, c->nchunk_c, c->d_cpart.p, act);
+    c->launches++;
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(e->hsi.data(), c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+  if (e->mixed)
+    CK(cudaMemcpyAsync(e->hdmax.data(), c->d_dmax.p, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaMemcpyAsync(e->cpart.data(), c->d_cpart.p, sizeof(double) * e->cpart.size(), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaMemcpyAsync(&e->herr, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (timed) toc(7);
+  e->pending = 1;
+  return PNFAM_OK;
+}
+
+// wait for the evaluation in flight, update every active slot and retire the
+// slots that converged or reached max_iter
+static int engine_finish(pnfam_engine* e) {
+  if (!e->pending) return PNFAM_OK;
+  pnfam_ctx* c = e->c;
+  CK(cudaStreamSynchronize(c->stream));
+  e->pending = 0;
+  if (e->herr) {
+    cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream);
+    e->herr = 0;
+    return fail(PNFAM_ECUDA, "a wait on the tensor cores gave up (field projection)");
+  }
+  const pnfam_solver_opts_t& o = e->o;
+  const int nops = e->nops;
+  const double pi = 3.141592653589793238462643;
+  for (int p = 0; p < e->P; ++p) {
+    if (!e->active[p]) continue;
+    const bool was_anchor = !e->mixed || e->anchor[p] || e->it[p] == 0;
+    e->si[p] = e->hsi[p];
+    if (!std::isfinite(e->si[p])) return fail(PNFAM_ENONFINITE, "non-finite residual");
+    for (int k = 0; k < nops; ++k) {
+      double a = 0.0, b = 0.0;
+      for (int ch = 0; ch < c->nchunk_c; ++ch) {
+        a += e->cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k];
+        b += e->cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k + 1];
       }
+      e->sre[(size_t)p * nops + k] = -a / pi;
+      e->sim[(size_t)p * nops + k] = -b / pi;
+    }
+    const int it = ++e->it[p];
+    engine_hist(e, p);
+    const double si = e->si[p];
+    if (was_anchor) {
+      if (si < o.convergence_epsilon) { engine_retire(e, p, it); continue; }
+      if (e->mixed) { e->anchor[p] = 0; e->best[p] = si; e->since_best[p] = 0; }
+    } else {
+      double dm;
+      std::memcpy(&dm, &e->hdmax[p], sizeof dm);
+      const bool near = dm <= pnfam_engine::NEAR * o.convergence_epsilon;
+      if (si < o.convergence_epsilon && near) { engine_retire(e, p, it); continue; }
+      if (si < e->best[p] * 0.5) { e->best[p] = si; e->since_best[p] = 0; } else { ++e->since_best[p]; }
+      // the stagnation window doubles with every anchor it has triggered
+      const bool stalled = e->since_best[p] >= (5 << std::min(e->nstall[p], 4));
+      if (!near && (si < e->switch_si || stalled)) { e->anchor[p] = 1; e->nstall[p] += stalled; }
+    }
+    if (it == o.max_iter) engine_retire(e, p, -1);
+  }
+  return PNFAM_OK;
+}
+
+static int engine_nactive(const pnfam_engine* e) {
+  int n = 0;
+  for (int a : e->active) n += a;
+  return n;
+}
+
+extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
+                               const pnfam_solver_opts_t* o, double* re_S, double* im_S, int* iters,
+                               double* si_out, double* hist) {
+  g_err.clear();
+  if (!c || !o || !re_w || !im_w || !re_S || !im_S || !iters || !si_out || P <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_solve: bad argument");
+  if (c->engine) return fail(PNFAM_ESTATE, "pnfam_gpu_solve: the context's solve buffers belong to an engine");
+  pnfam_engine e;
+  int rc = engine_setup(&e, c, P, o);
+  if (rc) { g_err = "pnfam_gpu_solve: " + g_err; return rc; }
+  e.hist = hist;
+  CK(cudaEventRecord(c->evt[0], c->stream));
+  engine_admit(&e, P, re_w, im_w, nullptr);
+  while (engine_nactive(&e) > 0) {
+    if ((rc = engine_launch(&e)) || (rc = engine_finish(&e))) {
+      cudaStreamSynchronize(c->stream);
+      g_err = "pnfam_gpu_solve: " + g_err;
+      return rc;
     }
   }
   CK(cudaEventRecord(c->evt[1], c->stream));
@@ -885,15 +1077,85 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
     cudaEventElapsedTime(&ms, c->evt[0], c->evt[1]);
     c->total_ms = ms;
   }
-  for (int p = 0; p < P; ++p) {
-    iters[p] = conv[p];
-    si_out[p] = si[p];
-    for (int k = 0; k < nops; ++k) {
-      re_S[(size_t)p * nops + k] = sre[(size_t)p * nops + k];
-      im_S[(size_t)p * nops + k] = sim[(size_t)p * nops + k];
+  const int nops = c->nops;
+  for (size_t k = 0; k < e.done.size(); ++k) {
+    const int p = (int)e.done[k].tag;
+    iters[p] = e.done[k].iters;
+    si_out[p] = e.done[k].si;
+    for (int q = 0; q < nops; ++q) {
+      re_S[(size_t)p * nops + q] = e.done_re[k * nops + q];
+      im_S[(size_t)p * nops + q] = e.done_im[k * nops + q];
     }
   }
   return PNFAM_OK;
+}
+
+// ---- continuous-batching engine (C ABI) ----
+extern "C" int pnfam_gpu_engine_create(pnfam_ctx_t* c, int slots, const pnfam_solver_opts_t* o,
+                                       pnfam_engine_t** out) {
+  g_err.clear();
+  if (!c || !o || !out || slots <= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_engine_create: bad argument");
+  if (c->engine) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_create: the context already has an engine");
+  pnfam_engine* e = new pnfam_engine;
+  int rc = engine_setup(e, c, slots, o);
+  if (rc) { delete e; g_err = "pnfam_gpu_engine_create: " + g_err; return rc; }
+  c->engine = e;
+  *out = e;
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_engine_admit(pnfam_engine_t* e, int n, const double* re_w, const double* im_w,
+                                      const long long* tags) {
+  g_err.clear();
+  if (!e || n < 0 || (n > 0 && (!re_w || !im_w))) return -fail(PNFAM_EINVAL, "pnfam_gpu_engine_admit: bad argument");
+  if (!e->c) return -fail(PNFAM_ESTATE, "pnfam_gpu_engine_admit: the context was freed");
+  if (e->pending) return -fail(PNFAM_ESTATE, "pnfam_gpu_engine_admit: an evaluation is in flight");
+  return engine_admit(e, n, re_w, im_w, tags);
+}
+
+extern "C" int pnfam_gpu_engine_launch(pnfam_engine_t* e) {
+  g_err.clear();
+  if (!e) return fail(PNFAM_EINVAL, "pnfam_gpu_engine_launch: NULL engine");
+  if (!e->c) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: the context was freed");
+  if (e->pending) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: an evaluation is in flight");
+  const int rc = engine_launch(e);
+  if (rc) { cudaStreamSynchronize(e->c->stream); e->pending = 0; g_err = "pnfam_gpu_engine_launch: " + g_err; }
+  return rc;
+}
+
+extern "C" int pnfam_gpu_engine_finish(pnfam_engine_t* e, int maxout, long long* tags, double* re_S, double* im_S,
+                                       int* iters, double* si, int* nout) {
+  g_err.clear();
+  if (!e || !nout || maxout < 0 || (maxout > 0 && (!tags || !re_S || !im_S || !iters || !si)))
+    return fail(PNFAM_EINVAL, "pnfam_gpu_engine_finish: bad argument");
+  if (!e->c) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_finish: the context was freed");
+  int rc = engine_finish(e);
+  if (rc) { g_err = "pnfam_gpu_engine_finish: " + g_err; return rc; }
+  const int nops = e->nops;
+  const int n = std::min<int>(maxout, (int)e->done.size());
+  for (int k = 0; k < n; ++k) {
+    tags[k] = e->done[k].tag; iters[k] = e->done[k].iters; si[k] = e->done[k].si;
+    for (int q = 0; q < nops; ++q) {
+      re_S[(size_t)k * nops + q] = e->done_re[(size_t)k * nops + q];
+      im_S[(size_t)k * nops + q] = e->done_im[(size_t)k * nops + q];
+    }
+  }
+  e->done.erase(e->done.begin(), e->done.begin() + n);
+  e->done_re.erase(e->done_re.begin(), e->done_re.begin() + (size_t)n * nops);
+  e->done_im.erase(e->done_im.begin(), e->done_im.begin() + (size_t)n * nops);
+  *nout = n;
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_engine_active(const pnfam_engine_t* e) { return e ? engine_nactive(e) : 0; }
+
+extern "C" void pnfam_gpu_engine_free(pnfam_engine_t* e) {
+  if (!e) return;
+  if (e->c) {
+    if (e->pending) cudaStreamSynchronize(e->c->stream);
+    e->c->engine = nullptr;
+  }
+  delete e;
 }
 
 extern "C" int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* c, const double* re_rho_pn, const double* im_rho_pn,
@@ -929,15 +1191,72 @@ extern "C" int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* c, const double* re_rho_p
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasis B = c->devbasis<double>();
   const int* act = c->d_active.p;
-  k_density<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p, act);
+  k_density<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<double>(), c->stream>>>(
+      B, d0, d1, c->G, c->d_dpart.p, act);
   k_meanfield<<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
-  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-  k_hproj<<<dim3((unsigned)c->htasks.size(), 1), 256, smem, c->stream>>>(B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
+  k_hproj<<<dim3((unsigned)c->htasks.size(), 1), 256, hproj_smem_bytes<double>(), c->stream>>>(
+      B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
   for (int k = 0; k < 8; ++k)
     CK(cudaMemcpyAsync(outp[k], c->d_hsp.p + (k & 1) * 4 * nxy + qout[k] * nxy, nb, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* c, const double* re_rho_pn, const double* im_rho_pn,
+                                                const double* re_kp, const double* im_kp, const double* re_rho_np,
+                                                const double* im_rho_np, const double* re_km, const double* im_km,
+                                                double* re_h_pn, double* im_h_pn, double* re_dp, double* im_dp,
+                                                double* re_h_np, double* im_h_np, double* re_dm, double* im_dm) {
+  g_err.clear();
+  if (!c) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_mixed: NULL context");
+  if (!c->have_op) return fail(PNFAM_ESTATE, "pnfam_gpu_calc_hamiltonian_mixed: call pnfam_gpu_set_operator first");
+  const void* in[8] = {re_rho_pn, im_rho_pn, re_kp, im_kp, re_rho_np, im_rho_np, re_km, im_km};
+  void* outp[8] = {re_h_pn, im_h_pn, re_dp, im_dp, re_h_np, im_h_np, re_dm, im_dm};
+  for (int k = 0; k < 8; ++k)
+    if (!in[k] || !outp[k]) return fail(PNFAM_EINVAL, "pnfam_gpu_calc_hamiltonian_mixed: NULL array");
+  int rc = ensure_buffers(c, std::max(1, c->cap_P), std::max(1, c->cap_M));
+  if (rc) return rc;
+  c->cap_P = std::max(1, c->cap_P); c->cap_M = std::max(1, c->cap_M);
+  if ((rc = ensure_buffers32(c, c->cap_P))) return rc;
+  const long long nxy = c->nxy;
+  const size_t nb = sizeof(double) * nxy;
+  const int qin[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(c->d_rsp.p + (k & 1) * 4 * nxy + qin[k] * nxy, in[k], nb, cudaMemcpyHostToDevice, c->stream));
+  std::vector<int> one = {1}, zero = {0};
+  CK(cudaMemcpyAsync(c->d_active.p, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_actlist.p, zero.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  k_to_f32<<<1024, 256, 0, c->stream>>>(c->d_rsp.p, c->d_rsp32.p, 8 * nxy, 1, 0, nullptr);
+  DensCallT<float> d0, d1;
+  d0.rho = c->d_rsp32.p + 0 * nxy; d0.rho_sp = 8 * nxy; d0.rho_spl = 4 * nxy;
+  d0.rcols = c->d_fc.p; d0.roffs = c->d_foff.p;
+  d0.kap = c->d_rsp32.p + 1 * nxy; d0.kap_sp = 8 * nxy; d0.kap_spl = 4 * nxy;
+  d0.kcols = c->d_xtc.p; d0.koffs = c->d_xtoff.p;
+  d1.rho = c->d_rsp32.p + 3 * nxy; d1.rho_sp = 8 * nxy; d1.rho_spl = 4 * nxy;
+  d1.rcols = c->d_fc.p; d1.roffs = c->d_foff.p;
+  d1.kap = c->d_rsp32.p + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
+  d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
+  const DevBasisT<float> B = c->devbasis<float>();
+  const int* act = c->d_active.p;
+  k_density<float><<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<float>(), c->stream>>>(
+      B, d0, d1, c->G, c->d_dpart32.p, act);
+  k_meanfield<float><<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart32.p, c->d_mf32.p, act);
+  k_hproj_tc<<<dim3((unsigned)c->htasks_tc.size(), 1), 256, hproj_tc_smem_bytes(), c->stream>>>(
+      B, c->d_htasks_tc.p, c->d_actlist.p, 1, c->d_mf32.p, c->d_hsp32.p, nxy, c->d_err.p);
+  k_to_f64<<<dim3(1024, 1), 256, 0, c->stream>>>(c->d_hsp32.p, c->d_hsp.p, 8 * nxy, 0, nullptr);
+  CK(cudaGetLastError());
+  const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
+  for (int k = 0; k < 8; ++k)
+    CK(cudaMemcpyAsync(outp[k], c->d_hsp.p + (k & 1) * 4 * nxy + qout[k] * nxy, nb, cudaMemcpyDeviceToHost, c->stream));
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (herr) {
+    cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream);
+    return fail(PNFAM_ECUDA, "pnfam_gpu_calc_hamiltonian_mixed: a wait on the tensor cores gave up");
+  }
   return PNFAM_OK;
 }
 
@@ -1011,8 +1330,8 @@ int noalloc_setup(unsigned char** out) {
     if (e != cudaSuccess)
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaGetSymbolAddress: ") +
                                    cudaGetErrorString(e));
-    const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-    e = cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hproj_smem_bytes<double>());
     if (e != cudaSuccess)
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaFuncSetAttribute: ") +
                                    cudaGetErrorString(e));
@@ -1141,10 +1460,10 @@ extern "C" int pnfam_gpu_calc_hamiltonian_noalloc(
   d1.rcols = ints + 3 * NA_MAX_NB; d1.roffs = longs;
   d1.kap = rsp + 2 * nf; d1.kap_sp = 8 * nf; d1.kap_spl = 4 * nf;
   d1.kcols = ints + 5 * NA_MAX_NB; d1.koffs = longs + 2 * NA_MAX_NB;
-  k_density<<<dim3((nghl + DRT - 1) / DRT, NA_G, 2), 256, 0, st>>>(B, d0, d1, NA_G, dpart, act);
+  k_density<<<dim3((nghl + DRT - 1) / DRT, NA_G, 2), 256, density_smem_bytes<double>(), st>>>(B, d0, d1, NA_G,
+                                                                                             dpart, act);
   k_meanfield<<<dim3((nghl + 127) / 128, 2), 128, 0, st>>>(B, NA_G, dpart, mf, act);
-  const size_t smem = (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
-  k_hproj<<<dim3((unsigned)c.htasks.size(), 1), 256, smem, st>>>(B, dtasks, mf, hsp, nf, act);
+  k_hproj<<<dim3((unsigned)c.htasks.size(), 1), 256, hproj_smem_bytes<double>(), st>>>(B, dtasks, mf, hsp, nf, act);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
   for (int k = 0; k < 8; ++k)

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tc.cuh"
+
 namespace pnfam {
 
 // ---------------------------------------------------------------------------
@@ -149,23 +151,130 @@ struct DensCallT {
 };
 using DensCall = DensCallT<double>;
 
-#define DRT 32   // mesh points per CTA
-#define DBC 8    // b columns per chunk
-#define DAK 16   // a rows per chunk
-
-template <class T>
-__device__ __forceinline__ T red8(T v) {
-  v += __shfl_xor_sync(0xffffffffu, v, 4);
-  v += __shfl_xor_sync(0xffffffffu, v, 2);
-  v += __shfl_xor_sync(0xffffffffu, v, 1);
-  return v;
+// four consecutive elements from shared memory (16-byte aligned) as 128-bit loads
+__device__ __forceinline__ void lds4(const float* p, float (&v)[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&v)[4]) {
+  const double2 t0 = reinterpret_cast<const double2*>(p)[0], t1 = reinterpret_cast<const double2*>(p)[1];
+  v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
 }
 
-// grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT r x DBC b
-// dpart: [P][2][G][2*ND][nghl]
+#define DRT 32   // mesh points per CTA
+
+// b columns per thread: 4 consecutive columns per lane, 8 lanes
+template <class T> struct DensTile {
+  static constexpr int BT = 4;
+  static constexpr int BW = 8 * BT;              // b columns per chunk (8 lanes x BT)
+  static constexpr int BWP = BW + 4;             // padded row: conflict-free transposed staging
+  static constexpr int AK = sizeof(T) >= 8 ? 16 : 32;  // a rows per chunk
+};
+
 template <class T>
-__global__ void __launch_bounds__(256) k_density(DevBasisT<T> B, DensCallT<T> c0, DensCallT<T> c1, int G,
-                                                 T* __restrict__ dpart, const int* __restrict__ active) {
+__host__ __device__ constexpr size_t density_smem_bytes() {
+  return (size_t)(DensTile<T>::AK * DRT * 4 + 2 * DensTile<T>::AK * DensTile<T>::BWP) * sizeof(T);
+}
+
+// contributions of one column b at one mesh point from the rows of the SAME spin
+// as b (S) or of the OPPOSITE spin (O); P = phi_q(b, r), sg = spin of b,
+// sig = +1 if b is spin down (pnfam_hamiltonian_blas.f90:124-711)
+template <class T>
+__device__ __forceinline__ void dens_same(T (&acc)[2 * ND], const T (&Sr)[4], const T (&Si)[4], const T (&P)[4],
+                                          T sg) {
+  const T h5 = T(0.5);
+#define ACC(k, re, im) { acc[2 * (k)] += (re); acc[2 * (k) + 1] += (im); }
+  T xr, xi;
+  xr = Sr[0] * P[0]; xi = Si[0] * P[0];
+  ACC(D_RHO, xr, xi);
+  ACC(D_SZ, sg * xr, sg * xi);
+  xr = h5 * (Sr[0] * P[2] + Sr[2] * P[0]); xi = h5 * (Si[0] * P[2] + Si[2] * P[0]);
+  ACC(D_JP, xr, xi);
+  ACC(D_TJPZ, sg * xr, sg * xi);
+  xr = Sr[1] * P[1] + Sr[2] * P[2] + Sr[3] * P[3]; xi = Si[1] * P[1] + Si[2] * P[2] + Si[3] * P[3];
+  ACC(D_TAU, xr, xi);
+  ACC(D_TZ, sg * xr, sg * xi);
+  xr = h5 * (Sr[0] * P[1] - Sr[1] * P[0]); xi = h5 * (Si[0] * P[1] - Si[1] * P[0]);
+  ACC(D_JR, -xi, xr);
+  ACC(D_TJRZ, -sg * xi, sg * xr);
+  xr = h5 * (Sr[0] * P[3] - Sr[3] * P[0]); xi = h5 * (Si[0] * P[3] - Si[3] * P[0]);
+  ACC(D_JZ, -xi, xr);
+  ACC(D_TJZZ, -sg * xi, sg * xr);
+  ACC(D_GS, sg * (Sr[0] * P[3] + Sr[3] * P[0]), sg * (Si[0] * P[3] + Si[3] * P[0]));
+  ACC(D_FR, h5 * sg * (Sr[1] * P[3] + Sr[3] * P[1]), h5 * sg * (Si[1] * P[3] + Si[3] * P[1]));
+  {
+    const T ar = h5 * sg * (Sr[2] * P[3] - Sr[3] * P[2]), ai = h5 * sg * (Si[2] * P[3] - Si[3] * P[2]);
+    ACC(D_FP, -ai, ar);
+  }
+  ACC(D_FZ, sg * Sr[3] * P[3], sg * Si[3] * P[3]);
+}
+
+template <class T>
+__device__ __forceinline__ void dens_opp(T (&acc)[2 * ND], const T (&Or)[4], const T (&Oi)[4], const T (&P)[4],
+                                         T sig) {
+  const T h5 = T(0.5);
+  T xr, xi;
+  ACC(D_GS, sig * (Or[0] * P[2] - Or[2] * P[0]) + (Or[0] * P[1] + Or[1] * P[0]),
+      sig * (Oi[0] * P[2] - Oi[2] * P[0]) + (Oi[0] * P[1] + Oi[1] * P[0]));
+  ACC(D_FR, Or[1] * P[1] + sig * h5 * (Or[1] * P[2] - Or[2] * P[1]),
+      Oi[1] * P[1] + sig * h5 * (Oi[1] * P[2] - Oi[2] * P[1]));
+  {
+    const T ar = sig * Or[2] * P[2] + h5 * (Or[2] * P[1] - Or[1] * P[2]);
+    const T ai = sig * Oi[2] * P[2] + h5 * (Oi[2] * P[1] - Oi[1] * P[2]);
+    ACC(D_FP, -ai, ar);
+  }
+  ACC(D_FZ, h5 * (Or[3] * P[1] + sig * Or[3] * P[2] + Or[1] * P[3] - sig * Or[2] * P[3]),
+      h5 * (Oi[3] * P[1] + sig * Oi[3] * P[2] + Oi[1] * P[3] - sig * Oi[2] * P[3]));
+  xr = Or[0] * P[0]; xi = Oi[0] * P[0];
+  ACC(D_SR, xr, xi);
+  ACC(D_SP, -sig * xi, sig * xr);
+  xr = h5 * (Or[2] * P[0] + Or[0] * P[2]); xi = h5 * (Oi[2] * P[0] + Oi[0] * P[2]);
+  ACC(D_TJPR, xr, xi);
+  ACC(D_TJPP, -sig * xi, sig * xr);
+  xr = Or[1] * P[1] + Or[2] * P[2] + Or[3] * P[3]; xi = Oi[1] * P[1] + Oi[2] * P[2] + Oi[3] * P[3];
+  ACC(D_TR, xr, xi);
+  ACC(D_TP, -sig * xi, sig * xr);
+  xr = h5 * (Or[0] * P[1] - Or[1] * P[0]); xi = h5 * (Oi[0] * P[1] - Oi[1] * P[0]);
+  ACC(D_TJRR, -xi, xr);
+  ACC(D_TJRP, -sig * xr, -sig * xi);
+  xr = h5 * (Or[0] * P[3] - Or[3] * P[0]); xi = h5 * (Oi[0] * P[3] - Oi[3] * P[0]);
+  ACC(D_TJZR, -xi, xr);
+  ACC(D_TJZP, -sig * xr, -sig * xi);
+}
+
+// W_q(r, b) += sum over the staged rows a of phi_q(a, r) rho(a, b), q < NQ
+template <class T, int NH, int NQ, int AK, int BWP>
+__device__ __forceinline__ void dens_rows(const T* sphi, const T* srho, int na, int rl, int bl,
+                                          T (&W)[NH][4][4][2]) {
+  for (int aa = 0; aa < na; ++aa) {
+    T f4[4];
+    lds4(&sphi[(aa * DRT + rl) * 4], f4);
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
+      T xr[4], xi[4];
+      lds4(&srho[(0 * AK + aa) * BWP + 4 * bl + 32 * h], xr);
+      lds4(&srho[(1 * AK + aa) * BWP + 4 * bl + 32 * h], xi);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          W[h][i][q][0] = fma(f4[q], xr[i], W[h][i][q][0]);
+          W[h][i][q][1] = fma(f4[q], xi[i], W[h][i][q][1]);
+        }
+    }
+  }
+}
+
+// grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT mesh points x 8 column lanes.
+// Thread (r, lane) owns mesh point r and columns b0 + 4*lane + i + 32*h of each chunk;
+// W_q(r, b) = sum_a phi_q(a, r) rho_ab is accumulated over the rows of one spin, then
+// folded into the thread's 28 complex densities, which are reduced over the 8 lanes
+// at the end.  dpart: [P][2][G][2*ND][nghl]
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) >= 8 ? 1 : 2) k_density(DevBasisT<T> B, DensCallT<T> c0, DensCallT<T> c1, int G,
+                                                    T* __restrict__ dpart, const int* __restrict__ active) {
+  constexpr int BT = DensTile<T>::BT, NH = BT / 4, BW = DensTile<T>::BW, BWP = DensTile<T>::BWP;
+  constexpr int AK = DensTile<T>::AK;
   const int p = blockIdx.z >> 1, call = blockIdx.z & 1;
   if (!active[p]) return;
   const DensCallT<T>& C = call ? c1 : c0;
@@ -175,212 +284,124 @@ __global__ void __launch_bounds__(256) k_density(DevBasisT<T> B, DensCallT<T> c0
   const int nghl = B.nghl;
   const int r = r0 + rl;
   const bool rok = r < nghl;
-  __shared__ T acc[2 * ND][DRT];
-  __shared__ T sphi[4][DAK][DRT];
-  __shared__ T srho[2][DAK][DBC];
-  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) (&acc[0][0])[e] = 0;
-  __syncthreads();
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sphi = reinterpret_cast<T*>(smraw);   // [AK][DRT][4]
+  T* srho = sphi + AK * DRT * 4;            // [2 pl][AK][BWP]
   const long long ps = (long long)B.dqp * nghl;
-  const T h5 = (T)0.5, two = (T)2;
+  T acc[2 * ND];
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) acc[k] = T(0);
 
-#define ACC(k, re, im)                                   \
-  {                                                      \
-    const T vr_ = red8<T>(re), vi_ = red8<T>(im);       \
-    if (bl == 0) { acc[2 * (k)][rl] += vr_; acc[2 * (k) + 1][rl] += vi_; } \
-  }
-
-  // ---------------- normal densities ----------------
-  for (int ix = g; ix < B.nb; ix += G) {
-    const int iy = C.rcols[ix];
-    if (iy < 0) continue;
-    const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
-    const int sa = B.st[ix], sb = B.st[iy];
-    const T* rho = C.rho + (long long)p * C.rho_sp + C.roffs[ix];
-    for (int b0 = 0; b0 < dc; b0 += DBC) {
-      const int b = b0 + bl;
-      T w[2][4][2];
+  for (int kind = 0; kind < 2; ++kind) {  // 0: normal densities, 1: pairing densities
+    const int* cols = kind == 0 ? C.rcols : C.kcols;
+    const long long* offs = kind == 0 ? C.roffs : C.koffs;
+    const T* base = kind == 0 ? C.rho : C.kap;
+    const long long bsp = kind == 0 ? C.rho_sp : C.kap_sp, bspl = kind == 0 ? C.rho_spl : C.kap_spl;
+    const int nq = kind == 0 ? 4 : 1;
+    for (int ix = g; ix < B.nb; ix += G) {
+      const int iy = cols[ix];
+      if (iy < 0) continue;
+      const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
+      const int sa = B.st[ix], sb = B.st[iy];
+      const T* mat = base + (long long)p * bsp + offs[ix];
+      for (int b0 = 0; b0 < dc; b0 += BW) {
+        // this thread's columns: spin (0 outside the block or the mesh) and phi_q(b, r),
+        // loaded ahead of the row loop
+        T sgb[NH][4], Pb[NH][4][4];
 #pragma unroll
-      for (int s = 0; s < 2; ++s)
+        for (int h = 0; h < NH; ++h)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { w[s][q][0] = 0; w[s][q][1] = 0; }
-      for (int a0 = 0; a0 < d; a0 += DAK) {
-        const int na = min(DAK, d - a0);
-        for (int e = threadIdx.x; e < 4 * DAK * DRT; e += 256) {
-          const int q = e / (DAK * DRT), rem = e % (DAK * DRT), aa = rem / DRT, rr = rem % DRT;
-          T v = 0;
-          if (aa < na && r0 + rr < nghl) v = B.phi[q * ps + (long long)(sa + a0 + aa) * nghl + r0 + rr];
-          sphi[q][aa][rr] = v;
-        }
-        for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
-          const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
-          T v = 0;
-          if (aa < na && b0 + bb < dc) v = rho[(long long)pl * C.rho_spl + (a0 + aa) + (long long)(b0 + bb) * d];
-          srho[pl][aa][bb] = v;
-        }
-        __syncthreads();
-        // spin-up rows first: split the chunk at the spin boundary
-        const int nup_here = max(0, min(na, nu - a0));
-        for (int aa = 0; aa < nup_here; ++aa) {
-          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
+          for (int i = 0; i < 4; ++i) {
+            const int b = b0 + 4 * bl + i + 32 * h;
+            const bool ok = rok && b < dc;
+            sgb[h][i] = ok ? (T)B.ns[sb + b] : T(0);
+            const long long jb = sb + (ok ? b : 0);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const T f = sphi[q][aa][rl];
-            w[0][q][0] = fma(f, re, w[0][q][0]); w[0][q][1] = fma(f, im, w[0][q][1]);
+            for (int q = 0; q < 4; ++q) Pb[h][i][q] = (ok && q < nq) ? B.phi[q * ps + jb * nghl + r] : T(0);
           }
-        }
-        for (int aa = nup_here; aa < na; ++aa) {
-          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
+        for (int s = 0; s < 2; ++s) {  // rows of spin up [0, nu), then spin down [nu, d)
+          const int alo = s == 0 ? 0 : nu, ahi = s == 0 ? nu : d;
+          if (alo >= ahi) continue;
+          T W[NH][4][4][2];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const T f = sphi[q][aa][rl];
-            w[1][q][0] = fma(f, re, w[1][q][0]); w[1][q][1] = fma(f, im, w[1][q][1]);
+          for (int h = 0; h < NH; ++h)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int q = 0; q < 4; ++q) { W[h][i][q][0] = T(0); W[h][i][q][1] = T(0); }
+          for (int a0 = alo; a0 < ahi; a0 += AK) {
+            const int na = min(AK, ahi - a0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < AK * DRT; e += blockDim.x) {
+              const int rr = e % DRT, aa = e / DRT;
+              T v[4] = {T(0), T(0), T(0), T(0)};
+              if (aa < na && r0 + rr < nghl) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  if (q < nq) v[q] = B.phi[q * ps + (long long)(sa + a0 + aa) * nghl + r0 + rr];
+              }
+              T* dst = &sphi[(aa * DRT + rr) * 4];
+              dst[0] = v[0]; dst[1] = v[1]; dst[2] = v[2]; dst[3] = v[3];
+            }
+            // 8 consecutive rows x 4 columns per warp: coalesced reads, conflict-free writes
+            for (int e = threadIdx.x; e < 2 * AK * BW; e += blockDim.x) {
+              const int aa = (e & 7) + 8 * ((e >> 5) % (AK / 8));
+              const int bb = ((e >> 3) & 3) + 4 * ((e >> 5) / (AK / 8) % (BW / 4));
+              const int pl = e / (AK * BW);
+              T v = T(0);
+              if (aa < na && b0 + bb < dc) v = mat[(long long)pl * bspl + (a0 + aa) + (long long)(b0 + bb) * d];
+              srho[(pl * AK + aa) * BWP + bb] = v;
+            }
+            __syncthreads();
+            if (kind == 0) dens_rows<T, NH, 4, AK, BWP>(sphi, srho, na, rl, bl, W);
+            else dens_rows<T, NH, 1, AK, BWP>(sphi, srho, na, rl, bl, W);
           }
-        }
-        __syncthreads();
-      }
-      // epilogue: contributions of column b at mesh point r
-      T P0 = 0, P1 = 0, P2 = 0, P3 = 0, sg = 0;
-      const bool ok = rok && b < dc;
-      if (ok) {
-        const int jb = sb + b;
-        P0 = B.phi[0 * ps + (long long)jb * nghl + r];
-        P1 = B.phi[1 * ps + (long long)jb * nghl + r];
-        P2 = B.phi[2 * ps + (long long)jb * nghl + r];
-        P3 = B.phi[3 * ps + (long long)jb * nghl + r];
-        sg = (T)B.ns[jb];
-      }
-      const int si = (sg > 0) ? 0 : 1;  // same-spin set of wfa
-      // select S (same spin as b) and O (opposite)
-      T Sr[4], Si[4], Or[4], Oi[4];
+          // fold the rows of spin s into the densities
+          const T srow = s == 0 ? T(1) : T(-1);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        Sr[q] = si == 0 ? w[0][q][0] : w[1][q][0]; Si[q] = si == 0 ? w[0][q][1] : w[1][q][1];
-        Or[q] = si == 0 ? w[1][q][0] : w[0][q][0]; Oi[q] = si == 0 ? w[1][q][1] : w[0][q][1];
-        if (!ok) { Sr[q] = Si[q] = Or[q] = Oi[q] = 0; }
-      }
-      const T sig = (sg < 0) ? (T)1 : (T)-1;  // +1 if b is spin down
-      T xr, xi;
-      // diagonal in spin
-      xr = Sr[0] * P0; xi = Si[0] * P0;
-      ACC(D_RHO, xr, xi);
-      ACC(D_SZ, sg * xr, sg * xi);
-      xr = h5 * (Sr[0] * P2 + Sr[2] * P0); xi = h5 * (Si[0] * P2 + Si[2] * P0);
-      ACC(D_JP, xr, xi);
-      ACC(D_TJPZ, sg * xr, sg * xi);
-      xr = Sr[1] * P1 + Sr[2] * P2 + Sr[3] * P3; xi = Si[1] * P1 + Si[2] * P2 + Si[3] * P3;
-      ACC(D_TAU, xr, xi);
-      ACC(D_TZ, sg * xr, sg * xi);
-      xr = h5 * (Sr[0] * P1 - Sr[1] * P0); xi = h5 * (Si[0] * P1 - Si[1] * P0);
-      ACC(D_JR, -xi, xr);
-      ACC(D_TJRZ, -sg * xi, sg * xr);
-      xr = h5 * (Sr[0] * P3 - Sr[3] * P0); xi = h5 * (Si[0] * P3 - Si[3] * P0);
-      ACC(D_JZ, -xi, xr);
-      ACC(D_TJZZ, -sg * xi, sg * xr);
-      // gs: diagonal part + off-diagonal parts
-      {
-        T gr = sg * (Sr[0] * P3 + Sr[3] * P0), gi = sg * (Si[0] * P3 + Si[3] * P0);
-        gr += sig * (Or[0] * P2 - Or[2] * P0) + (Or[0] * P1 + Or[1] * P0);
-        gi += sig * (Oi[0] * P2 - Oi[2] * P0) + (Oi[0] * P1 + Oi[1] * P0);
-        ACC(D_GS, gr, gi);
-      }
-      {
-                T fr = h5 * sg * (Sr[1] * P3 + Sr[3] * P1), fi = h5 * sg * (Si[1] * P3 + Si[3] * P1);
-        fr += Or[1] * P1 + sig * h5 * (Or[1] * P2 - Or[2] * P1);
-        fi += Oi[1] * P1 + sig * h5 * (Oi[1] * P2 - Oi[2] * P1);
-        ACC(D_FR, fr, fi);
-      }
-      {
-        // fp += i*sg*(S2P3 - S3P2)/2 + i*(sig*O2P2 + (O2P1 - O1P2)/2)
-                const T ar = h5 * sg * (Sr[2] * P3 - Sr[3] * P2) + sig * Or[2] * P2 + h5 * (Or[2] * P1 - Or[1] * P2);
-        const T ai = h5 * sg * (Si[2] * P3 - Si[3] * P2) + sig * Oi[2] * P2 + h5 * (Oi[2] * P1 - Oi[1] * P2);
-        ACC(D_FP, -ai, ar);
-      }
-      {
-                T zr = sg * Sr[3] * P3, zi = sg * Si[3] * P3;
-        zr += h5 * (Or[3] * P1 + sig * Or[3] * P2 + Or[1] * P3 - sig * Or[2] * P3);
-        zi += h5 * (Oi[3] * P1 + sig * Oi[3] * P2 + Oi[1] * P3 - sig * Oi[2] * P3);
-        ACC(D_FZ, zr, zi);
-      }
-      // not diagonal in spin
-      xr = Or[0] * P0; xi = Oi[0] * P0;
-      ACC(D_SR, xr, xi);
-      ACC(D_SP, -sig * xi, sig * xr);
-      xr = h5 * (Or[2] * P0 + Or[0] * P2); xi = h5 * (Oi[2] * P0 + Oi[0] * P2);
-      ACC(D_TJPR, xr, xi);
-      ACC(D_TJPP, -sig * xi, sig * xr);
-      xr = Or[1] * P1 + Or[2] * P2 + Or[3] * P3; xi = Oi[1] * P1 + Oi[2] * P2 + Oi[3] * P3;
-      ACC(D_TR, xr, xi);
-      ACC(D_TP, -sig * xi, sig * xr);
-      xr = h5 * (Or[0] * P1 - Or[1] * P0); xi = h5 * (Oi[0] * P1 - Oi[1] * P0);
-      ACC(D_TJRR, -xi, xr);
-      ACC(D_TJRP, -sig * xr, -sig * xi);
-      xr = h5 * (Or[0] * P3 - Or[3] * P0); xi = h5 * (Oi[0] * P3 - Oi[3] * P0);
-      ACC(D_TJZR, -xi, xr);
-      ACC(D_TJZP, -sig * xr, -sig * xi);
-    }
-  }
-  // ---------------- pairing densities ----------------
-  for (int ix = g; ix < B.nb; ix += G) {
-    const int iy = C.kcols[ix];
-    if (iy < 0) continue;
-    const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
-    const int sa = B.st[ix], sb = B.st[iy];
-    const T* kap = C.kap + (long long)p * C.kap_sp + C.koffs[ix];
-    for (int b0 = 0; b0 < dc; b0 += DBC) {
-      const int b = b0 + bl;
-      T w[2][2] = {{0, 0}, {0, 0}};
-      for (int a0 = 0; a0 < d; a0 += DAK) {
-        const int na = min(DAK, d - a0);
-        for (int e = threadIdx.x; e < DAK * DRT; e += 256) {
-          const int aa = e / DRT, rr = e % DRT;
-          T v = 0;
-          if (aa < na && r0 + rr < nghl) v = B.phi[(long long)(sa + a0 + aa) * nghl + r0 + rr];
-          sphi[0][aa][rr] = v;
+          for (int h = 0; h < NH; ++h)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const T sg = sgb[h][i];
+              if (sg == T(0)) continue;
+              const T sig = sg < T(0) ? T(1) : T(-1);
+              T Wr[4], Wi[4], Pq[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) { Wr[q] = W[h][i][q][0]; Wi[q] = W[h][i][q][1]; Pq[q] = Pb[h][i][q]; }
+              if (kind == 0) {
+                if (sg == srow) dens_same(acc, Wr, Wi, Pq, sg);
+                else dens_opp(acc, Wr, Wi, Pq, sig);
+              } else {
+                const T two = T(2);
+                if (sg == srow) {
+                  const T xr = two * Wr[0] * Pq[0], xi = two * Wi[0] * Pq[0];
+                  ACC(D_SBR, sig * xr, sig * xi);
+                  ACC(D_SBP, xi, -xr);
+                } else {
+                  const T xr = two * Wr[0] * Pq[0], xi = two * Wi[0] * Pq[0];
+                  ACC(D_RB, -sg * xr, -sg * xi);
+                  ACC(D_SBZ, xr, xi);
+                }
+              }
+            }
         }
-        for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
-          const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
-          T v = 0;
-          if (aa < na && b0 + bb < dc) v = kap[(long long)pl * C.kap_spl + (a0 + aa) + (long long)(b0 + bb) * d];
-          srho[pl][aa][bb] = v;
-        }
-        __syncthreads();
-        const int nup_here = max(0, min(na, nu - a0));
-        for (int aa = 0; aa < nup_here; ++aa) {
-          const T f = sphi[0][aa][rl];
-          w[0][0] = fma(f, srho[0][aa][bl], w[0][0]); w[0][1] = fma(f, srho[1][aa][bl], w[0][1]);
-        }
-        for (int aa = nup_here; aa < na; ++aa) {
-          const T f = sphi[0][aa][rl];
-          w[1][0] = fma(f, srho[0][aa][bl], w[1][0]); w[1][1] = fma(f, srho[1][aa][bl], w[1][1]);
-        }
-        __syncthreads();
       }
-      T P0 = 0, sg = 0;
-      const bool ok = rok && b < dc;
-      if (ok) {
-        const int jb = sb + b;
-        P0 = B.phi[(long long)jb * nghl + r];
-        sg = (T)B.ns[jb];
-      }
-      const int si = (sg > 0) ? 0 : 1;
-      T Sr = si == 0 ? w[0][0] : w[1][0], Si = si == 0 ? w[0][1] : w[1][1];
-      T Or = si == 0 ? w[1][0] : w[0][0], Oi = si == 0 ? w[1][1] : w[0][1];
-      if (!ok) { Sr = Si = Or = Oi = 0; }
-      const T sig = (sg < 0) ? (T)1 : (T)-1;
-      T xr = two * Or * P0, xi = two * Oi * P0;
-      ACC(D_RB, -sg * xr, -sg * xi);
-      ACC(D_SBZ, xr, xi);
-      xr = two * Sr * P0; xi = two * Si * P0;
-      ACC(D_SBR, sig * xr, sig * xi);
-      ACC(D_SBP, xi, -xr);
     }
   }
 #undef ACC
-  __syncthreads();
-  T* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
-  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) {
-    const int k = e / DRT, rr = e % DRT;
-    if (r0 + rr < nghl) out[(long long)k * nghl + r0 + rr] = acc[k][rr];
+  // reduce over the 8 column lanes (same warp, low 3 bits of the lane)
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) {
+    T v = acc[k];
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    acc[k] = v;
+  }
+  if (bl == 0 && rok) {
+    T* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k) out[(long long)k * nghl + r] = acc[k];
   }
 }
 
@@ -620,22 +641,34 @@ __global__ void __launch_bounds__(128) k_meanfield(DevBasisT<T> B, int G, const 
 // ---------------------------------------------------------------------------
 struct HTask {
   int ix, iy;      // block row / column
-  int a0, na;      // row tile inside block ix (spin-uniform)
-  int b0, nbc;     // column tile inside block iy
+  int a0, na;      // row range inside block ix (spin-uniform), na <= 4*rows
+  int b0, nbc;     // column range inside block iy, nbc <= 4*cols
   int sa;          // spin of the rows (+1/-1)
   int mode;        // 0: mean field (5 components), 1: pairing (1 component)
   int call;        // 0: pn, 1: np
   int outq;        // HSP quadrant 0..3 (m11, m12, m21, m22)
+  int rows, cols;  // thread grid: each thread owns 4 rows x 4 columns, rows*cols <= 256
   long long ooff;  // block offset inside the quadrant
 };
 
-#define HRC 16   // mesh points per K chunk
+enum { HP_MAXR = 32, HP_MAXC = 32, HP_LD = 4 * HP_MAXR + 4 };  // HP_LD: padded row length
 
-// grid (ntasks, P); 256 threads (16x16, 2x2 outputs each); dynamic smem
+// mesh points per K chunk: the shared-memory footprint is the same for FP32 and FP64
+template <class T> struct HpChunk { static constexpr int KR = sizeof(T) >= 8 ? 4 : 8; };
+
 template <class T>
-__global__ void __launch_bounds__(256) k_hproj(DevBasisT<T> B, const HTask* __restrict__ tasks,
+__host__ __device__ constexpr size_t hproj_smem_bytes() {
+  // sA [5][KR][HP_LD] + sPb [5][KR][HP_LD] + sH [5][KR][HP_LD][2] + sMF [25][2][2][KR]
+  return (size_t)(5 * HpChunk<T>::KR * HP_LD * 4 + 25 * 4 * HpChunk<T>::KR) * sizeof(T);
+}
+
+
+// grid (ntasks, P); 256 threads, each a 4 x 4 (complex) output tile; dynamic smem
+template <class T>
+__global__ void __launch_bounds__(256, 1) k_hproj(DevBasisT<T> B, const HTask* __restrict__ tasks,
                                                const T* __restrict__ mf, T* __restrict__ hsp,
                                                long long nxy, const int* __restrict__ active) {
+  constexpr int KR = HpChunk<T>::KR;
   const int p = blockIdx.y;
   if (!active[p]) return;
   const HTask Th = tasks[blockIdx.x];
@@ -643,92 +676,290 @@ __global__ void __launch_bounds__(256) k_hproj(DevBasisT<T> B, const HTask* __re
   const long long ps = (long long)B.dqp * nghl;
   const int nc = Th.mode == 0 ? 5 : 1;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* sA = reinterpret_cast<T*>(smraw);     // [5][32][HRC]
-  T* sPb = sA + 5 * 32 * HRC;               // [5][32][HRC]
-  T* sMF = sPb + 5 * 32 * HRC;              // [25][2 sb][2 re/im][HRC]
-  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][32][2][HRC]
-  __shared__ signed char sns[32];
+  T* sA = reinterpret_cast<T*>(smraw);      // [5][KR][HP_LD]  phi_q(a, r)
+  T* sPb = sA + 5 * KR * HP_LD;              // [5][KR][HP_LD]  phi_iz(b, r)
+  T* sH = sPb + 5 * KR * HP_LD;              // [5][KR][HP_LD][2] hpsi_q(r, b) (re, im)
+  T* sMF = sH + 5 * KR * HP_LD * 2;          // [25][2 sb][2 re/im][KR]
+  __shared__ signed char sns[4 * HP_MAXC];
   const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
-  if (threadIdx.x < 32) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
+  const int na4 = 4 * Th.rows, nb4 = 4 * Th.cols;
+  for (int i = threadIdx.x; i < nb4; i += blockDim.x) sns[i] = i < Th.nbc ? B.ns[jb0 + i] : (signed char)1;
   const T* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * nghl;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  T ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
-  for (int r0 = 0; r0 < nghl; r0 += HRC) {
-    const int nr = min(HRC, nghl - r0);
+  const int ta = threadIdx.x % Th.rows, tb = threadIdx.x / Th.rows;
+  const bool worker = tb < Th.cols;
+  T ar[4][4], ai[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { ar[i][j] = T(0); ai[i][j] = T(0); }
+  for (int r0 = 0; r0 < nghl; r0 += KR) {
+    const int nr = min(KR, nghl - r0);
     __syncthreads();
-    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
-      const int q = e / (32 * HRC), rem = e % (32 * HRC), aa = rem / HRC, rr = rem % HRC;
-      T va = 0, vb = 0;
-      if (rr < nr) {
-        if (aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
-        if (aa < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + aa) * nghl + r0 + rr];
-      }
-      sA[(q * 32 + aa) * HRC + rr] = va;
-      sPb[(q * 32 + aa) * HRC + rr] = vb;
+    // basis functions of the rows and columns, r fastest (coalesced), zero padded
+    for (int e = threadIdx.x; e < nc * na4 * KR; e += blockDim.x) {
+      const int rr = e % KR, rem = e / KR, aa = rem % na4, q = rem / na4;
+      T v = T(0);
+      if (rr < nr && aa < Th.na) v = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
+      sA[(q * KR + rr) * HP_LD + aa] = v;
+    }
+    for (int e = threadIdx.x; e < 5 * nb4 * KR; e += blockDim.x) {
+      const int rr = e % KR, rem = e / KR, bb = rem % nb4, q = rem / nb4;
+      if (Th.mode != 0 && q > 0) continue;
+      T v = T(0);
+      if (rr < nr && bb < Th.nbc) v = B.phi[q * ps + (long long)(jb0 + bb) * nghl + r0 + rr];
+      sPb[(q * KR + rr) * HP_LD + bb] = v;
     }
     if (Th.mode == 0) {
-      for (int e = threadIdx.x; e < 25 * 2 * 2 * HRC; e += 256) {
-        const int pair = e / (4 * HRC), rem = e % (4 * HRC), sb = rem / (2 * HRC), rem2 = rem % (2 * HRC);
-        const int ri = rem2 / HRC, rr = rem2 % HRC;
+      for (int e = threadIdx.x; e < 25 * 4 * KR; e += blockDim.x) {
+        const int rr = e % KR, rem = e / KR, ri = rem % 2, sb = (rem / 2) % 2, pair = rem / 4;
         const int iy = pair / 5, iz = pair % 5;
-        T v = 0;
+        T v = T(0);
         if (rr < nr) v = mfp[((long long)mfslot(iy, iz, Th.sa, sb == 0 ? 1 : -1) * 2 + ri) * nghl + r0 + rr];
         sMF[e] = v;
       }
     } else {
-      for (int e = threadIdx.x; e < 2 * 2 * HRC; e += 256) {
-        const int sb = e / (2 * HRC), rem = e % (2 * HRC), ri = rem / HRC, rr = rem % HRC;
+      for (int e = threadIdx.x; e < 4 * KR; e += blockDim.x) {
+        const int rr = e % KR, rem = e / KR, ri = rem % 2, sb = rem / 2;
         const int slot = 100 + (Th.sa < 0 ? 2 : 0) + sb;
-        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : (T)0;
+        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : T(0);
       }
     }
     __syncthreads();
-    // hpsi(iy, b, r) = sum_iz mf(iy, iz, sa, s_b)(r) phi_iz(b, r)
-    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
-      const int iy = e / (32 * HRC), rem = e % (32 * HRC), bb = rem / HRC, rr = rem % HRC;
+    // hpsi(q, b, r) = sum_iz mf(q, iz, sa, s_b)(r) phi_iz(b, r)
+    for (int e = threadIdx.x; e < nc * KR * nb4; e += blockDim.x) {
+      const int bb = e % nb4, rem = e / nb4, rr = rem % KR, q = rem / KR;
       const int sb = sns[bb] > 0 ? 0 : 1;
-      T hr = 0, hi = 0;
+      T hr = T(0), hi = T(0);
       if (Th.mode == 0) {
 #pragma unroll
         for (int iz = 0; iz < 5; ++iz) {
-          const T f = sPb[(iz * 32 + bb) * HRC + rr];
-          const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
-          hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
+          const T f = sPb[(iz * KR + rr) * HP_LD + bb];
+          const T* m = &sMF[(((q * 5 + iz) * 2 + sb) * 2) * KR + rr];
+          hr = fma(m[0], f, hr); hi = fma(m[KR], f, hi);
         }
       } else {
-        const T f = sPb[bb * HRC + rr];
-        hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
+        const T f = sPb[rr * HP_LD + bb];
+        hr = sMF[(sb * 2) * KR + rr] * f; hi = sMF[(sb * 2 + 1) * KR + rr] * f;
       }
-      sH[((iy * 32 + bb) * 2) * HRC + rr] = hr;
-      sH[((iy * 32 + bb) * 2 + 1) * HRC + rr] = hi;
+      T* h = &sH[((q * KR + rr) * HP_LD + bb) * 2];
+      h[0] = hr; h[1] = hi;
     }
     __syncthreads();
-    for (int q = 0; q < nc; ++q) {
-      for (int rr = 0; rr < HRC; ++rr) {
-        const T a0 = sA[(q * 32 + ty * 2) * HRC + rr], a1 = sA[(q * 32 + ty * 2 + 1) * HRC + rr];
-        const T h0r = sH[((q * 32 + tx * 2) * 2) * HRC + rr], h0i = sH[((q * 32 + tx * 2) * 2 + 1) * HRC + rr];
-        const T h1r = sH[((q * 32 + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * 32 + tx * 2 + 1) * 2 + 1) * HRC + rr];
-        ar[0][0] = fma(a0, h0r, ar[0][0]); ai[0][0] = fma(a0, h0i, ai[0][0]);
-        ar[0][1] = fma(a0, h1r, ar[0][1]); ai[0][1] = fma(a0, h1i, ai[0][1]);
-        ar[1][0] = fma(a1, h0r, ar[1][0]); ai[1][0] = fma(a1, h0i, ai[1][0]);
-        ar[1][1] = fma(a1, h1r, ar[1][1]); ai[1][1] = fma(a1, h1i, ai[1][1]);
+    if (worker) {
+      for (int q = 0; q < nc; ++q) {
+#pragma unroll
+        for (int rr = 0; rr < KR; ++rr) {
+          T a4[4], h0[4], h1[4];
+          lds4(&sA[(q * KR + rr) * HP_LD + 4 * ta], a4);
+          const T* hp = &sH[((q * KR + rr) * HP_LD + 4 * tb) * 2];
+          lds4(hp, h0);      // (re, im) of columns 0, 1
+          lds4(hp + 4, h1);  // (re, im) of columns 2, 3
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            ar[i][0] = fma(a4[i], h0[0], ar[i][0]); ai[i][0] = fma(a4[i], h0[1], ai[i][0]);
+            ar[i][1] = fma(a4[i], h0[2], ar[i][1]); ai[i][1] = fma(a4[i], h0[3], ai[i][1]);
+            ar[i][2] = fma(a4[i], h1[0], ar[i][2]); ai[i][2] = fma(a4[i], h1[1], ai[i][2]);
+            ar[i][3] = fma(a4[i], h1[2], ar[i][3]); ai[i][3] = fma(a4[i], h1[3], ai[i][3]);
+          }
+        }
       }
     }
   }
+  if (!worker) return;
   const int ld = B.db[Th.ix];
   T* ore = hsp + ((long long)p * 2 + 0) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
   T* oim = hsp + ((long long)p * 2 + 1) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int a = ty * 2 + i, b = tx * 2 + j;
+    for (int j = 0; j < 4; ++j) {
+      const int a = 4 * ta + i, b = 4 * tb + j;
       if (a < Th.na && b < Th.nbc) {
         const long long e = (Th.a0 + a) + (long long)(Th.b0 + b) * ld;
-        ore[e] = (T)2 * ar[i][j];
-        oim[e] = (T)2 * ai[i][j];
+        ore[e] = T(2) * ar[i][j];
+        oim[e] = T(2) * ai[i][j];
       }
     }
+}
+
+// ---------------------------------------------------------------------------
+// field projection on the tensor cores (FP32 data, 3xTF32 products).
+// One CTA computes, for one (block pair, spin segment of the rows) and up to pg
+// points, D[m][n] = sum_k hpsi[k][m] phi[k][n] with
+//   m = pl*64 + j, j = (point in the group)*nbc + b   (rows: Re, then Im of hpsi)
+//   n = a (the rows of the output block, N padded to np)
+//   k = (q, r), 32 mesh points of one component q per chunk.
+// hpsi is generated on the fly from the field tensor (as in k_hproj) into shared
+// memory; D accumulates in tensor memory and out_ab = 2 D.
+// ---------------------------------------------------------------------------
+struct HTaskTC {
+  int ix, iy, a0, na, b0, nbc, sa, mode, call, outq;
+  int np;          // N of the MMA: na rounded up to 16
+  int pg;          // points per CTA (pg * nbc <= 64)
+  long long ooff;
+};
+enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8 };
+
+__host__ __device__ constexpr size_t hproj_tc_smem_bytes() {
+  return (size_t)(2 * 128 * HTC_K + 2 * HTC_MAXN * HTC_K + 5 * HTC_MAXB * HTC_K + HTC_MAXPG * 2 * 5 * 2 * HTC_K) *
+         sizeof(float);
+}
+
+// four consecutive floats of row `row` (mesh points r..r+3 of one state), zero outside
+__device__ __forceinline__ float4 ld_row4(const float* __restrict__ src, int r, int nghl, bool ok) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!ok) return v;
+  if ((nghl & 3) == 0 && r + 3 < nghl) return *reinterpret_cast<const float4*>(src + r);
+  if (r < nghl) v.x = src[r];
+  if (r + 1 < nghl) v.y = src[r + 1];
+  if (r + 2 < nghl) v.z = src[r + 2];
+  if (r + 3 < nghl) v.w = src[r + 3];
+  return v;
+}
+
+__device__ __forceinline__ void st_split4(float* hi, float* lo, float4 v) {
+  float4 h, l;
+  tc::split(v.x, h.x, l.x); tc::split(v.y, h.y, l.y); tc::split(v.z, h.z, l.z); tc::split(v.w, h.w, l.w);
+  *reinterpret_cast<float4*>(hi) = h;
+  *reinterpret_cast<float4*>(lo) = l;
+}
+
+// grid (ntasks, point groups); 256 threads; dynamic smem hproj_tc_smem_bytes()
+// actlist[nact]: the points to evaluate; err: set to 1 if a wait on the tensor
+// cores gave up (the CTA then writes nothing)
+__global__ void __launch_bounds__(256, 1) k_hproj_tc(DevBasisT<float> B, const HTaskTC* __restrict__ tasks,
+                                                     const int* __restrict__ actlist, int nact,
+                                                     const float* __restrict__ mf, float* __restrict__ hsp,
+                                                     long long nxy, int* __restrict__ err) {
+  const HTaskTC Th = tasks[blockIdx.x];
+  const int g0 = blockIdx.y * Th.pg;
+  if (g0 >= nact) return;
+  const int npg = min(Th.pg, nact - g0);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* sAh = reinterpret_cast<float*>(smraw);
+  float* sAl = sAh + 128 * HTC_K;
+  float* sBh = sAl + 128 * HTC_K;
+  float* sBl = sBh + HTC_MAXN * HTC_K;
+  float* sPhiB = sBl + HTC_MAXN * HTC_K;         // [5][64 b][32 r]
+  float* sMF = sPhiB + 5 * HTC_MAXB * HTC_K;      // [pg][2 pl][5 iz][2 sb][32 r]
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tslot;
+  __shared__ signed char sns[HTC_MAXB];
+  __shared__ int spt[HTC_MAXPG];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nbc = Th.nbc, NP = Th.np, nj = npg * nbc;
+  const int nghl = B.nghl;
+  const long long ps = (long long)B.dqp * nghl;
+  const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
+  const int nc = Th.mode == 0 ? 5 : 1;
+  const uint32_t ncols = NP <= 32 ? 32u : NP <= 64 ? 64u : NP <= 128 ? 128u : 256u;
+  if (tid < HTC_MAXB) sns[tid] = tid < nbc ? B.ns[jb0 + tid] : (signed char)1;
+  if (tid < HTC_MAXPG) spt[tid] = tid < npg ? actlist[g0 + tid] : 0;
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  if (warp == 0) tc::tmem_alloc(&tslot, ncols);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  const uint32_t idesc = tc::idesc_tf32(128, NP);
+  bool ok = true;
+  int chunk = 0;
+  for (int q = 0; q < nc; ++q) {
+    for (int r0 = 0; r0 < nghl; r0 += HTC_K, ++chunk) {
+      if (chunk > 0 && !tc::mbar_wait(&mbar, (chunk - 1) & 1)) ok = false;  // operands free again
+      if (!__syncthreads_and(ok)) { ok = false; break; }
+      tc::fence_after();
+      // basis functions of the columns and the field of each point, current q
+      for (int e = tid; e < nc * HTC_MAXB * 8; e += blockDim.x) {
+        const int r4 = e & 7, b = (e >> 3) % HTC_MAXB, iz = e / (8 * HTC_MAXB);
+        const float4 v = ld_row4(B.phi + iz * ps + (long long)(jb0 + b) * nghl, r0 + 4 * r4, nghl, b < nbc);
+        *reinterpret_cast<float4*>(&sPhiB[(iz * HTC_MAXB + b) * HTC_K + 4 * r4]) = v;
+      }
+      for (int e = tid; e < npg * 2 * nc * 2 * 8; e += blockDim.x) {
+        const int r4 = e & 7, sb = (e >> 3) & 1, iz = (e >> 4) % nc, pl = (e / (16 * nc)) & 1,
+                  pi = e / (32 * nc);
+        const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb == 0 ? 1 : -1) : 100 + (Th.sa < 0 ? 2 : 0) + sb;
+        const float* src = mf + ((long long)spt[pi] * 2 + Th.call) * NMF * 2 * nghl + ((long long)slot * 2 + pl) * nghl;
+        const float4 v = ld_row4(src, r0 + 4 * r4, nghl, true);
+        *reinterpret_cast<float4*>(&sMF[((((pi * 2 + pl) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]) = v;
+      }
+      __syncthreads();
+      // A operand: hpsi rows (Re at j, Im at 64 + j), 4 mesh points per item
+      for (int e = tid; e < HTC_MAXB * 8; e += blockDim.x) {
+        const int j = e % HTC_MAXB, r4 = e / HTC_MAXB;
+        float4 hr = make_float4(0.f, 0.f, 0.f, 0.f), hi = hr;
+        if (j < nj) {
+          const int pi = j / nbc, b = j % nbc;
+          const int sb = sns[b] > 0 ? 0 : 1;
+          for (int iz = 0; iz < nc; ++iz) {
+            const float4 f = *reinterpret_cast<const float4*>(&sPhiB[(iz * HTC_MAXB + b) * HTC_K + 4 * r4]);
+            const float4 mr = *reinterpret_cast<const float4*>(&sMF[((((pi * 2 + 0) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]);
+            const float4 mi = *reinterpret_cast<const float4*>(&sMF[((((pi * 2 + 1) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]);
+            hr.x = fmaf(mr.x, f.x, hr.x); hr.y = fmaf(mr.y, f.y, hr.y); hr.z = fmaf(mr.z, f.z, hr.z); hr.w = fmaf(mr.w, f.w, hr.w);
+            hi.x = fmaf(mi.x, f.x, hi.x); hi.y = fmaf(mi.y, f.y, hi.y); hi.z = fmaf(mi.z, f.z, hi.z); hi.w = fmaf(mi.w, f.w, hi.w);
+          }
+        }
+        const int o_re = tc::cm_off(j, 4 * r4, 128), o_im = tc::cm_off(64 + j, 4 * r4, 128);
+        st_split4(sAh + o_re, sAl + o_re, hr);
+        st_split4(sAh + o_im, sAl + o_im, hi);
+      }
+      // B operand: phi_q(a, r) of the output rows
+      for (int e = tid; e < NP * 8; e += blockDim.x) {
+        const int n = e % NP, r4 = e / NP;
+        const float4 v = ld_row4(B.phi + q * ps + (long long)(ja0 + n) * nghl, r0 + 4 * r4, nghl, n < Th.na);
+        const int o = tc::cm_off(n, 4 * r4, NP);
+        st_split4(sBh + o, sBl + o, v);
+      }
+      tc::fence_async_smem();
+      tc::fence_before();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after();
+        const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(NP / 8) * 128;
+#pragma unroll
+        for (int ks = 0; ks < HTC_K / 8; ++ks) {
+          const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
+          const uint64_t ah = tc::sdesc(tc::smem_u32(sAh) + oa, lboA, 128);
+          const uint64_t al = tc::sdesc(tc::smem_u32(sAl) + oa, lboA, 128);
+          const uint64_t bh = tc::sdesc(tc::smem_u32(sBh) + ob, lboB, 128);
+          const uint64_t bl = tc::sdesc(tc::smem_u32(sBl) + ob, lboB, 128);
+          tc::mma_tf32(tmem, ah, bh, idesc, chunk > 0 || ks > 0);
+          tc::mma_tf32(tmem, ah, bl, idesc, true);
+          tc::mma_tf32(tmem, al, bh, idesc, true);
+        }
+        tc::mma_commit(&mbar);
+      }
+    }
+    if (!ok) break;
+  }
+  // the last commit covers every MMA issued; wait for it (again, bounded, after a
+  // failed wait) so that nothing is in flight when the tensor memory is released
+  if (chunk > 0 && !tc::mbar_wait(&mbar, (chunk - 1) & 1)) ok = false;
+  ok = __syncthreads_and(ok);
+  tc::fence_after();
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else if (warp < 4) {
+    // epilogue: lane m of TMEM = row m; every lane of the warp takes part in the loads
+    const int m = tid, pl = m >> 6, j = m & 63;
+    const bool mine = j < nj;
+    const int pi = mine ? j / nbc : 0, b = mine ? j % nbc : 0;
+    const int ld = B.db[Th.ix];
+    float* out = hsp + ((long long)spt[pi] * 2 + pl) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff +
+                 (long long)(Th.b0 + b) * ld + Th.a0;
+    for (int n0 = 0; n0 < NP; n0 += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
+      if (mine) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          if (n0 + i < Th.na) out[n0 + i] = 2.f * v[i];
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
 }
 
 // ---------------------------------------------------------------------------
@@ -741,15 +972,17 @@ __global__ void k_green(long long nxy, int P, const double* __restrict__ hqp, co
                         const double* __restrict__ E1, const double* __restrict__ E2,
                         const double* __restrict__ wre, const double* __restrict__ wim, double quench,
                         double* __restrict__ vout, const int* __restrict__ active,
-                        const int* __restrict__ corr, const double* __restrict__ radd) {
+                        const int* __restrict__ corr, const double* __restrict__ radd,
+                        const int* __restrict__ zeroh) {
   const int p = blockIdx.y;
   if (!active[p]) return;
   const long long n2 = 2 * nxy;
   const double wr = wre[p], wi = wim[p];
   const bool cstep = corr && corr[p];
+  const bool useh = hqp && !(zeroh && zeroh[p]);  // zeroh: H = 0 (the field of X = 0)
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n2; e += (long long)gridDim.x * blockDim.x) {
     double hr = 0.0, hi = 0.0;
-    if (hqp) { hr = quench * hqp[(long long)p * 2 * n2 + e]; hi = quench * hqp[(long long)p * 2 * n2 + n2 + e]; }
+    if (useh) { hr = quench * hqp[(long long)p * 2 * n2 + e]; hi = quench * hqp[(long long)p * 2 * n2 + n2 + e]; }
     if (!cstep) hr += fqp[e];
     // G = -1/(E1 + E2 -/+ w): X (e < nxy) uses -w, Y uses +w
     const double sgn = e < nxy ? -1.0 : 1.0;
@@ -850,7 +1083,8 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
 }
 
 // normalise column ipos by 1/|df_ipos| and form the dots
-// dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used
+// dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used;
+// each warp reduces its share per k with shuffles, one barrier at the end
 __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __restrict__ norm,
                                                   const int* __restrict__ active) {
   const int p = blockIdx.y;
@@ -860,39 +1094,52 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   int iu, ipos, inext;
   bro_slots(it, S.M, iu, ipos, inext);
   const bool upd = it >= 2;
-  __shared__ double sh[32];
+  __shared__ double wsum[8][2 * 64];
   const double* vo = S.vout + (long long)p * S.N;
   const int chunk = (S.N + S.nchunk - 1) / S.nchunk;
   const int e0 = blockIdx.x * chunk, e1 = min(S.N, e0 + chunk);
   double* dfp = S.df + (long long)p * S.M * S.N;
   double* dvp = S.dv + (long long)p * S.M * S.N;
+  double* fi = dfp + (long long)ipos * S.N;
   if (upd) {
     const double sc = norm[p];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      dfp[(long long)ipos * S.N + e] *= sc;
+      fi[e] *= sc;
       dvp[(long long)ipos * S.N + e] *= sc;
     }
   }
   __syncthreads();
-  double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   for (int k = 0; k < iu; ++k) {
     double a = 0.0, b = 0.0;
     const double* fk = dfp + (long long)k * S.N;
-    const double* fi = dfp + (long long)ipos * S.N;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      a = fma(fk[e], fi[e], a);
-      b = fma(fk[e], vo[e], b);
+      const double f = fk[e];
+      a = fma(f, fi[e], a);
+      b = fma(f, vo[e], b);
     }
-    const double sa = block_sum(a, sh);
-    const double sb = block_sum(b, sh);
-    if (threadIdx.x == 0) { pt[2 + k] = sa; pt[2 + 64 + k] = sb; }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (l == 0) { wsum[w][k] = a; wsum[w][64 + k] = b; }
+  }
+  __syncthreads();
+  double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
+  const int nw = blockDim.x >> 5;
+  for (int k = threadIdx.x; k < iu; k += blockDim.x) {
+    double sa = 0.0, sb = 0.0;
+    for (int i = 0; i < nw; ++i) { sa += wsum[i][k]; sb += wsum[i][64 + k]; }
+    pt[2 + k] = sa; pt[2 + 64 + k] = sb;
   }
 }
 
-// one CTA per point: reduce partials; stage 0: si and 1/|df_ipos|; stage 1:
-// maintain beta (M x M) and solve beta*gamma = work
-__global__ void k_bro_solve(BroState S, int stage, double w0, double* __restrict__ si, double* __restrict__ norm,
-                            double* __restrict__ beta, double* __restrict__ gamma, const int* __restrict__ active) {
+// one CTA (256 threads) per point: reduce partials; stage 0: si and 1/|df_ipos|;
+// stage 1: maintain beta (M x M) and solve beta*gamma = work by Gaussian
+// elimination with partial pivoting (rows updated in parallel)
+__global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double w0, double* __restrict__ si,
+                                                   double* __restrict__ norm, double* __restrict__ beta,
+                                                   double* __restrict__ gamma, const int* __restrict__ active) {
   const int p = blockIdx.x;
   if (!active[p]) return;
   const double* pt = S.part + (long long)p * S.nchunk * BRO_NPART;
@@ -911,38 +1158,55 @@ __global__ void k_bro_solve(BroState S, int stage, double w0, double* __restrict
   bro_slots(it, S.M, n, ipos, inext);
   __shared__ double A[64][65];
   __shared__ double x[64];
+  __shared__ double f[64];
+  __shared__ int piv;
   const int M = S.M;
   double* bp = beta + (long long)p * M * M;
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < n; ++k) {
-      double dd = 0.0, wk = 0.0;
-      for (int c = 0; c < S.nchunk; ++c) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
-      if (k != ipos) { bp[k * M + ipos] = dd; bp[ipos * M + k] = dd; }
-      x[k] = wk;
+  const int tid = threadIdx.x;
+  for (int k = tid; k < n; k += blockDim.x) {
+    double dd = 0.0, wk = 0.0;
+    for (int c = 0; c < S.nchunk; ++c) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
+    if (k != ipos) { bp[k * M + ipos] = dd; bp[ipos * M + k] = dd; }
+    x[k] = wk;
+  }
+  __syncthreads();
+  for (int k = tid; k < n; k += blockDim.x) bp[k * M + k] = w0 * w0 + 1.0;
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) A[e / n][e % n] = bp[(e / n) * M + (e % n)];
+  __syncthreads();
+  for (int c = 0; c < n; ++c) {
+    if (tid == 0) {
+      int pv = c;
+      for (int r = c + 1; r < n; ++r) if (fabs(A[r][c]) > fabs(A[pv][c])) pv = r;
+      piv = pv;
     }
-    for (int k = 0; k < n; ++k) bp[k * M + k] = w0 * w0 + 1.0;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) A[i][j] = bp[i * M + j];
-    // Gaussian elimination with partial pivoting
-    for (int c = 0; c < n; ++c) {
-      int piv = c;
-      for (int r = c + 1; r < n; ++r) if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
-      if (piv != c) {
-        for (int j = 0; j < n; ++j) { const double t = A[c][j]; A[c][j] = A[piv][j]; A[piv][j] = t; }
-        const double t = x[c]; x[c] = x[piv]; x[piv] = t;
-      }
-      for (int r = c + 1; r < n; ++r) {
-        const double f = A[r][c] / A[c][c];
-        for (int j = c; j < n; ++j) A[r][j] -= f * A[c][j];
-        x[r] -= f * x[c];
-      }
+    __syncthreads();
+    const int pv = piv;
+    if (pv != c) {
+      for (int j = tid; j < n; j += blockDim.x) { const double t = A[c][j]; A[c][j] = A[pv][j]; A[pv][j] = t; }
+      if (tid == 0) { const double t = x[c]; x[c] = x[pv]; x[pv] = t; }
+      __syncthreads();
     }
+    for (int r = c + 1 + tid; r < n; r += blockDim.x) f[r] = A[r][c] / A[c][c];
+    __syncthreads();
+    const int nr = n - c - 1, nc = n - c;
+    for (int e = tid; e < nr * nc; e += blockDim.x) {
+      const int r = c + 1 + e / nc, j = c + e % nc;
+      A[r][j] -= f[r] * A[c][j];
+    }
+    for (int r = c + 1 + tid; r < n; r += blockDim.x) x[r] -= f[r] * x[c];
+    __syncthreads();
+  }
+  // back substitution, one warp
+  if (tid < 32) {
     for (int r = n - 1; r >= 0; --r) {
-      double s = x[r];
-      for (int j = r + 1; j < n; ++j) s -= A[r][j] * x[j];
-      x[r] = s / A[r][r];
+      double s = 0.0;
+      for (int j = r + 1 + tid; j < n; j += 32) s += A[r][j] * x[j];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (tid == 0) x[r] = (x[r] - s) / A[r][r];
+      __syncwarp();
     }
-    for (int k = 0; k < n; ++k) gamma[(long long)p * 64 + k] = x[k];
+    for (int k = tid; k < n; k += 32) gamma[(long long)p * 64 + k] = x[k];
   }
 }
 

@@ -79,6 +79,23 @@ class GPUSolver:
     def nxy(self) -> int:
         return int(self.lib.pnfam_gpu_nxy(self.ctx))
 
+    @staticmethod
+    def options(max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None, timed=False, precision=0,
+                switch_exp=0):
+        if alpha_mix is None:
+            from .pnfam_setup import ALPHA_MIX as alpha_mix
+        o = _lib.SolverOpts()
+        o.max_iter = int(max_iter); o.broyden_history_size = int(broyden_m)
+        o.convergence_epsilon = float(eps); o.alpha_mix = float(alpha_mix)
+        o.quench_residual_int = float(quench); o.precision = int(precision)
+        o.reserved[0] = 1 if timed else 0
+        o.reserved[1] = int(switch_exp)
+        return o
+
+    def engine(self, slots, **opts) -> "Engine":
+        """Continuous-batching engine on this context (see Engine)."""
+        return Engine(self, slots, self.options(**opts))
+
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
               history=False, timed=False, precision=0, switch_exp=0) -> SolveResult:
         """precision 0: FP64 throughout (the reference's arithmetic and iteration
@@ -88,20 +105,13 @@ class GPUSolver:
         FP64 anchor evaluation is taken when si < 10**-switch_exp (default
         100*eps) or si stops falling."""
         import time
-        if alpha_mix is None:
-            from .pnfam_setup import ALPHA_MIX as alpha_mix
         w = np.atleast_1d(np.asarray(omegas, dtype=complex))
         P = len(w)
         wre = np.ascontiguousarray(w.real); wim = np.ascontiguousarray(w.imag)
         reS = np.zeros(P * self.nops); imS = np.zeros(P * self.nops)
         iters = np.zeros(P, dtype=np.int32); si = np.zeros(P)
         hist = np.full(P * (max_iter + 1) * 3, np.nan) if history else None
-        o = _lib.SolverOpts()
-        o.max_iter = int(max_iter); o.broyden_history_size = int(broyden_m)
-        o.convergence_epsilon = float(eps); o.alpha_mix = float(alpha_mix)
-        o.quench_residual_int = float(quench); o.precision = int(precision)
-        o.reserved[0] = 1 if timed else 0
-        o.reserved[1] = int(switch_exp)
+        o = self.options(max_iter, eps, broyden_m, quench, alpha_mix, timed, precision, switch_exp)
         t0 = time.perf_counter()
         _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
                                             _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
@@ -117,23 +127,95 @@ class GPUSolver:
                  "strength", "total", "point_iterations_fp64", "point_iterations_fp32")
         return dict(zip(names, ms.tolist())), int(n.value)
 
-    def calc_hamiltonian(self, rho_pn, kp, rho_np, km):
+    def calc_hamiltonian(self, rho_pn, kp, rho_np, km, mixed=False):
         """Plugin seam: complex flat arrays (nxy) in the structures documented in
-        include/pnfam_gpu.h; returns (h_pn, Delta+, h_np, Delta-) complex."""
+        include/pnfam_gpu.h; returns (h_pn, Delta+, h_np, Delta-) complex.
+        mixed=True evaluates in FP32 with the tensor-core projection (the
+        kernels of the mixed form's increment evaluations)."""
         n = self.nxy
         ins = []
         for a in (rho_pn, kp, rho_np, km):
             a = np.asarray(a, dtype=complex)
             ins += [np.ascontiguousarray(a.real), np.ascontiguousarray(a.imag)]
         outs = [np.zeros(n) for _ in range(8)]
-        _lib.check(self.lib.pnfam_gpu_calc_hamiltonian(self.ctx, *[_lib.dptr(x) for x in ins],
-                                                       *[_lib.dptr(x) for x in outs]))
+        fn = self.lib.pnfam_gpu_calc_hamiltonian_mixed if mixed else self.lib.pnfam_gpu_calc_hamiltonian
+        _lib.check(fn(self.ctx, *[_lib.dptr(x) for x in ins], *[_lib.dptr(x) for x in outs]))
         return tuple(outs[2 * k] + 1j * outs[2 * k + 1] for k in range(4))
 
     def close(self):
         if getattr(self, "ctx", None) is not None and self.ctx.value:
             self.lib.pnfam_gpu_free(self.ctx)
             self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class PointResult:
+    tag: int
+    S: np.ndarray         # [1 + n_xterms] complex strength and cross terms
+    iters: int            # iteration at convergence, -1 if max_iter was reached
+    si: float
+
+
+class Engine:
+    """Continuous batching on one context (pnfam_gpu_engine_*): ``slots`` omega
+    points iterate together, each on its own counter; ``admit`` fills free
+    slots, ``launch`` enqueues one iteration of every active slot (asynchronous,
+    on the context's own stream, so engines of different contexts overlap on
+    the GPU) and ``finish`` waits for it and returns the points that finished."""
+
+    def __init__(self, solver: GPUSolver, slots: int, opts):
+        self.solver = solver
+        self.lib = solver.lib
+        self.slots = int(slots)
+        self.nops = solver.nops
+        eng = C.c_void_p()
+        _lib.check(self.lib.pnfam_gpu_engine_create(solver.ctx, self.slots, C.byref(opts), C.byref(eng)))
+        self.eng = eng
+        n = self.slots
+        self._tags = np.zeros(n, dtype=np.int64)
+        self._re = np.zeros(n * self.nops); self._im = np.zeros(n * self.nops)
+        self._it = np.zeros(n, dtype=np.int32); self._si = np.zeros(n)
+
+    @property
+    def active(self) -> int:
+        return int(self.lib.pnfam_gpu_engine_active(self.eng))
+
+    def admit(self, omegas, tags) -> int:
+        w = np.atleast_1d(np.asarray(omegas, dtype=complex))
+        wre = np.ascontiguousarray(w.real); wim = np.ascontiguousarray(w.imag)
+        t = np.ascontiguousarray(tags, dtype=np.int64)
+        k = int(self.lib.pnfam_gpu_engine_admit(self.eng, len(w), _lib.dptr(wre), _lib.dptr(wim),
+                                                t.ctypes.data_as(C.POINTER(C.c_longlong))))
+        if k < 0:
+            _lib.check(-k)
+        return k
+
+    def launch(self):
+        _lib.check(self.lib.pnfam_gpu_engine_launch(self.eng))
+
+    def finish(self):
+        out = []
+        while True:
+            n = C.c_int()
+            _lib.check(self.lib.pnfam_gpu_engine_finish(
+                self.eng, self.slots, self._tags.ctypes.data_as(C.POINTER(C.c_longlong)), _lib.dptr(self._re),
+                _lib.dptr(self._im), _lib.iptr(self._it), _lib.dptr(self._si), C.byref(n)))
+            for k in range(n.value):
+                S = self._re[k * self.nops:(k + 1) * self.nops] + 1j * self._im[k * self.nops:(k + 1) * self.nops]
+                out.append(PointResult(int(self._tags[k]), S.copy(), int(self._it[k]), float(self._si[k])))
+            if n.value < self.slots:
+                return out
+
+    def close(self):
+        if getattr(self, "eng", None) is not None and self.eng.value:
+            self.lib.pnfam_gpu_engine_free(self.eng)
+            self.eng = C.c_void_p()
 
     def __del__(self):
         try:

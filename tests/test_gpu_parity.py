@@ -275,3 +275,41 @@ def test_large_basis_calc_hamiltonian(large_case):
     for g, key in zip(got, ("h_pn", "dp", "h_np", "dm")):
         want = np.concatenate([b.reshape(-1, order="F") for b in ref[key] if b is not None])
         assert np.max(np.abs(g - want)) <= 1e-11 * np.max(np.abs(want)), key
+
+
+def _mixed_vs_fp64(c, seed):
+    """pnfam_gpu_calc_hamiltonian_mixed (FP32 densities and fields, tensor-core
+    projection with 3xTF32 products) against the FP64 entry point on random
+    densities; returns the worst error relative to each field's largest element."""
+    from pynfam_gb300.solver import GPUSolver
+    h = c.hfb
+    gpu = GPUSolver(h, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    fc, xc, yc, xtc, ytc = _structures(c.F, h.nb)
+    rng = np.random.default_rng(seed)
+    ins = []
+    for cols in (fc, xtc, fc, ytc):
+        n = BlockMatrix.empty(cols, h.db).nelem
+        ins.append(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    want = gpu.calc_hamiltonian(*ins)
+    got = gpu.calc_hamiltonian(*ins, mixed=True)
+    gpu.close()
+    worst = 0.0
+    for g, w in zip(got, want):
+        assert np.all(np.isfinite(g))
+        worst = max(worst, float(np.max(np.abs(g - w)) / np.max(np.abs(w))))
+    return worst
+
+
+@pytest.mark.parametrize("case,op", [("S40", "RS1-K1"), ("S40", "GT-K0"), ("Kr116", "P-K0")])
+def test_mixed_field_matches_fp64(case, op):
+    c, _ = case_for(case, op, 0)
+    worst = _mixed_vs_fp64(c, 3)
+    print(f"{case} {op}: mixed field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
+
+
+def test_large_basis_mixed_field_matches_fp64(large_case):
+    worst = _mixed_vs_fp64(large_case, 4)
+    print(f"N_sh=12 162Gd GT-K1: mixed field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
