@@ -232,7 +232,9 @@ long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
  * broyden, strength; filled only when opts.reserved[0] != 0), then, if
  * nstage > 8, the whole solve's device time (CUDA events on the solver's
  * stream), if nstage > 10 the FP64 and FP32 point-iterations of the solve,
- * and the number of kernel launches. */
+ * then (entries 11-15) the first five stages of the FP32 evaluations of the
+ * mixed form (entries 0-4 then hold the FP64 evaluations only), and the number
+ * of kernel launches.  An engine's figures accumulate from its creation. */
 int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
                            long long* launches);
 

@@ -15,6 +15,7 @@
 #include <mutex>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -111,6 +112,30 @@ struct TaskList {
   }
 };
 
+// the same tasks for the tensor-core kernel (FP32 data)
+struct TaskListTC {
+  std::vector<GemmTaskTC> tasks;
+  DBuf<GemmTaskTC> d_tasks;
+  int maxrows = 0;
+  void build(const TaskList& tl) {
+    tasks.clear();
+    maxrows = 0;
+    for (const GemmTask& g : tl.tasks) {
+      GemmTaskTC t;
+      memset(&t, 0, sizeof(t));
+      t.M = g.M; t.N = g.N; t.K = g.K; t.nterm = g.nterm;
+      for (int i = 0; i < g.nterm; ++i) t.t[i] = g.t[i];
+      t.rcase = g.t[0].abuf >= B_STATE ? 0 : 1;
+      t.mrows = t.rcase == 0 ? g.M : g.N;
+      t.ncols = t.rcase == 0 ? g.N : g.M;
+      t.npad = std::max(16, (t.ncols + 15) / 16 * 16);
+      t.coff = g.coff; t.cbuf = g.cbuf; t.ldc = g.ldc;
+      maxrows = std::max(maxrows, t.mrows);
+      tasks.push_back(t);
+    }
+  }
+};
+
 static GemmTerm mkterm(const MatRef& A, const MatRef& B, double a_re, double a_im) {
   GemmTerm g;
   memset(&g, 0, sizeof(g));
@@ -146,9 +171,11 @@ struct pnfam_ctx {
   DBuf<long long> d_foff, d_xtoff, d_ytoff;
   DBuf<double> d_fops;   // [nops][2*nxy] operator and cross terms in the QP basis
   TaskList k1a, k1b, k2a, k2b;
+  TaskListTC t1a, t1b, t2a, t2b;   // FP32 evaluation on the tensor cores
   std::vector<HTask> htasks;
   DBuf<HTask> d_htasks;
   std::vector<HTaskTC> htasks_tc;   // tensor-core field projection (FP32 data)
+  int tc_npmax = 16;                  // largest N of those tiles
   DBuf<HTaskTC> d_htasks_tc;
   DBuf<int> d_actlist;   // [P] points of the current FP32 evaluation (tensor-core tiles)
   DBuf<int> d_err;       // set by a tensor-core kernel whose wait gave up
@@ -170,11 +197,17 @@ struct pnfam_ctx {
   long long pit64 = 0, pit32 = 0;   // point-iterations per precision in the last solve
   int G = 1;
   int nsm = 1;
+  int maxdb = 0;
+  // FP32 densities on the tensor cores (k_density_tc) instead of the SIMT kernel,
+  // chosen at context creation by PNFAM_GB300_TC_DENSITY=1; off by default: on
+  // N_sh = 16 the SIMT kernel is still the faster of the two
+  bool tc_density = false;
   int nchunk_bro = 1, nchunk_c = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t evt[2] = {nullptr, nullptr};   // whole-solve device time
-  double stage_ms[8] = {0};
+  double stage_ms[8] = {0};     // FP64 evaluations (0-4) and the common stages (5-7)
+  double stage32_ms[5] = {0};   // FP32 evaluations of the mixed form
   double total_ms = 0.0;
   long long launches = 0;
   pnfam_engine* engine = nullptr;   // the engine using this context's solve buffers
@@ -202,6 +235,7 @@ struct pnfam_ctx {
     k1b.d_tasks.release(); k1b.d_tile2task.release();
     k2a.d_tasks.release(); k2a.d_tile2task.release();
     k2b.d_tasks.release(); k2b.d_tile2task.release();
+    t1a.d_tasks.release(); t1b.d_tasks.release(); t2a.d_tasks.release(); t2b.d_tasks.release();
     if (ev[0]) cudaEventDestroy(ev[0]);
     if (ev[1]) cudaEventDestroy(ev[1]);
     if (evt[0]) cudaEventDestroy(evt[0]);
@@ -360,6 +394,7 @@ static void build_tasks(pnfam_ctx* c) {
   // tensor-core tiles: rows of the output block (N <= 128, padded to 16) against up to
   // 64 columns x pg points (M = 128 = Re and Im of 64 hpsi rows)
   c->htasks_tc.clear();
+  c->tc_npmax = 16;
   auto add_tc = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
     const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
     const int seg[3] = {0, nu, d};
@@ -377,6 +412,7 @@ static void build_tasks(pnfam_ctx* c) {
           h.np = std::max(16, cdiv(na, 16) * 16);
           h.pg = std::max(1, std::min<int>(HTC_MAXPG, HTC_MAXB / h.nbc));
           c->htasks_tc.push_back(h);
+          c->tc_npmax = std::max(c->tc_npmax, h.np);
         }
       }
     }
@@ -448,6 +484,17 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, con
   return PNFAM_OK;
 }
 
+// FP32 stage on the tensor cores for the nact points listed in c->d_actlist
+static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact) {
+  if (tl.tasks.empty() || nact <= 0) return PNFAM_OK;
+  dim3 grid((unsigned)tl.tasks.size(), (unsigned)((2 * nact * tl.maxrows + 127) / 128));
+  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), c->stream>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_actlist.p, nact,
+                                                                     c->d_err.p);
+  c->launches++;
+  CK(cudaGetLastError());
+  return PNFAM_OK;
+}
+
 static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
   return launch_gemm<double>(c, tl, P, active, c->d_bufs.p);
 }
@@ -465,7 +512,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
     cudaEventSynchronize(c->ev[1]);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
-    c->stage_ms[k] += ms;
+    (std::is_same<T, float>::value ? c->stage32_ms : c->stage_ms)[k] += ms;
   };
   constexpr bool f32 = std::is_same<T, float>::value;
   const BufDescT<T>* bufs;
@@ -477,8 +524,13 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   }
   int rc;
   tic();
-  if ((rc = launch_gemm<T>(c, c->k1a, P, act, bufs))) return rc;
-  if ((rc = launch_gemm<T>(c, c->k1b, P, act, bufs))) return rc;
+  if constexpr (f32) {
+    if ((rc = launch_gemm_tc(c, c->t1a, nact))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t1b, nact))) return rc;
+  } else {
+    if ((rc = launch_gemm<T>(c, c->k1a, P, act, bufs))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k1b, P, act, bufs))) return rc;
+  }
   toc(0);
   const long long nxy = c->nxy;
   DensCallT<T> d0, d1;
@@ -495,8 +547,23 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   const int ntr = (c->nghl + DRT - 1) / DRT;
   const int na = std::max(nact, 1);
   const int G = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
+  int Gm = G;   // block-row groups of the partial densities
+  bool dens_done = false;
   tic();
-  {
+  if constexpr (f32) {
+    if (c->maxdb <= 128 && c->tc_density) {
+      // tensor cores: c->d_actlist holds the nact points of this evaluation
+      DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
+      DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
+      Gm = std::max(1, std::min(c->G, (c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
+      k_density_tc<<<dim3(ntr, Gm, 2 * na), DTC_THREADS, density_tc_smem_bytes(), c->stream>>>(
+          B, t0, t1, Gm, c->d_actlist.p, dpart, c->d_err.p);
+      c->launches++;
+      CK(cudaGetLastError());
+      dens_done = true;
+    }
+  }
+  if (!dens_done) {
     dim3 grid(ntr, G, 2 * P);
     k_density<T><<<grid, 256, density_smem_bytes<T>(), c->stream>>>(B, d0, d1, G, dpart, act);
     c->launches++;
@@ -506,7 +573,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   tic();
   {
     dim3 grid((c->nghl + 127) / 128, 2 * P);
-    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, G, dpart, mf, act);
+    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, Gm, dpart, mf, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -515,8 +582,8 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   if constexpr (f32) {
     // tensor cores: c->d_actlist holds the nact points of this evaluation
     dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
-    k_hproj_tc<<<grid, 256, hproj_tc_smem_bytes(), c->stream>>>(B, c->d_htasks_tc.p, c->d_actlist.p, nact, mf, hsp,
-                                                                 nxy, c->d_err.p);
+    k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), c->stream>>>(
+        B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, hsp, nxy, c->d_err.p);
     c->launches++;
     CK(cudaGetLastError());
   } else {
@@ -528,8 +595,13 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   }
   toc(3);
   tic();
-  if ((rc = launch_gemm<T>(c, c->k2a, P, act, bufs))) return rc;
-  if ((rc = launch_gemm<T>(c, c->k2b, P, act, bufs))) return rc;
+  if constexpr (f32) {
+    if ((rc = launch_gemm_tc(c, c->t2a, nact))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t2b, nact))) return rc;
+  } else {
+    if ((rc = launch_gemm<T>(c, c->k2a, P, act, bufs))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k2b, P, act, bufs))) return rc;
+  }
   toc(4);
   return PNFAM_OK;
 }
@@ -596,6 +668,11 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
   c->nb = basis->nb;
   c->nghl = basis->nghl;
   c->db.assign(basis->db, basis->db + c->nb);
+  c->maxdb = c->nb > 0 ? *std::max_element(c->db.begin(), c->db.end()) : 0;
+  {
+    const char* v = std::getenv("PNFAM_GB300_TC_DENSITY");
+    c->tc_density = v && v[0] == '1';
+  }
   c->nup.assign(basis->num_spin_up, basis->num_spin_up + c->nb);
   c->st.resize(c->nb);
   c->tr.resize(c->nb);
@@ -645,7 +722,11 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
       cudaFuncSetAttribute(k_hproj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)hproj_smem_bytes<float>()) != cudaSuccess ||
       cudaFuncSetAttribute(k_hproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)hproj_tc_smem_bytes()) != cudaSuccess) {
+                           (int)hproj_tc_smem_bytes(HTC_MAXN)) != cudaSuccess ||
+      cudaFuncSetAttribute(k_density_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)density_tc_smem_bytes()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)gemm_tc_smem_bytes()) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
   }
@@ -720,6 +801,16 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (2 * nf) / 4096));
   build_tasks(c);
   CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
+  {
+    TaskList* src[4] = {&c->k1a, &c->k1b, &c->k2a, &c->k2b};
+    TaskListTC* dst[4] = {&c->t1a, &c->t1b, &c->t2a, &c->t2b};
+    for (int k = 0; k < 4; ++k) {
+      dst[k]->build(*src[k]);
+      for (const GemmTaskTC& t : dst[k]->tasks)
+        if (t.ncols > 256) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: block larger than 256");
+      CK(upload(dst[k]->d_tasks, dst[k]->tasks.data(), dst[k]->tasks.size()));
+    }
+  }
   CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
   CK(upload(c->d_htasks_tc, c->htasks_tc.data(), c->htasks_tc.size()));
   c->have_op = true;
@@ -822,6 +913,7 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
   e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
   for (int k = 0; k < 8; ++k) c->stage_ms[k] = 0.0;
+  for (int k = 0; k < 5; ++k) c->stage32_ms[k] = 0.0;
   c->pit64 = 0; c->pit32 = 0; c->launches = 0;
   return PNFAM_OK;
 }
@@ -1240,11 +1332,18 @@ extern "C" int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* c, const double* re
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasisT<float> B = c->devbasis<float>();
   const int* act = c->d_active.p;
-  k_density<float><<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<float>(), c->stream>>>(
-      B, d0, d1, c->G, c->d_dpart32.p, act);
+  if (c->maxdb <= 128 && c->tc_density) {
+    DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
+    DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
+    k_density_tc<<<dim3((c->nghl + 31) / 32, c->G, 2), DTC_THREADS, density_tc_smem_bytes(), c->stream>>>(
+        B, t0, t1, c->G, c->d_actlist.p, c->d_dpart32.p, c->d_err.p);
+  } else {
+    k_density<float><<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<float>(), c->stream>>>(
+        B, d0, d1, c->G, c->d_dpart32.p, act);
+  }
   k_meanfield<float><<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart32.p, c->d_mf32.p, act);
-  k_hproj_tc<<<dim3((unsigned)c->htasks_tc.size(), 1), 256, hproj_tc_smem_bytes(), c->stream>>>(
-      B, c->d_htasks_tc.p, c->d_actlist.p, 1, c->d_mf32.p, c->d_hsp32.p, nxy, c->d_err.p);
+  k_hproj_tc<<<dim3((unsigned)c->htasks_tc.size(), 1), HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), c->stream>>>(
+      B, c->d_htasks_tc.p, c->d_actlist.p, 1, c->tc_npmax, c->d_mf32.p, c->d_hsp32.p, nxy, c->d_err.p);
   k_to_f64<<<dim3(1024, 1), 256, 0, c->stream>>>(c->d_hsp32.p, c->d_hsp.p, 8 * nxy, 0, nullptr);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
@@ -1267,6 +1366,7 @@ extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, in
   for (int k = 0; k < nstage && k < 8; ++k) stage_ms[k] = c->stage_ms[k];
   if (nstage > 8) stage_ms[8] = c->total_ms;
   if (nstage > 10) { stage_ms[9] = (double)c->pit64; stage_ms[10] = (double)c->pit32; }
+  for (int k = 11; k < nstage && k < 16; ++k) stage_ms[k] = c->stage32_ms[k - 11];
   if (launches) *launches = c->launches;
   return PNFAM_OK;
 }

@@ -113,6 +113,185 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks
 }
 
 // ---------------------------------------------------------------------------
+// grouped block GEMM on the tensor cores (FP32 data, 3xTF32 products).
+// Every term multiplies a per-point block (state, intermediate, field) by a
+// ground-state block (U or V) shared by all points.  The per-point operand is
+// put on the M side of the MMA so that the rows of all active points and both
+// planes (Re, Im) fill 128-row tiles:
+//   case 0 (per-point operand on the left):  D[i][j] = C[i][j],  D = op(P) op(S)
+//   case 1 (per-point operand on the right): D[j][i] = C[i][j],  D = op(P)^T op(S)^T
+// Rows: (point, plane, i) with i fastest; columns padded to a multiple of 16.
+// ---------------------------------------------------------------------------
+struct GemmTaskTC {
+  int M, N, K, nterm;
+  int rcase;              // 0 or 1, as above
+  int mrows, ncols, npad; // D rows per (point, plane), D columns, padded columns
+  GemmTerm t[PNFAM_MAXTERM];
+  long long coff;
+  int cbuf, ldc;
+};
+enum { GTC_K = 16, GTC_PROD = 256, GTC_THREADS = GTC_PROD + 32 };
+
+__host__ __device__ constexpr size_t gemm_tc_smem_bytes() {
+  return (size_t)2 * (2 * 128 * GTC_K + 2 * 256 * GTC_K) * sizeof(float);
+}
+
+// grid (ntasks, row tiles of 128); HTC_THREADS threads; dynamic smem gemm_tc_smem_bytes()
+__global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __restrict__ tasks,
+                                                            const BufDescT<float>* __restrict__ bufs,
+                                                            const int* __restrict__ actlist, int nact,
+                                                            int* __restrict__ err) {
+  const GemmTaskTC& Tk = tasks[blockIdx.x];
+  const int rows_total = 2 * nact * Tk.mrows;
+  const int R0 = blockIdx.y * 128;
+  if (R0 >= rows_total) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* stage_base = reinterpret_cast<float*>(smraw);
+  const int stage_floats = 2 * 128 * GTC_K + 2 * 256 * GTC_K;
+  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
+  __shared__ uint32_t tslot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int NP = Tk.npad, K = Tk.K, mr = Tk.mrows;
+  const int nkc = (K + GTC_K - 1) / GTC_K;
+  const int nchunk = Tk.nterm * nkc;
+  const uint32_t ncols = NP <= 32 ? 32u : NP <= 64 ? 64u : NP <= 128 ? 128u : 256u;
+  if (tid == 0) {
+    tc::mbar_init(&full_bar[0], GTC_PROD); tc::mbar_init(&full_bar[1], GTC_PROD);
+    tc::mbar_init(&empty_bar[0], 1); tc::mbar_init(&empty_bar[1], 1);
+    abort_flag = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tslot, ncols);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  if (warp < GTC_PROD / 32) {
+    // ---------------- producers ----------------
+    for (int c = 0; c < nchunk; ++c) {
+      const int st = c & 1;
+      if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
+      float* sAh = stage_base + st * stage_floats;
+      float* sAl = sAh + 128 * GTC_K;
+      float* sBh = sAl + 128 * GTC_K;
+      float* sBl = sBh + 256 * GTC_K;
+      const GemmTerm& tm = Tk.t[c / nkc];
+      const int k0 = (c % nkc) * GTC_K;
+      // which operand of the term is the per-point one
+      const bool pa = Tk.rcase == 0;
+      const int pbuf = pa ? tm.abuf : tm.bbuf, sbuf = pa ? tm.bbuf : tm.abuf;
+      const long long poff = pa ? tm.aoff : tm.boff, soff = pa ? tm.boff : tm.aoff;
+      const int pld = pa ? tm.lda : tm.ldb, sld = pa ? tm.ldb : tm.lda;
+      const int ptr_ = pa ? tm.tA : tm.tB, str_ = pa ? tm.tB : tm.tA;
+      if (!abort_flag) {
+        // A[m][k]: row m = (point, plane, i); case 0: op(P)[i][k], case 1: op(P)[k][i]
+        for (int e = tid; e < 128 * (GTC_K / 4); e += GTC_PROD) {
+          const int m = e & 127, k4 = e >> 7, R = R0 + m;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (R < rows_total) {
+            const int i = R % mr, rest = R / mr, pl = rest & 1, p = actlist[rest >> 1];
+            const BufDescT<float> d = bufs[pbuf];
+            const float* P = d.base + (long long)p * d.sp + (long long)pl * d.spl + poff;
+            const float al = (float)tm.alpha[pl];
+            // element (i, k) of op(P) (case 0) or (k, i) of op(P) (case 1): stride in k
+            const bool kfast = pa ? ptr_ != 0 : ptr_ == 0;
+            const long long si = kfast ? pld : 1, sk = kfast ? 1 : pld;
+            float x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int k = k0 + 4 * k4 + u;
+              x[u] = k < K ? al * P[(long long)i * si + (long long)k * sk] : 0.f;
+            }
+            v = make_float4(x[0], x[1], x[2], x[3]);
+          }
+          const int o = tc::cm_off(m, 4 * k4, 128);
+          st_split4(sAh + o, sAl + o, v);
+        }
+        // B[n][k]: case 0: op(S)[k][n], case 1: op(S)[n][k]
+        for (int e = tid; e < NP * (GTC_K / 4); e += GTC_PROD) {
+          const int n = e % NP, k4 = e / NP;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (n < Tk.ncols) {
+            const float* S = bufs[sbuf].base + soff;
+            const bool kfast = pa ? str_ == 0 : str_ != 0;
+            const long long sn = kfast ? sld : 1, sk = kfast ? 1 : sld;
+            float x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int k = k0 + 4 * k4 + u;
+              x[u] = k < K ? S[(long long)n * sn + (long long)k * sk] : 0.f;
+            }
+            v = make_float4(x[0], x[1], x[2], x[3]);
+          }
+          const int o = tc::cm_off(n, 4 * k4, NP);
+          st_split4(sBh + o, sBl + o, v);
+        }
+      }
+      tc::fence_async_smem();
+      tc::mbar_arrive(&full_bar[st]);
+    }
+  } else if (tid == GTC_PROD) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t idesc = tc::idesc_tf32(128, NP);
+    const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(NP / 8) * 128;
+    for (int c = 0; c < nchunk; ++c) {
+      const int st = c & 1;
+      if (!abort_flag && !tc::mbar_wait(&full_bar[st], (c >> 1) & 1)) abort_flag = 1;
+      tc::fence_after();
+      if (!abort_flag) {
+        const float* sAh = stage_base + st * stage_floats;
+        const float* sAl = sAh + 128 * GTC_K;
+        const float* sBh = sAl + 128 * GTC_K;
+        const float* sBl = sBh + 256 * GTC_K;
+#pragma unroll
+        for (int ks = 0; ks < GTC_K / 8; ++ks) {
+          const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
+          const uint64_t ah = tc::sdesc(tc::smem_u32(sAh) + oa, lboA, 128);
+          const uint64_t al = tc::sdesc(tc::smem_u32(sAl) + oa, lboA, 128);
+          const uint64_t bh = tc::sdesc(tc::smem_u32(sBh) + ob, lboB, 128);
+          const uint64_t bl = tc::sdesc(tc::smem_u32(sBl) + ob, lboB, 128);
+          tc::mma_tf32(tmem, ah, bh, idesc, c > 0 || ks > 0);
+          tc::mma_tf32(tmem, ah, bl, idesc, true);
+          tc::mma_tf32(tmem, al, bh, idesc, true);
+        }
+      }
+      tc::mma_commit(&empty_bar[st]);
+    }
+  }
+  const int last = nchunk - 1;
+  bool ok = nchunk == 0 || tc::mbar_wait(&empty_bar[last & 1], (last >> 1) & 1);
+  ok = __syncthreads_and(ok && !abort_flag);
+  tc::fence_after();
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else if (warp < 4) {
+    const int m = tid, R = R0 + m;
+    const bool mine = R < rows_total;
+    const int i = mine ? R % mr : 0, rest = mine ? R / mr : 0, pl = rest & 1;
+    const int p = mine ? actlist[rest >> 1] : 0;
+    const BufDescT<float> d = bufs[Tk.cbuf];
+    float* C = d.base + (long long)p * d.sp + (long long)pl * d.spl + Tk.coff;
+    for (int n0 = 0; n0 < NP; n0 += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
+      if (mine) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int n = n0 + u;
+          if (n < Tk.ncols) {
+            if (Tk.rcase == 0) C[i + (long long)n * Tk.ldc] = v[u];
+            else C[n + (long long)i * Tk.ldc] = v[u];
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
 // basis on device
 // ---------------------------------------------------------------------------
 template <class T>
@@ -403,6 +582,357 @@ __global__ void __launch_bounds__(256, sizeof(T) >= 8 ? 1 : 2) k_density(DevBasi
 #pragma unroll
     for (int k = 0; k < 2 * ND; ++k) out[(long long)k * nghl + r] = acc[k];
   }
+}
+
+// ---------------------------------------------------------------------------
+// densities on the tensor cores (FP32 data, 3xTF32 products).
+// A CTA owns 32 mesh points r of one point p and one call, and walks the block
+// rows of its group.  For every (block row, spin s of the rows) "unit":
+//   W[m][n] = sum_{a in s} phi_q(a, r) rho(a, b; pl),  m = q*32 + (r - r0),
+//                                                     n = pl*dc + b
+// is accumulated in tensor memory (two accumulators, units alternate), and
+// folded by warps 0-7 into the 28 local densities: warp w reads the TMEM lanes
+// of component q = w % 4 and half of the columns, and adds the terms of the
+// density formulas (pnfam_hamiltonian_blas.f90:124-711) that contain W_q.
+// Warp 8 issues the MMAs.  The partial densities of the 8 warps are summed at
+// the end.  dpart: [P][2][G][2*ND][nghl]
+// ---------------------------------------------------------------------------
+enum { DTC_K = 16, DTC_MAXN = 256, DTC_PROD = 256, DTC_THREADS = DTC_PROD + 32 };
+
+__host__ __device__ constexpr size_t density_tc_smem_bytes() {
+  // two stages of A (128 x 16, hi and lo) and B (256 x 16, hi and lo); the end-of-CTA
+  // reduction buffer [8 warps][2*ND][32] reuses the same memory
+  return (size_t)2 * (2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K) * sizeof(float);
+}
+
+// the terms of the density formulas that contain W_q of rows with the SAME spin as b
+template <int Q>
+__device__ __forceinline__ void fold_same(float (&acc)[2 * ND], float wr, float wi, const float (&P)[4], float sg) {
+  const float h5 = 0.5f;
+#define A_(k, re, im) { acc[2 * (k)] += (re); acc[2 * (k) + 1] += (im); }
+  if (Q == 0) {
+    A_(D_RHO, wr * P[0], wi * P[0]);
+    A_(D_SZ, sg * wr * P[0], sg * wi * P[0]);
+    A_(D_JP, h5 * wr * P[2], h5 * wi * P[2]);
+    A_(D_TJPZ, sg * h5 * wr * P[2], sg * h5 * wi * P[2]);
+    A_(D_JR, -h5 * wi * P[1], h5 * wr * P[1]);
+    A_(D_TJRZ, -sg * h5 * wi * P[1], sg * h5 * wr * P[1]);
+    A_(D_JZ, -h5 * wi * P[3], h5 * wr * P[3]);
+    A_(D_TJZZ, -sg * h5 * wi * P[3], sg * h5 * wr * P[3]);
+    A_(D_GS, sg * wr * P[3], sg * wi * P[3]);
+  } else if (Q == 1) {
+    A_(D_TAU, wr * P[1], wi * P[1]);
+    A_(D_TZ, sg * wr * P[1], sg * wi * P[1]);
+    A_(D_JR, h5 * wi * P[0], -h5 * wr * P[0]);
+    A_(D_TJRZ, sg * h5 * wi * P[0], -sg * h5 * wr * P[0]);
+    A_(D_FR, h5 * sg * wr * P[3], h5 * sg * wi * P[3]);
+  } else if (Q == 2) {
+    A_(D_JP, h5 * wr * P[0], h5 * wi * P[0]);
+    A_(D_TJPZ, sg * h5 * wr * P[0], sg * h5 * wi * P[0]);
+    A_(D_TAU, wr * P[2], wi * P[2]);
+    A_(D_TZ, sg * wr * P[2], sg * wi * P[2]);
+    A_(D_FP, -h5 * sg * wi * P[3], h5 * sg * wr * P[3]);
+  } else {
+    A_(D_TAU, wr * P[3], wi * P[3]);
+    A_(D_TZ, sg * wr * P[3], sg * wi * P[3]);
+    A_(D_JZ, h5 * wi * P[0], -h5 * wr * P[0]);
+    A_(D_TJZZ, sg * h5 * wi * P[0], -sg * h5 * wr * P[0]);
+    A_(D_GS, sg * wr * P[0], sg * wi * P[0]);
+    A_(D_FR, h5 * sg * wr * P[1], h5 * sg * wi * P[1]);
+    A_(D_FP, h5 * sg * wi * P[2], -h5 * sg * wr * P[2]);
+    A_(D_FZ, sg * wr * P[3], sg * wi * P[3]);
+  }
+}
+
+// the terms that contain W_q of rows with the OPPOSITE spin to b (sig = +1 if b is spin down)
+template <int Q>
+__device__ __forceinline__ void fold_opp(float (&acc)[2 * ND], float wr, float wi, const float (&P)[4], float sig) {
+  const float h5 = 0.5f;
+  if (Q == 0) {
+    A_(D_GS, sig * wr * P[2] + wr * P[1], sig * wi * P[2] + wi * P[1]);
+    A_(D_SR, wr * P[0], wi * P[0]);
+    A_(D_SP, -sig * wi * P[0], sig * wr * P[0]);
+    A_(D_TJPR, h5 * wr * P[2], h5 * wi * P[2]);
+    A_(D_TJPP, -sig * h5 * wi * P[2], sig * h5 * wr * P[2]);
+    A_(D_TJRR, -h5 * wi * P[1], h5 * wr * P[1]);
+    A_(D_TJRP, -sig * h5 * wr * P[1], -sig * h5 * wi * P[1]);
+    A_(D_TJZR, -h5 * wi * P[3], h5 * wr * P[3]);
+    A_(D_TJZP, -sig * h5 * wr * P[3], -sig * h5 * wi * P[3]);
+  } else if (Q == 1) {
+    A_(D_GS, wr * P[0], wi * P[0]);
+    A_(D_FR, wr * P[1] + sig * h5 * wr * P[2], wi * P[1] + sig * h5 * wi * P[2]);
+    A_(D_FP, h5 * wi * P[2], -h5 * wr * P[2]);
+    A_(D_FZ, h5 * wr * P[3], h5 * wi * P[3]);
+    A_(D_TR, wr * P[1], wi * P[1]);
+    A_(D_TP, -sig * wi * P[1], sig * wr * P[1]);
+    A_(D_TJRR, h5 * wi * P[0], -h5 * wr * P[0]);
+    A_(D_TJRP, sig * h5 * wr * P[0], sig * h5 * wi * P[0]);
+  } else if (Q == 2) {
+    A_(D_GS, -sig * wr * P[0], -sig * wi * P[0]);
+    A_(D_FR, -sig * h5 * wr * P[1], -sig * h5 * wi * P[1]);
+    A_(D_FP, -(sig * wi * P[2] + h5 * wi * P[1]), sig * wr * P[2] + h5 * wr * P[1]);
+    A_(D_FZ, -sig * h5 * wr * P[3], -sig * h5 * wi * P[3]);
+    A_(D_TJPR, h5 * wr * P[0], h5 * wi * P[0]);
+    A_(D_TJPP, -sig * h5 * wi * P[0], sig * h5 * wr * P[0]);
+    A_(D_TR, wr * P[2], wi * P[2]);
+    A_(D_TP, -sig * wi * P[2], sig * wr * P[2]);
+  } else {
+    A_(D_FZ, h5 * (wr * P[1] + sig * wr * P[2]), h5 * (wi * P[1] + sig * wi * P[2]));
+    A_(D_TR, wr * P[3], wi * P[3]);
+    A_(D_TP, -sig * wi * P[3], sig * wr * P[3]);
+    A_(D_TJZR, h5 * wi * P[0], -h5 * wr * P[0]);
+    A_(D_TJZP, sig * h5 * wr * P[0], sig * h5 * wi * P[0]);
+  }
+}
+#undef A_
+
+struct DensTCArgs {
+  const float* rho; long long rho_sp, rho_spl;   // as DensCallT, per call
+  const int* rcols; const long long* roffs;
+  const float* kap; long long kap_sp, kap_spl;
+  const int* kcols; const long long* koffs;
+};
+
+// grid (ceil(nghl/32), G, 2*nact); DTC_THREADS threads; dynamic smem density_tc_smem_bytes()
+__global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> B, DensTCArgs c0, DensTCArgs c1, int G,
+                                                               const int* __restrict__ actlist,
+                                                               float* __restrict__ dpart, int* __restrict__ err) {
+  const int p = actlist[blockIdx.z >> 1], call = blockIdx.z & 1;
+  const DensTCArgs& C = call ? c1 : c0;
+  const int g = blockIdx.y;
+  const int r0 = blockIdx.x * 32;
+  const int nghl = B.nghl;
+  const long long ps = (long long)B.dqp * nghl;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* stage_base = reinterpret_cast<float*>(smraw);
+  const int stage_floats = 2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K;
+  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2], accf_bar[2], acce_bar[2];
+  __shared__ uint32_t tslot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    tc::mbar_init(&full_bar[0], DTC_PROD); tc::mbar_init(&full_bar[1], DTC_PROD);
+    tc::mbar_init(&empty_bar[0], 1); tc::mbar_init(&empty_bar[1], 1);
+    tc::mbar_init(&accf_bar[0], 1); tc::mbar_init(&accf_bar[1], 1);
+    tc::mbar_init(&acce_bar[0], DTC_PROD); tc::mbar_init(&acce_bar[1], DTC_PROD);
+    abort_flag = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  float acc[2 * ND];
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
+  // the units in order: (kind, block row, spin of the rows), non-empty only
+  auto unit_info = [&](int kind, int ix, int s, int& iy, int& d, int& dc, int& alo, int& ahi) {
+    const int* cols = kind == 0 ? C.rcols : C.kcols;
+    iy = cols[ix];
+    if (iy < 0) return false;
+    d = B.db[ix]; dc = B.db[iy];
+    const int nu = B.nup[ix];
+    alo = s == 0 ? 0 : nu; ahi = s == 0 ? nu : d;
+    return alo < ahi;
+  };
+  if (warp < DTC_PROD / 32) {
+    // ---------------- producers and folders ----------------
+    int cc = 0, u = 0;
+    // the unit being folded lags one behind the unit being produced
+    int pkind = -1, pix = 0, ps_ = 0;
+    auto fold = [&](int kind, int ix, int s, int uu) {
+      int iy, d, dc, alo, ahi;
+      unit_info(kind, ix, s, iy, d, dc, alo, ahi);
+      const int acc_i = uu & 1;
+      if (!abort_flag && !tc::mbar_wait(&accf_bar[acc_i], (uu >> 1) & 1)) abort_flag = 1;
+      tc::fence_after();
+      const int q = warp & 3, half = warp >> 2;
+      const int r = r0 + lane;
+      const int sbase = B.st[iy];
+      const float srow = s == 0 ? 1.f : -1.f;
+      const int nb8 = (dc + 7) / 8;
+      const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
+      const bool active_q = kind == 0 || q == 0;
+      for (int c8 = c8lo; c8 < c8hi; ++c8) {
+        float wre[8], wim[8];
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc_i * 256);
+        tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
+        tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
+        if (abort_flag || !active_q || r >= nghl) continue;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int b = 8 * c8 + i;
+          if (b >= dc) break;
+          const int jb = sbase + b;
+          const float sg = (float)B.ns[jb];
+          float P[4];
+          if (kind == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) P[k] = B.phi[k * ps + (long long)jb * nghl + r];
+            const bool same = sg == srow;
+            const float sig = sg < 0.f ? 1.f : -1.f;
+            switch (q) {
+              case 0: if (same) fold_same<0>(acc, wre[i], wim[i], P, sg); else fold_opp<0>(acc, wre[i], wim[i], P, sig); break;
+              case 1: if (same) fold_same<1>(acc, wre[i], wim[i], P, sg); else fold_opp<1>(acc, wre[i], wim[i], P, sig); break;
+              case 2: if (same) fold_same<2>(acc, wre[i], wim[i], P, sg); else fold_opp<2>(acc, wre[i], wim[i], P, sig); break;
+              default: if (same) fold_same<3>(acc, wre[i], wim[i], P, sg); else fold_opp<3>(acc, wre[i], wim[i], P, sig); break;
+            }
+          } else {
+            const float p0 = B.phi[(long long)jb * nghl + r];
+            const float xr = 2.f * wre[i] * p0, xi = 2.f * wim[i] * p0;
+            const float sig = sg < 0.f ? 1.f : -1.f;
+            if (sg == srow) {
+              acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
+              acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
+            } else {
+              acc[2 * D_RB] += -sg * xr; acc[2 * D_RB + 1] += -sg * xi;
+              acc[2 * D_SBZ] += xr; acc[2 * D_SBZ + 1] += xi;
+            }
+          }
+        }
+      }
+      tc::fence_before();
+      tc::mbar_arrive(&acce_bar[acc_i]);
+    };
+    for (int kind = 0; kind < 2; ++kind) {
+      const long long bsp = kind == 0 ? C.rho_sp : C.kap_sp, bspl = kind == 0 ? C.rho_spl : C.kap_spl;
+      const float* base = kind == 0 ? C.rho : C.kap;
+      const long long* offs = kind == 0 ? C.roffs : C.koffs;
+      const int nq = kind == 0 ? 4 : 1;
+      for (int ix = g; ix < B.nb; ix += G) {
+        for (int s = 0; s < 2; ++s) {
+          int iy, d, dc, alo, ahi;
+          if (!unit_info(kind, ix, s, iy, d, dc, alo, ahi)) continue;
+          const float* mat = base + (long long)p * bsp + offs[ix];
+          const int sa = B.st[ix];
+          const int npad = (2 * dc + 15) / 16 * 16;
+          const int nk = (ahi - alo + DTC_K - 1) / DTC_K;
+          for (int kc = 0; kc < nk; ++kc, ++cc) {
+            const int st = cc & 1;
+            if (cc >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((cc >> 1) - 1) & 1)) abort_flag = 1;
+            float* sAh = stage_base + st * stage_floats;
+            float* sAl = sAh + 128 * DTC_K;
+            float* sBh = sAl + 128 * DTC_K;
+            float* sBl = sBh + DTC_MAXN * DTC_K;
+            const int a0 = alo + kc * DTC_K;
+            if (!abort_flag) {
+              // A[m = q*32 + l][k] = phi_q(a0 + k, r0 + l)
+              for (int e = tid; e < 128 * (DTC_K / 4); e += DTC_PROD) {
+                const int m = e & 127, k4 = e >> 7;
+                const int q = m >> 5, r = r0 + (m & 31);
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (q < nq && r < nghl) {
+                  const float* src = B.phi + q * ps + (long long)(sa + a0 + 4 * k4) * nghl + r;
+                  const int a = a0 + 4 * k4;
+                  if (a < ahi) v.x = src[0];
+                  if (a + 1 < ahi) v.y = src[nghl];
+                  if (a + 2 < ahi) v.z = src[2 * nghl];
+                  if (a + 3 < ahi) v.w = src[3 * nghl];
+                }
+                const int o = tc::cm_off(m, 4 * k4, 128);
+                st_split4(sAh + o, sAl + o, v);
+              }
+              // B[n = pl*dc + b][k] = rho(a0 + k, b; pl)
+              for (int e = tid; e < npad * (DTC_K / 4); e += DTC_PROD) {
+                const int n = e % npad, k4 = e / npad;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (n < 2 * dc) {
+                  const int pl = n >= dc ? 1 : 0, b = n - pl * dc;
+                  const float* src = mat + (long long)pl * bspl + (long long)b * d + a0 + 4 * k4;
+                  const int a = a0 + 4 * k4;
+                  if (a < ahi) v.x = src[0];
+                  if (a + 1 < ahi) v.y = src[1];
+                  if (a + 2 < ahi) v.z = src[2];
+                  if (a + 3 < ahi) v.w = src[3];
+                }
+                const int o = tc::cm_off(n, 4 * k4, npad);
+                st_split4(sBh + o, sBl + o, v);
+              }
+            }
+            tc::fence_async_smem();
+            tc::mbar_arrive(&full_bar[st]);
+          }
+          if (pkind >= 0) fold(pkind, pix, ps_, u - 1);
+          pkind = kind; pix = ix; ps_ = s;
+          ++u;
+        }
+      }
+    }
+    if (pkind >= 0) fold(pkind, pix, ps_, u - 1);
+  } else if (tid == DTC_PROD) {
+    // ---------------- MMA issuer ----------------
+    int cc = 0, u = 0;
+    for (int kind = 0; kind < 2; ++kind) {
+      for (int ix = g; ix < B.nb; ix += G) {
+        for (int s = 0; s < 2; ++s) {
+          int iy, d, dc, alo, ahi;
+          if (!unit_info(kind, ix, s, iy, d, dc, alo, ahi)) continue;
+          const int acc_i = u & 1;
+          // the fold of the unit that used this accumulator two units ago is done
+          if (u >= 2 && !abort_flag && !tc::mbar_wait(&acce_bar[acc_i], ((u >> 1) - 1) & 1)) abort_flag = 1;
+          tc::fence_after();
+          const int npad = (2 * dc + 15) / 16 * 16;
+          const uint32_t idesc = tc::idesc_tf32(128, npad);
+          const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(npad / 8) * 128;
+          const int nk = (ahi - alo + DTC_K - 1) / DTC_K;
+          const uint32_t dacc = tmem + (uint32_t)(acc_i * 256);
+          for (int kc = 0; kc < nk; ++kc, ++cc) {
+            const int st = cc & 1;
+            if (!abort_flag && !tc::mbar_wait(&full_bar[st], (cc >> 1) & 1)) abort_flag = 1;
+            tc::fence_after();
+            if (!abort_flag) {
+              const float* sAh = stage_base + st * stage_floats;
+              const float* sAl = sAh + 128 * DTC_K;
+              const float* sBh = sAl + 128 * DTC_K;
+              const float* sBl = sBh + DTC_MAXN * DTC_K;
+#pragma unroll
+              for (int ks = 0; ks < DTC_K / 8; ++ks) {
+                const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
+                const uint64_t ah = tc::sdesc(tc::smem_u32(sAh) + oa, lboA, 128);
+                const uint64_t al = tc::sdesc(tc::smem_u32(sAl) + oa, lboA, 128);
+                const uint64_t bh = tc::sdesc(tc::smem_u32(sBh) + ob, lboB, 128);
+                const uint64_t bl = tc::sdesc(tc::smem_u32(sBl) + ob, lboB, 128);
+                tc::mma_tf32(dacc, ah, bh, idesc, kc > 0 || ks > 0);
+                tc::mma_tf32(dacc, ah, bl, idesc, true);
+                tc::mma_tf32(dacc, al, bh, idesc, true);
+              }
+            }
+            tc::mma_commit(&empty_bar[st]);
+          }
+          tc::mma_commit(&accf_bar[acc_i]);   // W of this unit complete
+          ++u;
+        }
+      }
+    }
+    // nothing may be in flight when the tensor memory is released (the folds wait for
+    // every unit, but not after an abort)
+    if (u > 0 && !tc::mbar_wait(&accf_bar[(u - 1) & 1], ((u - 1) >> 1) & 1)) abort_flag = 1;
+  }
+  // all folds done (each arrived on its accumulator's empty barrier); sum the 8 warps
+  tc::fence_before();
+  const bool ok = __syncthreads_and(!abort_flag);
+  float* red = stage_base;   // [8][2*ND][32], the stages are no longer in use
+  if (warp < 8) {
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k) red[(warp * 2 * ND + k) * 32 + lane] = acc[k];
+  }
+  __syncthreads();
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    float* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
+    for (int e = tid; e < 2 * ND * 32; e += blockDim.x) {
+      const int k = e / 32, l = e % 32;
+      if (r0 + l >= nghl) continue;
+      float v = 0.f;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) v += red[(w * 2 * ND + k) * 32 + l];
+      out[(long long)k * nghl + r0 + l] = v;
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -789,8 +1319,12 @@ __global__ void __launch_bounds__(256, 1) k_hproj(DevBasisT<T> B, const HTask* _
 //   m = pl*64 + j, j = (point in the group)*nbc + b   (rows: Re, then Im of hpsi)
 //   n = a (the rows of the output block, N padded to np)
 //   k = (q, r), 32 mesh points of one component q per chunk.
-// hpsi is generated on the fly from the field tensor (as in k_hproj) into shared
-// memory; D accumulates in tensor memory and out_ab = 2 D.
+// Warps 0-7 produce the operands of a chunk (hpsi generated from the field
+// tensor and the column basis functions, the row basis functions staged) into
+// one of two shared-memory stages; warp 8 issues the MMAs of a chunk as soon as
+// its stage is full and releases the stage through tcgen05.commit, so operand
+// production and tensor-core work overlap.  D accumulates in tensor memory and
+// out_ab = 2 D.
 // ---------------------------------------------------------------------------
 struct HTaskTC {
   int ix, iy, a0, na, b0, nbc, sa, mode, call, outq;
@@ -798,52 +1332,31 @@ struct HTaskTC {
   int pg;          // points per CTA (pg * nbc <= 64)
   long long ooff;
 };
-enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8 };
+enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
 
-__host__ __device__ constexpr size_t hproj_tc_smem_bytes() {
-  return (size_t)(2 * 128 * HTC_K + 2 * HTC_MAXN * HTC_K + 5 * HTC_MAXB * HTC_K + HTC_MAXPG * 2 * 5 * 2 * HTC_K) *
-         sizeof(float);
+// dynamic shared memory for tiles of at most npmax output rows: two stages of
+// A (128 x 32, hi and lo) and B (npmax x 32, hi and lo)
+__host__ __device__ constexpr size_t hproj_tc_smem_bytes(int npmax) {
+  return (size_t)2 * (2 * 128 * HTC_K + 2 * npmax * HTC_K) * sizeof(float);
 }
 
-// four consecutive floats of row `row` (mesh points r..r+3 of one state), zero outside
-__device__ __forceinline__ float4 ld_row4(const float* __restrict__ src, int r, int nghl, bool ok) {
-  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (!ok) return v;
-  if ((nghl & 3) == 0 && r + 3 < nghl) return *reinterpret_cast<const float4*>(src + r);
-  if (r < nghl) v.x = src[r];
-  if (r + 1 < nghl) v.y = src[r + 1];
-  if (r + 2 < nghl) v.z = src[r + 2];
-  if (r + 3 < nghl) v.w = src[r + 3];
-  return v;
-}
-
-__device__ __forceinline__ void st_split4(float* hi, float* lo, float4 v) {
-  float4 h, l;
-  tc::split(v.x, h.x, l.x); tc::split(v.y, h.y, l.y); tc::split(v.z, h.z, l.z); tc::split(v.w, h.w, l.w);
-  *reinterpret_cast<float4*>(hi) = h;
-  *reinterpret_cast<float4*>(lo) = l;
-}
-
-// grid (ntasks, point groups); 256 threads; dynamic smem hproj_tc_smem_bytes()
+// grid (ntasks, point groups); HTC_THREADS threads; dynamic smem hproj_tc_smem_bytes(npmax)
 // actlist[nact]: the points to evaluate; err: set to 1 if a wait on the tensor
 // cores gave up (the CTA then writes nothing)
-__global__ void __launch_bounds__(256, 1) k_hproj_tc(DevBasisT<float> B, const HTaskTC* __restrict__ tasks,
-                                                     const int* __restrict__ actlist, int nact,
-                                                     const float* __restrict__ mf, float* __restrict__ hsp,
-                                                     long long nxy, int* __restrict__ err) {
+__global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B, const HTaskTC* __restrict__ tasks,
+                                                             const int* __restrict__ actlist, int nact, int npmax,
+                                                             const float* __restrict__ mf, float* __restrict__ hsp,
+                                                             long long nxy, int* __restrict__ err) {
   const HTaskTC Th = tasks[blockIdx.x];
   const int g0 = blockIdx.y * Th.pg;
   if (g0 >= nact) return;
   const int npg = min(Th.pg, nact - g0);
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* sAh = reinterpret_cast<float*>(smraw);
-  float* sAl = sAh + 128 * HTC_K;
-  float* sBh = sAl + 128 * HTC_K;
-  float* sBl = sBh + HTC_MAXN * HTC_K;
-  float* sPhiB = sBl + HTC_MAXN * HTC_K;         // [5][64 b][32 r]
-  float* sMF = sPhiB + 5 * HTC_MAXB * HTC_K;      // [pg][2 pl][5 iz][2 sb][32 r]
-  __shared__ __align__(8) uint64_t mbar;
+  float* stage_base = reinterpret_cast<float*>(smraw);
+  const int stage_floats = 2 * 128 * HTC_K + 2 * npmax * HTC_K;
+  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tslot;
+  __shared__ volatile int abort_flag;
   __shared__ signed char sns[HTC_MAXB];
   __shared__ int spt[HTC_MAXPG];
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -852,70 +1365,92 @@ __global__ void __launch_bounds__(256, 1) k_hproj_tc(DevBasisT<float> B, const H
   const long long ps = (long long)B.dqp * nghl;
   const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
   const int nc = Th.mode == 0 ? 5 : 1;
+  const int nrc = (nghl + HTC_K - 1) / HTC_K;   // chunks per component
+  const int nchunk = nc * nrc;
   const uint32_t ncols = NP <= 32 ? 32u : NP <= 64 ? 64u : NP <= 128 ? 128u : 256u;
   if (tid < HTC_MAXB) sns[tid] = tid < nbc ? B.ns[jb0 + tid] : (signed char)1;
   if (tid < HTC_MAXPG) spt[tid] = tid < npg ? actlist[g0 + tid] : 0;
-  if (tid == 0) tc::mbar_init(&mbar, 1);
+  if (tid == 0) {
+    tc::mbar_init(&full_bar[0], HTC_PROD); tc::mbar_init(&full_bar[1], HTC_PROD);
+    tc::mbar_init(&empty_bar[0], 1); tc::mbar_init(&empty_bar[1], 1);
+    abort_flag = 0;
+  }
   if (warp == 0) tc::tmem_alloc(&tslot, ncols);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = tslot;
-  const uint32_t idesc = tc::idesc_tf32(128, NP);
-  bool ok = true;
-  int chunk = 0;
-  for (int q = 0; q < nc; ++q) {
-    for (int r0 = 0; r0 < nghl; r0 += HTC_K, ++chunk) {
-      if (chunk > 0 && !tc::mbar_wait(&mbar, (chunk - 1) & 1)) ok = false;  // operands free again
-      if (!__syncthreads_and(ok)) { ok = false; break; }
-      tc::fence_after();
-      // basis functions of the columns and the field of each point, current q
-      for (int e = tid; e < nc * HTC_MAXB * 8; e += blockDim.x) {
-        const int r4 = e & 7, b = (e >> 3) % HTC_MAXB, iz = e / (8 * HTC_MAXB);
-        const float4 v = ld_row4(B.phi + iz * ps + (long long)(jb0 + b) * nghl, r0 + 4 * r4, nghl, b < nbc);
-        *reinterpret_cast<float4*>(&sPhiB[(iz * HTC_MAXB + b) * HTC_K + 4 * r4]) = v;
-      }
-      for (int e = tid; e < npg * 2 * nc * 2 * 8; e += blockDim.x) {
-        const int r4 = e & 7, sb = (e >> 3) & 1, iz = (e >> 4) % nc, pl = (e / (16 * nc)) & 1,
-                  pi = e / (32 * nc);
-        const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb == 0 ? 1 : -1) : 100 + (Th.sa < 0 ? 2 : 0) + sb;
-        const float* src = mf + ((long long)spt[pi] * 2 + Th.call) * NMF * 2 * nghl + ((long long)slot * 2 + pl) * nghl;
-        const float4 v = ld_row4(src, r0 + 4 * r4, nghl, true);
-        *reinterpret_cast<float4*>(&sMF[((((pi * 2 + pl) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]) = v;
-      }
-      __syncthreads();
-      // A operand: hpsi rows (Re at j, Im at 64 + j), 4 mesh points per item
-      for (int e = tid; e < HTC_MAXB * 8; e += blockDim.x) {
-        const int j = e % HTC_MAXB, r4 = e / HTC_MAXB;
-        float4 hr = make_float4(0.f, 0.f, 0.f, 0.f), hi = hr;
-        if (j < nj) {
-          const int pi = j / nbc, b = j % nbc;
-          const int sb = sns[b] > 0 ? 0 : 1;
-          for (int iz = 0; iz < nc; ++iz) {
-            const float4 f = *reinterpret_cast<const float4*>(&sPhiB[(iz * HTC_MAXB + b) * HTC_K + 4 * r4]);
-            const float4 mr = *reinterpret_cast<const float4*>(&sMF[((((pi * 2 + 0) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]);
-            const float4 mi = *reinterpret_cast<const float4*>(&sMF[((((pi * 2 + 1) * 5 + iz) * 2 + sb) * HTC_K) + 4 * r4]);
-            hr.x = fmaf(mr.x, f.x, hr.x); hr.y = fmaf(mr.y, f.y, hr.y); hr.z = fmaf(mr.z, f.z, hr.z); hr.w = fmaf(mr.w, f.w, hr.w);
-            hi.x = fmaf(mi.x, f.x, hi.x); hi.y = fmaf(mi.y, f.y, hi.y); hi.z = fmaf(mi.z, f.z, hi.z); hi.w = fmaf(mi.w, f.w, hi.w);
+  const float* mfbase = mf + (long long)Th.call * NMF * 2 * nghl;
+  if (warp < HTC_PROD / 32) {
+    // ---------------- producers ----------------
+    // chunks in mesh-point-major order: the column basis functions phi_iz(b, r) of a
+    // thread's two A items stay in registers for the nc components of one r range
+    float4 fz[2][5];
+    for (int c = 0; c < nchunk; ++c) {
+      const int st = c & 1;
+      if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
+      float* sAh = stage_base + st * stage_floats;
+      float* sAl = sAh + 128 * HTC_K;
+      float* sBh = sAl + 128 * HTC_K;
+      float* sBl = sBh + npmax * HTC_K;
+      const int q = c % nc, r0 = (c / nc) * HTC_K;
+      if (!abort_flag) {
+        // A: hpsi rows, Re at j, Im at 64 + j, four mesh points per item
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+          const int e = tid + it * HTC_PROD;
+          const int j = e % HTC_MAXB, r4 = e / HTC_MAXB, r = r0 + 4 * r4;
+          float4 hr = make_float4(0.f, 0.f, 0.f, 0.f), hi = hr;
+          if (j < nj) {
+            const int pi = j / nbc, b = j % nbc;
+            const int sb = sns[b] > 0 ? 1 : -1;
+            if (q == 0) {
+#pragma unroll
+              for (int iz = 0; iz < 5; ++iz)
+                if (iz < nc) fz[it][iz] = ld_row4(B.phi + iz * ps + (long long)(jb0 + b) * nghl, r, nghl, true);
+            }
+            const float* mp = mfbase + (long long)spt[pi] * 2 * NMF * 2 * nghl;
+            float4 mr[5], mi[5];
+#pragma unroll
+            for (int iz = 0; iz < 5; ++iz) {
+              if (iz < nc) {
+                const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb) : 100 + (Th.sa < 0 ? 2 : 0) + (sb < 0 ? 1 : 0);
+                mr[iz] = ld_row4(mp + (long long)slot * 2 * nghl, r, nghl, true);
+                mi[iz] = ld_row4(mp + ((long long)slot * 2 + 1) * nghl, r, nghl, true);
+              }
+            }
+#pragma unroll
+            for (int iz = 0; iz < 5; ++iz)
+              if (iz < nc) { fma4(hr, mr[iz], fz[it][iz]); fma4(hi, mi[iz], fz[it][iz]); }
           }
+          const int o_re = tc::cm_off(j, 4 * r4, 128), o_im = tc::cm_off(64 + j, 4 * r4, 128);
+          st_split4(sAh + o_re, sAl + o_re, hr);
+          st_split4(sAh + o_im, sAl + o_im, hi);
         }
-        const int o_re = tc::cm_off(j, 4 * r4, 128), o_im = tc::cm_off(64 + j, 4 * r4, 128);
-        st_split4(sAh + o_re, sAl + o_re, hr);
-        st_split4(sAh + o_im, sAl + o_im, hi);
-      }
-      // B operand: phi_q(a, r) of the output rows
-      for (int e = tid; e < NP * 8; e += blockDim.x) {
-        const int n = e % NP, r4 = e / NP;
-        const float4 v = ld_row4(B.phi + q * ps + (long long)(ja0 + n) * nghl, r0 + 4 * r4, nghl, n < Th.na);
-        const int o = tc::cm_off(n, 4 * r4, NP);
-        st_split4(sBh + o, sBl + o, v);
+        // B: phi_q(a, r) of the output rows
+        for (int e = tid; e < NP * 8; e += HTC_PROD) {
+          const int n = e % NP, r4 = e / NP;
+          const float4 v = ld_row4(B.phi + q * ps + (long long)(ja0 + n) * nghl, r0 + 4 * r4, nghl, n < Th.na);
+          const int o = tc::cm_off(n, 4 * r4, NP);
+          st_split4(sBh + o, sBl + o, v);
+        }
       }
       tc::fence_async_smem();
-      tc::fence_before();
-      __syncthreads();
-      if (tid == 0) {
-        tc::fence_after();
-        const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(NP / 8) * 128;
+      tc::mbar_arrive(&full_bar[st]);
+    }
+  } else if (tid == HTC_PROD) {
+    // ---------------- MMA issuer (one thread of warp 8) ----------------
+    const uint32_t idesc = tc::idesc_tf32(128, NP);
+    const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(NP / 8) * 128;
+    for (int c = 0; c < nchunk; ++c) {
+      const int st = c & 1;
+      if (!abort_flag && !tc::mbar_wait(&full_bar[st], (c >> 1) & 1)) abort_flag = 1;
+      tc::fence_after();
+      if (!abort_flag) {
+        const float* sAh = stage_base + st * stage_floats;
+        const float* sAl = sAh + 128 * HTC_K;
+        const float* sBh = sAl + 128 * HTC_K;
+        const float* sBl = sBh + npmax * HTC_K;
 #pragma unroll
         for (int ks = 0; ks < HTC_K / 8; ++ks) {
           const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
@@ -923,19 +1458,18 @@ __global__ void __launch_bounds__(256, 1) k_hproj_tc(DevBasisT<float> B, const H
           const uint64_t al = tc::sdesc(tc::smem_u32(sAl) + oa, lboA, 128);
           const uint64_t bh = tc::sdesc(tc::smem_u32(sBh) + ob, lboB, 128);
           const uint64_t bl = tc::sdesc(tc::smem_u32(sBl) + ob, lboB, 128);
-          tc::mma_tf32(tmem, ah, bh, idesc, chunk > 0 || ks > 0);
+          tc::mma_tf32(tmem, ah, bh, idesc, c > 0 || ks > 0);
           tc::mma_tf32(tmem, ah, bl, idesc, true);
           tc::mma_tf32(tmem, al, bh, idesc, true);
         }
-        tc::mma_commit(&mbar);
       }
+      tc::mma_commit(&empty_bar[st]);   // stage free (and, for the last chunk, D complete)
     }
-    if (!ok) break;
   }
-  // the last commit covers every MMA issued; wait for it (again, bounded, after a
-  // failed wait) so that nothing is in flight when the tensor memory is released
-  if (chunk > 0 && !tc::mbar_wait(&mbar, (chunk - 1) & 1)) ok = false;
-  ok = __syncthreads_and(ok);
+  // every MMA issued before the last commit has completed once its phase flips
+  const int last = nchunk - 1;
+  bool ok = tc::mbar_wait(&empty_bar[last & 1], (last >> 1) & 1);
+  ok = __syncthreads_and(ok && !abort_flag);
   tc::fence_after();
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);

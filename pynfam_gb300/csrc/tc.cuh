@@ -81,6 +81,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
   return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread
 __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
   asm volatile(
@@ -109,4 +113,30 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 }
 
 }  // namespace tc
+
+// operand staging helpers: four consecutive floats of one row (mesh points r..r+3 of
+// one state), zero outside the mesh or when !ok
+__device__ __forceinline__ float4 ld_row4(const float* __restrict__ src, int r, int nghl, bool ok) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!ok) return v;
+  if ((nghl & 3) == 0 && r + 3 < nghl) return *reinterpret_cast<const float4*>(src + r);
+  if (r < nghl) v.x = src[r];
+  if (r + 1 < nghl) v.y = src[r + 1];
+  if (r + 2 < nghl) v.z = src[r + 2];
+  if (r + 3 < nghl) v.w = src[r + 3];
+  return v;
+}
+
+__device__ __forceinline__ void st_split4(float* hi, float* lo, float4 v) {
+  float4 h, l;
+  tc::split(v.x, h.x, l.x); tc::split(v.y, h.y, l.y); tc::split(v.z, h.z, l.z); tc::split(v.w, h.w, l.w);
+  *reinterpret_cast<float4*>(hi) = h;
+  *reinterpret_cast<float4*>(lo) = l;
+}
+
+__device__ __forceinline__ void fma4(float4& acc, float4 m, float4 f) {
+  acc.x = fmaf(m.x, f.x, acc.x); acc.y = fmaf(m.y, f.y, acc.y);
+  acc.z = fmaf(m.z, f.z, acc.z); acc.w = fmaf(m.w, f.w, acc.w);
+}
+
 }  // namespace pnfam

@@ -121,10 +121,13 @@ class GPUSolver:
                            hist.reshape(P, max_iter + 1, 3) if hist is not None else None, dt)
 
     def last_profile(self):
-        ms = np.zeros(11); n = C.c_longlong()
-        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 11, C.byref(n)))
+        """Per-stage device ms of the last solve (or of this context's engine so far);
+        the *_fp32 entries are the FP32 evaluations of the mixed form."""
+        ms = np.zeros(16); n = C.c_longlong()
+        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 16, C.byref(n)))
         names = ("k1_blockgemm", "density", "meanfield", "field_projection", "k2_blockgemm", "green", "broyden",
-                 "strength", "total", "point_iterations_fp64", "point_iterations_fp32")
+                 "strength", "total", "point_iterations_fp64", "point_iterations_fp32", "k1_blockgemm_fp32",
+                 "density_fp32", "meanfield_fp32", "field_projection_fp32", "k2_blockgemm_fp32")
         return dict(zip(names, ms.tolist())), int(n.value)
 
     def calc_hamiltonian(self, rho_pn, kp, rho_np, km, mixed=False):

@@ -313,3 +313,14 @@ def test_large_basis_mixed_field_matches_fp64(large_case):
     worst = _mixed_vs_fp64(large_case, 4)
     print(f"N_sh=12 162Gd GT-K1: mixed field worst relative error {worst:.2e}")
     assert worst <= 1e-5
+
+
+def test_tensor_core_density_matches_fp64(monkeypatch):
+    """The tensor-core density kernel (selected by PNFAM_GB300_TC_DENSITY=1 when the
+    context is created) in the mixed field evaluation, against the FP64 field."""
+    monkeypatch.setenv("PNFAM_GB300_TC_DENSITY", "1")
+    for case, op in (("S40", "RS1-K1"), ("Kr116", "P-K0")):
+        c, _ = case_for(case, op, 0)
+        worst = _mixed_vs_fp64(c, 5)
+        print(f"{case} {op}: mixed field (tensor-core densities) worst relative error {worst:.2e}")
+        assert worst <= 1e-5
