@@ -365,31 +365,21 @@ static void build_tasks(pnfam_ctx* c) {
                  {{1.0, 1.0}, c->ublk(UL, i, 1), H(3, j, c->foff, c->fc, 1), c->vblk(VR, j, 0)}},
                 B_HQP, nxy + c->yoff[i], c->db[i], c->db[y]);
   }
-  // ---- field projection tasks: spin-uniform row ranges, 4x4 outputs per thread,
-  // tiles sized to the blocks (at most 128 rows or columns, 256 threads) ----
+  // ---- FP64 field projection tasks: spin-uniform 32 x 32 tiles ----
   c->htasks.clear();
   auto cdiv = [](int a, int b) { return (a + b - 1) / b; };
   auto add_h = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
     const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
     const int seg[3] = {0, nu, d};
-    for (int s = 0; s < 2; ++s) {
-      const int nseg = seg[s + 1] - seg[s];
-      if (nseg <= 0) continue;
-      const int wa = cdiv(nseg, cdiv(nseg, 4 * HP_MAXR));
-      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += wa) {
-        const int na = std::min(wa, seg[s + 1] - a0), rows = cdiv(na, 4);
-        const int cmax = std::min<int>(HP_MAXC, 256 / rows);
-        const int wb = cdiv(dc, cdiv(dc, 4 * cmax));
-        for (int b0 = 0; b0 < dc; b0 += wb) {
+    for (int s = 0; s < 2; ++s)
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += 32)
+        for (int b0 = 0; b0 < dc; b0 += 32) {
           HTask h;
-          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = na;
-          h.b0 = b0; h.nbc = std::min(wb, dc - b0); h.sa = s == 0 ? 1 : -1;
+          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = std::min(32, seg[s + 1] - a0);
+          h.b0 = b0; h.nbc = std::min(32, dc - b0); h.sa = s == 0 ? 1 : -1;
           h.mode = mode; h.call = call; h.outq = outq; h.ooff = ooff;
-          h.rows = rows; h.cols = cdiv(h.nbc, 4);
           c->htasks.push_back(h);
         }
-      }
-    }
   };
   // tensor-core tiles: rows of the output block (N <= 128, padded to 16) against up to
   // 64 columns x pg points (M = 128 = Re and Im of 64 hpsi rows)
@@ -543,10 +533,12 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   d1.kap = rsp + 2 * nxy; d1.kap_sp = 8 * nxy; d1.kap_spl = 4 * nxy;
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasisT<T> B = c->devbasis<T>();
-  // block-row groups: enough CTAs to fill the GPU twice over for the active points
+  // block-row groups: FP32, enough CTAs to fill the GPU twice over for the active
+  // points; FP64, always the context's group count, so that a point's sums (and its
+  // result) do not depend on which other points share the evaluation
   const int ntr = (c->nghl + DRT - 1) / DRT;
   const int na = std::max(nact, 1);
-  const int G = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
+  const int G = f32 ? std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na))) : c->G;
   int Gm = G;   // block-row groups of the partial densities
   bool dens_done = false;
   tic();
@@ -555,7 +547,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
       // tensor cores: c->d_actlist holds the nact points of this evaluation
       DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
       DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
-      Gm = std::max(1, std::min(c->G, (c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
+      Gm = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
       k_density_tc<<<dim3(ntr, Gm, 2 * na), DTC_THREADS, density_tc_smem_bytes(), c->stream>>>(
           B, t0, t1, Gm, c->d_actlist.p, dpart, c->d_err.p);
       c->launches++;
@@ -565,7 +557,8 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   }
   if (!dens_done) {
     dim3 grid(ntr, G, 2 * P);
-    k_density<T><<<grid, 256, density_smem_bytes<T>(), c->stream>>>(B, d0, d1, G, dpart, act);
+    if constexpr (f32) k_density<float><<<grid, 256, density_smem_bytes<float>(), c->stream>>>(B, d0, d1, G, dpart, act);
+    else k_density_fp64<<<grid, 256, 0, c->stream>>>(B, d0, d1, G, dpart, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -587,9 +580,8 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
     c->launches++;
     CK(cudaGetLastError());
   } else {
-    const size_t smem = hproj_smem_bytes<T>();
     dim3 grid((unsigned)c->htasks.size(), P);
-    k_hproj<T><<<grid, 256, smem, c->stream>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
+    k_hproj_fp64<<<grid, 256, hproj_fp64_smem_bytes(), c->stream>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -717,10 +709,8 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
   }
-  if (cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)hproj_smem_bytes<double>()) != cudaSuccess ||
-      cudaFuncSetAttribute(k_hproj<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)hproj_smem_bytes<float>()) != cudaSuccess ||
+  if (cudaFuncSetAttribute(k_hproj_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)hproj_fp64_smem_bytes()) != cudaSuccess ||
       cudaFuncSetAttribute(k_hproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)hproj_tc_smem_bytes(HTC_MAXN)) != cudaSuccess ||
       cudaFuncSetAttribute(k_density_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -797,7 +787,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
     for (int i = 0; i < nb; ++i) nrows += c->fc[i] >= 0;
     c->G = std::max(1, std::min(nrows, (2 * std::max(nsm, 1) + ntr - 1) / ntr));
   }
-  c->nchunk_bro = (int)std::min<long long>(64, std::max<long long>(1, (4 * nf) / 4096));
+  c->nchunk_bro = (int)((4 * nf + BRO_CHUNK - 1) / BRO_CHUNK);
   c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (2 * nf) / 4096));
   build_tasks(c);
   CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
@@ -1283,10 +1273,10 @@ extern "C" int pnfam_gpu_calc_hamiltonian(pnfam_ctx_t* c, const double* re_rho_p
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasis B = c->devbasis<double>();
   const int* act = c->d_active.p;
-  k_density<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<double>(), c->stream>>>(
-      B, d0, d1, c->G, c->d_dpart.p, act);
+  k_density_fp64<<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, 0, c->stream>>>(B, d0, d1, c->G, c->d_dpart.p,
+                                                                                 act);
   k_meanfield<<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart.p, c->d_mf.p, act);
-  k_hproj<<<dim3((unsigned)c->htasks.size(), 1), 256, hproj_smem_bytes<double>(), c->stream>>>(
+  k_hproj_fp64<<<dim3((unsigned)c->htasks.size(), 1), 256, hproj_fp64_smem_bytes(), c->stream>>>(
       B, c->d_htasks.p, c->d_mf.p, c->d_hsp.p, nxy, act);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
@@ -1430,8 +1420,8 @@ int noalloc_setup(unsigned char** out) {
     if (e != cudaSuccess)
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaGetSymbolAddress: ") +
                                    cudaGetErrorString(e));
-    e = cudaFuncSetAttribute(k_hproj<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hproj_smem_bytes<double>());
+    e = cudaFuncSetAttribute(k_hproj_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hproj_fp64_smem_bytes());
     if (e != cudaSuccess)
       return fail(PNFAM_ECUDA, std::string("pnfam_gpu_calc_hamiltonian_noalloc: cudaFuncSetAttribute: ") +
                                    cudaGetErrorString(e));
@@ -1560,10 +1550,10 @@ extern "C" int pnfam_gpu_calc_hamiltonian_noalloc(
   d1.rcols = ints + 3 * NA_MAX_NB; d1.roffs = longs;
   d1.kap = rsp + 2 * nf; d1.kap_sp = 8 * nf; d1.kap_spl = 4 * nf;
   d1.kcols = ints + 5 * NA_MAX_NB; d1.koffs = longs + 2 * NA_MAX_NB;
-  k_density<<<dim3((nghl + DRT - 1) / DRT, NA_G, 2), 256, density_smem_bytes<double>(), st>>>(B, d0, d1, NA_G,
-                                                                                             dpart, act);
+  k_density_fp64<<<dim3((nghl + DRT - 1) / DRT, NA_G, 2), 256, 0, st>>>(B, d0, d1, NA_G, dpart, act);
   k_meanfield<<<dim3((nghl + 127) / 128, 2), 128, 0, st>>>(B, NA_G, dpart, mf, act);
-  k_hproj<<<dim3((unsigned)c.htasks.size(), 1), 256, hproj_smem_bytes<double>(), st>>>(B, dtasks, mf, hsp, nf, act);
+  k_hproj_fp64<<<dim3((unsigned)c.htasks.size(), 1), 256, hproj_fp64_smem_bytes(), st>>>(B, dtasks, mf, hsp, nf,
+                                                                                       act);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};
   for (int k = 0; k < 8; ++k)

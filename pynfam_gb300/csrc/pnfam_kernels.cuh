@@ -585,24 +585,266 @@ __global__ void __launch_bounds__(256, sizeof(T) >= 8 ? 1 : 2) k_density(DevBasi
 }
 
 // ---------------------------------------------------------------------------
+// FP64 densities (the drop-in form and the anchors of the mixed form): a CTA of
+// 32 mesh points x 8 column lanes; each lane accumulates W for one column b over
+// chunks of DAK rows and folds it into the densities with shuffle reductions over
+// the 8 lanes.  FP64 is bound by the DFMA rate, so the tiles follow the blocks
+// closely (8 columns per chunk, rows exact).
+// ---------------------------------------------------------------------------
+#define DBC 8    // b columns per chunk
+#define DAK 16   // a rows per chunk
+
+__device__ __forceinline__ double red8(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+
+// grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT r x DBC b
+// dpart: [P][2][G][2*ND][nghl]
+__global__ void __launch_bounds__(256) k_density_fp64(DevBasis B, DensCall c0, DensCall c1, int G,
+                                                      double* __restrict__ dpart, const int* __restrict__ active) {
+  using T = double;
+  const int p = blockIdx.z >> 1, call = blockIdx.z & 1;
+  if (!active[p]) return;
+  const DensCall& C = call ? c1 : c0;
+  const int g = blockIdx.y;
+  const int r0 = blockIdx.x * DRT;
+  const int rl = threadIdx.x >> 3, bl = threadIdx.x & 7;
+  const int nghl = B.nghl;
+  const int r = r0 + rl;
+  const bool rok = r < nghl;
+  __shared__ T acc[2 * ND][DRT];
+  __shared__ T sphi[4][DAK][DRT];  // static smem: ~33 KB
+  __shared__ T srho[2][DAK][DBC];
+  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) (&acc[0][0])[e] = 0;
+  __syncthreads();
+  const long long ps = (long long)B.dqp * nghl;
+  const T h5 = (T)0.5, two = (T)2;
+
+#define ACC(k, re, im)                                   \
+  {                                                      \
+    const T vr_ = red8(re), vi_ = red8(im);       \
+    if (bl == 0) { acc[2 * (k)][rl] += vr_; acc[2 * (k) + 1][rl] += vi_; } \
+  }
+
+  // ---------------- normal densities ----------------
+  for (int ix = g; ix < B.nb; ix += G) {
+    const int iy = C.rcols[ix];
+    if (iy < 0) continue;
+    const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
+    const int sa = B.st[ix], sb = B.st[iy];
+    const T* rho = C.rho + (long long)p * C.rho_sp + C.roffs[ix];
+    for (int b0 = 0; b0 < dc; b0 += DBC) {
+      const int b = b0 + bl;
+      T w[2][4][2];
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { w[s][q][0] = 0; w[s][q][1] = 0; }
+      for (int a0 = 0; a0 < d; a0 += DAK) {
+        const int na = min(DAK, d - a0);
+        for (int e = threadIdx.x; e < 4 * DAK * DRT; e += 256) {
+          const int q = e / (DAK * DRT), rem = e % (DAK * DRT), aa = rem / DRT, rr = rem % DRT;
+          T v = 0;
+          if (aa < na && r0 + rr < nghl) v = B.phi[q * ps + (long long)(sa + a0 + aa) * nghl + r0 + rr];
+          sphi[q][aa][rr] = v;
+        }
+        for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
+          const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
+          T v = 0;
+          if (aa < na && b0 + bb < dc) v = rho[(long long)pl * C.rho_spl + (a0 + aa) + (long long)(b0 + bb) * d];
+          srho[pl][aa][bb] = v;
+        }
+        __syncthreads();
+        // spin-up rows first: split the chunk at the spin boundary
+        const int nup_here = max(0, min(na, nu - a0));
+        for (int aa = 0; aa < nup_here; ++aa) {
+          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const T f = sphi[q][aa][rl];
+            w[0][q][0] = fma(f, re, w[0][q][0]); w[0][q][1] = fma(f, im, w[0][q][1]);
+          }
+        }
+        for (int aa = nup_here; aa < na; ++aa) {
+          const T re = srho[0][aa][bl], im = srho[1][aa][bl];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const T f = sphi[q][aa][rl];
+            w[1][q][0] = fma(f, re, w[1][q][0]); w[1][q][1] = fma(f, im, w[1][q][1]);
+          }
+        }
+        __syncthreads();
+      }
+      // epilogue: contributions of column b at mesh point r
+      T P0 = 0, P1 = 0, P2 = 0, P3 = 0, sg = 0;
+      const bool ok = rok && b < dc;
+      if (ok) {
+        const int jb = sb + b;
+        P0 = B.phi[0 * ps + (long long)jb * nghl + r];
+        P1 = B.phi[1 * ps + (long long)jb * nghl + r];
+        P2 = B.phi[2 * ps + (long long)jb * nghl + r];
+        P3 = B.phi[3 * ps + (long long)jb * nghl + r];
+        sg = (T)B.ns[jb];
+      }
+      const int si = (sg > 0) ? 0 : 1;  // same-spin set of wfa
+      // select S (same spin as b) and O (opposite)
+      T Sr[4], Si[4], Or[4], Oi[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        Sr[q] = si == 0 ? w[0][q][0] : w[1][q][0]; Si[q] = si == 0 ? w[0][q][1] : w[1][q][1];
+        Or[q] = si == 0 ? w[1][q][0] : w[0][q][0]; Oi[q] = si == 0 ? w[1][q][1] : w[0][q][1];
+        if (!ok) { Sr[q] = Si[q] = Or[q] = Oi[q] = 0; }
+      }
+      const T sig = (sg < 0) ? (T)1 : (T)-1;  // +1 if b is spin down
+      T xr, xi;
+      // diagonal in spin
+      xr = Sr[0] * P0; xi = Si[0] * P0;
+      ACC(D_RHO, xr, xi);
+      ACC(D_SZ, sg * xr, sg * xi);
+      xr = h5 * (Sr[0] * P2 + Sr[2] * P0); xi = h5 * (Si[0] * P2 + Si[2] * P0);
+      ACC(D_JP, xr, xi);
+      ACC(D_TJPZ, sg * xr, sg * xi);
+      xr = Sr[1] * P1 + Sr[2] * P2 + Sr[3] * P3; xi = Si[1] * P1 + Si[2] * P2 + Si[3] * P3;
+      ACC(D_TAU, xr, xi);
+      ACC(D_TZ, sg * xr, sg * xi);
+      xr = h5 * (Sr[0] * P1 - Sr[1] * P0); xi = h5 * (Si[0] * P1 - Si[1] * P0);
+      ACC(D_JR, -xi, xr);
+      ACC(D_TJRZ, -sg * xi, sg * xr);
+      xr = h5 * (Sr[0] * P3 - Sr[3] * P0); xi = h5 * (Si[0] * P3 - Si[3] * P0);
+      ACC(D_JZ, -xi, xr);
+      ACC(D_TJZZ, -sg * xi, sg * xr);
+      // gs: diagonal part + off-diagonal parts
+      {
+        T gr = sg * (Sr[0] * P3 + Sr[3] * P0), gi = sg * (Si[0] * P3 + Si[3] * P0);
+        gr += sig * (Or[0] * P2 - Or[2] * P0) + (Or[0] * P1 + Or[1] * P0);
+        gi += sig * (Oi[0] * P2 - Oi[2] * P0) + (Oi[0] * P1 + Oi[1] * P0);
+        ACC(D_GS, gr, gi);
+      }
+      {
+                T fr = h5 * sg * (Sr[1] * P3 + Sr[3] * P1), fi = h5 * sg * (Si[1] * P3 + Si[3] * P1);
+        fr += Or[1] * P1 + sig * h5 * (Or[1] * P2 - Or[2] * P1);
+        fi += Oi[1] * P1 + sig * h5 * (Oi[1] * P2 - Oi[2] * P1);
+        ACC(D_FR, fr, fi);
+      }
+      {
+        // fp += i*sg*(S2P3 - S3P2)/2 + i*(sig*O2P2 + (O2P1 - O1P2)/2)
+                const T ar = h5 * sg * (Sr[2] * P3 - Sr[3] * P2) + sig * Or[2] * P2 + h5 * (Or[2] * P1 - Or[1] * P2);
+        const T ai = h5 * sg * (Si[2] * P3 - Si[3] * P2) + sig * Oi[2] * P2 + h5 * (Oi[2] * P1 - Oi[1] * P2);
+        ACC(D_FP, -ai, ar);
+      }
+      {
+                T zr = sg * Sr[3] * P3, zi = sg * Si[3] * P3;
+        zr += h5 * (Or[3] * P1 + sig * Or[3] * P2 + Or[1] * P3 - sig * Or[2] * P3);
+        zi += h5 * (Oi[3] * P1 + sig * Oi[3] * P2 + Oi[1] * P3 - sig * Oi[2] * P3);
+        ACC(D_FZ, zr, zi);
+      }
+      // not diagonal in spin
+      xr = Or[0] * P0; xi = Oi[0] * P0;
+      ACC(D_SR, xr, xi);
+      ACC(D_SP, -sig * xi, sig * xr);
+      xr = h5 * (Or[2] * P0 + Or[0] * P2); xi = h5 * (Oi[2] * P0 + Oi[0] * P2);
+      ACC(D_TJPR, xr, xi);
+      ACC(D_TJPP, -sig * xi, sig * xr);
+      xr = Or[1] * P1 + Or[2] * P2 + Or[3] * P3; xi = Oi[1] * P1 + Oi[2] * P2 + Oi[3] * P3;
+      ACC(D_TR, xr, xi);
+      ACC(D_TP, -sig * xi, sig * xr);
+      xr = h5 * (Or[0] * P1 - Or[1] * P0); xi = h5 * (Oi[0] * P1 - Oi[1] * P0);
+      ACC(D_TJRR, -xi, xr);
+      ACC(D_TJRP, -sig * xr, -sig * xi);
+      xr = h5 * (Or[0] * P3 - Or[3] * P0); xi = h5 * (Oi[0] * P3 - Oi[3] * P0);
+      ACC(D_TJZR, -xi, xr);
+      ACC(D_TJZP, -sig * xr, -sig * xi);
+    }
+  }
+  // ---------------- pairing densities ----------------
+  for (int ix = g; ix < B.nb; ix += G) {
+    const int iy = C.kcols[ix];
+    if (iy < 0) continue;
+    const int d = B.db[ix], dc = B.db[iy], nu = B.nup[ix];
+    const int sa = B.st[ix], sb = B.st[iy];
+    const T* kap = C.kap + (long long)p * C.kap_sp + C.koffs[ix];
+    for (int b0 = 0; b0 < dc; b0 += DBC) {
+      const int b = b0 + bl;
+      T w[2][2] = {{0, 0}, {0, 0}};
+      for (int a0 = 0; a0 < d; a0 += DAK) {
+        const int na = min(DAK, d - a0);
+        for (int e = threadIdx.x; e < DAK * DRT; e += 256) {
+          const int aa = e / DRT, rr = e % DRT;
+          T v = 0;
+          if (aa < na && r0 + rr < nghl) v = B.phi[(long long)(sa + a0 + aa) * nghl + r0 + rr];
+          sphi[0][aa][rr] = v;
+        }
+        for (int e = threadIdx.x; e < 2 * DAK * DBC; e += 256) {
+          const int pl = e / (DAK * DBC), rem = e % (DAK * DBC), aa = rem / DBC, bb = rem % DBC;
+          T v = 0;
+          if (aa < na && b0 + bb < dc) v = kap[(long long)pl * C.kap_spl + (a0 + aa) + (long long)(b0 + bb) * d];
+          srho[pl][aa][bb] = v;
+        }
+        __syncthreads();
+        const int nup_here = max(0, min(na, nu - a0));
+        for (int aa = 0; aa < nup_here; ++aa) {
+          const T f = sphi[0][aa][rl];
+          w[0][0] = fma(f, srho[0][aa][bl], w[0][0]); w[0][1] = fma(f, srho[1][aa][bl], w[0][1]);
+        }
+        for (int aa = nup_here; aa < na; ++aa) {
+          const T f = sphi[0][aa][rl];
+          w[1][0] = fma(f, srho[0][aa][bl], w[1][0]); w[1][1] = fma(f, srho[1][aa][bl], w[1][1]);
+        }
+        __syncthreads();
+      }
+      T P0 = 0, sg = 0;
+      const bool ok = rok && b < dc;
+      if (ok) {
+        const int jb = sb + b;
+        P0 = B.phi[(long long)jb * nghl + r];
+        sg = (T)B.ns[jb];
+      }
+      const int si = (sg > 0) ? 0 : 1;
+      T Sr = si == 0 ? w[0][0] : w[1][0], Si = si == 0 ? w[0][1] : w[1][1];
+      T Or = si == 0 ? w[1][0] : w[0][0], Oi = si == 0 ? w[1][1] : w[0][1];
+      if (!ok) { Sr = Si = Or = Oi = 0; }
+      const T sig = (sg < 0) ? (T)1 : (T)-1;
+      T xr = two * Or * P0, xi = two * Oi * P0;
+      ACC(D_RB, -sg * xr, -sg * xi);
+      ACC(D_SBZ, xr, xi);
+      xr = two * Sr * P0; xi = two * Si * P0;
+      ACC(D_SBR, sig * xr, sig * xi);
+      ACC(D_SBP, xi, -xr);
+    }
+  }
+#undef ACC
+  __syncthreads();
+  T* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
+  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) {
+    const int k = e / DRT, rr = e % DRT;
+    if (r0 + rr < nghl) out[(long long)k * nghl + r0 + rr] = acc[k][rr];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // densities on the tensor cores (FP32 data, 3xTF32 products).
 // A CTA owns 32 mesh points r of one point p and one call, and walks the block
 // rows of its group.  For every (block row, spin s of the rows) "unit":
 //   W[m][n] = sum_{a in s} phi_q(a, r) rho(a, b; pl),  m = q*32 + (r - r0),
 //                                                     n = pl*dc + b
-// is accumulated in tensor memory (two accumulators, units alternate), and
-// folded by warps 0-7 into the 28 local densities: warp w reads the TMEM lanes
-// of component q = w % 4 and half of the columns, and adds the terms of the
-// density formulas (pnfam_hamiltonian_blas.f90:124-711) that contain W_q.
-// Warp 8 issues the MMAs.  The partial densities of the 8 warps are summed at
-// the end.  dpart: [P][2][G][2*ND][nghl]
+// is accumulated in tensor memory (one accumulator of up to 256 columns, so two
+// CTAs share an SM), and folded by warps 0-7 into the 28 local densities: warp w
+// reads the TMEM lanes of component q = w % 4 and half of the columns, and adds
+// the terms of the density formulas (pnfam_hamiltonian_blas.f90:124-711) that
+// contain W_q, with the column basis functions phi_q'(b, r) staged in shared
+// memory once per block.  Warp 8 issues the MMAs.  The partial densities of the
+// 8 warps are summed at the end.  dpart: [P][2][G][2*ND][nghl]
 // ---------------------------------------------------------------------------
-enum { DTC_K = 16, DTC_MAXN = 256, DTC_PROD = 256, DTC_THREADS = DTC_PROD + 32 };
+enum { DTC_K = 8, DTC_MAXN = 256, DTC_MAXB = 128, DTC_PROD = 256, DTC_THREADS = DTC_PROD + 32 };
 
 __host__ __device__ constexpr size_t density_tc_smem_bytes() {
-  // two stages of A (128 x 16, hi and lo) and B (256 x 16, hi and lo); the end-of-CTA
-  // reduction buffer [8 warps][2*ND][32] reuses the same memory
-  return (size_t)2 * (2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K) * sizeof(float);
+  // two stages of A (128 x 8, hi and lo) and B (256 x 8, hi and lo), then the column
+  // basis functions [128 b][32 r][4 q]; the end-of-CTA reduction buffer
+  // [8 warps][2*ND][32] reuses the same memory
+  return (size_t)(2 * (2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K) + DTC_MAXB * 32 * 4) * sizeof(float);
 }
 
 // the terms of the density formulas that contain W_q of rows with the SAME spin as b
@@ -694,7 +936,7 @@ struct DensTCArgs {
 };
 
 // grid (ceil(nghl/32), G, 2*nact); DTC_THREADS threads; dynamic smem density_tc_smem_bytes()
-__global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> B, DensTCArgs c0, DensTCArgs c1, int G,
+__global__ void __launch_bounds__(DTC_THREADS, 2) k_density_tc(DevBasisT<float> B, DensTCArgs c0, DensTCArgs c1, int G,
                                                                const int* __restrict__ actlist,
                                                                float* __restrict__ dpart, int* __restrict__ err) {
   const int p = actlist[blockIdx.z >> 1], call = blockIdx.z & 1;
@@ -706,18 +948,18 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
   extern __shared__ __align__(16) unsigned char smraw[];
   float* stage_base = reinterpret_cast<float*>(smraw);
   const int stage_floats = 2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K;
-  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2], accf_bar[2], acce_bar[2];
+  float* sPb = stage_base + 2 * stage_floats;   // [b][r][q'] column basis functions of the block
+  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2], accf_bar, acce_bar;
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     tc::mbar_init(&full_bar[0], DTC_PROD); tc::mbar_init(&full_bar[1], DTC_PROD);
     tc::mbar_init(&empty_bar[0], 1); tc::mbar_init(&empty_bar[1], 1);
-    tc::mbar_init(&accf_bar[0], 1); tc::mbar_init(&accf_bar[1], 1);
-    tc::mbar_init(&acce_bar[0], DTC_PROD); tc::mbar_init(&acce_bar[1], DTC_PROD);
+    tc::mbar_init(&accf_bar, 1); tc::mbar_init(&acce_bar, DTC_PROD);
     abort_flag = 0;
   }
-  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -725,7 +967,6 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
   float acc[2 * ND];
 #pragma unroll
   for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
-  // the units in order: (kind, block row, spin of the rows), non-empty only
   auto unit_info = [&](int kind, int ix, int s, int& iy, int& d, int& dc, int& alo, int& ahi) {
     const int* cols = kind == 0 ? C.rcols : C.kcols;
     iy = cols[ix];
@@ -737,63 +978,7 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
   };
   if (warp < DTC_PROD / 32) {
     // ---------------- producers and folders ----------------
-    int cc = 0, u = 0;
-    // the unit being folded lags one behind the unit being produced
-    int pkind = -1, pix = 0, ps_ = 0;
-    auto fold = [&](int kind, int ix, int s, int uu) {
-      int iy, d, dc, alo, ahi;
-      unit_info(kind, ix, s, iy, d, dc, alo, ahi);
-      const int acc_i = uu & 1;
-      if (!abort_flag && !tc::mbar_wait(&accf_bar[acc_i], (uu >> 1) & 1)) abort_flag = 1;
-      tc::fence_after();
-      const int q = warp & 3, half = warp >> 2;
-      const int r = r0 + lane;
-      const int sbase = B.st[iy];
-      const float srow = s == 0 ? 1.f : -1.f;
-      const int nb8 = (dc + 7) / 8;
-      const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
-      const bool active_q = kind == 0 || q == 0;
-      for (int c8 = c8lo; c8 < c8hi; ++c8) {
-        float wre[8], wim[8];
-        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc_i * 256);
-        tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
-        tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
-        if (abort_flag || !active_q || r >= nghl) continue;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int b = 8 * c8 + i;
-          if (b >= dc) break;
-          const int jb = sbase + b;
-          const float sg = (float)B.ns[jb];
-          float P[4];
-          if (kind == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) P[k] = B.phi[k * ps + (long long)jb * nghl + r];
-            const bool same = sg == srow;
-            const float sig = sg < 0.f ? 1.f : -1.f;
-            switch (q) {
-              case 0: if (same) fold_same<0>(acc, wre[i], wim[i], P, sg); else fold_opp<0>(acc, wre[i], wim[i], P, sig); break;
-              case 1: if (same) fold_same<1>(acc, wre[i], wim[i], P, sg); else fold_opp<1>(acc, wre[i], wim[i], P, sig); break;
-              case 2: if (same) fold_same<2>(acc, wre[i], wim[i], P, sg); else fold_opp<2>(acc, wre[i], wim[i], P, sig); break;
-              default: if (same) fold_same<3>(acc, wre[i], wim[i], P, sg); else fold_opp<3>(acc, wre[i], wim[i], P, sig); break;
-            }
-          } else {
-            const float p0 = B.phi[(long long)jb * nghl + r];
-            const float xr = 2.f * wre[i] * p0, xi = 2.f * wim[i] * p0;
-            const float sig = sg < 0.f ? 1.f : -1.f;
-            if (sg == srow) {
-              acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
-              acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
-            } else {
-              acc[2 * D_RB] += -sg * xr; acc[2 * D_RB + 1] += -sg * xi;
-              acc[2 * D_SBZ] += xr; acc[2 * D_SBZ + 1] += xi;
-            }
-          }
-        }
-      }
-      tc::fence_before();
-      tc::mbar_arrive(&acce_bar[acc_i]);
-    };
+    int cc = 0, u = 0, staged_iy = -1, staged_kind = -1;
     for (int kind = 0; kind < 2; ++kind) {
       const long long bsp = kind == 0 ? C.rho_sp : C.kap_sp, bspl = kind == 0 ? C.rho_spl : C.kap_spl;
       const float* base = kind == 0 ? C.rho : C.kap;
@@ -852,13 +1037,74 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
             tc::fence_async_smem();
             tc::mbar_arrive(&full_bar[st]);
           }
-          if (pkind >= 0) fold(pkind, pix, ps_, u - 1);
-          pkind = kind; pix = ix; ps_ = s;
+          // ---- fold this unit: the column basis functions of block iy (staged once per block)
+          if (iy != staged_iy || kind != staged_kind) {
+            asm volatile("bar.sync 1, %0;" ::"r"(DTC_PROD) : "memory");   // previous fold done with sPb
+            const int sb = B.st[iy];
+            for (int e = tid; e < dc * 32; e += DTC_PROD) {
+              const int b = e >> 5, l = e & 31, r = r0 + l;
+              float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (r < nghl) {
+                const float* src = B.phi + (long long)(sb + b) * nghl + r;
+                v.x = src[0];
+                if (kind == 0) { v.y = src[ps]; v.z = src[2 * ps]; v.w = src[3 * ps]; }
+              }
+              *reinterpret_cast<float4*>(&sPb[(b * 32 + l) * 4]) = v;
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(DTC_PROD) : "memory");
+            staged_iy = iy; staged_kind = kind;
+          }
+          if (!abort_flag && !tc::mbar_wait(&accf_bar, u & 1)) abort_flag = 1;
+          tc::fence_after();
+          {
+            const int q = warp & 3, half = warp >> 2;
+            const int r = r0 + lane;
+            const int sbase = B.st[iy];
+            const float srow = s == 0 ? 1.f : -1.f;
+            const int nb8 = (dc + 7) / 8;
+            const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
+            const bool active_q = kind == 0 || q == 0;
+            const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+            for (int c8 = c8lo; c8 < c8hi; ++c8) {
+              float wre[8], wim[8];
+              tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
+              tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
+              if (abort_flag || !active_q || r >= nghl) continue;
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                const int b = 8 * c8 + i;
+                if (b >= dc) break;
+                const float sg = (float)B.ns[sbase + b];
+                const float sig = sg < 0.f ? 1.f : -1.f;
+                const float4 pv = *reinterpret_cast<const float4*>(&sPb[(b * 32 + lane) * 4]);
+                const float P[4] = {pv.x, pv.y, pv.z, pv.w};
+                if (kind == 0) {
+                  const bool same = sg == srow;
+                  switch (q) {
+                    case 0: if (same) fold_same<0>(acc, wre[i], wim[i], P, sg); else fold_opp<0>(acc, wre[i], wim[i], P, sig); break;
+                    case 1: if (same) fold_same<1>(acc, wre[i], wim[i], P, sg); else fold_opp<1>(acc, wre[i], wim[i], P, sig); break;
+                    case 2: if (same) fold_same<2>(acc, wre[i], wim[i], P, sg); else fold_opp<2>(acc, wre[i], wim[i], P, sig); break;
+                    default: if (same) fold_same<3>(acc, wre[i], wim[i], P, sg); else fold_opp<3>(acc, wre[i], wim[i], P, sig); break;
+                  }
+                } else {
+                  const float xr = 2.f * wre[i] * P[0], xi = 2.f * wim[i] * P[0];
+                  if (sg == srow) {
+                    acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
+                    acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
+                  } else {
+                    acc[2 * D_RB] += -sg * xr; acc[2 * D_RB + 1] += -sg * xi;
+                    acc[2 * D_SBZ] += xr; acc[2 * D_SBZ + 1] += xi;
+                  }
+                }
+              }
+            }
+          }
+          tc::fence_before();
+          tc::mbar_arrive(&acce_bar);   // accumulator free for the next unit
           ++u;
         }
       }
     }
-    if (pkind >= 0) fold(pkind, pix, ps_, u - 1);
   } else if (tid == DTC_PROD) {
     // ---------------- MMA issuer ----------------
     int cc = 0, u = 0;
@@ -867,15 +1113,13 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
         for (int s = 0; s < 2; ++s) {
           int iy, d, dc, alo, ahi;
           if (!unit_info(kind, ix, s, iy, d, dc, alo, ahi)) continue;
-          const int acc_i = u & 1;
-          // the fold of the unit that used this accumulator two units ago is done
-          if (u >= 2 && !abort_flag && !tc::mbar_wait(&acce_bar[acc_i], ((u >> 1) - 1) & 1)) abort_flag = 1;
+          // the fold of the previous unit has read the accumulator
+          if (u >= 1 && !abort_flag && !tc::mbar_wait(&acce_bar, (u - 1) & 1)) abort_flag = 1;
           tc::fence_after();
           const int npad = (2 * dc + 15) / 16 * 16;
           const uint32_t idesc = tc::idesc_tf32(128, npad);
           const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(npad / 8) * 128;
           const int nk = (ahi - alo + DTC_K - 1) / DTC_K;
-          const uint32_t dacc = tmem + (uint32_t)(acc_i * 256);
           for (int kc = 0; kc < nk; ++kc, ++cc) {
             const int st = cc & 1;
             if (!abort_flag && !tc::mbar_wait(&full_bar[st], (cc >> 1) & 1)) abort_flag = 1;
@@ -885,30 +1129,25 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
               const float* sAl = sAh + 128 * DTC_K;
               const float* sBh = sAl + 128 * DTC_K;
               const float* sBl = sBh + DTC_MAXN * DTC_K;
-#pragma unroll
-              for (int ks = 0; ks < DTC_K / 8; ++ks) {
-                const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
-                const uint64_t ah = tc::sdesc(tc::smem_u32(sAh) + oa, lboA, 128);
-                const uint64_t al = tc::sdesc(tc::smem_u32(sAl) + oa, lboA, 128);
-                const uint64_t bh = tc::sdesc(tc::smem_u32(sBh) + ob, lboB, 128);
-                const uint64_t bl = tc::sdesc(tc::smem_u32(sBl) + ob, lboB, 128);
-                tc::mma_tf32(dacc, ah, bh, idesc, kc > 0 || ks > 0);
-                tc::mma_tf32(dacc, ah, bl, idesc, true);
-                tc::mma_tf32(dacc, al, bh, idesc, true);
-              }
+              const uint64_t ah = tc::sdesc(tc::smem_u32(sAh), lboA, 128);
+              const uint64_t al = tc::sdesc(tc::smem_u32(sAl), lboA, 128);
+              const uint64_t bh = tc::sdesc(tc::smem_u32(sBh), lboB, 128);
+              const uint64_t bl = tc::sdesc(tc::smem_u32(sBl), lboB, 128);
+              tc::mma_tf32(tmem, ah, bh, idesc, kc > 0);
+              tc::mma_tf32(tmem, ah, bl, idesc, true);
+              tc::mma_tf32(tmem, al, bh, idesc, true);
             }
             tc::mma_commit(&empty_bar[st]);
           }
-          tc::mma_commit(&accf_bar[acc_i]);   // W of this unit complete
+          tc::mma_commit(&accf_bar);   // W of this unit complete
           ++u;
         }
       }
     }
-    // nothing may be in flight when the tensor memory is released (the folds wait for
-    // every unit, but not after an abort)
-    if (u > 0 && !tc::mbar_wait(&accf_bar[(u - 1) & 1], ((u - 1) >> 1) & 1)) abort_flag = 1;
+    // nothing may be in flight when the tensor memory is released
+    if (u > 0 && !tc::mbar_wait(&accf_bar, (u - 1) & 1)) abort_flag = 1;
   }
-  // all folds done (each arrived on its accumulator's empty barrier); sum the 8 warps
+  // all folds done; sum the 8 warps
   tc::fence_before();
   const bool ok = __syncthreads_and(!abort_flag);
   float* red = stage_base;   // [8][2*ND][32], the stages are no longer in use
@@ -932,7 +1171,7 @@ __global__ void __launch_bounds__(DTC_THREADS, 1) k_density_tc(DevBasisT<float> 
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_free(tmem, 512);
+  if (warp == 0) tc::tmem_free(tmem, 256);
 }
 
 // ---------------------------------------------------------------------------
@@ -1171,34 +1410,28 @@ __global__ void __launch_bounds__(128) k_meanfield(DevBasisT<T> B, int G, const 
 // ---------------------------------------------------------------------------
 struct HTask {
   int ix, iy;      // block row / column
-  int a0, na;      // row range inside block ix (spin-uniform), na <= 4*rows
-  int b0, nbc;     // column range inside block iy, nbc <= 4*cols
+  int a0, na;      // row tile inside block ix (spin-uniform), na <= 32
+  int b0, nbc;     // column tile inside block iy, nbc <= 32
   int sa;          // spin of the rows (+1/-1)
   int mode;        // 0: mean field (5 components), 1: pairing (1 component)
   int call;        // 0: pn, 1: np
   int outq;        // HSP quadrant 0..3 (m11, m12, m21, m22)
-  int rows, cols;  // thread grid: each thread owns 4 rows x 4 columns, rows*cols <= 256
   long long ooff;  // block offset inside the quadrant
 };
 
-enum { HP_MAXR = 32, HP_MAXC = 32, HP_LD = 4 * HP_MAXR + 4 };  // HP_LD: padded row length
+#define HRC 16   // mesh points per K chunk
 
-// mesh points per K chunk: the shared-memory footprint is the same for FP32 and FP64
-template <class T> struct HpChunk { static constexpr int KR = sizeof(T) >= 8 ? 4 : 8; };
-
-template <class T>
-__host__ __device__ constexpr size_t hproj_smem_bytes() {
-  // sA [5][KR][HP_LD] + sPb [5][KR][HP_LD] + sH [5][KR][HP_LD][2] + sMF [25][2][2][KR]
-  return (size_t)(5 * HpChunk<T>::KR * HP_LD * 4 + 25 * 4 * HpChunk<T>::KR) * sizeof(T);
+// FP64 field projection: 32 x 32 output tiles (na, nbc <= 32), 2 x 2 outputs per
+// thread; warps whose rows lie beyond the tile's na skip the FMAs (the DFMA rate is
+// the bound).  grid (ntasks, P); 256 threads; dynamic smem hproj_fp64_smem_bytes()
+__host__ __device__ constexpr size_t hproj_fp64_smem_bytes() {
+  return (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
 }
 
-
-// grid (ntasks, P); 256 threads, each a 4 x 4 (complex) output tile; dynamic smem
-template <class T>
-__global__ void __launch_bounds__(256, 1) k_hproj(DevBasisT<T> B, const HTask* __restrict__ tasks,
-                                               const T* __restrict__ mf, T* __restrict__ hsp,
-                                               long long nxy, const int* __restrict__ active) {
-  constexpr int KR = HpChunk<T>::KR;
+__global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __restrict__ tasks,
+                                                    const double* __restrict__ mf, double* __restrict__ hsp,
+                                                    long long nxy, const int* __restrict__ active) {
+  using T = double;
   const int p = blockIdx.y;
   if (!active[p]) return;
   const HTask Th = tasks[blockIdx.x];
@@ -1206,111 +1439,99 @@ __global__ void __launch_bounds__(256, 1) k_hproj(DevBasisT<T> B, const HTask* _
   const long long ps = (long long)B.dqp * nghl;
   const int nc = Th.mode == 0 ? 5 : 1;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* sA = reinterpret_cast<T*>(smraw);      // [5][KR][HP_LD]  phi_q(a, r)
-  T* sPb = sA + 5 * KR * HP_LD;              // [5][KR][HP_LD]  phi_iz(b, r)
-  T* sH = sPb + 5 * KR * HP_LD;              // [5][KR][HP_LD][2] hpsi_q(r, b) (re, im)
-  T* sMF = sH + 5 * KR * HP_LD * 2;          // [25][2 sb][2 re/im][KR]
-  __shared__ signed char sns[4 * HP_MAXC];
+  T* sA = reinterpret_cast<T*>(smraw);     // [5][32][HRC]
+  T* sPb = sA + 5 * 32 * HRC;               // [5][32][HRC]
+  T* sMF = sPb + 5 * 32 * HRC;              // [25][2 sb][2 re/im][HRC]
+  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][32][2][HRC]
+  __shared__ signed char sns[32];
   const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
-  const int na4 = 4 * Th.rows, nb4 = 4 * Th.cols;
-  for (int i = threadIdx.x; i < nb4; i += blockDim.x) sns[i] = i < Th.nbc ? B.ns[jb0 + i] : (signed char)1;
+  if (threadIdx.x < 32) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
   const T* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * nghl;
-  const int ta = threadIdx.x % Th.rows, tb = threadIdx.x / Th.rows;
-  const bool worker = tb < Th.cols;
-  T ar[4][4], ai[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) { ar[i][j] = T(0); ai[i][j] = T(0); }
-  for (int r0 = 0; r0 < nghl; r0 += KR) {
-    const int nr = min(KR, nghl - r0);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
+  for (int r0 = 0; r0 < nghl; r0 += HRC) {
+    const int nr = min(HRC, nghl - r0);
     __syncthreads();
-    // basis functions of the rows and columns, r fastest (coalesced), zero padded
-    for (int e = threadIdx.x; e < nc * na4 * KR; e += blockDim.x) {
-      const int rr = e % KR, rem = e / KR, aa = rem % na4, q = rem / na4;
-      T v = T(0);
-      if (rr < nr && aa < Th.na) v = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
-      sA[(q * KR + rr) * HP_LD + aa] = v;
-    }
-    for (int e = threadIdx.x; e < 5 * nb4 * KR; e += blockDim.x) {
-      const int rr = e % KR, rem = e / KR, bb = rem % nb4, q = rem / nb4;
-      if (Th.mode != 0 && q > 0) continue;
-      T v = T(0);
-      if (rr < nr && bb < Th.nbc) v = B.phi[q * ps + (long long)(jb0 + bb) * nghl + r0 + rr];
-      sPb[(q * KR + rr) * HP_LD + bb] = v;
+    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
+      const int q = e / (32 * HRC), rem = e % (32 * HRC), aa = rem / HRC, rr = rem % HRC;
+      T va = 0, vb = 0;
+      if (rr < nr) {
+        if (aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
+        if (aa < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + aa) * nghl + r0 + rr];
+      }
+      sA[(q * 32 + aa) * HRC + rr] = va;
+      sPb[(q * 32 + aa) * HRC + rr] = vb;
     }
     if (Th.mode == 0) {
-      for (int e = threadIdx.x; e < 25 * 4 * KR; e += blockDim.x) {
-        const int rr = e % KR, rem = e / KR, ri = rem % 2, sb = (rem / 2) % 2, pair = rem / 4;
+      for (int e = threadIdx.x; e < 25 * 2 * 2 * HRC; e += 256) {
+        const int pair = e / (4 * HRC), rem = e % (4 * HRC), sb = rem / (2 * HRC), rem2 = rem % (2 * HRC);
+        const int ri = rem2 / HRC, rr = rem2 % HRC;
         const int iy = pair / 5, iz = pair % 5;
-        T v = T(0);
+        T v = 0;
         if (rr < nr) v = mfp[((long long)mfslot(iy, iz, Th.sa, sb == 0 ? 1 : -1) * 2 + ri) * nghl + r0 + rr];
         sMF[e] = v;
       }
     } else {
-      for (int e = threadIdx.x; e < 4 * KR; e += blockDim.x) {
-        const int rr = e % KR, rem = e / KR, ri = rem % 2, sb = rem / 2;
+      for (int e = threadIdx.x; e < 2 * 2 * HRC; e += 256) {
+        const int sb = e / (2 * HRC), rem = e % (2 * HRC), ri = rem / HRC, rr = rem % HRC;
         const int slot = 100 + (Th.sa < 0 ? 2 : 0) + sb;
-        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : T(0);
+        sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : (T)0;
       }
     }
     __syncthreads();
-    // hpsi(q, b, r) = sum_iz mf(q, iz, sa, s_b)(r) phi_iz(b, r)
-    for (int e = threadIdx.x; e < nc * KR * nb4; e += blockDim.x) {
-      const int bb = e % nb4, rem = e / nb4, rr = rem % KR, q = rem / KR;
+    // hpsi(iy, b, r) = sum_iz mf(iy, iz, sa, s_b)(r) phi_iz(b, r)
+    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
+      const int iy = e / (32 * HRC), rem = e % (32 * HRC), bb = rem / HRC, rr = rem % HRC;
       const int sb = sns[bb] > 0 ? 0 : 1;
-      T hr = T(0), hi = T(0);
+      T hr = 0, hi = 0;
       if (Th.mode == 0) {
 #pragma unroll
         for (int iz = 0; iz < 5; ++iz) {
-          const T f = sPb[(iz * KR + rr) * HP_LD + bb];
-          const T* m = &sMF[(((q * 5 + iz) * 2 + sb) * 2) * KR + rr];
-          hr = fma(m[0], f, hr); hi = fma(m[KR], f, hi);
+          const T f = sPb[(iz * 32 + bb) * HRC + rr];
+          const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
+          hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
         }
       } else {
-        const T f = sPb[rr * HP_LD + bb];
-        hr = sMF[(sb * 2) * KR + rr] * f; hi = sMF[(sb * 2 + 1) * KR + rr] * f;
+        const T f = sPb[bb * HRC + rr];
+        hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
       }
-      T* h = &sH[((q * KR + rr) * HP_LD + bb) * 2];
-      h[0] = hr; h[1] = hi;
+      sH[((iy * 32 + bb) * 2) * HRC + rr] = hr;
+      sH[((iy * 32 + bb) * 2 + 1) * HRC + rr] = hi;
     }
     __syncthreads();
-    if (worker) {
-      for (int q = 0; q < nc; ++q) {
-#pragma unroll
-        for (int rr = 0; rr < KR; ++rr) {
-          T a4[4], h0[4], h1[4];
-          lds4(&sA[(q * KR + rr) * HP_LD + 4 * ta], a4);
-          const T* hp = &sH[((q * KR + rr) * HP_LD + 4 * tb) * 2];
-          lds4(hp, h0);      // (re, im) of columns 0, 1
-          lds4(hp + 4, h1);  // (re, im) of columns 2, 3
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            ar[i][0] = fma(a4[i], h0[0], ar[i][0]); ai[i][0] = fma(a4[i], h0[1], ai[i][0]);
-            ar[i][1] = fma(a4[i], h0[2], ar[i][1]); ai[i][1] = fma(a4[i], h0[3], ai[i][1]);
-            ar[i][2] = fma(a4[i], h1[0], ar[i][2]); ai[i][2] = fma(a4[i], h1[1], ai[i][2]);
-            ar[i][3] = fma(a4[i], h1[2], ar[i][3]); ai[i][3] = fma(a4[i], h1[3], ai[i][3]);
-          }
-        }
+    // rows 4w..4w+3 of warp w: nothing to do when they are all beyond na
+    if (4 * (threadIdx.x >> 5) < Th.na)
+    for (int q = 0; q < nc; ++q) {
+      for (int rr = 0; rr < HRC; ++rr) {
+        const T a0 = sA[(q * 32 + ty * 2) * HRC + rr], a1 = sA[(q * 32 + ty * 2 + 1) * HRC + rr];
+        const T h0r = sH[((q * 32 + tx * 2) * 2) * HRC + rr], h0i = sH[((q * 32 + tx * 2) * 2 + 1) * HRC + rr];
+        const T h1r = sH[((q * 32 + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * 32 + tx * 2 + 1) * 2 + 1) * HRC + rr];
+        ar[0][0] = fma(a0, h0r, ar[0][0]); ai[0][0] = fma(a0, h0i, ai[0][0]);
+        ar[0][1] = fma(a0, h1r, ar[0][1]); ai[0][1] = fma(a0, h1i, ai[0][1]);
+        ar[1][0] = fma(a1, h0r, ar[1][0]); ai[1][0] = fma(a1, h0i, ai[1][0]);
+        ar[1][1] = fma(a1, h1r, ar[1][1]); ai[1][1] = fma(a1, h1i, ai[1][1]);
       }
     }
   }
-  if (!worker) return;
   const int ld = B.db[Th.ix];
   T* ore = hsp + ((long long)p * 2 + 0) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
   T* oim = hsp + ((long long)p * 2 + 1) * 4 * nxy + (long long)Th.outq * nxy + Th.ooff;
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 2; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int a = 4 * ta + i, b = 4 * tb + j;
+    for (int j = 0; j < 2; ++j) {
+      const int a = ty * 2 + i, b = tx * 2 + j;
       if (a < Th.na && b < Th.nbc) {
         const long long e = (Th.a0 + a) + (long long)(Th.b0 + b) * ld;
-        ore[e] = T(2) * ar[i][j];
-        oim[e] = T(2) * ai[i][j];
+        ore[e] = (T)2 * ar[i][j];
+        oim[e] = (T)2 * ai[i][j];
       }
     }
 }
+
+// ---------------------------------------------------------------------------
+// Green's function update: vout = G o (q*H + F); layout [P][Re X|Y, Im X|Y]
+// ---------------------------------------------------------------------------
 
 // ---------------------------------------------------------------------------
 // field projection on the tensor cores (FP32 data, 3xTF32 products).
@@ -1335,9 +1556,10 @@ struct HTaskTC {
 enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
 
 // dynamic shared memory for tiles of at most npmax output rows: two stages of
-// A (128 x 32, hi and lo) and B (npmax x 32, hi and lo)
+// A (128 x 32, hi and lo) and B (npmax x 32, hi and lo), then the field tensor
+// of the current chunk [pg][2 sb][5 iz][2 re/im][32 r]
 __host__ __device__ constexpr size_t hproj_tc_smem_bytes(int npmax) {
-  return (size_t)2 * (2 * 128 * HTC_K + 2 * npmax * HTC_K) * sizeof(float);
+  return (size_t)(2 * (2 * 128 * HTC_K + 2 * npmax * HTC_K) + HTC_MAXPG * 2 * 5 * 2 * HTC_K) * sizeof(float);
 }
 
 // grid (ntasks, point groups); HTC_THREADS threads; dynamic smem hproj_tc_smem_bytes(npmax)
@@ -1354,6 +1576,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
   extern __shared__ __align__(16) unsigned char smraw[];
   float* stage_base = reinterpret_cast<float*>(smraw);
   const int stage_floats = 2 * 128 * HTC_K + 2 * npmax * HTC_K;
+  float* sMF = stage_base + 2 * stage_floats;   // [pg][2 sb][5 iz][2 re/im][32 r]
   __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -1394,6 +1617,22 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
       float* sBh = sAl + 128 * HTC_K;
       float* sBl = sBh + npmax * HTC_K;
       const int q = c % nc, r0 = (c / nc) * HTC_K;
+      // the field tensor of this chunk (component q, mesh points r0..r0+31) of every
+      // point of the group, shared by all rows; the barriers keep one chunk's copy
+      // from being overwritten while another chunk's rows are generated
+      asm volatile("bar.sync 1, %0;" ::"r"(HTC_PROD) : "memory");
+      for (int e = tid; e < npg * 2 * 5 * 2 * 8; e += HTC_PROD) {
+        const int r4 = e & 7, ri = (e >> 3) & 1, iz = (e >> 4) % 5, sbi = (e / 80) & 1, pi = e / 160;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (iz < nc) {
+          const int sb = sbi == 0 ? 1 : -1;
+          const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb) : 100 + (Th.sa < 0 ? 2 : 0) + sbi;
+          const float* mp = mfbase + (long long)spt[pi] * 2 * NMF * 2 * nghl;
+          v = ld_row4(mp + ((long long)slot * 2 + ri) * nghl, r0 + 4 * r4, nghl, true);
+        }
+        *reinterpret_cast<float4*>(&sMF[((((pi * 2 + sbi) * 5 + iz) * 2 + ri) * HTC_K) + 4 * r4]) = v;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(HTC_PROD) : "memory");
       if (!abort_flag) {
         // A: hpsi rows, Re at j, Im at 64 + j, four mesh points per item
 #pragma unroll
@@ -1403,25 +1642,19 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
           float4 hr = make_float4(0.f, 0.f, 0.f, 0.f), hi = hr;
           if (j < nj) {
             const int pi = j / nbc, b = j % nbc;
-            const int sb = sns[b] > 0 ? 1 : -1;
+            const int sbi = sns[b] > 0 ? 0 : 1;
             if (q == 0) {
 #pragma unroll
               for (int iz = 0; iz < 5; ++iz)
                 if (iz < nc) fz[it][iz] = ld_row4(B.phi + iz * ps + (long long)(jb0 + b) * nghl, r, nghl, true);
             }
-            const float* mp = mfbase + (long long)spt[pi] * 2 * NMF * 2 * nghl;
-            float4 mr[5], mi[5];
-#pragma unroll
-            for (int iz = 0; iz < 5; ++iz) {
-              if (iz < nc) {
-                const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb) : 100 + (Th.sa < 0 ? 2 : 0) + (sb < 0 ? 1 : 0);
-                mr[iz] = ld_row4(mp + (long long)slot * 2 * nghl, r, nghl, true);
-                mi[iz] = ld_row4(mp + ((long long)slot * 2 + 1) * nghl, r, nghl, true);
-              }
-            }
+            const float* m = &sMF[(((pi * 2 + sbi) * 5) * 2) * HTC_K + 4 * r4];
 #pragma unroll
             for (int iz = 0; iz < 5; ++iz)
-              if (iz < nc) { fma4(hr, mr[iz], fz[it][iz]); fma4(hi, mi[iz], fz[it][iz]); }
+              if (iz < nc) {
+                fma4(hr, *reinterpret_cast<const float4*>(m + (iz * 2 + 0) * HTC_K), fz[it][iz]);
+                fma4(hi, *reinterpret_cast<const float4*>(m + (iz * 2 + 1) * HTC_K), fz[it][iz]);
+              }
           }
           const int o_re = tc::cm_off(j, 4 * r4, 128), o_im = tc::cm_off(64 + j, 4 * r4, 128);
           st_split4(sAh + o_re, sAl + o_re, hr);
@@ -1550,6 +1783,7 @@ struct BroState {
   const int* modep; // [P] BRO_*
 };
 enum { BRO_NPART = 2 + 2 * 64 };  // 0: max|vout|, 1: |df_ipos|^2, 2..: dots
+enum { BRO_CHUNK = 1024 };          // elements per CTA of the Broyden kernels (4 per thread)
 
 // history slots of Broyden iteration `it` (Fortran integer division truncates
 // toward zero, as C++ does): iter_used columns in use, ipos the column updated
@@ -1595,8 +1829,7 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
   double* df = upd ? S.df + ((long long)p * S.M + ipos) * S.N : nullptr;
   double* dv = upd ? S.dv + ((long long)p * S.M + ipos) * S.N : nullptr;
   double mx = 0.0, nn = 0.0;
-  const int chunk = (S.N + S.nchunk - 1) / S.nchunk;
-  const int e0 = blockIdx.x * chunk, e1 = min(S.N, e0 + chunk);
+  const int e0 = blockIdx.x * BRO_CHUNK, e1 = min(S.N, e0 + BRO_CHUNK);
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const double v = vo[e] - vi[e];
     vo[e] = v;
@@ -1617,8 +1850,10 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
 }
 
 // normalise column ipos by 1/|df_ipos| and form the dots
-// dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used;
-// each warp reduces its share per k with shuffles, one barrier at the end
+// dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used.
+// A CTA covers BRO_CHUNK elements, four per thread, so df_ipos and vout are read
+// once (into registers) and every df_k once; each warp reduces its share per k
+// with shuffles, one barrier at the end.
 __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __restrict__ norm,
                                                   const int* __restrict__ active) {
   const int p = blockIdx.y;
@@ -1630,27 +1865,36 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   const bool upd = it >= 2;
   __shared__ double wsum[8][2 * 64];
   const double* vo = S.vout + (long long)p * S.N;
-  const int chunk = (S.N + S.nchunk - 1) / S.nchunk;
-  const int e0 = blockIdx.x * chunk, e1 = min(S.N, e0 + chunk);
   double* dfp = S.df + (long long)p * S.M * S.N;
   double* dvp = S.dv + (long long)p * S.M * S.N;
   double* fi = dfp + (long long)ipos * S.N;
-  if (upd) {
-    const double sc = norm[p];
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      fi[e] *= sc;
-      dvp[(long long)ipos * S.N + e] *= sc;
+  const int e0 = blockIdx.x * BRO_CHUNK + threadIdx.x;
+  const double sc = upd ? norm[p] : 0.0;
+  double f4[4], v4[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int e = e0 + u * 256;
+    f4[u] = 0.0; v4[u] = 0.0;
+    if (e < S.N) {
+      if (upd) {
+        f4[u] = fi[e] * sc;
+        fi[e] = f4[u];
+        dvp[(long long)ipos * S.N + e] *= sc;
+      }
+      v4[u] = vo[e];
     }
   }
-  __syncthreads();
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   for (int k = 0; k < iu; ++k) {
-    double a = 0.0, b = 0.0;
     const double* fk = dfp + (long long)k * S.N;
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const double f = fk[e];
-      a = fma(f, fi[e], a);
-      b = fma(f, vo[e], b);
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * 256;
+      // column ipos itself: its normalised values are the ones in registers
+      const double f = e < S.N ? (k == ipos && upd ? f4[u] : fk[e]) : 0.0;
+      a = fma(f, f4[u], a);
+      b = fma(f, v4[u], b);
     }
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -1660,10 +1904,9 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   }
   __syncthreads();
   double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
-  const int nw = blockDim.x >> 5;
   for (int k = threadIdx.x; k < iu; k += blockDim.x) {
     double sa = 0.0, sb = 0.0;
-    for (int i = 0; i < nw; ++i) { sa += wsum[i][k]; sb += wsum[i][64 + k]; }
+    for (int i = 0; i < 8; ++i) { sa += wsum[i][k]; sb += wsum[i][64 + k]; }
     pt[2 + k] = sa; pt[2 + 64 + k] = sb;
   }
 }
@@ -1677,12 +1920,22 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   const int p = blockIdx.x;
   if (!active[p]) return;
   const double* pt = S.part + (long long)p * S.nchunk * BRO_NPART;
+  const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+  __shared__ double red[8][2];
   if (stage == 0) {
-    if (threadIdx.x == 0) {
-      double m = 0.0, s = 0.0;
-      for (int c = 0; c < S.nchunk; ++c) { m = fmax(m, pt[c * BRO_NPART]); s += pt[c * BRO_NPART + 1]; }
-      si[p] = m;
-      norm[p] = s > 0.0 ? 1.0 / sqrt(s) : 0.0;
+    double m = 0.0, s = 0.0;
+    for (int c = tid; c < S.nchunk; c += blockDim.x) { m = fmax(m, pt[c * BRO_NPART]); s += pt[c * BRO_NPART + 1]; }
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (l == 0) { red[w][0] = m; red[w][1] = s; }
+    __syncthreads();
+    if (tid == 0) {
+      double mm = 0.0, ss = 0.0;
+      for (int i = 0; i < 8; ++i) { mm = fmax(mm, red[i][0]); ss += red[i][1]; }
+      si[p] = mm;
+      norm[p] = ss > 0.0 ? 1.0 / sqrt(ss) : 0.0;
     }
     return;
   }
@@ -1696,12 +1949,17 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   __shared__ int piv;
   const int M = S.M;
   double* bp = beta + (long long)p * M * M;
-  const int tid = threadIdx.x;
-  for (int k = tid; k < n; k += blockDim.x) {
+  for (int k = w; k < n; k += 8) {   // one warp per k: sum the chunk partials
     double dd = 0.0, wk = 0.0;
-    for (int c = 0; c < S.nchunk; ++c) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
-    if (k != ipos) { bp[k * M + ipos] = dd; bp[ipos * M + k] = dd; }
-    x[k] = wk;
+    for (int c = l; c < S.nchunk; c += 32) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
+    for (int o = 16; o > 0; o >>= 1) {
+      dd += __shfl_xor_sync(0xffffffffu, dd, o);
+      wk += __shfl_xor_sync(0xffffffffu, wk, o);
+    }
+    if (l == 0) {
+      if (k != ipos) { bp[k * M + ipos] = dd; bp[ipos * M + k] = dd; }
+      x[k] = wk;
+    }
   }
   __syncthreads();
   for (int k = tid; k < n; k += blockDim.x) bp[k * M + k] = w0 * w0 + 1.0;

@@ -52,15 +52,14 @@ def test_engine_refills_slots_and_matches_batch_solve():
     gpu.close()
     assert sorted(got) == list(range(len(w)))
     assert steps < int(np.sum(ref.iters)) / 3   # points overlapped in the slots
-    # the same kernels and Broyden steps per point; only the grouping of the density
-    # sums follows the number of active points, so agreement is to rounding level
+    # the same kernels, sums and Broyden steps per point whatever else is in flight
     worst = 0.0
     for i in range(len(w)):
         assert got[i].iters == ref.iters[i], (i, got[i].iters, ref.iters[i])
         want = ref.re_S[i] + 1j * ref.im_S[i]
         rel = np.max(np.abs(got[i].S - want)) / np.max(np.abs(want))
         worst = max(worst, rel)
-        assert rel <= 1e-9, (i, rel)
+        assert rel <= 1e-13, (i, rel)
     print(f"engine vs batch solve: {steps} steps, worst relative difference {worst:.1e}")
 
 
