@@ -422,6 +422,76 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_serve_stream(args):
+    """Serving stream (the BASELINE serving configuration, scaled by --stream-scale):
+    nuclei drawn (seeded) from the three recorded ground states (40S, 116Kr, 162Gd)
+    re-diagonalised in a basis of N_sh drawn from --nsh, each requesting GT- K = 0
+    and K = 1 strengths on a CIRCLE contour of 40-200 points (times the scale);
+    Poisson arrivals at each rate of --rates; engines admitted within a device-memory
+    budget (--budget-gb, 150 GB); mixed form to 1e-9.  (The synthetic Bogoliubov
+    states of the batching configuration give a FAM iteration that does not converge,
+    so they cannot stand in for converged throughput.)  One JSON line per rate."""
+    import torch
+    from pynfam_gb300.contour import circle
+    from pynfam_gb300.namelist import defaults, parse_namelist_text
+    from pynfam_gb300.pnfam_setup import setup_case
+    from pynfam_gb300.serve import Request, Server, poisson_arrivals, slot_bytes
+    from pynfam_gb300.solver import GPUSolver
+    from pynfam_gb300.synthetic import ground_state
+    rng = np.random.default_rng(args.stream_seed)
+    nshs = [int(x) for x in args.nsh.split(",")]
+    names = ("S40", "Kr116", "Gd162")
+    nuclei = sorted({(str(rng.choice(names)), int(rng.choice(nshs))) for _ in range(args.nuclei)})
+    cases, states = {}, {}
+    t0 = time.perf_counter()
+    for name, nsh in nuclei:
+        hfb = ground_state(os.path.join(ROOT, "tests", "golden", f"{name}.hel"), nsh)
+        with open(os.path.join(ROOT, "tests", "golden", f"{name}.json")) as fh:
+            inter = parse_namelist_text(json.load(fh)["interaction"])["interaction"]
+        for k in (0, 1):
+            nml = defaults()
+            nml["interaction"].update({kk: v for kk, v in inter.items() if v is not None})
+            nml["interaction"]["require_self_consistency"] = False
+            nml["ext_field"].update(operator_name="GT", operator_k=k, beta_type="-", compute_crossterms=False)
+            nml["solver"].update(SOLVER)
+            cases[(name, nsh, k)] = setup_case(nml, None, hfb=hfb)
+    setup_s = time.perf_counter() - t0
+    slots = args.stream_slots
+    M = SOLVER["broyden_history_size"]
+
+    def engine_bytes(key, n):
+        c = cases[key]
+        h = c.hfb
+        ground = 12 * (5 * h.dqp * h.nghl + 4 * int(sum(int(b.size) for b in h.Up)))
+        return n * slot_bytes(c.F.mat.nelem, M, True) + ground
+
+    def factory(key, n):
+        c = cases[key]
+        g = GPUSolver(c.hfb, c.couplings)
+        g.set_operator(c.F, c.G)
+        return g.engine(n, owns_solver=True, **solver_kw(c, 1, MIXED_EPS))
+
+    keys = list(cases)
+    npts = {key: max(4, int(round(rng.integers(40, 201) * args.stream_scale))) for key in keys}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        arr = poisson_arrivals(len(keys), rate, seed=args.stream_seed)
+        order = rng.permutation(len(keys))
+        reqs = [Request(i, keys[j], circle(-15.0, 35.0, 2 * npts[keys[j]]), float(arr[i]))
+                for i, j in enumerate(order)]
+        torch.cuda.synchronize()
+        server = Server(factory, engine_bytes, slots=slots, budget_bytes=int(args.budget_gb * 1e9))
+        out, st = server.run(reqs)
+        torch.cuda.synchronize()
+        line = {"serve_stream": True, "rate_req_per_s": rate, "requests": len(reqs),
+                "nuclei": [f"{n} N_sh={s_}" for n, s_ in nuclei], "points": st.points, "converged": st.converged,
+                "wall_s": st.wall, "points_per_s": st.points / st.wall, "converged_per_s": st.converged / st.wall,
+                "latency_ms": {"p50": st.percentile(50) * 1e3, "p99": st.percentile(99) * 1e3},
+                "peak_engines": st.peak_engines, "peak_gb": st.peak_bytes / 1e9, "slots_per_engine": slots,
+                "setup_s": setup_s, "form": f"mixed, epsilon {MIXED_EPS}",
+                "data": "recorded ground states re-diagonalised in larger bases"}
+        print(json.dumps(line, default=_plain), flush=True)
+
+
 def run_solve_only(args):
     from pynfam_gb300.solver import GPUSolver
     cases, omegas = workload(args.points, OPERATORS[:1])
@@ -429,7 +499,7 @@ def run_solve_only(args):
     s = case.nml["solver"]
     kw = dict(max_iter=args.max_iter or s["max_iter"], eps=args.eps or s["convergence_epsilon"],
               broyden_m=s["broyden_history_size"] if args.broyden_m is None else args.broyden_m,
-              quench=case.quench, precision=args.precision)
+              quench=case.quench, precision=args.precision, switch_exp=args.switch_exp)
     gpu = GPUSolver(case.hfb, case.couplings)
     gpu.set_operator(case.F, case.G)
     for _ in range(args.warmup):
@@ -462,11 +532,24 @@ def main():
     ap.add_argument("--max-iter", type=int, default=None, help="solve-only: max_iter override")
     ap.add_argument("--broyden-m", type=int, default=None, help="solve-only: Broyden history override")
     ap.add_argument("--timed", action="store_true", help="solve-only: per-stage event timing")
+    ap.add_argument("--switch-exp", type=int, default=0,
+                    help="solve-only: mixed form takes its first FP64 anchor below si = 10**-switch_exp")
+    ap.add_argument("--serve-stream", action="store_true",
+                    help="serving stream of several nuclei and bases with Poisson arrivals (one JSON line per rate)")
+    ap.add_argument("--nuclei", type=int, default=6, help="serve-stream: nuclei drawn (with repeats)")
+    ap.add_argument("--nsh", default="8,12,16", help="serve-stream: N_sh values to draw from")
+    ap.add_argument("--rates", default="5,50,200", help="serve-stream: request arrival rates (1/s)")
+    ap.add_argument("--stream-scale", type=float, default=0.25, help="serve-stream: points per request x scale")
+    ap.add_argument("--stream-slots", type=int, default=32, help="serve-stream: slots per engine")
+    ap.add_argument("--stream-seed", type=int, default=0)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--solve-only", action="store_true",
                     help="one operator, batch solves only (no serving, e2e or CPU legs); used for kernel profiling")
     args = ap.parse_args()
     if args.solve_only:
         run_solve_only(args)
+    elif args.serve_stream:
+        run_serve_stream(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -941,6 +941,32 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
   return k;
 }
 
+// one Broyden step of every active slot
+static int broyden_step(pnfam_ctx* c, pnfam_engine* e, int any_bro, const int* d_itp, const int* d_mode) {
+  const int P = e->P, N = e->N;
+  const int* act = c->d_active.p;
+  BroState S;
+  S.N = N; S.M = std::max(e->M, 1); S.alpha = e->o.alpha_mix;
+  S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
+  S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
+  S.itp = d_itp; S.modep = d_mode;
+  const double w0 = 0.01;
+  dim3 grid(c->nchunk_bro, P);
+  k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
+  k_bro_solve<<<P, 256, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+  c->launches += 2;
+  if (any_bro) {
+    k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
+    k_bro_solve<<<P, 256, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
+    c->launches += 2;
+  }
+  dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
+  k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
+  c->launches++;
+  CK(cudaGetLastError());
+  return PNFAM_OK;
+}
+
 // enqueue one evaluation (and Broyden step) for every active slot
 static int engine_launch(pnfam_engine* e) {
   pnfam_ctx* c = e->c;
@@ -1033,29 +1059,10 @@ static int engine_launch(pnfam_engine* e) {
     CK(cudaGetLastError());
   }
   toc(5);
-  // ---- Broyden (pnfam_broyden.f90:117-216), each slot at its own iteration ----
+  // ---- Broyden (pnfam_broyden.f90:117-216), each slot at its own iteration, FP64
+  // history in both forms ----
   tic();
-  {
-    BroState S;
-    S.N = N; S.M = std::max(e->M, 1); S.alpha = e->o.alpha_mix;
-    S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
-    S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
-    S.itp = d_itp; S.modep = d_mode;
-    const double w0 = 0.01;
-    dim3 grid(c->nchunk_bro, P);
-    k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
-    k_bro_solve<<<P, 256, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
-    c->launches += 2;
-    if (any_bro) {
-      k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
-      k_bro_solve<<<P, 256, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
-      c->launches += 2;
-    }
-    dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
-    k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
-    c->launches++;
-    CK(cudaGetLastError());
-  }
+  if ((rc = broyden_step(c, e, any_bro, d_itp, d_mode))) return rc;
   toc(6);
   tic();
   {

@@ -928,6 +928,42 @@ __device__ __forceinline__ void fold_opp(float (&acc)[2 * ND], float wr, float w
 }
 #undef A_
 
+// fold the W_q rows of one unit (this warp's component Q, its column half) into the
+// densities; KIND 0: normal densities, 1: pairing densities (Q = 0)
+template <int Q, int KIND>
+__device__ __forceinline__ void fold_unit(float (&acc)[2 * ND], uint32_t lane_base, const float* sPb, int lane,
+                                          int dc, int nub, int s, int c8lo, int c8hi, bool skip) {
+  for (int c8 = c8lo; c8 < c8hi; ++c8) {
+    float wre[8], wim[8];
+    tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
+    tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
+    if (skip) continue;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int b = 8 * c8 + i;
+      if (b >= dc) break;
+      const bool up = b < nub;
+      const float sg = up ? 1.f : -1.f, sig = up ? -1.f : 1.f;
+      const bool same = up == (s == 0);
+      const float4 pv = *reinterpret_cast<const float4*>(&sPb[(b * 32 + lane) * 4]);
+      const float P[4] = {pv.x, pv.y, pv.z, pv.w};
+      if (KIND == 0) {
+        if (same) fold_same<Q>(acc, wre[i], wim[i], P, sg);
+        else fold_opp<Q>(acc, wre[i], wim[i], P, sig);
+      } else {
+        const float xr = 2.f * wre[i] * P[0], xi = 2.f * wim[i] * P[0];
+        if (same) {
+          acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
+          acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
+        } else {
+          acc[2 * D_RB] += -sg * xr; acc[2 * D_RB + 1] += -sg * xi;
+          acc[2 * D_SBZ] += xr; acc[2 * D_SBZ + 1] += xi;
+        }
+      }
+    }
+  }
+}
+
 struct DensTCArgs {
   const float* rho; long long rho_sp, rho_spl;   // as DensCallT, per call
   const int* rcols; const long long* roffs;
@@ -1058,45 +1094,22 @@ __global__ void __launch_bounds__(DTC_THREADS, 2) k_density_tc(DevBasisT<float> 
           tc::fence_after();
           {
             const int q = warp & 3, half = warp >> 2;
-            const int r = r0 + lane;
-            const int sbase = B.st[iy];
-            const float srow = s == 0 ? 1.f : -1.f;
             const int nb8 = (dc + 7) / 8;
             const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
-            const bool active_q = kind == 0 || q == 0;
             const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-            for (int c8 = c8lo; c8 < c8hi; ++c8) {
-              float wre[8], wim[8];
-              tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
-              tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
-              if (abort_flag || !active_q || r >= nghl) continue;
-#pragma unroll
-              for (int i = 0; i < 8; ++i) {
-                const int b = 8 * c8 + i;
-                if (b >= dc) break;
-                const float sg = (float)B.ns[sbase + b];
-                const float sig = sg < 0.f ? 1.f : -1.f;
-                const float4 pv = *reinterpret_cast<const float4*>(&sPb[(b * 32 + lane) * 4]);
-                const float P[4] = {pv.x, pv.y, pv.z, pv.w};
-                if (kind == 0) {
-                  const bool same = sg == srow;
-                  switch (q) {
-                    case 0: if (same) fold_same<0>(acc, wre[i], wim[i], P, sg); else fold_opp<0>(acc, wre[i], wim[i], P, sig); break;
-                    case 1: if (same) fold_same<1>(acc, wre[i], wim[i], P, sg); else fold_opp<1>(acc, wre[i], wim[i], P, sig); break;
-                    case 2: if (same) fold_same<2>(acc, wre[i], wim[i], P, sg); else fold_opp<2>(acc, wre[i], wim[i], P, sig); break;
-                    default: if (same) fold_same<3>(acc, wre[i], wim[i], P, sg); else fold_opp<3>(acc, wre[i], wim[i], P, sig); break;
-                  }
-                } else {
-                  const float xr = 2.f * wre[i] * P[0], xi = 2.f * wim[i] * P[0];
-                  if (sg == srow) {
-                    acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
-                    acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
-                  } else {
-                    acc[2 * D_RB] += -sg * xr; acc[2 * D_RB + 1] += -sg * xi;
-                    acc[2 * D_SBZ] += xr; acc[2 * D_SBZ + 1] += xi;
-                  }
-                }
+            // columns b < nup(iy) are spin up: "same spin" as rows of spin s == 0
+            const int nub = B.nup[iy];
+            const bool skip = abort_flag || r0 + lane >= nghl;
+            if (kind == 0) {
+              switch (q) {
+                case 0: fold_unit<0, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
+                case 1: fold_unit<1, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
+                case 2: fold_unit<2, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
+                default: fold_unit<3, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
               }
+            } else {
+              // pairing densities: component 0 only; the other warps still take part in the loads
+              fold_unit<0, 1>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip || q != 0);
             }
           }
           tc::fence_before();

@@ -406,6 +406,12 @@ def load_hfb_solution(path) -> HFBSolution:
     hd = hfb_matrices(h, mb)
     qpn = diagonalise(h, hd, "n", float(h.N))
     qpp = diagonalise(h, hd, "p", float(h.Z))
+    return assemble(h, mb, qpn, qpp)
+
+
+def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution) -> HFBSolution:
+    """The pnFAM view of Omega>0 quasiparticles (hfbtho_solution.f90:164-459): TR
+    doubling, spin sort inside each block, pairing window."""
     rho_n = local_density(h, mb, qpn, float(h.N))
     rho_p = local_density(h, mb, qpp, float(h.Z))
 

@@ -92,9 +92,10 @@ class GPUSolver:
         o.reserved[1] = int(switch_exp)
         return o
 
-    def engine(self, slots, **opts) -> "Engine":
-        """Continuous-batching engine on this context (see Engine)."""
-        return Engine(self, slots, self.options(**opts))
+    def engine(self, slots, owns_solver=False, **opts) -> "Engine":
+        """Continuous-batching engine on this context (see Engine); with
+        owns_solver, closing the engine also frees this context."""
+        return Engine(self, slots, self.options(**opts), owns_solver)
 
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
               history=False, timed=False, precision=0, switch_exp=0) -> SolveResult:
@@ -172,8 +173,9 @@ class Engine:
     on the context's own stream, so engines of different contexts overlap on
     the GPU) and ``finish`` waits for it and returns the points that finished."""
 
-    def __init__(self, solver: GPUSolver, slots: int, opts):
+    def __init__(self, solver: GPUSolver, slots: int, opts, owns_solver=False):
         self.solver = solver
+        self.owns_solver = owns_solver
         self.lib = solver.lib
         self.slots = int(slots)
         self.nops = solver.nops
@@ -219,6 +221,8 @@ class Engine:
         if getattr(self, "eng", None) is not None and self.eng.value:
             self.lib.pnfam_gpu_engine_free(self.eng)
             self.eng = C.c_void_p()
+        if getattr(self, "owns_solver", False):
+            self.solver.close()
 
     def __del__(self):
         try:

@@ -70,3 +70,44 @@ def ground_state(hel_path: str, n00: int):
     if n00 != h.n00:
         h = extend_basis(h, n00)
     return load_hfb_solution(h)
+
+
+def bogoliubov_nucleus(hel_path: str, n00: int, seed: int, parity: bool = False):
+    """A synthetic Bogoliubov ground state in the full N_sh = n00 basis: per block
+    and isospin, U = A diag(u), V = B diag(v) with A, B the Q factors of Gaussian
+    matrices, v_k^2 = 1/(1 + exp((e_k - lambda)/0.8 MeV)), e_k uniform in
+    [-40, 40] MeV, lambda = -8 MeV and E_k = sqrt((e_k - lambda)^2 + 1.2^2) MeV.
+    Neutrons use `seed`, protons `seed + 10**6`; blocks are drawn in block order.
+    The mesh, the oscillator lengths and Z, N come from the recorded ``.hel``
+    (the couplings follow from the synthetic densities).  ``parity=False`` gives
+    Omega-only blocks."""
+    from .hel import read_hel
+    from .hfb_solution import QPSolution, assemble, build_mesh_basis
+    h = read_hel(hel_path)
+    if abs(h.bz - h.bp) > 1e-12:
+        raise ValueError("the synthetic basis needs a spherical oscillator basis (bz == bp)")
+    g = copy.copy(h)
+    g.ID, g.nr, g.nz, g.nl, g.ns = hfbtho_basis(n00, parity=parity)
+    g.n00 = n00
+    g.nb = len(g.ID)
+    g.nt = int(g.ID.sum())
+    mb = build_mesh_basis(g)
+    lam = -8.0
+
+    def draw(rng):
+        E, U, V, act = [], [], [], []
+        for d in g.ID:
+            d = int(d)
+            A = np.linalg.qr(rng.standard_normal((d, d)))[0]
+            Bm = np.linalg.qr(rng.standard_normal((d, d)))[0]
+            e = rng.uniform(-40.0, 40.0, d)
+            v2 = 1.0 / (1.0 + np.exp((e - lam) / 0.8))
+            U.append(A * np.sqrt(1.0 - v2)[None, :])
+            V.append(Bm * np.sqrt(v2)[None, :])
+            E.append(np.sqrt((e - lam) ** 2 + 1.2 ** 2))
+            act.append(np.ones(d, dtype=bool))
+        return QPSolution(E, U, V, act, lam)
+
+    qpn = draw(np.random.default_rng(seed))
+    qpp = draw(np.random.default_rng(seed + 10 ** 6))
+    return assemble(g, mb, qpn, qpp)

@@ -20,6 +20,9 @@ import sys
 import tarfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# 40S in the N_sh = 8 basis (parity-split blocks up to 25, 165 states): the
+# reference's recorded GT runs on it are empty
+INPUT_ONLY = {"S40_nsh8": "S40_GT_2bc_reruntest/000000"}
 CASES = {
     # case name -> directory (relative to <reference>/tests)
     "S40": "S40_GT_All/000000",
@@ -117,6 +120,12 @@ def main(ref_root: str):
             json.dump({"case": case, "source": f"tests/{rel}", "interaction": "&interaction\n" + interaction + "\n/\n",
                        "operators": ops}, fh, separators=(",", ":"))
         print(case, {k: len(v) for k, v in ops.items()})
+    # ground states without recorded FAM outputs (their .dat files are empty): inputs
+    # of the oracle-versus-GPU parity tests
+    for case, rel in INPUT_ONLY.items():
+        shutil.copyfile(os.path.join(ref_root, "tests", rel, "hfb_soln", "hfbtho_output.hel"),
+                        os.path.join(HERE, f"{case}.hel"))
+        print(case, "ground state only")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,170 @@
+"""Parity at the benchmark configurations that have no recorded FAM outputs.
+
+Config 1: 40S in the N_sh = 8 basis (the reference's own ground state; its
+recorded GT runs are empty), GT- K = 0 on 40 points of the half circle
+(centre 10 MeV, radius 25 MeV), Broyden history 7 and mixing 0.4, epsilon 1e-7.
+The FP64 GPU form is held to the CPU oracle (same iteration count, complex
+strengths to 1e-8 of |S|: rounding differences grow over the ~40 Broyden steps),
+and the mixed form to the FP64 fixed point (1e-6).
+
+Config 2: a synthetic Bogoliubov ground state (seed 1) in the N_sh = 12 basis
+with Omega-only blocks (up to 91), GT- K = 0 and K = 1 at Im omega = 0.5 MeV,
+Re omega uniform in [-10, 30] MeV: the first iterations against the oracle, and
+the mixed form against the FP64 fixed point.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from golden_cases import GOLDEN
+from oracle.fam_oracle import FAMOracle
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-6
+INTERACTION = {"interaction_name": "SKOP", "require_self_consistency": True, "require_gauge_invariance": True,
+               "force_j2_terms": False, "vpair_t0": -346.352, "override_cs0": 128.279, "override_csr": 0.0,
+               "override_cds": 0.0}
+
+
+def _case(hfb, k, M, self_consistent=True):
+    from pynfam_gb300.namelist import defaults
+    from pynfam_gb300.pnfam_setup import setup_case
+    nml = defaults()
+    nml["interaction"].update(INTERACTION)
+    nml["interaction"]["require_self_consistency"] = self_consistent
+    nml["ext_field"].update(operator_name="GT", operator_k=k, beta_type="-", compute_crossterms=False)
+    nml["solver"].update(max_iter=300, convergence_epsilon=1e-7, broyden_history_size=M)
+    return setup_case(nml, None, hfb=hfb)
+
+
+def _mixed_vs_fixed_point(c, omegas, M, alpha):
+    from pynfam_gb300.solver import GPUSolver
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    kw = dict(broyden_m=M, quench=c.quench, alpha_mix=alpha)
+    exact = gpu.solve(omegas, max_iter=1000, eps=1e-12, **kw)
+    mixed = gpu.solve(omegas, max_iter=1000, eps=1e-9, precision=1, **kw)
+    gpu.close()
+    worst, n = 0.0, 0
+    for i in range(len(omegas)):
+        if exact.iters[i] < 0:
+            continue
+        assert mixed.iters[i] >= 0, (i, mixed.si[i])
+        w = complex(exact.re_S[i, 0], exact.im_S[i, 0])
+        g = complex(mixed.re_S[i, 0], mixed.im_S[i, 0])
+        for a, b in ((g.real, w.real), (g.imag, w.imag)):
+            assert abs(a - b) <= REL * abs(b) + 1e-12 * abs(w), (i, a, b)
+        worst = max(worst, abs(g - w) / abs(w))
+        n += 1
+    return worst, n
+
+
+@pytest.fixture(scope="module")
+def config1():
+    from pynfam_gb300.contour import circle
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    hfb = load_hfb_solution(os.path.join(GOLDEN, "S40_nsh8.hel"))
+    assert int(hfb.n00) == 8 and int(max(hfb.db)) == 25 and int(hfb.dqp) == 330
+    return _case(hfb, 0, 7), circle(-15.0, 35.0, 80)
+
+
+def test_config1_fp64_matches_oracle(config1):
+    from pynfam_gb300.solver import GPUSolver
+    c, omegas = config1
+    assert len(omegas) == 40
+    idx = [0, 5, 20, 39]
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    r = gpu.solve(omegas[idx], max_iter=300, eps=1e-7, broyden_m=7, quench=c.quench, alpha_mix=0.4)
+    gpu.close()
+    orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench, alpha_mix=0.4)
+    nconv = 0
+    for k, i in enumerate(idx):
+        ref = orc.solve(complex(omegas[i]), max_iter=300, eps=1e-7, broyden_m=7)
+        assert int(r.iters[k]) == ref.iter_conv, (i, r.iters[k], ref.iter_conv)
+        if ref.iter_conv < 0:
+            continue   # not converged in 300 iterations in either (the point next to the real axis)
+        nconv += 1
+        g = complex(r.re_S[k, 0], r.im_S[k, 0])
+        w = complex(ref.re_str[0], ref.im_str[0])
+        assert abs(g - w) <= 1e-8 * abs(w), (i, g, w)
+    assert nconv >= 2
+
+
+def test_config1_mixed_matches_fp64_fixed_point(config1):
+    c, omegas = config1
+    worst, n = _mixed_vs_fixed_point(c, omegas, 7, 0.4)
+    print(f"config 1: {n} points, mixed form worst relative error vs FP64 fixed point {worst:.2e}")
+    assert n >= 30
+
+
+@pytest.fixture(scope="module")
+def config2():
+    from pynfam_gb300.synthetic import bogoliubov_nucleus
+    hfb = bogoliubov_nucleus(os.path.join(GOLDEN, "Gd162.hel"), 12, seed=1, parity=False)
+    assert int(max(hfb.db)) == 91 and int(hfb.dqp) == 910
+    rng = np.random.default_rng(1)
+    omegas = rng.uniform(-10.0, 30.0, 12) + 0.5j
+    return hfb, omegas
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_config2_synthetic_field_split_precision_vs_fp64(config2, k):
+    """The split-precision (3xTF32 tensor-core) field evaluation against FP64 on the
+    synthetic state, whose blocks (up to 91) take the multi-tile tensor-core paths."""
+    from pynfam_gb300.blockmatrix import BlockMatrix
+    from pynfam_gb300.solver import GPUSolver
+    hfb, _ = config2
+    c = _case(hfb, k, 50, self_consistent=False)
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    nb = hfb.nb
+    half = nb // 2
+    tr = np.array([(i + half) % nb for i in range(nb)])
+    fc = np.asarray(c.F.mat.cols)
+    xc = np.array([tr[fc[i]] if fc[i] >= 0 else -1 for i in range(nb)])
+    yc = np.array([fc[tr[i]] for i in range(nb)])
+    xtc = np.full(nb, -1); ytc = np.full(nb, -1)
+    for i in range(nb):
+        if xc[i] >= 0: xtc[xc[i]] = i
+        if yc[i] >= 0: ytc[yc[i]] = i
+    rng = np.random.default_rng(2 + k)
+    ins = []
+    for cols in (fc, xtc, fc, ytc):
+        n = BlockMatrix.empty(cols, hfb.db).nelem
+        ins.append(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    want = gpu.calc_hamiltonian(*ins)
+    got = gpu.calc_hamiltonian(*ins, mixed=True)
+    gpu.close()
+    worst = max(float(np.max(np.abs(g - w)) / np.max(np.abs(w))) for g, w in zip(got, want))
+    print(f"config 2 GT K={k}: split-precision field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_config2_synthetic_mixed_matches_fp64_fixed_point(config2, k):
+    """Every point whose FP64 iteration converges on the synthetic state converges in
+    the mixed form too, to the same fixed point (1e-6)."""
+    hfb, omegas = config2
+    c = _case(hfb, k, 50, self_consistent=False)
+    worst, n = _mixed_vs_fixed_point(c, omegas, 50, None)
+    print(f"config 2 GT K={k}: {n} of {len(omegas)} points converge; mixed form worst relative error "
+          f"vs FP64 fixed point {worst:.2e}")
+
+
+def test_config2_synthetic_history_matches_oracle(config2):
+    from pynfam_gb300.solver import GPUSolver
+    hfb, omegas = config2
+    c = _case(hfb, 1, 50, self_consistent=False)
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    r = gpu.solve([omegas[0]], max_iter=4, eps=1e-7, broyden_m=50, quench=c.quench, history=True)
+    gpu.close()
+    orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench)
+    ref = orc.solve(complex(omegas[0]), max_iter=4, eps=1e-7, broyden_m=50)
+    for h in ref.history:
+        g = r.hist[0, h[0]]
+        for a, b in ((g[0], h[2]), (g[1], h[3]), (g[2], h[4])):
+            assert abs(a - b) <= 1e-10 * max(abs(b), 1e-6), (h, g)
