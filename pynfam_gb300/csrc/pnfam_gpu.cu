@@ -206,6 +206,8 @@ struct pnfam_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t evt[2] = {nullptr, nullptr};   // whole-solve device time
+  cudaStream_t stream64 = nullptr;           // FP64 anchor evaluations beside the FP32 increments
+  cudaEvent_t evf[2] = {nullptr, nullptr};   // fork to / join from stream64
   double stage_ms[8] = {0};     // FP64 evaluations (0-4) and the common stages (5-7)
   double stage32_ms[5] = {0};   // FP32 evaluations of the mixed form
   double total_ms = 0.0;
@@ -240,6 +242,9 @@ struct pnfam_ctx {
     if (ev[1]) cudaEventDestroy(ev[1]);
     if (evt[0]) cudaEventDestroy(evt[0]);
     if (evt[1]) cudaEventDestroy(evt[1]);
+    if (evf[0]) cudaEventDestroy(evf[0]);
+    if (evf[1]) cudaEventDestroy(evf[1]);
+    if (stream64) cudaStreamDestroy(stream64);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -465,20 +470,21 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
 }
 
 template <class T>
-static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, const BufDescT<T>* bufs) {
+static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, const BufDescT<T>* bufs,
+                       cudaStream_t st) {
   if (tl.ntiles == 0) return PNFAM_OK;
   dim3 grid(tl.ntiles, 2 * P);
-  k_gemm<T><<<grid, 256, 0, c->stream>>>(tl.d_tasks.p, tl.d_tile2task.p, bufs, active);
+  k_gemm<T><<<grid, 256, 0, st>>>(tl.d_tasks.p, tl.d_tile2task.p, bufs, active);
   c->launches++;
   CK(cudaGetLastError());
   return PNFAM_OK;
 }
 
 // FP32 stage on the tensor cores for the nact points listed in c->d_actlist
-static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact) {
+static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact, cudaStream_t st) {
   if (tl.tasks.empty() || nact <= 0) return PNFAM_OK;
   dim3 grid((unsigned)tl.tasks.size(), (unsigned)((2 * nact * tl.maxrows + 127) / 128));
-  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), c->stream>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_actlist.p, nact,
+  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), st>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_actlist.p, nact,
                                                                      c->d_err.p);
   c->launches++;
   CK(cudaGetLastError());
@@ -486,7 +492,7 @@ static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact) {
 }
 
 static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
-  return launch_gemm<double>(c, tl, P, active, c->d_bufs.p);
+  return launch_gemm<double>(c, tl, P, active, c->d_bufs.p, c->stream);
 }
 
 // residual interaction of the points flagged in `act`: state (X, Y) -> hqp
@@ -494,11 +500,11 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
 // copy of the state and writes the FP32 hqp)
 template <class T>
 // P: batch size (grid extent), nact: points active in this evaluation
-static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed) {
-  auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
+static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed, cudaStream_t st) {
+  auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], st); };
   auto toc = [&](int k) {
     if (!timed) return;
-    cudaEventRecord(c->ev[1], c->stream);
+    cudaEventRecord(c->ev[1], st);
     cudaEventSynchronize(c->ev[1]);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
@@ -515,11 +521,11 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   int rc;
   tic();
   if constexpr (f32) {
-    if ((rc = launch_gemm_tc(c, c->t1a, nact))) return rc;
-    if ((rc = launch_gemm_tc(c, c->t1b, nact))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t1a, nact, st))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t1b, nact, st))) return rc;
   } else {
-    if ((rc = launch_gemm<T>(c, c->k1a, P, act, bufs))) return rc;
-    if ((rc = launch_gemm<T>(c, c->k1b, P, act, bufs))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k1a, P, act, bufs, st))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k1b, P, act, bufs, st))) return rc;
   }
   toc(0);
   const long long nxy = c->nxy;
@@ -548,7 +554,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
       DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
       DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
       Gm = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
-      k_density_tc<<<dim3(ntr, Gm, 2 * na), DTC_THREADS, density_tc_smem_bytes(), c->stream>>>(
+      k_density_tc<<<dim3(ntr, Gm, 2 * na), DTC_THREADS, density_tc_smem_bytes(), st>>>(
           B, t0, t1, Gm, c->d_actlist.p, dpart, c->d_err.p);
       c->launches++;
       CK(cudaGetLastError());
@@ -557,8 +563,8 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   }
   if (!dens_done) {
     dim3 grid(ntr, G, 2 * P);
-    if constexpr (f32) k_density<float><<<grid, 256, density_smem_bytes<float>(), c->stream>>>(B, d0, d1, G, dpart, act);
-    else k_density_fp64<<<grid, 256, 0, c->stream>>>(B, d0, d1, G, dpart, act);
+    if constexpr (f32) k_density<float><<<grid, 256, density_smem_bytes<float>(), st>>>(B, d0, d1, G, dpart, act);
+    else k_density_fp64<<<grid, 256, 0, st>>>(B, d0, d1, G, dpart, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -566,7 +572,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   tic();
   {
     dim3 grid((c->nghl + 127) / 128, 2 * P);
-    k_meanfield<T><<<grid, 128, 0, c->stream>>>(B, Gm, dpart, mf, act);
+    k_meanfield<T><<<grid, 128, 0, st>>>(B, Gm, dpart, mf, act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -575,24 +581,24 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed)
   if constexpr (f32) {
     // tensor cores: c->d_actlist holds the nact points of this evaluation
     dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
-    k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), c->stream>>>(
+    k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), st>>>(
         B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, hsp, nxy, c->d_err.p);
     c->launches++;
     CK(cudaGetLastError());
   } else {
     dim3 grid((unsigned)c->htasks.size(), P);
-    k_hproj_fp64<<<grid, 256, hproj_fp64_smem_bytes(), c->stream>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
+    k_hproj_fp64<<<grid, 256, hproj_fp64_smem_bytes(), st>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
     c->launches++;
     CK(cudaGetLastError());
   }
   toc(3);
   tic();
   if constexpr (f32) {
-    if ((rc = launch_gemm_tc(c, c->t2a, nact))) return rc;
-    if ((rc = launch_gemm_tc(c, c->t2b, nact))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t2a, nact, st))) return rc;
+    if ((rc = launch_gemm_tc(c, c->t2b, nact, st))) return rc;
   } else {
-    if ((rc = launch_gemm<T>(c, c->k2a, P, act, bufs))) return rc;
-    if ((rc = launch_gemm<T>(c, c->k2b, P, act, bufs))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k2a, P, act, bufs, st))) return rc;
+    if ((rc = launch_gemm<T>(c, c->k2b, P, act, bufs, st))) return rc;
   }
   toc(4);
   return PNFAM_OK;
@@ -705,7 +711,10 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
   }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
-      cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess) {
+      cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream64, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->evf[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
   }
@@ -1021,9 +1030,19 @@ static int engine_launch(pnfam_engine* e) {
   }
   const int* act = c->d_active.p;
   int rc;
+  bool split = false;
   if (!e->no_res) {
     CK(cudaMemcpyAsync(c->d_act64.p, e->act64.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-    if (n64 && (rc = residual_t<double>(c, P, n64, c->d_act64.p, timed))) return rc;
+    // FP64 (anchor) evaluations of some points and FP32 increment evaluations of the
+    // others use disjoint scratch and write disjoint rows of hqp: the FP64 ones run
+    // on the second stream, joined before the Green's function (not when stages are timed)
+    split = n64 && n32 && !timed;
+    if (split) {
+      CK(cudaEventRecord(c->evf[0], c->stream));
+      CK(cudaStreamWaitEvent(c->stream64, c->evf[0], 0));
+    }
+    if (n64 && (rc = residual_t<double>(c, P, n64, c->d_act64.p, timed, split ? c->stream64 : c->stream))) return rc;
+    if (split) CK(cudaEventRecord(c->evf[1], c->stream64));
     if (e->mixed) {
       CK(cudaMemcpyAsync(c->d_act32.p, e->act32.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
       if (n32) {
@@ -1034,13 +1053,14 @@ static int engine_launch(pnfam_engine* e) {
         CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
         k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
                                                c->d_dmax.p);
-        if ((rc = residual_t<float>(c, P, n32, c->d_act32.p, timed))) return rc;
+        if ((rc = residual_t<float>(c, P, n32, c->d_act32.p, timed, c->stream))) return rc;
         k_to_f64<<<vgrid, 256, 0, c->stream>>>(c->d_hqp32.p, c->d_hqp.p, N, N, c->d_act32.p);
         c->launches += 2;
         CK(cudaGetLastError());
       }
     }
   }
+  if (split) CK(cudaStreamWaitEvent(c->stream, c->evf[1], 0));
   const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
   const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
   tic();

@@ -1864,9 +1864,10 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
 
 // normalise column ipos by 1/|df_ipos| and form the dots
 // dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used.
-// A CTA covers BRO_CHUNK elements, four per thread, so df_ipos and vout are read
-// once (into registers) and every df_k once; each warp reduces its share per k
-// with shuffles, one barrier at the end.
+// A CTA covers BRO_CHUNK elements: the normalised df_ipos and vout of its chunk
+// are staged in shared memory, then each warp takes whole columns (k = warp,
+// warp + 8, ...), every lane streaming its share of the column with many loads
+// in flight, and one shuffle reduction per column.
 __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __restrict__ norm,
                                                   const int* __restrict__ active) {
   const int p = blockIdx.y;
@@ -1876,57 +1877,72 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   int iu, ipos, inext;
   bro_slots(it, S.M, iu, ipos, inext);
   const bool upd = it >= 2;
-  __shared__ double wsum[8][2 * 64];
+  __shared__ double sf[BRO_CHUNK], sv[BRO_CHUNK];
   const double* vo = S.vout + (long long)p * S.N;
   double* dfp = S.df + (long long)p * S.M * S.N;
   double* dvp = S.dv + (long long)p * S.M * S.N;
-  double* fi = dfp + (long long)ipos * S.N;
-  const int e0 = blockIdx.x * BRO_CHUNK + threadIdx.x;
+  const long long base = (long long)blockIdx.x * BRO_CHUNK;
+  const int len = (int)min((long long)BRO_CHUNK, (long long)S.N - base);
   const double sc = upd ? norm[p] : 0.0;
-  double f4[4], v4[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int e = e0 + u * 256;
-    f4[u] = 0.0; v4[u] = 0.0;
-    if (e < S.N) {
+  for (int i = threadIdx.x; i < BRO_CHUNK; i += blockDim.x) {
+    double f = 0.0, v = 0.0;
+    if (i < len) {
+      const long long e = base + i;
       if (upd) {
-        f4[u] = fi[e] * sc;
-        fi[e] = f4[u];
+        f = dfp[(long long)ipos * S.N + e] * sc;
+        dfp[(long long)ipos * S.N + e] = f;
         dvp[(long long)ipos * S.N + e] *= sc;
       }
-      v4[u] = vo[e];
+      v = vo[e];
     }
+    sf[i] = f;
+    sv[i] = v;
   }
+  __syncthreads();
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  for (int k = 0; k < iu; ++k) {
-    const double* fk = dfp + (long long)k * S.N;
+  double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
+  for (int k = w; k < iu; k += 8) {
     double a = 0.0, b = 0.0;
+    if (k == ipos && upd) {  // column ipos itself: its normalised values are in shared memory
+      for (int j = l; j < len; j += 32) {
+        const double f = sf[j];
+        a = fma(f, f, a);
+        b = fma(f, sv[j], b);
+      }
+    } else {
+      const double* fk = dfp + (long long)k * S.N + base;
+      if (len == BRO_CHUNK) {  // 16 loads of each lane in flight at a time
+        for (int h = 0; h < BRO_CHUNK; h += 16 * 32) {
+          double fv[16];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = e0 + u * 256;
-      // column ipos itself: its normalised values are the ones in registers
-      const double f = e < S.N ? (k == ipos && upd ? f4[u] : fk[e]) : 0.0;
-      a = fma(f, f4[u], a);
-      b = fma(f, v4[u], b);
+          for (int u = 0; u < 16; ++u) fv[u] = __ldcs(fk + h + u * 32 + l);
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            a = fma(fv[u], sf[h + u * 32 + l], a);
+            b = fma(fv[u], sv[h + u * 32 + l], b);
+          }
+        }
+      } else {
+        for (int j = l; j < len; j += 32) {
+          const double f = fk[j];
+          a = fma(f, sf[j], a);
+          b = fma(f, sv[j], b);
+        }
+      }
     }
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_xor_sync(0xffffffffu, a, o);
       b += __shfl_xor_sync(0xffffffffu, b, o);
     }
-    if (l == 0) { wsum[w][k] = a; wsum[w][64 + k] = b; }
-  }
-  __syncthreads();
-  double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
-  for (int k = threadIdx.x; k < iu; k += blockDim.x) {
-    double sa = 0.0, sb = 0.0;
-    for (int i = 0; i < 8; ++i) { sa += wsum[i][k]; sb += wsum[i][64 + k]; }
-    pt[2 + k] = sa; pt[2 + 64 + k] = sb;
+    if (l == 0) { pt[2 + k] = a; pt[2 + 64 + k] = b; }
   }
 }
 
 // one CTA (256 threads) per point: reduce partials; stage 0: si and 1/|df_ipos|;
 // stage 1: maintain beta (M x M) and solve beta*gamma = work by Gaussian
-// elimination with partial pivoting (rows updated in parallel)
+// elimination with partial pivoting (LAPACK dgesv's pivot choice: the first row
+// of largest magnitude), pivot search and row swap by one warp, row updates by
+// all warps
 __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double w0, double* __restrict__ si,
                                                    double* __restrict__ norm, double* __restrict__ beta,
                                                    double* __restrict__ gamma, const int* __restrict__ active) {
@@ -1959,7 +1975,6 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   __shared__ double A[64][65];
   __shared__ double x[64];
   __shared__ double f[64];
-  __shared__ int piv;
   const int M = S.M;
   double* bp = beta + (long long)p * M * M;
   for (int k = w; k < n; k += 8) {   // one warp per k: sum the chunk partials
@@ -1980,24 +1995,30 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   for (int e = tid; e < n * n; e += blockDim.x) A[e / n][e % n] = bp[(e / n) * M + (e % n)];
   __syncthreads();
   for (int c = 0; c < n; ++c) {
-    if (tid == 0) {
-      int pv = c;
-      for (int r = c + 1; r < n; ++r) if (fabs(A[r][c]) > fabs(A[pv][c])) pv = r;
-      piv = pv;
+    if (w == 0) {
+      double best = -1.0;
+      int br = n;
+      for (int r = c + l; r < n; r += 32) {
+        const double v = fabs(A[r][c]);
+        if (v > best) { best = v; br = r; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, br, o);
+        if (ob > best || (ob == best && orow < br)) { best = ob; br = orow; }
+      }
+      if (br >= n) br = c;  // no comparable entry (NaN column): keep the diagonal, as a serial scan does
+      if (br != c) {
+        for (int j = l; j < n; j += 32) { const double t = A[c][j]; A[c][j] = A[br][j]; A[br][j] = t; }
+        if (l == 0) { const double t = x[c]; x[c] = x[br]; x[br] = t; }
+      }
+      __syncwarp();
+      for (int r = c + 1 + l; r < n; r += 32) f[r] = A[r][c] / A[c][c];
     }
     __syncthreads();
-    const int pv = piv;
-    if (pv != c) {
-      for (int j = tid; j < n; j += blockDim.x) { const double t = A[c][j]; A[c][j] = A[pv][j]; A[pv][j] = t; }
-      if (tid == 0) { const double t = x[c]; x[c] = x[pv]; x[pv] = t; }
-      __syncthreads();
-    }
-    for (int r = c + 1 + tid; r < n; r += blockDim.x) f[r] = A[r][c] / A[c][c];
-    __syncthreads();
-    const int nr = n - c - 1, nc = n - c;
-    for (int e = tid; e < nr * nc; e += blockDim.x) {
-      const int r = c + 1 + e / nc, j = c + e % nc;
-      A[r][j] -= f[r] * A[c][j];
+    for (int r = c + 1 + w; r < n; r += 8) {
+      const double fr = f[r];
+      for (int j = c + 1 + l; j < n; j += 32) A[r][j] -= fr * A[c][j];
     }
     for (int r = c + 1 + tid; r < n; r += blockDim.x) x[r] -= f[r] * x[c];
     __syncthreads();
