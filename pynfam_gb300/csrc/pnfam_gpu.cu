@@ -194,14 +194,24 @@ struct pnfam_ctx {
   DBuf<BufDescT<float>> d_bufs32;
   DBuf<double> d_xsave, d_radd;   // [P][4nxy] mixed form: anchor X_a and its FP64 image g(X_a)
   DBuf<unsigned long long> d_dmax;  // [P] max|X - X_a| of the last increment evaluation
+  // tensor-core densities: unit tables per call, B chunks to lay out, pre-split A
+  std::vector<DUnitTC> dunits[2];
+  std::vector<DBChunkTC> bchunks;
+  std::vector<DAChunkTC> achunks;
+  DBuf<DUnitTC> d_dunits0, d_dunits1;
+  DBuf<DBChunkTC> d_bchunks;
+  DBuf<DAChunkTC> d_achunks;
+  DBuf<float> d_aphi;     // [ceil(nghl/32)][nachunk][DTC2_ACH], once per ground state
+  DBuf<float> d_bsplit;   // [P][bstride]
+  long long bstride = 0;
+  bool have_aphi = false;
   long long pit64 = 0, pit32 = 0;   // point-iterations per precision in the last solve
   int G = 1;
   int nsm = 1;
   int maxdb = 0;
-  // FP32 densities on the tensor cores (k_density_tc) instead of the SIMT kernel,
-  // chosen at context creation by PNFAM_GB300_TC_DENSITY=1; off by default: on
-  // N_sh = 16 the SIMT kernel is still the faster of the two
-  bool tc_density = false;
+  // FP32 densities on the tensor cores (k_density_tc2, the default) or on the SIMT
+  // cores (k_density<float>, PNFAM_GB300_TC_DENSITY=0 at context creation)
+  bool tc_density = true;
   int nchunk_bro = 1, nchunk_c = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -224,6 +234,8 @@ struct pnfam_ctx {
     for (auto* b : fb) b->release();
     d_bufs32.release();
     d_xsave.release(); d_radd.release(); d_dmax.release();
+    d_dunits0.release(); d_dunits1.release(); d_bchunks.release(); d_achunks.release(); d_aphi.release();
+    d_bsplit.release();
     for (auto* b : ib) b->release();
     d_ns.release();
     DBuf<double>* dbs[] = {&d_up, &d_vp, &d_un, &d_vn, &d_ep, &d_en, &d_phi, &d_wd, &d_crho, &d_cs,
@@ -420,6 +432,50 @@ static void build_tasks(pnfam_ctx* c) {
     if (c->xc[i] >= 0) add_tc(i, c->xc[i], 1, 0, 1, c->xoff[i]);
     if (c->yc[i] >= 0) add_tc(i, c->yc[i], 1, 1, 2, c->yoff[i]);
   }
+  // tensor-core densities: A chunks per (block, spin of the rows, 8 rows); units per
+  // call in the order (kind, ix, column range, spin), so that the two spins of one
+  // column range follow each other; B chunks with their place in a point's buffer
+  c->achunks.clear();
+  std::vector<int> aidx(2 * nb, 0);
+  for (int i = 0; i < nb; ++i) {
+    const int seg[3] = {0, c->nup[i], c->db[i]};
+    for (int s = 0; s < 2; ++s) {
+      aidx[2 * i + s] = (int)c->achunks.size();
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += 8) c->achunks.push_back(DAChunkTC{i, a0, seg[s + 1], 0});
+    }
+  }
+  c->bchunks.clear();
+  long long boff = 0;
+  for (int call = 0; call < 2; ++call) {
+    auto& U = c->dunits[call];
+    U.clear();
+    for (int kind = 0; kind < 2; ++kind) {
+      const std::vector<int>& cols = kind == 0 ? c->fc : (call == 0 ? c->xtc : c->ytc);
+      for (int ix = 0; ix < nb; ++ix) {
+        const int iy = cols[ix];
+        if (iy < 0) continue;
+        const int dc = c->db[iy];
+        const int nh = cdiv(dc, (int)DTC2_MAXNC), csz = cdiv(dc, nh);
+        const int seg[3] = {0, c->nup[ix], c->db[ix]};
+        for (int b0 = 0; b0 < dc; b0 += csz) {
+          const int nc = std::min(csz, dc - b0), npad = cdiv(2 * nc, 16) * 16;
+          for (int s = 0; s < 2; ++s) {
+            if (seg[s] >= seg[s + 1]) continue;
+            DUnitTC u;
+            u.kind = kind; u.ix = ix; u.iy = iy; u.s = s; u.b0 = b0; u.nc = nc; u.npad = npad;
+            u.nk = cdiv(seg[s + 1] - seg[s], 8); u.achunk = aidx[2 * ix + s]; u.nub = c->nup[iy]; u.boff = boff;
+            for (int kc = 0; kc < u.nk; ++kc) {
+              c->bchunks.push_back(DBChunkTC{call, kind, ix, seg[s] + 8 * kc, seg[s + 1], b0, nc, npad,
+                                             boff + (long long)kc * 16 * npad});
+            }
+            boff += (long long)u.nk * 16 * npad;
+            U.push_back(u);
+          }
+        }
+      }
+    }
+  }
+  c->bstride = (boff + 63) / 64 * 64;
 }
 
 // ---------------------------------------------------------------------------
@@ -549,13 +605,21 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
   bool dens_done = false;
   tic();
   if constexpr (f32) {
-    if (c->maxdb <= 128 && c->tc_density) {
-      // tensor cores: c->d_actlist holds the nact points of this evaluation
+    if (c->tc_density) {
+      // tensor cores: c->d_actlist holds the nact points of this evaluation; their
+      // densities are split and laid out first, then the units run on the tensor cores
       DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
       DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
-      Gm = std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na)));
-      k_density_tc<<<dim3(ntr, Gm, 2 * na), DTC_THREADS, density_tc_smem_bytes(), st>>>(
-          B, t0, t1, Gm, c->d_actlist.p, dpart, c->d_err.p);
+      const int ntr32 = (c->nghl + 31) / 32;
+      Gm = std::max(1, std::min(c->G, (2 * c->nsm + ntr32 * 2 * na - 1) / (ntr32 * 2 * na)));
+      if (!c->bchunks.empty()) {
+        k_dens_bsplit<<<dim3((unsigned)c->bchunks.size(), (unsigned)na), 256, 0, st>>>(
+            B, t0, t1, c->d_bchunks.p, c->d_actlist.p, c->d_bsplit.p, c->bstride);
+        c->launches++;
+      }
+      k_density_tc2<<<dim3(ntr32, Gm, 2 * na), DTC2_THREADS, density_tc2_smem_bytes(), st>>>(
+          B, c->d_dunits0.p, (int)c->dunits[0].size(), c->d_dunits1.p, (int)c->dunits[1].size(), c->d_aphi.p,
+          (int)c->achunks.size(), c->d_bsplit.p, c->bstride, Gm, c->d_actlist.p, dpart, c->d_err.p);
       c->launches++;
       CK(cudaGetLastError());
       dens_done = true;
@@ -631,6 +695,18 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   CK(dalloc(c->d_xsave, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_radd, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_dmax, (size_t)P));
+  if (c->tc_density) {
+    CK(dalloc(c->d_bsplit, (size_t)P * c->bstride));
+    if (!c->have_aphi) {
+      const int ntr = (c->nghl + 31) / 32, na = (int)c->achunks.size();
+      CK(dalloc(c->d_aphi, (size_t)ntr * na * DTC2_ACH));
+      if (na > 0) {
+        k_dens_asplit<<<dim3(na, ntr), 256, 0, c->stream>>>(c->devbasis<float>(), c->d_achunks.p, na, c->d_aphi.p);
+        CK(cudaGetLastError());
+      }
+      c->have_aphi = true;
+    }
+  }
   BufDescT<float> bd[NBUF];
   bd[B_UP] = {c->d_up32.p, 0, 0};
   bd[B_VP] = {c->d_vp32.p, 0, 0};
@@ -668,8 +744,9 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
   c->db.assign(basis->db, basis->db + c->nb);
   c->maxdb = c->nb > 0 ? *std::max_element(c->db.begin(), c->db.end()) : 0;
   {
+    // FP32 densities on the tensor cores unless PNFAM_GB300_TC_DENSITY=0 (SIMT kernel)
     const char* v = std::getenv("PNFAM_GB300_TC_DENSITY");
-    c->tc_density = v && v[0] == '1';
+    c->tc_density = !(v && v[0] == '0');
   }
   c->nup.assign(basis->num_spin_up, basis->num_spin_up + c->nb);
   c->st.resize(c->nb);
@@ -722,8 +799,8 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
                            (int)hproj_fp64_smem_bytes()) != cudaSuccess ||
       cudaFuncSetAttribute(k_hproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)hproj_tc_smem_bytes(HTC_MAXN)) != cudaSuccess ||
-      cudaFuncSetAttribute(k_density_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)density_tc_smem_bytes()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_density_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)density_tc2_smem_bytes()) != cudaSuccess ||
       cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)gemm_tc_smem_bytes()) != cudaSuccess) {
     delete c;
@@ -812,6 +889,10 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   }
   CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
   CK(upload(c->d_htasks_tc, c->htasks_tc.data(), c->htasks_tc.size()));
+  CK(upload(c->d_dunits0, c->dunits[0].data(), c->dunits[0].size()));
+  CK(upload(c->d_dunits1, c->dunits[1].data(), c->dunits[1].size()));
+  CK(upload(c->d_bchunks, c->bchunks.data(), c->bchunks.size()));
+  if (!c->have_aphi) CK(upload(c->d_achunks, c->achunks.data(), c->achunks.size()));
   c->have_op = true;
   int rc = ensure_buffers(c, std::max(1, c->cap_P), std::max(1, c->cap_M));
   if (rc) return rc;
@@ -1349,11 +1430,16 @@ extern "C" int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* c, const double* re
   d1.kcols = c->d_ytc.p; d1.koffs = c->d_ytoff.p;
   const DevBasisT<float> B = c->devbasis<float>();
   const int* act = c->d_active.p;
-  if (c->maxdb <= 128 && c->tc_density) {
+  if (c->tc_density) {
     DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
     DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
-    k_density_tc<<<dim3((c->nghl + 31) / 32, c->G, 2), DTC_THREADS, density_tc_smem_bytes(), c->stream>>>(
-        B, t0, t1, c->G, c->d_actlist.p, c->d_dpart32.p, c->d_err.p);
+    if (!c->bchunks.empty())
+      k_dens_bsplit<<<dim3((unsigned)c->bchunks.size(), 1), 256, 0, c->stream>>>(B, t0, t1, c->d_bchunks.p,
+                                                                                c->d_actlist.p, c->d_bsplit.p,
+                                                                                c->bstride);
+    k_density_tc2<<<dim3((c->nghl + 31) / 32, c->G, 2), DTC2_THREADS, density_tc2_smem_bytes(), c->stream>>>(
+        B, c->d_dunits0.p, (int)c->dunits[0].size(), c->d_dunits1.p, (int)c->dunits[1].size(), c->d_aphi.p,
+        (int)c->achunks.size(), c->d_bsplit.p, c->bstride, c->G, c->d_actlist.p, c->d_dpart32.p, c->d_err.p);
   } else {
     k_density<float><<<dim3((c->nghl + DRT - 1) / DRT, c->G, 2), 256, density_smem_bytes<float>(), c->stream>>>(
         B, d0, d1, c->G, c->d_dpart32.p, act);

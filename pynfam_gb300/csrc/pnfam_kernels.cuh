@@ -825,28 +825,10 @@ __global__ void __launch_bounds__(256) k_density_fp64(DevBasis B, DensCall c0, D
 }
 
 // ---------------------------------------------------------------------------
-// densities on the tensor cores (FP32 data, 3xTF32 products).
-// A CTA owns 32 mesh points r of one point p and one call, and walks the block
-// rows of its group.  For every (block row, spin s of the rows) "unit":
-//   W[m][n] = sum_{a in s} phi_q(a, r) rho(a, b; pl),  m = q*32 + (r - r0),
-//                                                     n = pl*dc + b
-// is accumulated in tensor memory (one accumulator of up to 256 columns, so two
-// CTAs share an SM), and folded by warps 0-7 into the 28 local densities: warp w
-// reads the TMEM lanes of component q = w % 4 and half of the columns, and adds
-// the terms of the density formulas (pnfam_hamiltonian_blas.f90:124-711) that
-// contain W_q, with the column basis functions phi_q'(b, r) staged in shared
-// memory once per block.  Warp 8 issues the MMAs.  The partial densities of the
-// 8 warps are summed at the end.  dpart: [P][2][G][2*ND][nghl]
+// fold of W_q(r, b) = sum_a phi_q(a, r) rho_ab into the 28 local densities, one
+// component q at a time (the terms of pnfam_hamiltonian_blas.f90:124-711 that
+// contain W_q), for the tensor-core density kernel
 // ---------------------------------------------------------------------------
-enum { DTC_K = 8, DTC_MAXN = 256, DTC_MAXB = 128, DTC_PROD = 256, DTC_THREADS = DTC_PROD + 32 };
-
-__host__ __device__ constexpr size_t density_tc_smem_bytes() {
-  // two stages of A (128 x 8, hi and lo) and B (256 x 8, hi and lo), then the column
-  // basis functions [128 b][32 r][4 q]; the end-of-CTA reduction buffer
-  // [8 warps][2*ND][32] reuses the same memory
-  return (size_t)(2 * (2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K) + DTC_MAXB * 32 * 4) * sizeof(float);
-}
-
 // the terms of the density formulas that contain W_q of rows with the SAME spin as b
 template <int Q>
 __device__ __forceinline__ void fold_same(float (&acc)[2 * ND], float wr, float wi, const float (&P)[4], float sg) {
@@ -928,21 +910,122 @@ __device__ __forceinline__ void fold_opp(float (&acc)[2 * ND], float wr, float w
 }
 #undef A_
 
-// fold the W_q rows of one unit (this warp's component Q, its column half) into the
-// densities; KIND 0: normal densities, 1: pairing densities (Q = 0)
+struct DensTCArgs {
+  const float* rho; long long rho_sp, rho_spl;   // as DensCallT, per call
+  const int* rcols; const long long* roffs;
+  const float* kap; long long kap_sp, kap_spl;
+  const int* kcols; const long long* koffs;
+};
+
+// ---------------------------------------------------------------------------
+// densities on the tensor cores with operands moved by the bulk-copy engine.
+// A unit is (kind, block row ix, spin s of its rows, columns [b0, b0 + nc) of the
+// block iy = cols[ix]), nc <= 64:
+//   W[m][n] = sum_{a in s} phi_q(a, r) rho(a, b; pl),  m = q*32 + l (r = r0 + l),
+//                                                     n = pl*nc + (b - b0)
+// with K (the rows a of spin s) in chunks of 8.  Both operands are split into TF32
+// high parts and remainders ahead of the kernel and laid out in the canonical
+// K-major core-matrix order: A (phi) once per ground state for every (ix, s, chunk,
+// 32-point mesh tile), B (rho of every active point) by k_dens_bsplit in each
+// evaluation.  In the kernel one thread copies A and B chunks into a ring of
+// DTC2_NS shared-memory stages (cp.async.bulk, completion on an mbarrier), one
+// thread issues the 3xTF32 MMAs into one of two 128-column TMEM accumulators,
+// and eight warps fold the finished accumulator into the 28 local densities
+// (warp w: component q = w % 4, half of the columns; fold_same / fold_opp) while
+// the other one fills.  dpart: [P][2][G][2*ND][nghl]
+// ---------------------------------------------------------------------------
+enum { DTC2_NS = 4, DTC2_FOLD = 256, DTC2_THREADS = DTC2_FOLD + 64, DTC2_MAXNC = 64 };
+enum { DTC2_ACH = 2 * 128 * 8,                   // floats of one A chunk (hi, lo)
+       DTC2_STAGE = DTC2_ACH + 2 * 128 * 8 };    // floats of one stage (A chunk, B chunk with npad <= 128)
+
+struct DUnitTC {
+  int kind, ix, iy, s;    // rows of block ix of spin s (0 up, 1 down), columns of block iy
+  int b0, nc, npad, nk;   // columns [b0, b0 + nc), N = 2*nc padded to 16, K chunks of 8
+  int achunk, nub;        // first A chunk of (ix, s); spin-up columns of block iy
+  long long boff;         // floats: first B chunk of the unit within a point's B buffer
+};
+struct DBChunkTC {        // one B chunk: rows [a0, min(a0 + 8, ahi)) of a unit's columns
+  int call, kind, ix, a0, ahi, b0, nc, npad;
+  long long dst;          // floats within a point's B buffer
+};
+struct DAChunkTC { int ix, a0, ahi, pad_; };
+
+__host__ __device__ constexpr size_t density_tc2_smem_bytes() {
+  // the stage ring, then the column basis functions [64 b][32 r][4 q]; the
+  // end-of-CTA reduction buffer [8 warps][2*ND][32] reuses the same memory
+  return (size_t)(DTC2_NS * DTC2_STAGE + DTC2_MAXNC * 32 * 4) * sizeof(float);
+}
+static_assert(8 * 2 * ND * 32 <= DTC2_NS * DTC2_STAGE + DTC2_MAXNC * 32 * 4, "reduction buffer");
+
+// A chunks (once per ground state): aphi[rt][chunk][hi | lo][128 x 8], rows m = q*32 + l
+// grid (nachunk, ceil(nghl/32)), 256 threads
+__global__ void __launch_bounds__(256) k_dens_asplit(DevBasisT<float> B, const DAChunkTC* __restrict__ chunks,
+                                                     int nachunk, float* __restrict__ aphi) {
+  const DAChunkTC ch = chunks[blockIdx.x];
+  const int r0 = blockIdx.y * 32, nghl = B.nghl;
+  const long long ps = (long long)B.dqp * nghl;
+  float* dst = aphi + ((long long)blockIdx.y * nachunk + blockIdx.x) * DTC2_ACH;
+  const int m = threadIdx.x & 127, k4 = threadIdx.x >> 7;
+  const int q = m >> 5, r = r0 + (m & 31);
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (r < nghl) {
+    const int a = ch.a0 + 4 * k4;
+    const float* src = B.phi + q * ps + (long long)(B.st[ch.ix] + a) * nghl + r;
+    if (a < ch.ahi) v.x = src[0];
+    if (a + 1 < ch.ahi) v.y = src[nghl];
+    if (a + 2 < ch.ahi) v.z = src[2 * nghl];
+    if (a + 3 < ch.ahi) v.w = src[3 * nghl];
+  }
+  const int o = tc::cm_off(m, 4 * k4, 128);
+  st_split4(dst + o, dst + 128 * 8 + o, v);
+}
+
+// B chunks of the listed points: bsplit[p][chunk.dst + (hi | lo)][npad x 8], rows n = pl*nc + b
+// grid (nbchunk, nact), 256 threads
+__global__ void __launch_bounds__(256) k_dens_bsplit(DevBasisT<float> B, DensTCArgs c0, DensTCArgs c1,
+                                                     const DBChunkTC* __restrict__ chunks,
+                                                     const int* __restrict__ actlist, float* __restrict__ bsplit,
+                                                     long long bstride) {
+  const DBChunkTC ch = chunks[blockIdx.x];
+  const int p = actlist[blockIdx.y];
+  const DensTCArgs& C = ch.call ? c1 : c0;
+  const float* base = ch.kind == 0 ? C.rho : C.kap;
+  const long long bsp = ch.kind == 0 ? C.rho_sp : C.kap_sp, bspl = ch.kind == 0 ? C.rho_spl : C.kap_spl;
+  const long long off = (ch.kind == 0 ? C.roffs : C.koffs)[ch.ix];
+  const float* mat = base + (long long)p * bsp + off;
+  const int d = B.db[ch.ix];
+  float* dst = bsplit + (long long)p * bstride + ch.dst;
+  for (int e = threadIdx.x; e < 2 * ch.npad; e += blockDim.x) {
+    const int n = e >> 1, k4 = e & 1;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (n < 2 * ch.nc) {
+      const int pl = n >= ch.nc ? 1 : 0, b = n - pl * ch.nc;
+      const int a = ch.a0 + 4 * k4;
+      const float* src = mat + (long long)pl * bspl + (long long)(ch.b0 + b) * d + a;
+      if (a < ch.ahi) v.x = src[0];
+      if (a + 1 < ch.ahi) v.y = src[1];
+      if (a + 2 < ch.ahi) v.z = src[2];
+      if (a + 3 < ch.ahi) v.w = src[3];
+    }
+    const int o = tc::cm_off(n, 4 * k4, ch.npad);
+    st_split4(dst + o, dst + ch.npad * 8 + o, v);
+  }
+}
+
+// fold the W_q rows of one unit from TMEM (this warp's component Q, columns
+// [c8lo, c8hi) in groups of 8; re at column b, im at nc + b)
 template <int Q, int KIND>
-__device__ __forceinline__ void fold_unit(float (&acc)[2 * ND], uint32_t lane_base, const float* sPb, int lane,
-                                          int dc, int nub, int s, int c8lo, int c8hi, bool skip) {
+__device__ __forceinline__ void fold_unit2(float (&acc)[2 * ND], uint32_t lane_base, const float* sPb, int lane,
+                                           int nc, int b0, int nub, int s, int c8lo, int c8hi, bool skip) {
   for (int c8 = c8lo; c8 < c8hi; ++c8) {
     float wre[8], wim[8];
-    tc::tmem_ld8(lane_base + (uint32_t)(8 * c8), wre);
-    tc::tmem_ld8(lane_base + (uint32_t)(dc + 8 * c8), wim);
+    tc::tmem_ld8x2(lane_base + (uint32_t)(8 * c8), lane_base + (uint32_t)(nc + 8 * c8), wre, wim);
     if (skip) continue;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int b = 8 * c8 + i;
-      if (b >= dc) break;
-      const bool up = b < nub;
+      if (b >= nc) break;
+      const bool up = b0 + b < nub;
       const float sg = up ? 1.f : -1.f, sig = up ? -1.f : 1.f;
       const bool same = up == (s == 0);
       const float4 pv = *reinterpret_cast<const float4*>(&sPb[(b * 32 + lane) * 4]);
@@ -964,35 +1047,28 @@ __device__ __forceinline__ void fold_unit(float (&acc)[2 * ND], uint32_t lane_ba
   }
 }
 
-struct DensTCArgs {
-  const float* rho; long long rho_sp, rho_spl;   // as DensCallT, per call
-  const int* rcols; const long long* roffs;
-  const float* kap; long long kap_sp, kap_spl;
-  const int* kcols; const long long* koffs;
-};
-
-// grid (ceil(nghl/32), G, 2*nact); DTC_THREADS threads; dynamic smem density_tc_smem_bytes()
-__global__ void __launch_bounds__(DTC_THREADS, 2) k_density_tc(DevBasisT<float> B, DensTCArgs c0, DensTCArgs c1, int G,
-                                                               const int* __restrict__ actlist,
-                                                               float* __restrict__ dpart, int* __restrict__ err) {
+// grid (ceil(nghl/32), G, 2*nact); DTC2_THREADS threads; dynamic smem density_tc2_smem_bytes().
+// A CTA takes the units of its call with ix % G == g for its mesh tile and point.
+__global__ void __launch_bounds__(DTC2_THREADS, 2) k_density_tc2(
+    DevBasisT<float> B, const DUnitTC* __restrict__ units0, int nunit0, const DUnitTC* __restrict__ units1,
+    int nunit1, const float* __restrict__ aphi, int nachunk, const float* __restrict__ bsplit, long long bstride,
+    int G, const int* __restrict__ actlist, float* __restrict__ dpart, int* __restrict__ err) {
   const int p = actlist[blockIdx.z >> 1], call = blockIdx.z & 1;
-  const DensTCArgs& C = call ? c1 : c0;
-  const int g = blockIdx.y;
-  const int r0 = blockIdx.x * 32;
+  const DUnitTC* units = call ? units1 : units0;
+  const int nunit = call ? nunit1 : nunit0;
+  const int g = blockIdx.y, rt = blockIdx.x, r0 = rt * 32;
   const int nghl = B.nghl;
   const long long ps = (long long)B.dqp * nghl;
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* stage_base = reinterpret_cast<float*>(smraw);
-  const int stage_floats = 2 * 128 * DTC_K + 2 * DTC_MAXN * DTC_K;
-  float* sPb = stage_base + 2 * stage_floats;   // [b][r][q'] column basis functions of the block
-  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2], accf_bar, acce_bar;
+  float* stages = reinterpret_cast<float*>(smraw);
+  float* sPb = stages + DTC2_NS * DTC2_STAGE;
+  __shared__ __align__(8) uint64_t full_bar[DTC2_NS], empty_bar[DTC2_NS], accf_bar[2], acce_bar[2];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    tc::mbar_init(&full_bar[0], DTC_PROD); tc::mbar_init(&full_bar[1], DTC_PROD);
-    tc::mbar_init(&empty_bar[0], 1); tc::mbar_init(&empty_bar[1], 1);
-    tc::mbar_init(&accf_bar, 1); tc::mbar_init(&acce_bar, DTC_PROD);
+    for (int i = 0; i < DTC2_NS; ++i) { tc::mbar_init(&full_bar[i], 1); tc::mbar_init(&empty_bar[i], 1); }
+    for (int j = 0; j < 2; ++j) { tc::mbar_init(&accf_bar[j], 1); tc::mbar_init(&acce_bar[j], DTC2_FOLD); }
     abort_flag = 0;
   }
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
@@ -1003,167 +1079,117 @@ __global__ void __launch_bounds__(DTC_THREADS, 2) k_density_tc(DevBasisT<float> 
   float acc[2 * ND];
 #pragma unroll
   for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
-  auto unit_info = [&](int kind, int ix, int s, int& iy, int& d, int& dc, int& alo, int& ahi) {
-    const int* cols = kind == 0 ? C.rcols : C.kcols;
-    iy = cols[ix];
-    if (iy < 0) return false;
-    d = B.db[ix]; dc = B.db[iy];
-    const int nu = B.nup[ix];
-    alo = s == 0 ? 0 : nu; ahi = s == 0 ? nu : d;
-    return alo < ahi;
-  };
-  if (warp < DTC_PROD / 32) {
-    // ---------------- producers and folders ----------------
-    int cc = 0, u = 0, staged_iy = -1, staged_kind = -1;
-    for (int kind = 0; kind < 2; ++kind) {
-      const long long bsp = kind == 0 ? C.rho_sp : C.kap_sp, bspl = kind == 0 ? C.rho_spl : C.kap_spl;
-      const float* base = kind == 0 ? C.rho : C.kap;
-      const long long* offs = kind == 0 ? C.roffs : C.koffs;
-      const int nq = kind == 0 ? 4 : 1;
-      for (int ix = g; ix < B.nb; ix += G) {
-        for (int s = 0; s < 2; ++s) {
-          int iy, d, dc, alo, ahi;
-          if (!unit_info(kind, ix, s, iy, d, dc, alo, ahi)) continue;
-          const float* mat = base + (long long)p * bsp + offs[ix];
-          const int sa = B.st[ix];
-          const int npad = (2 * dc + 15) / 16 * 16;
-          const int nk = (ahi - alo + DTC_K - 1) / DTC_K;
-          for (int kc = 0; kc < nk; ++kc, ++cc) {
-            const int st = cc & 1;
-            if (cc >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((cc >> 1) - 1) & 1)) abort_flag = 1;
-            float* sAh = stage_base + st * stage_floats;
-            float* sAl = sAh + 128 * DTC_K;
-            float* sBh = sAl + 128 * DTC_K;
-            float* sBl = sBh + DTC_MAXN * DTC_K;
-            const int a0 = alo + kc * DTC_K;
-            if (!abort_flag) {
-              // A[m = q*32 + l][k] = phi_q(a0 + k, r0 + l)
-              for (int e = tid; e < 128 * (DTC_K / 4); e += DTC_PROD) {
-                const int m = e & 127, k4 = e >> 7;
-                const int q = m >> 5, r = r0 + (m & 31);
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (q < nq && r < nghl) {
-                  const float* src = B.phi + q * ps + (long long)(sa + a0 + 4 * k4) * nghl + r;
-                  const int a = a0 + 4 * k4;
-                  if (a < ahi) v.x = src[0];
-                  if (a + 1 < ahi) v.y = src[nghl];
-                  if (a + 2 < ahi) v.z = src[2 * nghl];
-                  if (a + 3 < ahi) v.w = src[3 * nghl];
-                }
-                const int o = tc::cm_off(m, 4 * k4, 128);
-                st_split4(sAh + o, sAl + o, v);
-              }
-              // B[n = pl*dc + b][k] = rho(a0 + k, b; pl)
-              for (int e = tid; e < npad * (DTC_K / 4); e += DTC_PROD) {
-                const int n = e % npad, k4 = e / npad;
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (n < 2 * dc) {
-                  const int pl = n >= dc ? 1 : 0, b = n - pl * dc;
-                  const float* src = mat + (long long)pl * bspl + (long long)b * d + a0 + 4 * k4;
-                  const int a = a0 + 4 * k4;
-                  if (a < ahi) v.x = src[0];
-                  if (a + 1 < ahi) v.y = src[1];
-                  if (a + 2 < ahi) v.z = src[2];
-                  if (a + 3 < ahi) v.w = src[3];
-                }
-                const int o = tc::cm_off(n, 4 * k4, npad);
-                st_split4(sBh + o, sBl + o, v);
-              }
-            }
-            tc::fence_async_smem();
-            tc::mbar_arrive(&full_bar[st]);
+  if (warp < DTC2_FOLD / 32) {
+    // ---------------- fold warps ----------------
+    const int q = warp & 3, half = warp >> 2;
+    int u = 0, skind = -1, siy = -1, sb0 = -1;
+    for (int i = 0; i < nunit; ++i) {
+      const DUnitTC U = units[i];
+      if (U.ix % G != g) continue;
+      const int j = u & 1;
+      if (U.kind != skind || U.iy != siy || U.b0 != sb0) {
+        // column basis functions of the unit's columns, once per column range
+        asm volatile("bar.sync 1, %0;" ::"r"(DTC2_FOLD) : "memory");   // previous fold done with sPb
+        const int sb = B.st[U.iy] + U.b0;
+        for (int e = tid; e < U.nc * 32; e += DTC2_FOLD) {
+          const int b = e >> 5, l = e & 31, r = r0 + l;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (r < nghl) {
+            const float* src = B.phi + (long long)(sb + b) * nghl + r;
+            v.x = src[0];
+            if (U.kind == 0) { v.y = src[ps]; v.z = src[2 * ps]; v.w = src[3 * ps]; }
           }
-          // ---- fold this unit: the column basis functions of block iy (staged once per block)
-          if (iy != staged_iy || kind != staged_kind) {
-            asm volatile("bar.sync 1, %0;" ::"r"(DTC_PROD) : "memory");   // previous fold done with sPb
-            const int sb = B.st[iy];
-            for (int e = tid; e < dc * 32; e += DTC_PROD) {
-              const int b = e >> 5, l = e & 31, r = r0 + l;
-              float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (r < nghl) {
-                const float* src = B.phi + (long long)(sb + b) * nghl + r;
-                v.x = src[0];
-                if (kind == 0) { v.y = src[ps]; v.z = src[2 * ps]; v.w = src[3 * ps]; }
-              }
-              *reinterpret_cast<float4*>(&sPb[(b * 32 + l) * 4]) = v;
-            }
-            asm volatile("bar.sync 1, %0;" ::"r"(DTC_PROD) : "memory");
-            staged_iy = iy; staged_kind = kind;
-          }
-          if (!abort_flag && !tc::mbar_wait(&accf_bar, u & 1)) abort_flag = 1;
-          tc::fence_after();
-          {
-            const int q = warp & 3, half = warp >> 2;
-            const int nb8 = (dc + 7) / 8;
-            const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
-            const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-            // columns b < nup(iy) are spin up: "same spin" as rows of spin s == 0
-            const int nub = B.nup[iy];
-            const bool skip = abort_flag || r0 + lane >= nghl;
-            if (kind == 0) {
-              switch (q) {
-                case 0: fold_unit<0, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
-                case 1: fold_unit<1, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
-                case 2: fold_unit<2, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
-                default: fold_unit<3, 0>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip); break;
-              }
-            } else {
-              // pairing densities: component 0 only; the other warps still take part in the loads
-              fold_unit<0, 1>(acc, lane_base, sPb, lane, dc, nub, s, c8lo, c8hi, skip || q != 0);
-            }
-          }
-          tc::fence_before();
-          tc::mbar_arrive(&acce_bar);   // accumulator free for the next unit
-          ++u;
+          *reinterpret_cast<float4*>(&sPb[(b * 32 + l) * 4]) = v;
         }
+        asm volatile("bar.sync 1, %0;" ::"r"(DTC2_FOLD) : "memory");
+        skind = U.kind; siy = U.iy; sb0 = U.b0;
       }
+      if (!abort_flag && !tc::mbar_wait(&accf_bar[j], (u >> 1) & 1)) abort_flag = 1;
+      tc::fence_after();
+      const int nb8 = (U.nc + 7) / 8;
+      const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
+      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(128 * j);
+      const bool skip = abort_flag || r0 + lane >= nghl;
+      if (U.kind == 0) {
+        switch (q) {
+          case 0: fold_unit2<0, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
+          case 1: fold_unit2<1, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
+          case 2: fold_unit2<2, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
+          default: fold_unit2<3, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
+        }
+      } else {
+        // pairing densities: component 0 only; the other warps still take part in the loads
+        fold_unit2<0, 1>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip || q != 0);
+      }
+      tc::fence_before();
+      tc::mbar_arrive(&acce_bar[j]);   // accumulator j free for the unit after next
+      ++u;
     }
-  } else if (tid == DTC_PROD) {
+  } else if (tid == DTC2_FOLD) {
     // ---------------- MMA issuer ----------------
     int cc = 0, u = 0;
-    for (int kind = 0; kind < 2; ++kind) {
-      for (int ix = g; ix < B.nb; ix += G) {
-        for (int s = 0; s < 2; ++s) {
-          int iy, d, dc, alo, ahi;
-          if (!unit_info(kind, ix, s, iy, d, dc, alo, ahi)) continue;
-          // the fold of the previous unit has read the accumulator
-          if (u >= 1 && !abort_flag && !tc::mbar_wait(&acce_bar, (u - 1) & 1)) abort_flag = 1;
-          tc::fence_after();
-          const int npad = (2 * dc + 15) / 16 * 16;
-          const uint32_t idesc = tc::idesc_tf32(128, npad);
-          const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(npad / 8) * 128;
-          const int nk = (ahi - alo + DTC_K - 1) / DTC_K;
-          for (int kc = 0; kc < nk; ++kc, ++cc) {
-            const int st = cc & 1;
-            if (!abort_flag && !tc::mbar_wait(&full_bar[st], (cc >> 1) & 1)) abort_flag = 1;
-            tc::fence_after();
-            if (!abort_flag) {
-              const float* sAh = stage_base + st * stage_floats;
-              const float* sAl = sAh + 128 * DTC_K;
-              const float* sBh = sAl + 128 * DTC_K;
-              const float* sBl = sBh + DTC_MAXN * DTC_K;
-              const uint64_t ah = tc::sdesc(tc::smem_u32(sAh), lboA, 128);
-              const uint64_t al = tc::sdesc(tc::smem_u32(sAl), lboA, 128);
-              const uint64_t bh = tc::sdesc(tc::smem_u32(sBh), lboB, 128);
-              const uint64_t bl = tc::sdesc(tc::smem_u32(sBl), lboB, 128);
-              tc::mma_tf32(tmem, ah, bh, idesc, kc > 0);
-              tc::mma_tf32(tmem, ah, bl, idesc, true);
-              tc::mma_tf32(tmem, al, bh, idesc, true);
-            }
-            tc::mma_commit(&empty_bar[st]);
-          }
-          tc::mma_commit(&accf_bar);   // W of this unit complete
-          ++u;
+    for (int i = 0; i < nunit; ++i) {
+      const DUnitTC U = units[i];
+      if (U.ix % G != g) continue;
+      const int j = u & 1;
+      if (u >= 2 && !abort_flag && !tc::mbar_wait(&acce_bar[j], ((u >> 1) - 1) & 1)) abort_flag = 1;
+      tc::fence_after();
+      const uint32_t idesc = tc::idesc_tf32(128, U.npad);
+      const uint32_t lboA = (128 / 8) * 128, lboB = (uint32_t)(U.npad / 8) * 128;
+      const uint32_t acc_t = tmem + (uint32_t)(128 * j);
+      for (int kc = 0; kc < U.nk; ++kc, ++cc) {
+        const int st = cc % DTC2_NS;
+        if (!abort_flag && !tc::mbar_wait(&full_bar[st], (cc / DTC2_NS) & 1)) abort_flag = 1;
+        tc::fence_after();
+        if (!abort_flag) {
+          const float* sAh = stages + st * DTC2_STAGE;
+          const float* sAl = sAh + 128 * 8;
+          const float* sBh = sAh + DTC2_ACH;
+          const float* sBl = sBh + U.npad * 8;
+          const uint64_t ah = tc::sdesc(tc::smem_u32(sAh), lboA, 128);
+          const uint64_t al = tc::sdesc(tc::smem_u32(sAl), lboA, 128);
+          const uint64_t bh = tc::sdesc(tc::smem_u32(sBh), lboB, 128);
+          const uint64_t bl = tc::sdesc(tc::smem_u32(sBl), lboB, 128);
+          tc::mma_tf32(acc_t, ah, bh, idesc, kc > 0);
+          tc::mma_tf32(acc_t, ah, bl, idesc, true);
+          tc::mma_tf32(acc_t, al, bh, idesc, true);
         }
+        tc::mma_commit(&empty_bar[st]);
       }
+      tc::mma_commit(&accf_bar[j]);   // W of this unit complete
+      ++u;
     }
     // nothing may be in flight when the tensor memory is released
-    if (u > 0 && !tc::mbar_wait(&accf_bar, (u - 1) & 1)) abort_flag = 1;
+    if (u > 0 && !tc::mbar_wait(&accf_bar[(u - 1) & 1], ((u - 1) >> 1) & 1)) abort_flag = 1;
+  } else if (tid == DTC2_FOLD + 32) {
+    // ---------------- bulk-copy producer ----------------
+    const float* asrc = aphi + (long long)rt * nachunk * DTC2_ACH;
+    const float* bsrc = bsplit + (long long)p * bstride;
+    int cc = 0;   // chunks issued, in order
+    for (int i = 0; i < nunit && !abort_flag; ++i) {
+      const DUnitTC U = units[i];
+      if (U.ix % G != g) continue;
+      const uint32_t bbytes = (uint32_t)U.npad * 64;
+      for (int kc = 0; kc < U.nk; ++kc) {
+        const int st = cc % DTC2_NS;
+        if (cc >= DTC2_NS && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((cc / DTC2_NS) - 1) & 1)) abort_flag = 1;
+        if (abort_flag) break;
+        float* sA = stages + st * DTC2_STAGE;
+        tc::mbar_expect_tx(&full_bar[st], (uint32_t)(DTC2_ACH * 4) + bbytes);
+        tc::bulk_g2s(sA, asrc + (long long)(U.achunk + kc) * DTC2_ACH, DTC2_ACH * 4, &full_bar[st]);
+        tc::bulk_g2s(sA + DTC2_ACH, bsrc + U.boff + (long long)kc * 16 * U.npad, bbytes, &full_bar[st]);
+        ++cc;
+      }
+    }
+    // no copy of this CTA may still be landing when the memory is reused: the last
+    // DTC2_NS chunks issued are the only ones that can be in flight
+    for (int k = cc > DTC2_NS ? cc - DTC2_NS : 0; k < cc; ++k)
+      if (!tc::mbar_wait(&full_bar[k % DTC2_NS], (k / DTC2_NS) & 1)) abort_flag = 1;
   }
   // all folds done; sum the 8 warps
   tc::fence_before();
   const bool ok = __syncthreads_and(!abort_flag);
-  float* red = stage_base;   // [8][2*ND][32], the stages are no longer in use
+  float* red = stages;   // [8][2*ND][32]; the stages are no longer in use
   if (warp < 8) {
 #pragma unroll
     for (int k = 0; k < 2 * ND; ++k) red[(warp * 2 * ND + k) * 32 + lane] = acc[k];

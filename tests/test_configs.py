@@ -110,12 +110,14 @@ def config2():
     return hfb, omegas
 
 
-@pytest.mark.parametrize("k", [0, 1])
-def test_config2_synthetic_field_split_precision_vs_fp64(config2, k):
+@pytest.mark.parametrize("k,tc_density", [(0, False), (1, False), (1, True)])
+def test_config2_synthetic_field_split_precision_vs_fp64(config2, k, tc_density, monkeypatch):
     """The split-precision (3xTF32 tensor-core) field evaluation against FP64 on the
-    synthetic state, whose blocks (up to 91) take the multi-tile tensor-core paths."""
+    synthetic state, whose blocks (up to 91) take the multi-tile tensor-core paths
+    (with tensor-core densities: two column ranges per block)."""
     from pynfam_gb300.blockmatrix import BlockMatrix
     from pynfam_gb300.solver import GPUSolver
+    monkeypatch.setenv("PNFAM_GB300_TC_DENSITY", "1" if tc_density else "0")
     hfb, _ = config2
     c = _case(hfb, k, 50, self_consistent=False)
     gpu = GPUSolver(c.hfb, c.couplings)
@@ -139,7 +141,8 @@ def test_config2_synthetic_field_split_precision_vs_fp64(config2, k):
     got = gpu.calc_hamiltonian(*ins, mixed=True)
     gpu.close()
     worst = max(float(np.max(np.abs(g - w)) / np.max(np.abs(w))) for g, w in zip(got, want))
-    print(f"config 2 GT K={k}: split-precision field worst relative error {worst:.2e}")
+    print(f"config 2 GT K={k} (tensor-core densities {tc_density}): split-precision field worst "
+          f"relative error {worst:.2e}")
     assert worst <= 1e-5
 
 

@@ -302,7 +302,10 @@ def _mixed_vs_fp64(c, seed):
 
 
 @pytest.mark.parametrize("case,op", [("S40", "RS1-K1"), ("S40", "GT-K0"), ("Kr116", "P-K0")])
-def test_mixed_field_matches_fp64(case, op):
+def test_mixed_field_matches_fp64(case, op, monkeypatch):
+    """The mixed field evaluation with the SIMT FP32 density kernel
+    (PNFAM_GB300_TC_DENSITY=0 when the context is created) against the FP64 field."""
+    monkeypatch.setenv("PNFAM_GB300_TC_DENSITY", "0")
     c, _ = case_for(case, op, 0)
     worst = _mixed_vs_fp64(c, 3)
     print(f"{case} {op}: mixed field worst relative error {worst:.2e}")
@@ -315,12 +318,35 @@ def test_large_basis_mixed_field_matches_fp64(large_case):
     assert worst <= 1e-5
 
 
-def test_tensor_core_density_matches_fp64(monkeypatch):
-    """The tensor-core density kernel (selected by PNFAM_GB300_TC_DENSITY=1 when the
-    context is created) in the mixed field evaluation, against the FP64 field."""
+def test_tensor_core_density_matches_fp64(monkeypatch, large_case):
+    """The tensor-core density kernel (the default; PNFAM_GB300_TC_DENSITY=0 when the
+    context is created selects the SIMT kernel) in the mixed field evaluation, against
+    the FP64 field."""
     monkeypatch.setenv("PNFAM_GB300_TC_DENSITY", "1")
-    for case, op in (("S40", "RS1-K1"), ("Kr116", "P-K0")):
-        c, _ = case_for(case, op, 0)
+    cases = [(f"{case} {op}", case_for(case, op, 0)[0]) for case, op in (("S40", "RS1-K1"), ("Kr116", "P-K0"))]
+    for name, c in cases + [("N_sh=12 162Gd GT-K1", large_case)]:
         worst = _mixed_vs_fp64(c, 5)
-        print(f"{case} {op}: mixed field (tensor-core densities) worst relative error {worst:.2e}")
+        print(f"{name}: mixed field (tensor-core densities) worst relative error {worst:.2e}")
         assert worst <= 1e-5
+
+
+@pytest.mark.parametrize("case,op", [("S40", "P-K0"), ("Gd162", "GT-K1")])
+def test_tensor_core_density_mixed_solve(monkeypatch, case, op):
+    """The mixed form with tensor-core densities reaches the FP64 fixed point (1e-6)."""
+    from pynfam_gb300.solver import GPUSolver
+    monkeypatch.setenv("PNFAM_GB300_TC_DENSITY", "1")
+    pts = golden(case)["operators"][op]
+    c, _ = case_for(case, op, 0)
+    omegas = [complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"]) for p in pts]
+    kw = dict(broyden_m=c.nml["solver"]["broyden_history_size"], quench=c.quench)
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    exact = gpu.solve(omegas, max_iter=1500, eps=TIGHT, **kw)
+    r = gpu.solve(omegas, max_iter=1500, eps=MIXED_EPS, precision=1, **kw)
+    gpu.close()
+    assert np.all(exact.iters >= 0) and np.all(r.iters >= 0), r.si
+    w = exact.re_S[:, 0] + 1j * exact.im_S[:, 0]
+    g = r.re_S[:, 0] + 1j * r.im_S[:, 0]
+    worst = float(np.max(np.abs(g - w) / np.abs(w)))
+    print(f"{case} {op} mixed form, tensor-core densities: worst rel err vs FP64 fixed point {worst:.2e}")
+    assert worst <= REL
