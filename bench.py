@@ -10,8 +10,8 @@ Workload (one "step" = one serving run to completion):
   requests      R requests per operator (default 2), each the P points of pynfam's
                 CIRCLE contour (centre 10 MeV, radius 25 MeV, Gauss-Legendre
                 angles, 2P points, first P used), all arriving at the start of
-                the step; each engine has P slots, so the second request's points
-                enter as the first request's points retire
+                the step; each engine has P slots (--slots), so the second
+                request's points enter as the first request's points retire
   solver        max_iter 300, Broyden history 50, SkO' residual interaction
   form          the mixed form (FP32 increment evaluations with 3xTF32 tensor-core
                 GEMMs, FP64 anchors, FP64 Broyden) converged to 1e-9, served by
@@ -210,9 +210,10 @@ def fixed_point(cases, omegas, P):
 class Stream:
     """One serving run of the workload's requests on resident contexts."""
 
-    def __init__(self, cases, omegas, precision, eps, nreq):
+    def __init__(self, cases, omegas, precision, eps, nreq, slots=None):
         from pynfam_gb300.solver import GPUSolver
         self.cases, self.omegas, self.precision, self.eps, self.nreq = cases, omegas, precision, eps, nreq
+        self.slots = slots or len(omegas)
         self.solvers = {}
         for op, c in zip(OPERATORS, cases):
             g = GPUSolver(c.hfb, c.couplings)
@@ -227,7 +228,7 @@ class Stream:
             return self.solvers[key].engine(slots, timed=timed, **kws[key])
         reqs = [Request(i * self.nreq + r, op, self.omegas, 0.0) for i, op in enumerate(OPERATORS)
                 for r in range(self.nreq)]
-        server = Server(factory, lambda key, n: 1, slots=len(self.omegas), budget_bytes=len(OPERATORS))
+        server = Server(factory, lambda key, n: 1, slots=self.slots, budget_bytes=len(OPERATORS))
         out, st = server.run(reqs)
         profs = {op: g.last_profile() for op, g in self.solvers.items()}
         return out, st, profs
@@ -304,7 +305,8 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     # ---- the mixed serving form: warm-up, then K timed serving runs ----
-    mixed = Stream(cases, omegas, 1, MIXED_EPS, R)
+    slots = args.slots or P
+    mixed = Stream(cases, omegas, 1, MIXED_EPS, R, slots)
     for _ in range(args.warmup):
         mixed.run()
     clocks = Clocks(local)
@@ -334,7 +336,7 @@ def run_gpu(args):
     out_t, st_t, profs_t = mixed.run(timed=True)
     mixed.close()
     # ---- the plain FP64 form (the drop-in) on the same stream ----
-    fp64 = Stream(cases, omegas, 0, SOLVER["convergence_epsilon"], R)
+    fp64 = Stream(cases, omegas, 0, SOLVER["convergence_epsilon"], R, slots)
     fp64.run()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -349,7 +351,7 @@ def run_gpu(args):
     for _ in range(2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s2 = Stream(cases, omegas, 1, MIXED_EPS, R)
+        s2 = Stream(cases, omegas, 1, MIXED_EPS, R, slots)
         out2, st2, _ = s2.run()
         s2.close()
         e2e_wall.append(time.perf_counter() - t0)
@@ -388,7 +390,7 @@ def run_gpu(args):
                                    f"GT- K=0 and K=1, {R} requests of {P} CIRCLE-contour points each per "
                                    f"operator per step, served",
                        "points_per_step": npts, "nghl": int(hf.nghl), "nxy": [int(c.F.mat.nelem) for c in cases],
-                       "form": f"mixed, epsilon {MIXED_EPS}", "engines": len(OPERATORS), "slots_per_engine": P,
+                       "form": f"mixed, epsilon {MIXED_EPS}", "engines": len(OPERATORS), "slots_per_engine": slots,
                        "l2": "256 MB buffer written between timed steps",
                        "parallelism": f"replicas{world}"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)) * 1e3, "p99": float(np.percentile(lat, 99)) * 1e3,
@@ -525,6 +527,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--points", type=int, default=32, help="omega points per request")
     ap.add_argument("--requests", type=int, default=2, help="requests per operator per step")
+    ap.add_argument("--slots", type=int, default=0, help="slots per engine (default: points per request)")
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--precision", type=int, default=0, choices=(0, 1),
                     help="solve-only: 0 FP64 throughout; 1 mixed form")

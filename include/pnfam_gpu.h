@@ -69,7 +69,8 @@ typedef struct {
                                  error is far below epsilon and convergence (si < epsilon) is
                                  accepted on an increment evaluation; farther out a point
                                  takes an FP64 anchor evaluation when si < 10^-reserved[1]
-                                 (default 100*epsilon) or si stops falling, and convergence
+                                 (default 100*epsilon) or si stops falling at the FP32 noise
+                                 floor (si <= 1e-3 max|X - X_a|), and convergence
                                  is accepted only on that anchor.  Every evaluation counts
                                  against max_iter.  Broyden, Green's function and strength
                                  are FP64 in both modes. */

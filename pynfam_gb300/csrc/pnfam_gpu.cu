@@ -929,6 +929,10 @@ struct pnfam_engine {
   bool no_res = false, mixed = false, timed = false;
   double switch_si = 0.0;
   static constexpr double NEAR = 1000.0;
+  // a stall of the increment iteration counts as the FP32 noise floor (and takes an
+  // anchor) only while si <= FLOOR * max|d|: far above that, FP32 rounding of the
+  // increment cannot be what holds the residual up, and an anchor would not help
+  static constexpr double FLOOR = 1e-3;
   // per slot (host)
   std::vector<int> active, it, anchor, since_best, nstall, fresh;
   std::vector<long long> tag;
@@ -981,8 +985,8 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   // evaluation.  A point is "near" its anchor while max|d| <= NEAR*epsilon, where
   // the FP32 error is far below epsilon.  Convergence (si < epsilon) is accepted on
   // an anchor or on a near increment evaluation; a far point takes an FP64 anchor
-  // when si < 10^-reserved[1] (default 100*epsilon) or si stops falling (the FP32
-  // noise floor).  Every evaluation counts against max_iter.
+  // when si < 10^-reserved[1] (default 100*epsilon) or si stops falling at the FP32
+  // noise floor (si <= FLOOR*max|d|).  Every evaluation counts against max_iter.
   e->switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
   e->timed = o->reserved[0] != 0;
   const int nops = e->nops;
@@ -1226,7 +1230,8 @@ static int engine_finish(pnfam_engine* e) {
       if (si < o.convergence_epsilon && near) { engine_retire(e, p, it); continue; }
       if (si < e->best[p] * 0.5) { e->best[p] = si; e->since_best[p] = 0; } else { ++e->since_best[p]; }
       // the stagnation window doubles with every anchor it has triggered
-      const bool stalled = e->since_best[p] >= (5 << std::min(e->nstall[p], 4));
+      const bool stalled = e->since_best[p] >= (5 << std::min(e->nstall[p], 4)) &&
+                           si <= pnfam_engine::FLOOR * dm;
       if (!near && (si < e->switch_si || stalled)) { e->anchor[p] = 1; e->nstall[p] += stalled; }
     }
     if (it == o.max_iter) engine_retire(e, p, -1);

@@ -1815,7 +1815,7 @@ struct BroState {
   double* vin;      // [P][N]
   double* vout;     // [P][N]
   double* df;       // [P][M][N]
-  double* dv;       // [P][M][N]
+  double* dv;       // [P][M][N]: u = dv + alpha*df for finished columns, raw vin in column inext
   double* part;     // [P][nchunk][NPART] block partials
   int nchunk;
   const int* itp;   // [P] Broyden iteration of each point
@@ -1888,7 +1888,7 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
   }
 }
 
-// normalise column ipos by 1/|df_ipos| and form the dots
+// normalise column ipos by 1/|df_ipos| (and finish its u column) and form the dots
 // dd[k] = df_k . df_ipos and wk[k] = df_k . vout for k < iter_used.
 // A CTA covers BRO_CHUNK elements: the normalised df_ipos and vout of its chunk
 // are staged in shared memory, then each warp takes whole columns (k = warp,
@@ -1917,7 +1917,9 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
       if (upd) {
         f = dfp[(long long)ipos * S.N + e] * sc;
         dfp[(long long)ipos * S.N + e] = f;
-        dvp[(long long)ipos * S.N + e] *= sc;
+        // the finished dv column is kept as u = dv + alpha*df, the only combination
+        // of the two that the update reads
+        dvp[(long long)ipos * S.N + e] = fma(S.alpha, f, dvp[(long long)ipos * S.N + e] * sc);
       }
       v = vo[e];
     }
@@ -1965,10 +1967,11 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
 }
 
 // one CTA (256 threads) per point: reduce partials; stage 0: si and 1/|df_ipos|;
-// stage 1: maintain beta (M x M) and solve beta*gamma = work by Gaussian
-// elimination with partial pivoting (LAPACK dgesv's pivot choice: the first row
-// of largest magnitude), pivot search and row swap by one warp, row updates by
-// all warps
+// stage 1: maintain beta (M x M) and solve beta*gamma = work.  beta is the Gram
+// matrix of the unit vectors df_k plus w0^2 on the diagonal, symmetric positive
+// definite (the reference factorises it with DSYTRF/DSYTRI, pnfam_broyden.f90:190-206):
+// here L D L^T without pivoting, one barrier per column, then two triangular solves
+// by one warp
 __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double w0, double* __restrict__ si,
                                                    double* __restrict__ norm, double* __restrict__ beta,
                                                    double* __restrict__ gamma, const int* __restrict__ active) {
@@ -2000,7 +2003,7 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   bro_slots(it, S.M, n, ipos, inext);
   __shared__ double A[64][65];
   __shared__ double x[64];
-  __shared__ double f[64];
+  __shared__ double dinv[2];   // 1/D of the current and the next column
   const int M = S.M;
   double* bp = beta + (long long)p * M * M;
   for (int k = w; k < n; k += 8) {   // one warp per k: sum the chunk partials
@@ -2019,50 +2022,39 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   for (int k = tid; k < n; k += blockDim.x) bp[k * M + k] = w0 * w0 + 1.0;
   __syncthreads();
   for (int e = tid; e < n * n; e += blockDim.x) A[e / n][e % n] = bp[(e / n) * M + (e % n)];
+  if (tid == 0 && n > 0) dinv[0] = 1.0 / A[0][0];
   __syncthreads();
+  // L D L^T in place: D on the diagonal, L[r][c] (r > c) in the upper triangle A[c][r]
   for (int c = 0; c < n; ++c) {
-    if (w == 0) {
-      double best = -1.0;
-      int br = n;
-      for (int r = c + l; r < n; r += 32) {
-        const double v = fabs(A[r][c]);
-        if (v > best) { best = v; br = r; }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int orow = __shfl_xor_sync(0xffffffffu, br, o);
-        if (ob > best || (ob == best && orow < br)) { best = ob; br = orow; }
-      }
-      if (br >= n) br = c;  // no comparable entry (NaN column): keep the diagonal, as a serial scan does
-      if (br != c) {
-        for (int j = l; j < n; j += 32) { const double t = A[c][j]; A[c][j] = A[br][j]; A[br][j] = t; }
-        if (l == 0) { const double t = x[c]; x[c] = x[br]; x[br] = t; }
-      }
-      __syncwarp();
-      for (int r = c + 1 + l; r < n; r += 32) f[r] = A[r][c] / A[c][c];
-    }
-    __syncthreads();
+    const double di = dinv[c & 1];
     for (int r = c + 1 + w; r < n; r += 8) {
-      const double fr = f[r];
-      for (int j = c + 1 + l; j < n; j += 32) A[r][j] -= fr * A[c][j];
+      const double lr = A[r][c] * di;
+      for (int j = c + 1 + l; j <= r; j += 32) A[r][j] -= lr * A[j][c];
+      if (l == 0) A[c][r] = lr;
+      // the next pivot is final as soon as its own update is done (warp 0, lane 0)
+      if (r == c + 1 && l == 0) dinv[(c + 1) & 1] = 1.0 / A[r][r];
     }
-    for (int r = c + 1 + tid; r < n; r += blockDim.x) x[r] -= f[r] * x[c];
     __syncthreads();
   }
-  // back substitution, one warp
+  // L y = work, y /= D, L^T gamma = y (columns in turn, one warp)
   if (tid < 32) {
-    for (int r = n - 1; r >= 0; --r) {
-      double s = 0.0;
-      for (int j = r + 1 + tid; j < n; j += 32) s += A[r][j] * x[j];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (tid == 0) x[r] = (x[r] - s) / A[r][r];
+    for (int c = 0; c < n; ++c) {
+      const double yc = x[c];
+      for (int r = c + 1 + tid; r < n; r += 32) x[r] -= A[c][r] * yc;
+      __syncwarp();
+    }
+    for (int r = tid; r < n; r += 32) x[r] /= A[r][r];
+    __syncwarp();
+    for (int c = n - 1; c >= 0; --c) {
+      const double gc = x[c];
+      for (int r = tid; r < c; r += 32) x[r] -= A[r][c] * gc;
       __syncwarp();
     }
     for (int k = tid; k < n; k += 32) gamma[(long long)p * 64 + k] = x[k];
   }
 }
 
-// BRO_BROYDEN: curv = alpha*vout - sum_i gamma_i (dv_i + alpha df_i);
+// BRO_BROYDEN: curv = alpha*vout - sum_i gamma_i u_i  (u_i = dv_i + alpha df_i);
 //              df[inext] = vout; dv[inext] = vin; vin += curv
 // BRO_LINEAR:  vin += alpha*vout;  BRO_NOMIX: vin += vout
 __global__ void __launch_bounds__(256) k_bro_update(BroState S, const double* __restrict__ gamma,
@@ -2083,10 +2075,8 @@ __global__ void __launch_bounds__(256) k_bro_update(BroState S, const double* __
     if (mode == BRO_NOMIX) { vi[e] += v; continue; }
     if (mode == BRO_LINEAR) { vi[e] += S.alpha * v; continue; }
     double c = S.alpha * v;
-    const double* dfp = S.df + (long long)p * S.M * S.N;
-    const double* dvp = S.dv + (long long)p * S.M * S.N;
-    for (int k = 0; k < iu; ++k)
-      c -= g[k] * (dvp[(long long)k * S.N + e] + S.alpha * dfp[(long long)k * S.N + e]);
+    const double* up = S.dv + (long long)p * S.M * S.N;
+    for (int k = 0; k < iu; ++k) c -= g[k] * up[(long long)k * S.N + e];
     const double old = vi[e];
     S.df[((long long)p * S.M + inext) * S.N + e] = v;
     S.dv[((long long)p * S.M + inext) * S.N + e] = old;
