@@ -930,9 +930,9 @@ struct DensTCArgs {
 // evaluation.  In the kernel one thread copies A and B chunks into a ring of
 // DTC2_NS shared-memory stages (cp.async.bulk, completion on an mbarrier), one
 // thread issues the 3xTF32 MMAs into one of two 128-column TMEM accumulators,
-// and eight warps fold the finished accumulator into the 28 local densities
-// (warp w: component q = w % 4, half of the columns; fold_same / fold_opp) while
-// the other one fills.  dpart: [P][2][G][2*ND][nghl]
+// and eight warps fold the finished accumulator (warp w: component q = w % 4, half
+// of the columns; sums per row spin and column spin, turned into the 28 local
+// densities at the end) while the other one fills.  dpart: [P][2][G][2*ND][nghl]
 // ---------------------------------------------------------------------------
 enum { DTC2_NS = 4, DTC2_FOLD = 256, DTC2_THREADS = DTC2_FOLD + 64, DTC2_MAXNC = 64 };
 enum { DTC2_ACH = 2 * 128 * 8,                   // floats of one A chunk (hi, lo)
@@ -1012,11 +1012,16 @@ __global__ void __launch_bounds__(256) k_dens_bsplit(DevBasisT<float> B, DensTCA
   }
 }
 
-// fold the W_q rows of one unit from TMEM (this warp's component Q, columns
-// [c8lo, c8hi) in groups of 8; re at column b, im at nc + b)
-template <int Q, int KIND>
-__device__ __forceinline__ void fold_unit2(float (&acc)[2 * ND], uint32_t lane_base, const float* sPb, int lane,
-                                           int nc, int b0, int nub, int s, int c8lo, int c8hi, bool skip) {
+// Every term of the density formulas is a fixed combination of the sums
+//   T[s][up][q'] = sum over the columns b of spin up (1) or down (0) and the rows a
+//                  of spin s of W_q(r, b) * phi_q'(b, r)   (re and im of W)
+// so a fold warp accumulates only these sums per column (8 FMAs) and turns them
+// into the 28 densities once, at the end (dtc2_densities).
+// sum_unit: the columns [8*c8lo, 8*c8hi) of one unit (re of W at TMEM column b, im at
+// nc + b); columns b < nupl are spin up.  KIND 1 (pairing): q' = 0 only.
+template <int KIND, int NQ>
+__device__ __forceinline__ void sum_unit(float (&T)[2][NQ][2], uint32_t lane_base, const float* sPb, int lane,
+                                         int nc, int nupl, int c8lo, int c8hi, bool skip) {
   for (int c8 = c8lo; c8 < c8hi; ++c8) {
     float wre[8], wim[8];
     tc::tmem_ld8x2(lane_base + (uint32_t)(8 * c8), lane_base + (uint32_t)(nc + 8 * c8), wre, wim);
@@ -1025,16 +1030,49 @@ __device__ __forceinline__ void fold_unit2(float (&acc)[2 * ND], uint32_t lane_b
     for (int i = 0; i < 8; ++i) {
       const int b = 8 * c8 + i;
       if (b >= nc) break;
-      const bool up = b0 + b < nub;
-      const float sg = up ? 1.f : -1.f, sig = up ? -1.f : 1.f;
-      const bool same = up == (s == 0);
       const float4 pv = *reinterpret_cast<const float4*>(&sPb[(b * 32 + lane) * 4]);
       const float P[4] = {pv.x, pv.y, pv.z, pv.w};
-      if (KIND == 0) {
-        if (same) fold_same<Q>(acc, wre[i], wim[i], P, sg);
-        else fold_opp<Q>(acc, wre[i], wim[i], P, sig);
+      if (b < nupl) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          T[1][q][0] = fmaf(wre[i], P[q], T[1][q][0]);
+          T[1][q][1] = fmaf(wim[i], P[q], T[1][q][1]);
+        }
       } else {
-        const float xr = 2.f * wre[i] * P[0], xi = 2.f * wim[i] * P[0];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          T[0][q][0] = fmaf(wre[i], P[q], T[0][q][0]);
+          T[0][q][1] = fmaf(wim[i], P[q], T[0][q][1]);
+        }
+      }
+    }
+  }
+}
+
+// the 28 densities of a fold warp of component Q from its sums: T0 (normal
+// densities) and T1 (pairing densities, component 0) per row spin s and column spin
+// up.  fold_same / fold_opp are linear in (wr, wi) * P, so a sum is folded as
+// (wr, wi, P) = (1, 0, Re sums) plus (0, 1, Im sums).
+template <int Q>
+__device__ __forceinline__ void dtc2_densities(float (&acc)[2 * ND], const float (&T0)[2][2][4][2],
+                                               const float (&T1)[2][2][1][2]) {
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int up = 0; up < 2; ++up) {
+      const bool same = (up == 1) == (s == 0);
+      const float sg = up ? 1.f : -1.f, sig = -sg;
+      const float Pre[4] = {T0[s][up][0][0], T0[s][up][1][0], T0[s][up][2][0], T0[s][up][3][0]};
+      const float Pim[4] = {T0[s][up][0][1], T0[s][up][1][1], T0[s][up][2][1], T0[s][up][3][1]};
+      if (same) {
+        fold_same<Q>(acc, 1.f, 0.f, Pre, sg);
+        fold_same<Q>(acc, 0.f, 1.f, Pim, sg);
+      } else {
+        fold_opp<Q>(acc, 1.f, 0.f, Pre, sig);
+        fold_opp<Q>(acc, 0.f, 1.f, Pim, sig);
+      }
+      if (Q == 0) {
+        const float xr = 2.f * T1[s][up][0][0], xi = 2.f * T1[s][up][0][1];
         if (same) {
           acc[2 * D_SBR] += sig * xr; acc[2 * D_SBR + 1] += sig * xi;
           acc[2 * D_SBP] += xi; acc[2 * D_SBP + 1] += -xr;
@@ -1044,7 +1082,6 @@ __device__ __forceinline__ void fold_unit2(float (&acc)[2 * ND], uint32_t lane_b
         }
       }
     }
-  }
 }
 
 // grid (ceil(nghl/32), G, 2*nact); DTC2_THREADS threads; dynamic smem density_tc2_smem_bytes().
@@ -1076,12 +1113,20 @@ __global__ void __launch_bounds__(DTC2_THREADS, 2) k_density_tc2(
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = tslot;
-  float acc[2 * ND];
+  const int q = warp & 3, half = warp >> 2;
+  float T0[2][2][4][2], T1[2][2][1][2];   // fold warps: [row spin s][column spin up][q'][re, im]
 #pragma unroll
-  for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) T0[a][b][k][c] = 0.f;
+        T1[a][b][0][c] = 0.f;
+      }
   if (warp < DTC2_FOLD / 32) {
     // ---------------- fold warps ----------------
-    const int q = warp & 3, half = warp >> 2;
     int u = 0, skind = -1, siy = -1, sb0 = -1;
     for (int i = 0; i < nunit; ++i) {
       const DUnitTC U = units[i];
@@ -1106,20 +1151,20 @@ __global__ void __launch_bounds__(DTC2_THREADS, 2) k_density_tc2(
       }
       if (!abort_flag && !tc::mbar_wait(&accf_bar[j], (u >> 1) & 1)) abort_flag = 1;
       tc::fence_after();
-      const int nb8 = (U.nc + 7) / 8;
-      const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
-      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(128 * j);
-      const bool skip = abort_flag || r0 + lane >= nghl;
-      if (U.kind == 0) {
-        switch (q) {
-          case 0: fold_unit2<0, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
-          case 1: fold_unit2<1, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
-          case 2: fold_unit2<2, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
-          default: fold_unit2<3, 0>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip); break;
+      // pairing units: only the warps of component 0 read their rows
+      if (U.kind == 0 || q == 0) {
+        const int nb8 = (U.nc + 7) / 8;
+        const int c8lo = half == 0 ? 0 : (nb8 + 1) / 2, c8hi = half == 0 ? (nb8 + 1) / 2 : nb8;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(128 * j);
+        const bool skip = abort_flag || r0 + lane >= nghl;
+        const int nupl = U.nub - U.b0;
+        if (U.kind == 0) {
+          if (U.s == 0) sum_unit<0, 4>(T0[0], lane_base, sPb, lane, U.nc, nupl, c8lo, c8hi, skip);
+          else sum_unit<0, 4>(T0[1], lane_base, sPb, lane, U.nc, nupl, c8lo, c8hi, skip);
+        } else {
+          if (U.s == 0) sum_unit<1, 1>(T1[0], lane_base, sPb, lane, U.nc, nupl, c8lo, c8hi, skip);
+          else sum_unit<1, 1>(T1[1], lane_base, sPb, lane, U.nc, nupl, c8lo, c8hi, skip);
         }
-      } else {
-        // pairing densities: component 0 only; the other warps still take part in the loads
-        fold_unit2<0, 1>(acc, lane_base, sPb, lane, U.nc, U.b0, U.nub, U.s, c8lo, c8hi, skip || q != 0);
       }
       tc::fence_before();
       tc::mbar_arrive(&acce_bar[j]);   // accumulator j free for the unit after next
@@ -1186,11 +1231,20 @@ __global__ void __launch_bounds__(DTC2_THREADS, 2) k_density_tc2(
     for (int k = cc > DTC2_NS ? cc - DTC2_NS : 0; k < cc; ++k)
       if (!tc::mbar_wait(&full_bar[k % DTC2_NS], (k / DTC2_NS) & 1)) abort_flag = 1;
   }
-  // all folds done; sum the 8 warps
+  // all folds done: each fold warp's densities from its sums, then the sum of the 8 warps
   tc::fence_before();
   const bool ok = __syncthreads_and(!abort_flag);
   float* red = stages;   // [8][2*ND][32]; the stages are no longer in use
   if (warp < 8) {
+    float acc[2 * ND];
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
+    switch (q) {
+      case 0: dtc2_densities<0>(acc, T0, T1); break;
+      case 1: dtc2_densities<1>(acc, T0, T1); break;
+      case 2: dtc2_densities<2>(acc, T0, T1); break;
+      default: dtc2_densities<3>(acc, T0, T1); break;
+    }
 #pragma unroll
     for (int k = 0; k < 2 * ND; ++k) red[(warp * 2 * ND + k) * 32 + lane] = acc[k];
   }
