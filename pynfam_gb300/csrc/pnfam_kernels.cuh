@@ -1277,220 +1277,224 @@ __host__ __device__ __forceinline__ int mfslot(int iy, int iz, int sa, int sb) {
   return ((iy * 5 + iz) * 2 + (sa < 0 ? 1 : 0)) * 2 + (sb < 0 ? 1 : 0);
 }
 
-struct cplx { double r, i; };
-__device__ __forceinline__ cplx cmk(double r, double i) { cplx c; c.r = r; c.i = i; return c; }
-__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return cmk(a.r + b.r, a.i + b.i); }
-__device__ __forceinline__ cplx csc(double s, cplx a) { return cmk(s * a.r, s * a.i); }
+// complex arithmetic of the mean field in the evaluation's precision S (FP64 for the
+// FP64 form and the anchors, FP32 for the increment evaluations of the mixed form)
+template <class S> struct cplxT { S r, i; };
+template <class S> __device__ __forceinline__ cplxT<S> cmk(S r, S i) { cplxT<S> c; c.r = r; c.i = i; return c; }
+template <class S> __device__ __forceinline__ cplxT<S> cadd(cplxT<S> a, cplxT<S> b) { return cmk<S>(a.r + b.r, a.i + b.i); }
+template <class S> __device__ __forceinline__ cplxT<S> csc(S s, cplxT<S> a) { return cmk<S>(s * a.r, s * a.i); }
 
 template <class T>
 __global__ void __launch_bounds__(128) k_meanfield(DevBasisT<T> B, int G, const T* __restrict__ dpart,
                                                    T* __restrict__ mfout, const int* __restrict__ active) {
+  using S = T;
+  using C = cplxT<S>;
   const int p = blockIdx.y >> 1, call = blockIdx.y & 1;
   if (!active[p]) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int nghl = B.nghl;
   if (r >= nghl) return;
-  cplx d[ND];
+  C d[ND];
   const T* dp = dpart + ((long long)p * 2 + call) * G * (2 * ND) * nghl;
-  const double wd = B.wdcori[r];
+  const S wd = B.wdcori[r];
   for (int k = 0; k < ND; ++k) {
-    double sr = 0.0, si = 0.0;
+    S sr = S(0.0), si = S(0.0);
     for (int g = 0; g < G; ++g) {
-      sr += (double)dp[((long long)g * 2 * ND + 2 * k) * nghl + r];
-      si += (double)dp[((long long)g * 2 * ND + 2 * k + 1) * nghl + r];
+      sr += (S)dp[((long long)g * 2 * ND + 2 * k) * nghl + r];
+      si += (S)dp[((long long)g * 2 * ND + 2 * k + 1) * nghl + r];
     }
-    d[k] = cmk(sr * wd, si * wd);
+    d[k] = cmk<S>(sr * wd, si * wd);
   }
-  const double crho = B.crho[r], cs = B.cs[r], cpair = B.cpair[r], cspair = B.cspair[r];
-  const double cdrho = B.sc[0], ctau = B.sc[1], ctj0 = B.sc[2], ctj1 = B.sc[3], ctj2 = B.sc[4], crdj = B.sc[5];
-  const double cds = B.sc[6], ct = B.sc[7], cj = B.sc[8], cgs = B.sc[9], cf = B.sc[10], csdj = B.sc[11];
-  cplx mf[NMF];
-  for (int k = 0; k < NMF; ++k) mf[k] = cmk(0.0, 0.0);
+  const S crho = B.crho[r], cs = B.cs[r], cpair = B.cpair[r], cspair = B.cspair[r];
+  const S cdrho = B.sc[0], ctau = B.sc[1], ctj0 = B.sc[2], ctj1 = B.sc[3], ctj2 = B.sc[4], crdj = B.sc[5];
+  const S cds = B.sc[6], ct = B.sc[7], cj = B.sc[8], cgs = B.sc[9], cf = B.sc[10], csdj = B.sc[11];
+  C mf[NMF];
+  for (int k = 0; k < NMF; ++k) mf[k] = cmk<S>(S(0.0), S(0.0));
 #define M_(iy, iz, sa, sb) mf[mfslot(iy, iz, sa, sb)]
-#define ADD(iy, iz, sa, sb, sym, v) M_(iy, iz, sa, sb) = cadd(M_(iy, iz, sa, sb), csc(sym, v))
-  const cplx rho = d[D_RHO], tau = d[D_TAU], tjrr = d[D_TJRR], tjpr = d[D_TJPR], tjzr = d[D_TJZR];
-  const cplx tjrp = d[D_TJRP], tjpp = d[D_TJPP], tjzp = d[D_TJZP], tjrz = d[D_TJRZ], tjpz = d[D_TJPZ];
-  const cplx tjzz = d[D_TJZZ], sr = d[D_SR], sp = d[D_SP], sz = d[D_SZ], tr = d[D_TR], tp = d[D_TP];
-  const cplx tz = d[D_TZ], jr = d[D_JR], jp = d[D_JP], jz = d[D_JZ], fr = d[D_FR], fp = d[D_FP];
-  const cplx fz = d[D_FZ], gs = d[D_GS];
-  const cplx t0 = csc(ctj0, cadd(cadd(tjrr, tjpp), tjzz));
-  const cplx t1a = csc(ctj1, cadd(tjzr, csc(-1.0, tjrz)));
-  const cplx t1b = csc(ctj1, cadd(tjpz, csc(-1.0, tjzp)));
-  const cplx t2a = csc(ctj2, cadd(tjrz, tjzr));
-  const cplx t2b = csc(ctj2, cadd(tjpz, tjzp));
-  cplx aux;
+#define ADD(iy, iz, sa, sb, sym, v) M_(iy, iz, sa, sb) = cadd<S>(M_(iy, iz, sa, sb), csc<S>(sym, v))
+  const C rho = d[D_RHO], tau = d[D_TAU], tjrr = d[D_TJRR], tjpr = d[D_TJPR], tjzr = d[D_TJZR];
+  const C tjrp = d[D_TJRP], tjpp = d[D_TJPP], tjzp = d[D_TJZP], tjrz = d[D_TJRZ], tjpz = d[D_TJPZ];
+  const C tjzz = d[D_TJZZ], sr = d[D_SR], sp = d[D_SP], sz = d[D_SZ], tr = d[D_TR], tp = d[D_TP];
+  const C tz = d[D_TZ], jr = d[D_JR], jp = d[D_JP], jz = d[D_JZ], fr = d[D_FR], fp = d[D_FP];
+  const C fz = d[D_FZ], gs = d[D_GS];
+  const C t0 = csc<S>(ctj0, cadd<S>(cadd<S>(tjrr, tjpp), tjzz));
+  const C t1a = csc<S>(ctj1, cadd<S>(tjzr, csc<S>(-S(1.0), tjrz)));
+  const C t1b = csc<S>(ctj1, cadd<S>(tjpz, csc<S>(-S(1.0), tjzp)));
+  const C t2a = csc<S>(ctj2, cadd<S>(tjrz, tjzr));
+  const C t2b = csc<S>(ctj2, cadd<S>(tjpz, tjzp));
+  C aux;
   // diagonal in spin (pnfam_hamiltonian_blas.f90:783-905)
-  M_(0, 0, 1, 1) = cadd(csc(2.0 * crho, rho), csc(ctau, tau));
+  M_(0, 0, 1, 1) = cadd<S>(csc<S>(S(2.0) * crho, rho), csc<S>(ctau, tau));
   M_(0, 0, -1, -1) = M_(0, 0, 1, 1);
-  aux = cadd(cadd(csc(2.0 * cs, sz), csc(ct, tz)), csc(cf, fz));
-  ADD(0, 0, 1, 1, 1.0, aux); ADD(0, 0, -1, -1, -1.0, aux);
+  aux = cadd<S>(cadd<S>(csc<S>(S(2.0) * cs, sz), csc<S>(ct, tz)), csc<S>(cf, fz));
+  ADD(0, 0, 1, 1, S(1.0), aux); ADD(0, 0, -1, -1, -S(1.0), aux);
 
-  M_(0, 1, 1, 1) = csc(-crdj, cadd(tjpz, csc(-1.0, tjzp)));
+  M_(0, 1, 1, 1) = csc<S>(-crdj, cadd<S>(tjpz, csc<S>(-S(1.0), tjzp)));
   M_(0, 1, -1, -1) = M_(0, 1, 1, 1);
-  aux = csc(-csdj, jp);
-  ADD(0, 1, 1, 1, 1.0, aux); ADD(0, 1, -1, -1, -1.0, aux);
+  aux = csc<S>(-csdj, jp);
+  ADD(0, 1, 1, 1, S(1.0), aux); ADD(0, 1, -1, -1, -S(1.0), aux);
   M_(1, 0, 1, 1) = M_(0, 1, 1, 1);
   M_(1, 0, -1, -1) = M_(0, 1, -1, -1);
-  aux = cmk(-t1a.i + 0.5 * t2a.i, t1a.r - 0.5 * t2a.r);
-  ADD(0, 1, 1, 1, 1.0, aux); ADD(0, 1, -1, -1, -1.0, aux);
-  ADD(1, 0, 1, 1, -1.0, aux); ADD(1, 0, -1, -1, 1.0, aux);
-  aux = cmk(cj * jr.i, -cj * jr.r);
-  ADD(0, 1, 1, 1, 1.0, aux); ADD(0, 1, -1, -1, 1.0, aux);
-  ADD(1, 0, 1, 1, -1.0, aux); ADD(1, 0, -1, -1, -1.0, aux);
+  aux = cmk<S>(-t1a.i + S(0.5) * t2a.i, t1a.r - S(0.5) * t2a.r);
+  ADD(0, 1, 1, 1, S(1.0), aux); ADD(0, 1, -1, -1, -S(1.0), aux);
+  ADD(1, 0, 1, 1, -S(1.0), aux); ADD(1, 0, -1, -1, S(1.0), aux);
+  aux = cmk<S>(cj * jr.i, -cj * jr.r);
+  ADD(0, 1, 1, 1, S(1.0), aux); ADD(0, 1, -1, -1, S(1.0), aux);
+  ADD(1, 0, 1, 1, -S(1.0), aux); ADD(1, 0, -1, -1, -S(1.0), aux);
 
-  M_(0, 2, 1, 1) = csc(cj, jp);
+  M_(0, 2, 1, 1) = csc<S>(cj, jp);
   M_(0, 2, -1, -1) = M_(0, 2, 1, 1);
-  aux = cadd(t1b, csc(0.5, t2b));
-  ADD(0, 2, 1, 1, 1.0, aux); ADD(0, 2, -1, -1, -1.0, aux);
+  aux = cadd<S>(t1b, csc<S>(S(0.5), t2b));
+  ADD(0, 2, 1, 1, S(1.0), aux); ADD(0, 2, -1, -1, -S(1.0), aux);
   M_(2, 0, 1, 1) = M_(0, 2, 1, 1);
   M_(2, 0, -1, -1) = M_(0, 2, -1, -1);
-  aux = cmk(-csdj * jr.i, csdj * jr.r);
-  ADD(0, 2, 1, 1, 1.0, aux); ADD(0, 2, -1, -1, -1.0, aux);
-  ADD(2, 0, 1, 1, -1.0, aux); ADD(2, 0, -1, -1, 1.0, aux);
-  aux = cmk(crdj * (tjzr.i - tjrz.i), -crdj * (tjzr.r - tjrz.r));
-  ADD(0, 2, 1, 1, 1.0, aux); ADD(0, 2, -1, -1, 1.0, aux);
-  ADD(2, 0, 1, 1, -1.0, aux); ADD(2, 0, -1, -1, -1.0, aux);
+  aux = cmk<S>(-csdj * jr.i, csdj * jr.r);
+  ADD(0, 2, 1, 1, S(1.0), aux); ADD(0, 2, -1, -1, -S(1.0), aux);
+  ADD(2, 0, 1, 1, -S(1.0), aux); ADD(2, 0, -1, -1, S(1.0), aux);
+  aux = cmk<S>(crdj * (tjzr.i - tjrz.i), -crdj * (tjzr.r - tjrz.r));
+  ADD(0, 2, 1, 1, S(1.0), aux); ADD(0, 2, -1, -1, S(1.0), aux);
+  ADD(2, 0, 1, 1, -S(1.0), aux); ADD(2, 0, -1, -1, -S(1.0), aux);
 
-  M_(0, 3, 1, 1) = csc(-crdj, cadd(tjrp, csc(-1.0, tjpr)));
+  M_(0, 3, 1, 1) = csc<S>(-crdj, cadd<S>(tjrp, csc<S>(-S(1.0), tjpr)));
   M_(0, 3, -1, -1) = M_(0, 3, 1, 1);
-  aux = csc(2.0 * cgs, gs);
-  ADD(0, 3, 1, 1, 1.0, aux); ADD(0, 3, -1, -1, -1.0, aux);
+  aux = csc<S>(S(2.0) * cgs, gs);
+  ADD(0, 3, 1, 1, S(1.0), aux); ADD(0, 3, -1, -1, -S(1.0), aux);
   M_(3, 0, 1, 1) = M_(0, 3, 1, 1);
   M_(3, 0, -1, -1) = M_(0, 3, -1, -1);
-  aux = cmk(t0.i - ctj2 * (tjrr.i + tjpp.i - 2.0 * tjzz.i) / 3.0,
-            -t0.r + ctj2 * (tjrr.r + tjpp.r - 2.0 * tjzz.r) / 3.0);
-  ADD(0, 3, 1, 1, 1.0, aux); ADD(0, 3, -1, -1, -1.0, aux);
-  ADD(3, 0, 1, 1, -1.0, aux); ADD(3, 0, -1, -1, 1.0, aux);
-  aux = cmk(cj * jz.i, -cj * jz.r);
-  ADD(0, 3, 1, 1, 1.0, aux); ADD(0, 3, -1, -1, 1.0, aux);
-  ADD(3, 0, 1, 1, -1.0, aux); ADD(3, 0, -1, -1, -1.0, aux);
+  aux = cmk<S>(t0.i - ctj2 * (tjrr.i + tjpp.i - S(2.0) * tjzz.i) / S(3.0),
+            -t0.r + ctj2 * (tjrr.r + tjpp.r - S(2.0) * tjzz.r) / S(3.0));
+  ADD(0, 3, 1, 1, S(1.0), aux); ADD(0, 3, -1, -1, -S(1.0), aux);
+  ADD(3, 0, 1, 1, -S(1.0), aux); ADD(3, 0, -1, -1, S(1.0), aux);
+  aux = cmk<S>(cj * jz.i, -cj * jz.r);
+  ADD(0, 3, 1, 1, S(1.0), aux); ADD(0, 3, -1, -1, S(1.0), aux);
+  ADD(3, 0, 1, 1, -S(1.0), aux); ADD(3, 0, -1, -1, -S(1.0), aux);
 
-  M_(0, 4, 1, 1) = csc(2.0 * cdrho, rho);
+  M_(0, 4, 1, 1) = csc<S>(S(2.0) * cdrho, rho);
   M_(0, 4, -1, -1) = M_(0, 4, 1, 1);
-  aux = csc(2.0 * cds, sz);
-  ADD(0, 4, 1, 1, 1.0, aux); ADD(0, 4, -1, -1, -1.0, aux);
+  aux = csc<S>(S(2.0) * cds, sz);
+  ADD(0, 4, 1, 1, S(1.0), aux); ADD(0, 4, -1, -1, -S(1.0), aux);
   M_(4, 0, 1, 1) = M_(0, 4, 1, 1);
   M_(4, 0, -1, -1) = M_(0, 4, -1, -1);
 
-  M_(1, 2, 1, 1) = csc(csdj, sz);
+  M_(1, 2, 1, 1) = csc<S>(csdj, sz);
   M_(1, 2, -1, -1) = M_(1, 2, 1, 1);
-  aux = csc(crdj, rho);
-  ADD(1, 2, 1, 1, 1.0, aux); ADD(1, 2, -1, -1, -1.0, aux);
+  aux = csc<S>(crdj, rho);
+  ADD(1, 2, 1, 1, S(1.0), aux); ADD(1, 2, -1, -1, -S(1.0), aux);
   M_(2, 1, 1, 1) = M_(1, 2, 1, 1);
   M_(2, 1, -1, -1) = M_(1, 2, -1, -1);
 
-  M_(1, 3, 1, 1) = csc(0.5 * cf, sr);
-  M_(1, 3, -1, -1) = csc(-1.0, M_(1, 3, 1, 1));
+  M_(1, 3, 1, 1) = csc<S>(S(0.5) * cf, sr);
+  M_(1, 3, -1, -1) = csc<S>(-S(1.0), M_(1, 3, 1, 1));
   M_(3, 1, 1, 1) = M_(1, 3, 1, 1);
   M_(3, 1, -1, -1) = M_(1, 3, -1, -1);
-  aux = cmk(-csdj * sp.i, csdj * sp.r);
-  ADD(1, 3, 1, 1, 1.0, aux); ADD(1, 3, -1, -1, 1.0, aux);
-  ADD(3, 1, 1, 1, -1.0, aux); ADD(3, 1, -1, -1, -1.0, aux);
+  aux = cmk<S>(-csdj * sp.i, csdj * sp.r);
+  ADD(1, 3, 1, 1, S(1.0), aux); ADD(1, 3, -1, -1, S(1.0), aux);
+  ADD(3, 1, 1, 1, -S(1.0), aux); ADD(3, 1, -1, -1, -S(1.0), aux);
 
-  M_(2, 3, 1, 1) = csc(-csdj, sr);
+  M_(2, 3, 1, 1) = csc<S>(-csdj, sr);
   M_(2, 3, -1, -1) = M_(2, 3, 1, 1);
-  aux = cmk(0.5 * cf * sp.i, -0.5 * cf * sp.r);
-  ADD(2, 3, 1, 1, 1.0, aux); ADD(2, 3, -1, -1, -1.0, aux);
+  aux = cmk<S>(S(0.5) * cf * sp.i, -S(0.5) * cf * sp.r);
+  ADD(2, 3, 1, 1, S(1.0), aux); ADD(2, 3, -1, -1, -S(1.0), aux);
   M_(3, 2, 1, 1) = M_(2, 3, -1, -1);
   M_(3, 2, -1, -1) = M_(2, 3, 1, 1);
 
-  M_(1, 1, 1, 1) = csc(4.0 * cdrho + ctau, rho);
+  M_(1, 1, 1, 1) = csc<S>(S(4.0) * cdrho + ctau, rho);
   M_(1, 1, -1, -1) = M_(1, 1, 1, 1);
-  aux = csc(4.0 * cds + ct, sz);
-  ADD(1, 1, 1, 1, 1.0, aux); ADD(1, 1, -1, -1, -1.0, aux);
+  aux = csc<S>(S(4.0) * cds + ct, sz);
+  ADD(1, 1, 1, 1, S(1.0), aux); ADD(1, 1, -1, -1, -S(1.0), aux);
   M_(2, 2, 1, 1) = M_(1, 1, 1, 1);
   M_(2, 2, -1, -1) = M_(1, 1, -1, -1);
   M_(3, 3, 1, 1) = M_(1, 1, 1, 1);
   M_(3, 3, -1, -1) = M_(1, 1, -1, -1);
-  aux = csc(cf, sz);
-  ADD(3, 3, 1, 1, 1.0, aux); ADD(3, 3, -1, -1, -1.0, aux);
+  aux = csc<S>(cf, sz);
+  ADD(3, 3, 1, 1, S(1.0), aux); ADD(3, 3, -1, -1, -S(1.0), aux);
 
   // not diagonal in spin (pnfam_hamiltonian_blas.f90:908-1094)
-  M_(0, 0, 1, -1) = cadd(cadd(csc(2.0 * cs, sr), csc(ct, tr)), csc(cf, fr));
+  M_(0, 0, 1, -1) = cadd<S>(cadd<S>(csc<S>(S(2.0) * cs, sr), csc<S>(ct, tr)), csc<S>(cf, fr));
   M_(0, 0, -1, 1) = M_(0, 0, 1, -1);
-  aux = cmk(2.0 * cs * sp.i + ct * tp.i + cf * fp.i, -2.0 * cs * sp.r - ct * tp.r - cf * fp.r);
-  ADD(0, 0, 1, -1, 1.0, aux); ADD(0, 0, -1, 1, -1.0, aux);
+  aux = cmk<S>(S(2.0) * cs * sp.i + ct * tp.i + cf * fp.i, -S(2.0) * cs * sp.r - ct * tp.r - cf * fp.r);
+  ADD(0, 0, 1, -1, S(1.0), aux); ADD(0, 0, -1, 1, -S(1.0), aux);
 
-  M_(0, 1, 1, -1) = csc(2.0 * cgs, gs);
+  M_(0, 1, 1, -1) = csc<S>(S(2.0) * cgs, gs);
   M_(0, 1, -1, 1) = M_(0, 1, 1, -1);
-  aux = cmk(csdj * jz.i, -csdj * jz.r);
-  ADD(0, 1, 1, -1, 1.0, aux); ADD(0, 1, -1, 1, -1.0, aux);
+  aux = cmk<S>(csdj * jz.i, -csdj * jz.r);
+  ADD(0, 1, 1, -1, S(1.0), aux); ADD(0, 1, -1, 1, -S(1.0), aux);
   M_(1, 0, 1, -1) = M_(0, 1, 1, -1);
   M_(1, 0, -1, 1) = M_(0, 1, -1, 1);
   M_(0, 2, 1, -1) = M_(0, 1, 1, -1);
   M_(2, 0, -1, 1) = M_(1, 0, -1, 1);
-  M_(2, 0, 1, -1) = csc(-1.0, M_(0, 2, 1, -1));
-  M_(0, 2, -1, 1) = csc(-1.0, M_(2, 0, -1, 1));
-  aux = csc(-ctj1, cadd(tjrp, csc(-1.0, tjpr)));
-  ADD(0, 1, 1, -1, 1.0, aux); ADD(0, 1, -1, 1, -1.0, aux); ADD(1, 0, 1, -1, -1.0, aux); ADD(1, 0, -1, 1, 1.0, aux);
-  ADD(0, 2, 1, -1, 1.0, aux); ADD(0, 2, -1, 1, 1.0, aux); ADD(2, 0, 1, -1, 1.0, aux); ADD(2, 0, -1, 1, 1.0, aux);
-  aux = cmk(t0.i, -t0.r);
-  ADD(0, 1, 1, -1, 1.0, aux); ADD(0, 1, -1, 1, 1.0, aux); ADD(1, 0, 1, -1, -1.0, aux); ADD(1, 0, -1, 1, -1.0, aux);
-  ADD(0, 2, 1, -1, 1.0, aux); ADD(0, 2, -1, 1, -1.0, aux); ADD(2, 0, 1, -1, 1.0, aux); ADD(2, 0, -1, 1, -1.0, aux);
-  aux = csc(-0.5 * ctj2, cadd(tjrp, tjpr));
-  ADD(0, 1, 1, -1, 1.0, aux); ADD(0, 1, -1, 1, -1.0, aux); ADD(1, 0, 1, -1, -1.0, aux); ADD(1, 0, -1, 1, 1.0, aux);
-  ADD(0, 2, 1, -1, -1.0, aux); ADD(0, 2, -1, 1, -1.0, aux); ADD(2, 0, 1, -1, -1.0, aux); ADD(2, 0, -1, 1, -1.0, aux);
-  aux = cmk(-ctj2 * (-2.0 * tjrr.i + tjpp.i + tjzz.i) / 3.0, ctj2 * (-2.0 * tjrr.r + tjpp.r + tjzz.r) / 3.0);
-  ADD(0, 1, 1, -1, 1.0, aux); ADD(0, 1, -1, 1, 1.0, aux); ADD(1, 0, 1, -1, -1.0, aux); ADD(1, 0, -1, 1, -1.0, aux);
-  aux = cmk(-ctj2 * (tjrr.i - 2.0 * tjpp.i + tjzz.i) / 3.0, ctj2 * (tjrr.r - 2.0 * tjpp.r + tjzz.r) / 3.0);
-  ADD(0, 2, 1, -1, 1.0, aux); ADD(0, 2, -1, 1, -1.0, aux); ADD(2, 0, 1, -1, 1.0, aux); ADD(2, 0, -1, 1, -1.0, aux);
+  M_(2, 0, 1, -1) = csc<S>(-S(1.0), M_(0, 2, 1, -1));
+  M_(0, 2, -1, 1) = csc<S>(-S(1.0), M_(2, 0, -1, 1));
+  aux = csc<S>(-ctj1, cadd<S>(tjrp, csc<S>(-S(1.0), tjpr)));
+  ADD(0, 1, 1, -1, S(1.0), aux); ADD(0, 1, -1, 1, -S(1.0), aux); ADD(1, 0, 1, -1, -S(1.0), aux); ADD(1, 0, -1, 1, S(1.0), aux);
+  ADD(0, 2, 1, -1, S(1.0), aux); ADD(0, 2, -1, 1, S(1.0), aux); ADD(2, 0, 1, -1, S(1.0), aux); ADD(2, 0, -1, 1, S(1.0), aux);
+  aux = cmk<S>(t0.i, -t0.r);
+  ADD(0, 1, 1, -1, S(1.0), aux); ADD(0, 1, -1, 1, S(1.0), aux); ADD(1, 0, 1, -1, -S(1.0), aux); ADD(1, 0, -1, 1, -S(1.0), aux);
+  ADD(0, 2, 1, -1, S(1.0), aux); ADD(0, 2, -1, 1, -S(1.0), aux); ADD(2, 0, 1, -1, S(1.0), aux); ADD(2, 0, -1, 1, -S(1.0), aux);
+  aux = csc<S>(-S(0.5) * ctj2, cadd<S>(tjrp, tjpr));
+  ADD(0, 1, 1, -1, S(1.0), aux); ADD(0, 1, -1, 1, -S(1.0), aux); ADD(1, 0, 1, -1, -S(1.0), aux); ADD(1, 0, -1, 1, S(1.0), aux);
+  ADD(0, 2, 1, -1, -S(1.0), aux); ADD(0, 2, -1, 1, -S(1.0), aux); ADD(2, 0, 1, -1, -S(1.0), aux); ADD(2, 0, -1, 1, -S(1.0), aux);
+  aux = cmk<S>(-ctj2 * (-S(2.0) * tjrr.i + tjpp.i + tjzz.i) / S(3.0), ctj2 * (-S(2.0) * tjrr.r + tjpp.r + tjzz.r) / S(3.0));
+  ADD(0, 1, 1, -1, S(1.0), aux); ADD(0, 1, -1, 1, S(1.0), aux); ADD(1, 0, 1, -1, -S(1.0), aux); ADD(1, 0, -1, 1, -S(1.0), aux);
+  aux = cmk<S>(-ctj2 * (tjrr.i - S(2.0) * tjpp.i + tjzz.i) / S(3.0), ctj2 * (tjrr.r - S(2.0) * tjpp.r + tjzz.r) / S(3.0));
+  ADD(0, 2, 1, -1, S(1.0), aux); ADD(0, 2, -1, 1, -S(1.0), aux); ADD(2, 0, 1, -1, S(1.0), aux); ADD(2, 0, -1, 1, -S(1.0), aux);
 
-  M_(0, 3, 1, -1) = csc(csdj, jp);
+  M_(0, 3, 1, -1) = csc<S>(csdj, jp);
   M_(0, 3, -1, 1) = M_(0, 3, 1, -1);
-  aux = cmk(-csdj * jr.i, csdj * jr.r);
-  ADD(0, 3, 1, -1, 1.0, aux); ADD(0, 3, -1, 1, -1.0, aux);
+  aux = cmk<S>(-csdj * jr.i, csdj * jr.r);
+  ADD(0, 3, 1, -1, S(1.0), aux); ADD(0, 3, -1, 1, -S(1.0), aux);
   M_(3, 0, 1, -1) = M_(0, 3, 1, -1);
   M_(3, 0, -1, 1) = M_(0, 3, -1, 1);
-  aux = cmk(t1a.i + 0.5 * t2a.i, -t1a.r - 0.5 * t2a.r);
-  ADD(0, 3, 1, -1, 1.0, aux); ADD(0, 3, -1, 1, 1.0, aux); ADD(3, 0, 1, -1, -1.0, aux); ADD(3, 0, -1, 1, -1.0, aux);
-  aux = cadd(t1b, csc(-0.5, t2b));
-  ADD(0, 3, 1, -1, 1.0, aux); ADD(0, 3, -1, 1, -1.0, aux); ADD(3, 0, 1, -1, -1.0, aux); ADD(3, 0, -1, 1, 1.0, aux);
+  aux = cmk<S>(t1a.i + S(0.5) * t2a.i, -t1a.r - S(0.5) * t2a.r);
+  ADD(0, 3, 1, -1, S(1.0), aux); ADD(0, 3, -1, 1, S(1.0), aux); ADD(3, 0, 1, -1, -S(1.0), aux); ADD(3, 0, -1, 1, -S(1.0), aux);
+  aux = cadd<S>(t1b, csc<S>(-S(0.5), t2b));
+  ADD(0, 3, 1, -1, S(1.0), aux); ADD(0, 3, -1, 1, -S(1.0), aux); ADD(3, 0, 1, -1, -S(1.0), aux); ADD(3, 0, -1, 1, S(1.0), aux);
 
-  M_(0, 4, 1, -1) = csc(2.0 * cds, sr);
+  M_(0, 4, 1, -1) = csc<S>(S(2.0) * cds, sr);
   M_(0, 4, -1, 1) = M_(0, 4, 1, -1);
-  aux = cmk(2.0 * cds * sp.i, -2.0 * cds * sp.r);
-  ADD(0, 4, 1, -1, 1.0, aux); ADD(0, 4, -1, 1, -1.0, aux);
+  aux = cmk<S>(S(2.0) * cds * sp.i, -S(2.0) * cds * sp.r);
+  ADD(0, 4, 1, -1, S(1.0), aux); ADD(0, 4, -1, 1, -S(1.0), aux);
   M_(4, 0, 1, -1) = M_(0, 4, 1, -1);
   M_(4, 0, -1, 1) = M_(0, 4, -1, 1);
 
-  M_(1, 2, 1, -1) = cmk(-0.5 * cf * sp.i, 0.5 * cf * sp.r);
+  M_(1, 2, 1, -1) = cmk<S>(-S(0.5) * cf * sp.i, S(0.5) * cf * sp.r);
   M_(1, 2, -1, 1) = M_(1, 2, 1, -1);
-  aux = csc(0.5 * cf, sr);
-  ADD(1, 2, 1, -1, 1.0, aux); ADD(1, 2, -1, 1, -1.0, aux);
-  M_(2, 1, 1, -1) = csc(-1.0, M_(1, 2, 1, -1));
-  M_(2, 1, -1, 1) = csc(-1.0, M_(1, 2, -1, 1));
+  aux = csc<S>(S(0.5) * cf, sr);
+  ADD(1, 2, 1, -1, S(1.0), aux); ADD(1, 2, -1, 1, -S(1.0), aux);
+  M_(2, 1, 1, -1) = csc<S>(-S(1.0), M_(1, 2, 1, -1));
+  M_(2, 1, -1, 1) = csc<S>(-S(1.0), M_(1, 2, -1, 1));
 
-  M_(1, 3, 1, -1) = csc(0.5 * cf, sz);
+  M_(1, 3, 1, -1) = csc<S>(S(0.5) * cf, sz);
   M_(1, 3, -1, 1) = M_(1, 3, 1, -1);
-  aux = csc(crdj, rho);
-  ADD(1, 3, 1, -1, 1.0, aux); ADD(1, 3, -1, 1, -1.0, aux);
+  aux = csc<S>(crdj, rho);
+  ADD(1, 3, 1, -1, S(1.0), aux); ADD(1, 3, -1, 1, -S(1.0), aux);
   M_(3, 1, 1, -1) = M_(1, 3, -1, 1);
   M_(3, 1, -1, 1) = M_(1, 3, 1, -1);
   M_(3, 2, 1, -1) = M_(3, 1, 1, -1);
   M_(2, 3, -1, 1) = M_(1, 3, -1, 1);
-  M_(2, 3, 1, -1) = csc(-1.0, M_(1, 3, 1, -1));
-  M_(3, 2, -1, 1) = csc(-1.0, M_(3, 1, -1, 1));
+  M_(2, 3, 1, -1) = csc<S>(-S(1.0), M_(1, 3, 1, -1));
+  M_(3, 2, -1, 1) = csc<S>(-S(1.0), M_(3, 1, -1, 1));
 
-  M_(3, 3, 1, -1) = csc(ct + 4.0 * cds, sr);
+  M_(3, 3, 1, -1) = csc<S>(ct + S(4.0) * cds, sr);
   M_(3, 3, -1, 1) = M_(3, 3, 1, -1);
-  aux = cmk((ct + 4.0 * cds) * sp.i, -(ct + 4.0 * cds) * sp.r);
-  ADD(3, 3, 1, -1, 1.0, aux); ADD(3, 3, -1, 1, -1.0, aux);
+  aux = cmk<S>((ct + S(4.0) * cds) * sp.i, -(ct + S(4.0) * cds) * sp.r);
+  ADD(3, 3, 1, -1, S(1.0), aux); ADD(3, 3, -1, 1, -S(1.0), aux);
   M_(1, 1, 1, -1) = M_(3, 3, 1, -1);
   M_(1, 1, -1, 1) = M_(3, 3, -1, 1);
-  aux = csc(cf, sr);
-  ADD(1, 1, 1, -1, 1.0, aux); ADD(1, 1, -1, 1, 1.0, aux);
+  aux = csc<S>(cf, sr);
+  ADD(1, 1, 1, -1, S(1.0), aux); ADD(1, 1, -1, 1, S(1.0), aux);
   M_(2, 2, 1, -1) = M_(3, 3, 1, -1);
   M_(2, 2, -1, 1) = M_(3, 3, -1, 1);
-  aux = cmk(cf * sp.i, -cf * sp.r);
-  ADD(2, 2, 1, -1, 1.0, aux); ADD(2, 2, -1, 1, -1.0, aux);
+  aux = cmk<S>(cf * sp.i, -cf * sp.r);
+  ADD(2, 2, 1, -1, S(1.0), aux); ADD(2, 2, -1, 1, -S(1.0), aux);
 #undef ADD
 #undef M_
   // pairing fields (pnfam_hamiltonian_blas.f90:1201-1208): index (sa, sb)
-  const cplx rb = d[D_RB], sbr = d[D_SBR], sbp = d[D_SBP], sbz = d[D_SBZ];
-  mf[100] = cmk(cspair * (sbr.r + sbp.i), cspair * (sbr.i - sbp.r));        // a+ b+
-  mf[101] = cmk(cpair * rb.r - cspair * sbz.r, cpair * rb.i - cspair * sbz.i); // a+ b-
-  mf[102] = cmk(-cpair * rb.r - cspair * sbz.r, -cpair * rb.i - cspair * sbz.i); // a- b+
-  mf[103] = cmk(cspair * (-sbr.r + sbp.i), cspair * (-sbr.i - sbp.r));      // a- b-
+  const C rb = d[D_RB], sbr = d[D_SBR], sbp = d[D_SBP], sbz = d[D_SBZ];
+  mf[100] = cmk<S>(cspair * (sbr.r + sbp.i), cspair * (sbr.i - sbp.r));        // a+ b+
+  mf[101] = cmk<S>(cpair * rb.r - cspair * sbz.r, cpair * rb.i - cspair * sbz.i); // a+ b-
+  mf[102] = cmk<S>(-cpair * rb.r - cspair * sbz.r, -cpair * rb.i - cspair * sbz.i); // a- b+
+  mf[103] = cmk<S>(cspair * (-sbr.r + sbp.i), cspair * (-sbr.i - sbp.r));      // a- b-
   T* out = mfout + ((long long)p * 2 + call) * NMF * 2 * nghl;
   for (int k = 0; k < NMF; ++k) {
     out[((long long)k * 2) * nghl + r] = (T)mf[k].r;
@@ -1647,6 +1651,9 @@ struct HTaskTC {
   long long ooff;
 };
 enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
+// B items (4 mesh points of one row) per producer thread, and how many of them are
+// loaded ahead of the field tensor (all of them for tiles of up to 64 rows)
+enum { HTC_BI = HTC_MAXN * (HTC_K / 4) / HTC_PROD, HTC_BE = 2 };
 
 // dynamic shared memory for tiles of at most npmax output rows: two stages of
 // A (128 x 32, hi and lo) and B (npmax x 32, hi and lo), then the field tensor
@@ -1700,8 +1707,31 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
   if (warp < HTC_PROD / 32) {
     // ---------------- producers ----------------
     // chunks in mesh-point-major order: the column basis functions phi_iz(b, r) of a
-    // thread's two A items stay in registers for the nc components of one r range
+    // thread's two A items stay in registers for the nc components of one r range.
+    // Everything that does not depend on the chunk is computed once: the hpsi row
+    // (point, column), spin and shared-memory offsets of the two A items, and the row,
+    // mesh offset and stage offset of the (at most HTC_BI) B items of this thread.
     float4 fz[2][5];
+    int a_m[2], a_row[2], a_ore[2], a_oim[2];   // a_row < 0: no hpsi row
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+      const int e = tid + it * HTC_PROD;
+      const int j = e % HTC_MAXB, r4 = e / HTC_MAXB;
+      const int pi = j < nj ? j / nbc : 0, b = j < nj ? j % nbc : 0;
+      const int sbi = sns[b] > 0 ? 0 : 1;
+      a_m[it] = (((pi * 2 + sbi) * 5) * 2) * HTC_K + 4 * r4;
+      a_row[it] = j < nj ? jb0 + b : -1;
+      a_ore[it] = tc::cm_off(j, 4 * r4, 128);
+      a_oim[it] = tc::cm_off(64 + j, 4 * r4, 128);
+    }
+    int b_row[HTC_BI], b_o[HTC_BI];   // b_row: basis row (-1: zero), b_o: stage offset (-1: none)
+#pragma unroll
+    for (int k = 0; k < HTC_BI; ++k) {
+      const int e = tid + k * HTC_PROD;
+      const int n = e % NP, r4 = e / NP;
+      b_row[k] = e < NP * 8 && n < Th.na ? ja0 + n : -1;
+      b_o[k] = e < NP * 8 ? tc::cm_off(n, 4 * r4, NP) : -1;
+    }
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
@@ -1710,6 +1740,14 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
       float* sBh = sAl + 128 * HTC_K;
       float* sBl = sBh + npmax * HTC_K;
       const int q = c % nc, r0 = (c / nc) * HTC_K;
+      // B: phi_q(a, r) of the output rows, loaded now so that these loads and the
+      // field-tensor loads below are in flight together
+      float4 bv[HTC_BE];
+#pragma unroll
+      for (int k = 0; k < HTC_BE; ++k) {
+        const int r = r0 + 4 * ((tid + k * HTC_PROD) / NP);
+        bv[k] = ld_row4(B.phi + q * ps + (long long)b_row[k] * nghl, r, nghl, b_row[k] >= 0);
+      }
       // the field tensor of this chunk (component q, mesh points r0..r0+31) of every
       // point of the group, shared by all rows; the barriers keep one chunk's copy
       // from being overwritten while another chunk's rows are generated
@@ -1730,18 +1768,15 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
         // A: hpsi rows, Re at j, Im at 64 + j, four mesh points per item
 #pragma unroll
         for (int it = 0; it < 2; ++it) {
-          const int e = tid + it * HTC_PROD;
-          const int j = e % HTC_MAXB, r4 = e / HTC_MAXB, r = r0 + 4 * r4;
+          const int r = r0 + 4 * ((tid + it * HTC_PROD) / HTC_MAXB);
           float4 hr = make_float4(0.f, 0.f, 0.f, 0.f), hi = hr;
-          if (j < nj) {
-            const int pi = j / nbc, b = j % nbc;
-            const int sbi = sns[b] > 0 ? 0 : 1;
+          if (a_row[it] >= 0) {
             if (q == 0) {
 #pragma unroll
               for (int iz = 0; iz < 5; ++iz)
-                if (iz < nc) fz[it][iz] = ld_row4(B.phi + iz * ps + (long long)(jb0 + b) * nghl, r, nghl, true);
+                if (iz < nc) fz[it][iz] = ld_row4(B.phi + iz * ps + (long long)a_row[it] * nghl, r, nghl, true);
             }
-            const float* m = &sMF[(((pi * 2 + sbi) * 5) * 2) * HTC_K + 4 * r4];
+            const float* m = &sMF[a_m[it]];
 #pragma unroll
             for (int iz = 0; iz < 5; ++iz)
               if (iz < nc) {
@@ -1749,17 +1784,19 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
                 fma4(hi, *reinterpret_cast<const float4*>(m + (iz * 2 + 1) * HTC_K), fz[it][iz]);
               }
           }
-          const int o_re = tc::cm_off(j, 4 * r4, 128), o_im = tc::cm_off(64 + j, 4 * r4, 128);
-          st_split4(sAh + o_re, sAl + o_re, hr);
-          st_split4(sAh + o_im, sAl + o_im, hi);
+          st_split4(sAh + a_ore[it], sAl + a_ore[it], hr);
+          st_split4(sAh + a_oim[it], sAl + a_oim[it], hi);
         }
-        // B: phi_q(a, r) of the output rows
-        for (int e = tid; e < NP * 8; e += HTC_PROD) {
-          const int n = e % NP, r4 = e / NP;
-          const float4 v = ld_row4(B.phi + q * ps + (long long)(ja0 + n) * nghl, r0 + 4 * r4, nghl, n < Th.na);
-          const int o = tc::cm_off(n, 4 * r4, NP);
-          st_split4(sBh + o, sBl + o, v);
-        }
+#pragma unroll
+        for (int k = 0; k < HTC_BE; ++k)
+          if (b_o[k] >= 0) st_split4(sBh + b_o[k], sBl + b_o[k], bv[k]);
+#pragma unroll
+        for (int k = HTC_BE; k < HTC_BI; ++k)   // tiles of more than 64 rows
+          if (b_o[k] >= 0) {
+            const int r = r0 + 4 * ((tid + k * HTC_PROD) / NP);
+            st_split4(sBh + b_o[k], sBl + b_o[k],
+                      ld_row4(B.phi + q * ps + (long long)b_row[k] * nghl, r, nghl, b_row[k] >= 0));
+          }
       }
       tc::fence_async_smem();
       tc::mbar_arrive(&full_bar[st]);
