@@ -174,6 +174,9 @@ struct pnfam_ctx {
   TaskListTC t1a, t1b, t2a, t2b;   // FP32 evaluation on the tensor cores
   std::vector<HTask> htasks;
   DBuf<HTask> d_htasks;
+  DBuf<float> d_gsplit;               // ground-state operands of the tensor-core GEMM tasks, pre-split
+  long long gsplit_floats = 0;
+  bool have_gsplit = false;
   std::vector<HTaskTC> htasks_tc;   // tensor-core field projection (FP32 data)
   int tc_npmax = 16;                  // largest N of those tiles
   DBuf<HTaskTC> d_htasks_tc;
@@ -245,6 +248,7 @@ struct pnfam_ctx {
     for (auto* b : dbs) b->release();
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
     d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
+    d_gsplit.release();
     k1a.d_tasks.release(); k1a.d_tile2task.release();
     k1b.d_tasks.release(); k1b.d_tile2task.release();
     k2a.d_tasks.release(); k2a.d_tile2task.release();
@@ -540,8 +544,8 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, con
 static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact, cudaStream_t st) {
   if (tl.tasks.empty() || nact <= 0) return PNFAM_OK;
   dim3 grid((unsigned)tl.tasks.size(), (unsigned)((2 * nact * tl.maxrows + 127) / 128));
-  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), st>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_actlist.p, nact,
-                                                                     c->d_err.p);
+  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), st>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_gsplit.p,
+                                                               c->d_actlist.p, nact, c->d_err.p);
   c->launches++;
   CK(cudaGetLastError());
   return PNFAM_OK;
@@ -718,6 +722,19 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   bd[B_HSP] = {c->d_hsp32.p, 8 * nxy, 4 * nxy};
   bd[B_HQP] = {c->d_hqp32.p, 4 * nxy, 2 * nxy};
   CK(upload(c->d_bufs32, bd, NBUF));
+  if (!c->have_gsplit) {
+    CK(dalloc(c->d_gsplit, (size_t)std::max(1LL, c->gsplit_floats)));
+    TaskListTC* lists[4] = {&c->t1a, &c->t1b, &c->t2a, &c->t2b};
+    for (TaskListTC* tl : lists) {
+      int mc = 0;
+      for (const GemmTaskTC& t : tl->tasks) mc = std::max(mc, t.nterm * ((t.K + GTC_K - 1) / GTC_K));
+      if (tl->tasks.empty() || mc == 0) continue;
+      k_gemm_bsplit<<<dim3((unsigned)tl->tasks.size(), (unsigned)mc), 256, 0, c->stream>>>(tl->d_tasks.p,
+                                                                                      c->d_bufs32.p, c->d_gsplit.p);
+      CK(cudaGetLastError());
+    }
+    c->have_gsplit = true;
+  }
   return PNFAM_OK;
 }
 
@@ -880,12 +897,18 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   {
     TaskList* src[4] = {&c->k1a, &c->k1b, &c->k2a, &c->k2b};
     TaskListTC* dst[4] = {&c->t1a, &c->t1b, &c->t2a, &c->t2b};
+    long long goff = 0;
     for (int k = 0; k < 4; ++k) {
       dst[k]->build(*src[k]);
-      for (const GemmTaskTC& t : dst[k]->tasks)
+      for (GemmTaskTC& t : dst[k]->tasks) {
         if (t.ncols > 256) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: block larger than 256");
+        t.bsoff = goff;   // the task's pre-split ground-state chunks
+        goff += (long long)t.nterm * ((t.K + GTC_K - 1) / GTC_K) * t.npad * 2 * GTC_K;
+      }
       CK(upload(dst[k]->d_tasks, dst[k]->tasks.data(), dst[k]->tasks.size()));
     }
+    c->gsplit_floats = goff;
+    c->have_gsplit = false;
   }
   CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
   CK(upload(c->d_htasks_tc, c->htasks_tc.data(), c->htasks_tc.size()));

@@ -129,6 +129,7 @@ struct GemmTaskTC {
   GemmTerm t[PNFAM_MAXTERM];
   long long coff;
   int cbuf, ldc;
+  long long bsoff;        // floats: the task's ground-state operand, split and laid out per chunk
 };
 enum { GTC_K = 16, GTC_PROD = 256, GTC_THREADS = GTC_PROD + 32 };
 
@@ -136,9 +137,52 @@ __host__ __device__ constexpr size_t gemm_tc_smem_bytes() {
   return (size_t)2 * (2 * 128 * GTC_K + 2 * 256 * GTC_K) * sizeof(float);
 }
 
+// the B tile of chunk c of a task: B[n][k] = op(S)[k0 + k][n] (case 0) or
+// op(S)[n][k0 + k] (case 1), n < ncols, zero elsewhere
+__device__ __forceinline__ float4 gemm_tc_b4(const GemmTaskTC& Tk, const BufDescT<float>* bufs, int c, int n, int k4) {
+  const int nkc = (Tk.K + GTC_K - 1) / GTC_K;
+  const GemmTerm& tm = Tk.t[c / nkc];
+  const int k0 = (c % nkc) * GTC_K;
+  const bool pa = Tk.rcase == 0;
+  const int sbuf = pa ? tm.bbuf : tm.abuf;
+  const long long soff = pa ? tm.boff : tm.aoff;
+  const int sld = pa ? tm.ldb : tm.lda, str_ = pa ? tm.tB : tm.tA;
+  float x[4] = {0.f, 0.f, 0.f, 0.f};
+  if (n < Tk.ncols) {
+    const float* S = bufs[sbuf].base + soff;
+    const bool kfast = pa ? str_ == 0 : str_ != 0;
+    const long long sn = kfast ? sld : 1, sk = kfast ? 1 : sld;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = k0 + 4 * k4 + u;
+      if (k < Tk.K) x[u] = S[(long long)n * sn + (long long)k * sk];
+    }
+  }
+  return make_float4(x[0], x[1], x[2], x[3]);
+}
+
+// the ground-state operand of every chunk of every task, split into TF32 hi and lo
+// in the canonical layout, once per operator: gsplit[bsoff + c*npad*2*GTC_K] = hi | lo
+// grid (ntasks, most chunks of a task), 256 threads
+__global__ void __launch_bounds__(256) k_gemm_bsplit(const GemmTaskTC* __restrict__ tasks,
+                                                     const BufDescT<float>* __restrict__ bufs,
+                                                     float* __restrict__ gsplit) {
+  const GemmTaskTC& Tk = tasks[blockIdx.x];
+  const int c = blockIdx.y;
+  if (c >= Tk.nterm * ((Tk.K + GTC_K - 1) / GTC_K)) return;
+  const int NP = Tk.npad;
+  float* dst = gsplit + Tk.bsoff + (long long)c * NP * 2 * GTC_K;
+  for (int e = threadIdx.x; e < NP * (GTC_K / 4); e += blockDim.x) {
+    const int n = e % NP, k4 = e / NP;
+    const int o = tc::cm_off(n, 4 * k4, NP);
+    st_split4(dst + o, dst + NP * GTC_K + o, gemm_tc_b4(Tk, bufs, c, n, k4));
+  }
+}
+
 // grid (ntasks, row tiles of 128); HTC_THREADS threads; dynamic smem gemm_tc_smem_bytes()
 __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __restrict__ tasks,
                                                             const BufDescT<float>* __restrict__ bufs,
+                                                            const float* __restrict__ gsplit,
                                                             const int* __restrict__ actlist, int nact,
                                                             int* __restrict__ err) {
   const GemmTaskTC& Tk = tasks[blockIdx.x];
@@ -168,21 +212,31 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
   const uint32_t tmem = tslot;
   if (warp < GTC_PROD / 32) {
     // ---------------- producers ----------------
+    int last_copy[2] = {-1, -1};   // thread 0: last chunk copied into each stage
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
       float* sAh = stage_base + st * stage_floats;
       float* sAl = sAh + 128 * GTC_K;
       float* sBh = sAl + 128 * GTC_K;
-      float* sBl = sBh + 256 * GTC_K;
+      bool issued = false;
+      if (tid == 0 && !abort_flag) {
+        // B: the ground-state operand of this chunk, pre-split (hi then lo, NP x GTC_K
+        // each); this thread's arrival on the stage comes with the copy
+        const uint32_t bbytes = (uint32_t)NP * GTC_K * 2 * 4;
+        tc::mbar_expect_tx(&full_bar[st], bbytes);
+        tc::bulk_g2s(sBh, gsplit + Tk.bsoff + (long long)c * NP * 2 * GTC_K, bbytes, &full_bar[st]);
+        issued = true;
+        last_copy[st] = c;
+      }
       const GemmTerm& tm = Tk.t[c / nkc];
       const int k0 = (c % nkc) * GTC_K;
       // which operand of the term is the per-point one
       const bool pa = Tk.rcase == 0;
-      const int pbuf = pa ? tm.abuf : tm.bbuf, sbuf = pa ? tm.bbuf : tm.abuf;
-      const long long poff = pa ? tm.aoff : tm.boff, soff = pa ? tm.boff : tm.aoff;
-      const int pld = pa ? tm.lda : tm.ldb, sld = pa ? tm.ldb : tm.lda;
-      const int ptr_ = pa ? tm.tA : tm.tB, str_ = pa ? tm.tB : tm.tA;
+      const int pbuf = pa ? tm.abuf : tm.bbuf;
+      const long long poff = pa ? tm.aoff : tm.boff;
+      const int pld = pa ? tm.lda : tm.ldb;
+      const int ptr_ = pa ? tm.tA : tm.tB;
       if (!abort_flag) {
         // A[m][k]: row m = (point, plane, i); case 0: op(P)[i][k], case 1: op(P)[k][i]
         for (int e = tid; e < 128 * (GTC_K / 4); e += GTC_PROD) {
@@ -207,29 +261,15 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
           const int o = tc::cm_off(m, 4 * k4, 128);
           st_split4(sAh + o, sAl + o, v);
         }
-        // B[n][k]: case 0: op(S)[k][n], case 1: op(S)[n][k]
-        for (int e = tid; e < NP * (GTC_K / 4); e += GTC_PROD) {
-          const int n = e % NP, k4 = e / NP;
-          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (n < Tk.ncols) {
-            const float* S = bufs[sbuf].base + soff;
-            const bool kfast = pa ? str_ == 0 : str_ != 0;
-            const long long sn = kfast ? sld : 1, sk = kfast ? 1 : sld;
-            float x[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const int k = k0 + 4 * k4 + u;
-              x[u] = k < K ? S[(long long)n * sn + (long long)k * sk] : 0.f;
-            }
-            v = make_float4(x[0], x[1], x[2], x[3]);
-          }
-          const int o = tc::cm_off(n, 4 * k4, NP);
-          st_split4(sBh + o, sBl + o, v);
-        }
       }
       tc::fence_async_smem();
-      tc::mbar_arrive(&full_bar[st]);
+      if (!issued) tc::mbar_arrive(&full_bar[st]);
     }
+    // no copy may still be landing when the memory is reused (the last two chunks
+    // are the only ones that can be in flight)
+    if (tid == 0)
+      for (int k = 0; k < 2; ++k)
+        if (last_copy[k] >= 0 && !tc::mbar_wait(&full_bar[k], (last_copy[k] >> 1) & 1)) abort_flag = 1;
   } else if (tid == GTC_PROD) {
     // ---------------- MMA issuer ----------------
     const uint32_t idesc = tc::idesc_tf32(128, NP);
@@ -242,7 +282,7 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
         const float* sAh = stage_base + st * stage_floats;
         const float* sAl = sAh + 128 * GTC_K;
         const float* sBh = sAl + 128 * GTC_K;
-        const float* sBl = sBh + 256 * GTC_K;
+        const float* sBl = sBh + NP * GTC_K;
 #pragma unroll
         for (int ks = 0; ks < GTC_K / 8; ++ks) {
           const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
@@ -1912,7 +1952,10 @@ struct BroState {
   const int* itp;   // [P] Broyden iteration of each point
   const int* modep; // [P] BRO_*
 };
-enum { BRO_NPART = 2 + 2 * 64 };  // 0: max|vout|, 1: |df_ipos|^2, 2..: dots
+// block partials, [P][BRO_NPART][nchunk] so that their reduction reads consecutive
+// chunks: j = 0: max|vout|, 1: |df_ipos|^2, 2 + k: df_k . df_ipos, 66 + k: df_k . vout
+enum { BRO_NPART = 2 + 2 * 64 };
+__device__ __forceinline__ long long bro_part(int nchunk, int p, int j) { return ((long long)p * BRO_NPART + j) * nchunk; }
 enum { BRO_CHUNK = 1024 };          // elements per CTA of the Broyden kernels (4 per thread)
 
 // history slots of Broyden iteration `it` (Fortran integer division truncates
@@ -1974,8 +2017,8 @@ __global__ void __launch_bounds__(256) k_bro_diff(BroState S, const int* __restr
   const double m = block_max(mx, sh);
   const double s = block_sum(nn, sh);
   if (threadIdx.x == 0) {
-    double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
-    pt[0] = m; pt[1] = s;
+    S.part[bro_part(S.nchunk, p, 0) + blockIdx.x] = m;
+    S.part[bro_part(S.nchunk, p, 1) + blockIdx.x] = s;
   }
 }
 
@@ -2019,7 +2062,7 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
   }
   __syncthreads();
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  double* pt = S.part + ((long long)p * S.nchunk + blockIdx.x) * BRO_NPART;
+  double* pt = S.part + bro_part(S.nchunk, p, 0) + blockIdx.x;
   for (int k = w; k < iu; k += 8) {
     double a = 0.0, b = 0.0;
     if (k == ipos && upd) {  // column ipos itself: its normalised values are in shared memory
@@ -2053,7 +2096,7 @@ __global__ void __launch_bounds__(256) k_bro_dots(BroState S, const double* __re
       a += __shfl_xor_sync(0xffffffffu, a, o);
       b += __shfl_xor_sync(0xffffffffu, b, o);
     }
-    if (l == 0) { pt[2 + k] = a; pt[2 + 64 + k] = b; }
+    if (l == 0) { pt[(long long)(2 + k) * S.nchunk] = a; pt[(long long)(2 + 64 + k) * S.nchunk] = b; }
   }
 }
 
@@ -2068,12 +2111,12 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
                                                    double* __restrict__ gamma, const int* __restrict__ active) {
   const int p = blockIdx.x;
   if (!active[p]) return;
-  const double* pt = S.part + (long long)p * S.nchunk * BRO_NPART;
+  const double* pt = S.part + bro_part(S.nchunk, p, 0);
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
   __shared__ double red[8][2];
   if (stage == 0) {
     double m = 0.0, s = 0.0;
-    for (int c = tid; c < S.nchunk; c += blockDim.x) { m = fmax(m, pt[c * BRO_NPART]); s += pt[c * BRO_NPART + 1]; }
+    for (int c = tid; c < S.nchunk; c += blockDim.x) { m = fmax(m, pt[c]); s += pt[S.nchunk + c]; }
     for (int o = 16; o > 0; o >>= 1) {
       m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
       s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -2099,7 +2142,10 @@ __global__ void __launch_bounds__(256) k_bro_solve(BroState S, int stage, double
   double* bp = beta + (long long)p * M * M;
   for (int k = w; k < n; k += 8) {   // one warp per k: sum the chunk partials
     double dd = 0.0, wk = 0.0;
-    for (int c = l; c < S.nchunk; c += 32) { dd += pt[c * BRO_NPART + 2 + k]; wk += pt[c * BRO_NPART + 2 + 64 + k]; }
+    const double* pd = pt + (long long)(2 + k) * S.nchunk;
+    const double* pw = pt + (long long)(2 + 64 + k) * S.nchunk;
+#pragma unroll 4
+    for (int c = l; c < S.nchunk; c += 32) { dd += pd[c]; wk += pw[c]; }
     for (int o = 16; o > 0; o >>= 1) {
       dd += __shfl_xor_sync(0xffffffffu, dd, o);
       wk += __shfl_xor_sync(0xffffffffu, wk, o);
