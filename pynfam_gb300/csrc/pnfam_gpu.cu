@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <type_traits>
 #include <mutex>
 #include <cmath>
@@ -180,6 +182,11 @@ struct pnfam_ctx {
   std::vector<HTaskTC> htasks_tc;   // tensor-core field projection (FP32 data)
   int tc_npmax = 16;                  // largest N of those tiles
   DBuf<HTaskTC> d_htasks_tc;
+  std::vector<HPTile> hptiles;        // their row tiles, with the pre-split basis functions
+  DBuf<HPTile> d_hptiles;
+  DBuf<float> d_hphi;
+  long long hphi_floats = 0;
+  bool have_hphi = false;
   DBuf<int> d_actlist;   // [P] points of the current FP32 evaluation (tensor-core tiles)
   DBuf<int> d_err;       // set by a tensor-core kernel whose wait gave up
   // per-solve buffers
@@ -248,7 +255,7 @@ struct pnfam_ctx {
     for (auto* b : dbs) b->release();
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
     d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
-    d_gsplit.release();
+    d_gsplit.release(); d_hptiles.release(); d_hphi.release();
     k1a.d_tasks.release(); k1a.d_tile2task.release();
     k1b.d_tasks.release(); k1b.d_tile2task.release();
     k2a.d_tasks.release(); k2a.d_tile2task.release();
@@ -435,6 +442,26 @@ static void build_tasks(pnfam_ctx* c) {
     if (c->fc[i] >= 0) { add_tc(i, c->fc[i], 0, 0, 0, c->foff[i]); add_tc(i, c->fc[i], 0, 1, 3, c->foff[i]); }
     if (c->xc[i] >= 0) add_tc(i, c->xc[i], 1, 0, 1, c->xoff[i]);
     if (c->yc[i] >= 0) add_tc(i, c->yc[i], 1, 1, 2, c->yoff[i]);
+  }
+  // pre-split row basis functions of the projection tiles, one copy per distinct
+  // (block, first row, rows)
+  c->hptiles.clear();
+  {
+    const long long nrc = (c->nghl + HTC_K - 1) / HTC_K;
+    std::map<std::tuple<int, int, int>, long long> seen;
+    long long off = 0;
+    for (HTaskTC& h : c->htasks_tc) {
+      const auto key = std::make_tuple(h.ix, h.a0, h.na);
+      auto it = seen.find(key);
+      if (it == seen.end()) {
+        it = seen.emplace(key, off).first;
+        c->hptiles.push_back(HPTile{h.ix, h.a0, h.na, h.np, off});
+        off += 5 * nrc * 64 * (long long)h.np;
+      }
+      h.tphi = it->second;
+    }
+    c->hphi_floats = off;
+    c->have_hphi = false;
   }
   // tensor-core densities: A chunks per (block, spin of the rows, 8 rows); units per
   // call in the order (kind, ix, column range, spin), so that the two spins of one
@@ -650,7 +677,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
     // tensor cores: c->d_actlist holds the nact points of this evaluation
     dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
     k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), st>>>(
-        B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, hsp, nxy, c->d_err.p);
+        B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, c->d_hphi.p, hsp, nxy, c->d_err.p);
     c->launches++;
     CK(cudaGetLastError());
   } else {
@@ -722,6 +749,16 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   bd[B_HSP] = {c->d_hsp32.p, 8 * nxy, 4 * nxy};
   bd[B_HQP] = {c->d_hqp32.p, 4 * nxy, 2 * nxy};
   CK(upload(c->d_bufs32, bd, NBUF));
+  if (!c->have_hphi) {
+    const int nrc = (c->nghl + HTC_K - 1) / HTC_K;
+    CK(dalloc(c->d_hphi, (size_t)std::max(1LL, c->hphi_floats)));
+    if (!c->hptiles.empty()) {
+      k_hproj_bsplit<<<dim3((unsigned)c->hptiles.size(), 5 * nrc), 256, 0, c->stream>>>(
+          c->devbasis<float>(), c->d_hptiles.p, nrc, c->d_hphi.p);
+      CK(cudaGetLastError());
+    }
+    c->have_hphi = true;
+  }
   if (!c->have_gsplit) {
     CK(dalloc(c->d_gsplit, (size_t)std::max(1LL, c->gsplit_floats)));
     TaskListTC* lists[4] = {&c->t1a, &c->t1b, &c->t2a, &c->t2b};
@@ -912,6 +949,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   }
   CK(upload(c->d_htasks, c->htasks.data(), c->htasks.size()));
   CK(upload(c->d_htasks_tc, c->htasks_tc.data(), c->htasks_tc.size()));
+  CK(upload(c->d_hptiles, c->hptiles.data(), c->hptiles.size()));
   CK(upload(c->d_dunits0, c->dunits[0].data(), c->dunits[0].size()));
   CK(upload(c->d_dunits1, c->dunits[1].data(), c->dunits[1].size()));
   CK(upload(c->d_bchunks, c->bchunks.data(), c->bchunks.size()));
@@ -1474,7 +1512,7 @@ extern "C" int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* c, const double* re
   }
   k_meanfield<float><<<dim3((c->nghl + 127) / 128, 2), 128, 0, c->stream>>>(B, c->G, c->d_dpart32.p, c->d_mf32.p, act);
   k_hproj_tc<<<dim3((unsigned)c->htasks_tc.size(), 1), HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), c->stream>>>(
-      B, c->d_htasks_tc.p, c->d_actlist.p, 1, c->tc_npmax, c->d_mf32.p, c->d_hsp32.p, nxy, c->d_err.p);
+      B, c->d_htasks_tc.p, c->d_actlist.p, 1, c->tc_npmax, c->d_mf32.p, c->d_hphi.p, c->d_hsp32.p, nxy, c->d_err.p);
   k_to_f64<<<dim3(1024, 1), 256, 0, c->stream>>>(c->d_hsp32.p, c->d_hsp.p, 8 * nxy, 0, nullptr);
   CK(cudaGetLastError());
   const int qout[8] = {0, 0, 1, 1, 3, 3, 2, 2};

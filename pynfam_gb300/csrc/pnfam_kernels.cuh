@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
   const uint32_t tmem = tslot;
   if (warp < GTC_PROD / 32) {
     // ---------------- producers ----------------
-    int last_copy[2] = {-1, -1};   // thread 0: last chunk copied into each stage
+    int lc0 = -1, lc1 = -1;   // thread 0: last chunk copied into stage 0, stage 1
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
         tc::mbar_expect_tx(&full_bar[st], bbytes);
         tc::bulk_g2s(sBh, gsplit + Tk.bsoff + (long long)c * NP * 2 * GTC_K, bbytes, &full_bar[st]);
         issued = true;
-        last_copy[st] = c;
+        if (st == 0) lc0 = c; else lc1 = c;
       }
       const GemmTerm& tm = Tk.t[c / nkc];
       const int k0 = (c % nkc) * GTC_K;
@@ -267,9 +267,10 @@ __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __
     }
     // no copy may still be landing when the memory is reused (the last two chunks
     // are the only ones that can be in flight)
-    if (tid == 0)
-      for (int k = 0; k < 2; ++k)
-        if (last_copy[k] >= 0 && !tc::mbar_wait(&full_bar[k], (last_copy[k] >> 1) & 1)) abort_flag = 1;
+    if (tid == 0) {
+      if (lc0 >= 0 && !tc::mbar_wait(&full_bar[0], (lc0 >> 1) & 1)) abort_flag = 1;
+      if (lc1 >= 0 && !tc::mbar_wait(&full_bar[1], (lc1 >> 1) & 1)) abort_flag = 1;
+    }
   } else if (tid == GTC_PROD) {
     // ---------------- MMA issuer ----------------
     const uint32_t idesc = tc::idesc_tf32(128, NP);
@@ -1677,23 +1678,42 @@ __global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __r
 //   m = pl*64 + j, j = (point in the group)*nbc + b   (rows: Re, then Im of hpsi)
 //   n = a (the rows of the output block, N padded to np)
 //   k = (q, r), 32 mesh points of one component q per chunk.
-// Warps 0-7 produce the operands of a chunk (hpsi generated from the field
-// tensor and the column basis functions, the row basis functions staged) into
-// one of two shared-memory stages; warp 8 issues the MMAs of a chunk as soon as
-// its stage is full and releases the stage through tcgen05.commit, so operand
-// production and tensor-core work overlap.  D accumulates in tensor memory and
-// out_ab = 2 D.
+// Warps 0-7 produce the A operand of a chunk (hpsi generated from the field
+// tensor and the column basis functions) into one of two shared-memory stages;
+// the B operand (the row basis functions, constant: split into TF32 hi and lo once
+// per operator in the canonical layout) is copied in by the bulk-copy engine.
+// Warp 8 issues the MMAs of a chunk as soon as its stage is full and releases the
+// stage through tcgen05.commit, so operand production and tensor-core work
+// overlap.  D accumulates in tensor memory and out_ab = 2 D.
 // ---------------------------------------------------------------------------
 struct HTaskTC {
   int ix, iy, a0, na, b0, nbc, sa, mode, call, outq;
   int np;          // N of the MMA: na rounded up to 16
   int pg;          // points per CTA (pg * nbc <= 64)
   long long ooff;
+  long long tphi;  // floats: the pre-split row basis functions of rows a0..a0+na of block ix
 };
 enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
-// B items (4 mesh points of one row) per producer thread, and how many of them are
-// loaded ahead of the field tensor (all of them for tiles of up to 64 rows)
-enum { HTC_BI = HTC_MAXN * (HTC_K / 4) / HTC_PROD, HTC_BE = 2 };
+// pre-split B operand of one row tile (rows a0..a0+na of block ix): for component q
+// and mesh chunk rc (32 points), [hi | lo][np x 32] at off + (q * nrc + rc) * 64 * np
+struct HPTile { int ix, a0, na, np; long long off; };
+
+// grid (ntiles, 5 * nrc), 256 threads
+__global__ void __launch_bounds__(256) k_hproj_bsplit(DevBasisT<float> B, const HPTile* __restrict__ tiles, int nrc,
+                                                      float* __restrict__ hphi) {
+  const HPTile t = tiles[blockIdx.x];
+  const int q = blockIdx.y / nrc, r0 = (blockIdx.y % nrc) * HTC_K;
+  const int nghl = B.nghl;
+  const long long ps = (long long)B.dqp * nghl;
+  float* dst = hphi + t.off + (long long)blockIdx.y * 64 * t.np;
+  const int ja0 = B.st[t.ix] + t.a0;
+  for (int e = threadIdx.x; e < t.np * 8; e += blockDim.x) {
+    const int n = e % t.np, r4 = e / t.np;
+    const float4 v = ld_row4(B.phi + q * ps + (long long)(ja0 + n) * nghl, r0 + 4 * r4, nghl, n < t.na);
+    const int o = tc::cm_off(n, 4 * r4, t.np);
+    st_split4(dst + o, dst + 32 * t.np + o, v);
+  }
+}
 
 // dynamic shared memory for tiles of at most npmax output rows: two stages of
 // A (128 x 32, hi and lo) and B (npmax x 32, hi and lo), then the field tensor
@@ -1707,7 +1727,8 @@ __host__ __device__ constexpr size_t hproj_tc_smem_bytes(int npmax) {
 // cores gave up (the CTA then writes nothing)
 __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B, const HTaskTC* __restrict__ tasks,
                                                              const int* __restrict__ actlist, int nact, int npmax,
-                                                             const float* __restrict__ mf, float* __restrict__ hsp,
+                                                             const float* __restrict__ mf,
+                                                             const float* __restrict__ hphi, float* __restrict__ hsp,
                                                              long long nxy, int* __restrict__ err) {
   const HTaskTC Th = tasks[blockIdx.x];
   const int g0 = blockIdx.y * Th.pg;
@@ -1726,7 +1747,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
   const int nbc = Th.nbc, NP = Th.np, nj = npg * nbc;
   const int nghl = B.nghl;
   const long long ps = (long long)B.dqp * nghl;
-  const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
+  const int jb0 = B.st[Th.iy] + Th.b0;
   const int nc = Th.mode == 0 ? 5 : 1;
   const int nrc = (nghl + HTC_K - 1) / HTC_K;   // chunks per component
   const int nchunk = nc * nrc;
@@ -1749,8 +1770,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
     // chunks in mesh-point-major order: the column basis functions phi_iz(b, r) of a
     // thread's two A items stay in registers for the nc components of one r range.
     // Everything that does not depend on the chunk is computed once: the hpsi row
-    // (point, column), spin and shared-memory offsets of the two A items, and the row,
-    // mesh offset and stage offset of the (at most HTC_BI) B items of this thread.
+    // (point, column), spin and shared-memory offsets of the two A items.
     float4 fz[2][5];
     int a_m[2], a_row[2], a_ore[2], a_oim[2];   // a_row < 0: no hpsi row
 #pragma unroll
@@ -1764,29 +1784,23 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
       a_ore[it] = tc::cm_off(j, 4 * r4, 128);
       a_oim[it] = tc::cm_off(64 + j, 4 * r4, 128);
     }
-    int b_row[HTC_BI], b_o[HTC_BI];   // b_row: basis row (-1: zero), b_o: stage offset (-1: none)
-#pragma unroll
-    for (int k = 0; k < HTC_BI; ++k) {
-      const int e = tid + k * HTC_PROD;
-      const int n = e % NP, r4 = e / NP;
-      b_row[k] = e < NP * 8 && n < Th.na ? ja0 + n : -1;
-      b_o[k] = e < NP * 8 ? tc::cm_off(n, 4 * r4, NP) : -1;
-    }
+    int lc0 = -1, lc1 = -1;   // thread 0: last chunk copied into stage 0, stage 1
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
       float* sAh = stage_base + st * stage_floats;
       float* sAl = sAh + 128 * HTC_K;
       float* sBh = sAl + 128 * HTC_K;
-      float* sBl = sBh + npmax * HTC_K;
       const int q = c % nc, r0 = (c / nc) * HTC_K;
-      // B: phi_q(a, r) of the output rows, loaded now so that these loads and the
-      // field-tensor loads below are in flight together
-      float4 bv[HTC_BE];
-#pragma unroll
-      for (int k = 0; k < HTC_BE; ++k) {
-        const int r = r0 + 4 * ((tid + k * HTC_PROD) / NP);
-        bv[k] = ld_row4(B.phi + q * ps + (long long)b_row[k] * nghl, r, nghl, b_row[k] >= 0);
+      bool issued = false;
+      if (tid == 0 && !abort_flag) {
+        // B: the row basis functions phi_q(a, r) of this chunk, pre-split (hi then lo,
+        // NP x 32 each); this thread's arrival on the stage comes with the copy
+        const uint32_t bbytes = (uint32_t)NP * HTC_K * 2 * 4;
+        tc::mbar_expect_tx(&full_bar[st], bbytes);
+        tc::bulk_g2s(sBh, hphi + Th.tphi + (long long)(q * nrc + c / nc) * 64 * NP, bbytes, &full_bar[st]);
+        issued = true;
+        if (st == 0) lc0 = c; else lc1 = c;
       }
       // the field tensor of this chunk (component q, mesh points r0..r0+31) of every
       // point of the group, shared by all rows; the barriers keep one chunk's copy
@@ -1827,19 +1841,15 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
           st_split4(sAh + a_ore[it], sAl + a_ore[it], hr);
           st_split4(sAh + a_oim[it], sAl + a_oim[it], hi);
         }
-#pragma unroll
-        for (int k = 0; k < HTC_BE; ++k)
-          if (b_o[k] >= 0) st_split4(sBh + b_o[k], sBl + b_o[k], bv[k]);
-#pragma unroll
-        for (int k = HTC_BE; k < HTC_BI; ++k)   // tiles of more than 64 rows
-          if (b_o[k] >= 0) {
-            const int r = r0 + 4 * ((tid + k * HTC_PROD) / NP);
-            st_split4(sBh + b_o[k], sBl + b_o[k],
-                      ld_row4(B.phi + q * ps + (long long)b_row[k] * nghl, r, nghl, b_row[k] >= 0));
-          }
       }
       tc::fence_async_smem();
-      tc::mbar_arrive(&full_bar[st]);
+      if (!issued) tc::mbar_arrive(&full_bar[st]);
+    }
+    // no copy may still be landing when the memory is reused (the last two chunks
+    // are the only ones that can be in flight)
+    if (tid == 0) {
+      if (lc0 >= 0 && !tc::mbar_wait(&full_bar[0], (lc0 >> 1) & 1)) abort_flag = 1;
+      if (lc1 >= 0 && !tc::mbar_wait(&full_bar[1], (lc1 >> 1) & 1)) abort_flag = 1;
     }
   } else if (tid == HTC_PROD) {
     // ---------------- MMA issuer (one thread of warp 8) ----------------
@@ -1853,7 +1863,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
         const float* sAh = stage_base + st * stage_floats;
         const float* sAl = sAh + 128 * HTC_K;
         const float* sBh = sAl + 128 * HTC_K;
-        const float* sBl = sBh + npmax * HTC_K;
+        const float* sBl = sBh + NP * HTC_K;
 #pragma unroll
         for (int ks = 0; ks < HTC_K / 8; ++ks) {
           const uint32_t oa = ks * 2 * lboA, ob = ks * 2 * lboB;
