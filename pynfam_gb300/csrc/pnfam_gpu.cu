@@ -204,6 +204,7 @@ struct pnfam_ctx {
   DBuf<BufDescT<float>> d_bufs32;
   DBuf<double> d_xsave, d_radd;   // [P][4nxy] mixed form: anchor X_a and its FP64 image g(X_a)
   DBuf<unsigned long long> d_dmax;  // [P] max|X - X_a| of the last increment evaluation
+  DBuf<double> d_lastf, d_lastv, d_tf, d_tv;  // [P][4nxy] mixed-form Broyden: raw vectors of the last step, raw differences
   // tensor-core densities: unit tables per call, B chunks to lay out, pre-split A
   std::vector<DUnitTC> dunits[2];
   std::vector<DBChunkTC> bchunks;
@@ -244,6 +245,7 @@ struct pnfam_ctx {
     for (auto* b : fb) b->release();
     d_bufs32.release();
     d_xsave.release(); d_radd.release(); d_dmax.release();
+    d_lastf.release(); d_lastv.release(); d_tf.release(); d_tv.release();
     d_dunits0.release(); d_dunits1.release(); d_bchunks.release(); d_achunks.release(); d_aphi.release();
     d_bsplit.release();
     for (auto* b : ib) b->release();
@@ -726,6 +728,10 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   CK(dalloc(c->d_xsave, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_radd, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_dmax, (size_t)P));
+  CK(dalloc(c->d_lastf, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_lastv, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_tf, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_tv, (size_t)P * 4 * nxy));
   if (c->tc_density) {
     CK(dalloc(c->d_bsplit, (size_t)P * c->bstride));
     if (!c->have_aphi) {
@@ -1096,7 +1102,8 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
   return k;
 }
 
-// one Broyden step of every active slot
+// one Broyden step of every active slot: FP64 history (FP64 form), pair-arithmetic
+// history (mixed form)
 static int broyden_step(pnfam_ctx* c, pnfam_engine* e, int any_bro, const int* d_itp, const int* d_mode) {
   const int P = e->P, N = e->N;
   const int* act = c->d_active.p;
@@ -1105,18 +1112,27 @@ static int broyden_step(pnfam_ctx* c, pnfam_engine* e, int any_bro, const int* d
   S.vin = c->d_state.p; S.vout = c->d_vout.p; S.df = c->d_df.p; S.dv = c->d_dv.p;
   S.part = c->d_bpart.p; S.nchunk = c->nchunk_bro;
   S.itp = d_itp; S.modep = d_mode;
+  BroState2 S2;
+  S2.N = N; S2.M = S.M; S2.alpha = S.alpha; S2.vin = S.vin; S2.vout = S.vout;
+  S2.df = reinterpret_cast<float2*>(c->d_df.p); S2.u = reinterpret_cast<float2*>(c->d_dv.p);
+  S2.lastf = c->d_lastf.p; S2.lastv = c->d_lastv.p; S2.tf = c->d_tf.p; S2.tv = c->d_tv.p;
+  S2.part = S.part; S2.nchunk = S.nchunk; S2.itp = d_itp; S2.modep = d_mode;
+  const bool pair = e->mixed;
   const double w0 = 0.01;
   dim3 grid(c->nchunk_bro, P);
-  k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
+  if (pair) k_bro_diff2<<<grid, 256, 0, c->stream>>>(S2, act);
+  else k_bro_diff<<<grid, 256, 0, c->stream>>>(S, act);
   k_bro_solve<<<P, 256, 0, c->stream>>>(S, 0, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
   c->launches += 2;
   if (any_bro) {
-    k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
+    if (pair) k_bro_dots2<<<grid, 256, 0, c->stream>>>(S2, c->d_norm.p, act);
+    else k_bro_dots<<<grid, 256, 0, c->stream>>>(S, c->d_norm.p, act);
     k_bro_solve<<<P, 256, 0, c->stream>>>(S, 1, w0, c->d_si.p, c->d_norm.p, c->d_beta.p, c->d_gamma.p, act);
     c->launches += 2;
   }
   dim3 ug((unsigned)std::min<long long>(4096, (N + 255) / 256), P);
-  k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
+  if (pair) k_bro_update2<<<ug, 256, 0, c->stream>>>(S2, c->d_gamma.p, act);
+  else k_bro_update<<<ug, 256, 0, c->stream>>>(S, c->d_gamma.p, act);
   c->launches++;
   CK(cudaGetLastError());
   return PNFAM_OK;
@@ -1225,8 +1241,7 @@ static int engine_launch(pnfam_engine* e) {
     CK(cudaGetLastError());
   }
   toc(5);
-  // ---- Broyden (pnfam_broyden.f90:117-216), each slot at its own iteration, FP64
-  // history in both forms ----
+  // ---- Broyden (pnfam_broyden.f90:117-216), each slot at its own iteration ----
   tic();
   if ((rc = broyden_step(c, e, any_bro, d_itp, d_mode))) return rc;
   toc(6);

@@ -2231,6 +2231,174 @@ __global__ void __launch_bounds__(256) k_bro_update(BroState S, const double* __
   }
 }
 
+// ---------------------------------------------------------------------------
+// Broyden of the mixed form.  The history columns df_k and u_k are kept as pairs
+// of floats (hi + lo, about 48 significant bits) and every product with them is
+// formed in pair arithmetic on the FP32 cores, which GB300 runs at dozens of times
+// its FP64 rate; the raw vout and vin of the previous step and this step's raw
+// differences stay FP64, so the secant pairs are formed before any rounding, and
+// the small solve is FP64 (k_bro_solve).  Same steps as k_bro_diff / k_bro_dots /
+// k_bro_update.
+// ---------------------------------------------------------------------------
+struct BroState2 {
+  int N;              // vector length (4*nxy)
+  int M;              // history size
+  double alpha;
+  double* vin;        // [P][N]
+  double* vout;       // [P][N]
+  float2* df;         // [P][M][N] finished columns df_k
+  float2* u;          // [P][M][N] finished columns u_k = dv_k + alpha*df_k
+  double* lastf;      // [P][N] raw vout of the previous step
+  double* lastv;      // [P][N] raw vin of the previous step
+  double* tf;         // [P][N] vout - lastf of this step (unnormalised)
+  double* tv;         // [P][N] vin - lastv of this step
+  double* part;       // [P][BRO_NPART][nchunk]
+  int nchunk;
+  const int* itp;
+  const int* modep;
+};
+
+__device__ __forceinline__ float2 pair_split(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ double pair_value(float2 a) { return (double)a.x + (double)a.y; }
+
+// s += a*b in pair arithmetic: the exact error of the leading product (FMA) and the
+// cross terms go to the low part, the leading sum is a two-sum (rounded operations
+// that the compiler may not contract)
+__device__ __forceinline__ void pair_fma(float2& s, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float t = __fadd_rn(s.x, p);
+  const float z = __fsub_rn(t, s.x);
+  const float err = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, z)), __fsub_rn(p, z));
+  s.x = t;
+  s.y = __fadd_rn(s.y, __fadd_rn(err, e));
+}
+
+// vout -= vin; max|vout|; tf = vout - lastf, tv = vin - lastv, |tf|^2
+__global__ void __launch_bounds__(256) k_bro_diff2(BroState2 S, const int* __restrict__ active) {
+  const int p = blockIdx.y;
+  if (!active[p]) return;
+  __shared__ double sh[32];
+  const int it = S.itp[p], mode = S.modep[p];
+  const bool upd = mode == BRO_BROYDEN && it >= 2;
+  const long long o = (long long)p * S.N;
+  double mx = 0.0, nn = 0.0;
+  const int e0 = blockIdx.x * BRO_CHUNK, e1 = min(S.N, e0 + BRO_CHUNK);
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const double vi = S.vin[o + e];
+    const double v = S.vout[o + e] - vi;
+    S.vout[o + e] = v;
+    mx = fmax(mx, fabs(v));
+    if (upd) {
+      const double f = v - S.lastf[o + e];
+      S.tf[o + e] = f;
+      S.tv[o + e] = vi - S.lastv[o + e];
+      nn = fma(f, f, nn);
+    }
+  }
+  const double m = block_max(mx, sh);
+  const double s = block_sum(nn, sh);
+  if (threadIdx.x == 0) {
+    S.part[bro_part(S.nchunk, p, 0) + blockIdx.x] = m;
+    S.part[bro_part(S.nchunk, p, 1) + blockIdx.x] = s;
+  }
+}
+
+// finish column ipos (df = tf/|tf|, u = tv/|tf| + alpha*df, stored as pairs) and form
+// the dots dd[k] = df_k . df_ipos and wk[k] = df_k . vout, one warp per column
+__global__ void __launch_bounds__(256) k_bro_dots2(BroState2 S, const double* __restrict__ norm,
+                                                   const int* __restrict__ active) {
+  const int p = blockIdx.y;
+  if (!active[p]) return;
+  const int it = S.itp[p], mode = S.modep[p];
+  if (mode != BRO_BROYDEN || it < 1) return;
+  int iu, ipos, inext;
+  bro_slots(it, S.M, iu, ipos, inext);
+  const bool upd = it >= 2;
+  __shared__ float2 sf[BRO_CHUNK], sv[BRO_CHUNK];
+  const long long o = (long long)p * S.N;
+  float2* dfp = S.df + (long long)p * S.M * S.N;
+  float2* up = S.u + (long long)p * S.M * S.N;
+  const long long base = (long long)blockIdx.x * BRO_CHUNK;
+  const int len = (int)min((long long)BRO_CHUNK, (long long)S.N - base);
+  const double sc = upd ? norm[p] : 0.0;
+  for (int i = threadIdx.x; i < BRO_CHUNK; i += blockDim.x) {
+    float2 f2 = make_float2(0.f, 0.f), v2 = f2;
+    if (i < len) {
+      const long long e = base + i;
+      if (upd) {
+        const double fn = S.tf[o + e] * sc;
+        f2 = pair_split(fn);
+        dfp[(long long)ipos * S.N + e] = f2;
+        up[(long long)ipos * S.N + e] = pair_split(fma(S.alpha, fn, S.tv[o + e] * sc));
+      }
+      v2 = pair_split(S.vout[o + e]);
+    }
+    sf[i] = f2;
+    sv[i] = v2;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  double* pt = S.part + bro_part(S.nchunk, p, 0) + blockIdx.x;
+  for (int k = w; k < iu; k += 8) {
+    float2 a = make_float2(0.f, 0.f), b = a;
+    if (k == ipos && upd) {   // the new column itself: its values are in shared memory
+      for (int j = l; j < len; j += 32) {
+        pair_fma(a, sf[j], sf[j]);
+        pair_fma(b, sf[j], sv[j]);
+      }
+    } else {
+      const float2* fk = dfp + (long long)k * S.N + base;
+#pragma unroll 8
+      for (int j = l; j < len; j += 32) {
+        const float2 x = __ldcs(fk + j);
+        pair_fma(a, x, sf[j]);
+        pair_fma(b, x, sv[j]);
+      }
+    }
+    double ad = pair_value(a), bd = pair_value(b);
+    for (int of = 16; of > 0; of >>= 1) {
+      ad += __shfl_xor_sync(0xffffffffu, ad, of);
+      bd += __shfl_xor_sync(0xffffffffu, bd, of);
+    }
+    if (l == 0) { pt[(long long)(2 + k) * S.nchunk] = ad; pt[(long long)(2 + 64 + k) * S.nchunk] = bd; }
+  }
+}
+
+// BRO_BROYDEN: vin += alpha*vout - sum_k gamma_k u_k; lastf = vout, lastv = vin (raw)
+// BRO_LINEAR:  vin += alpha*vout;  BRO_NOMIX: vin += vout
+__global__ void __launch_bounds__(256) k_bro_update2(BroState2 S, const double* __restrict__ gamma,
+                                                     const int* __restrict__ active) {
+  const int p = blockIdx.y;
+  if (!active[p]) return;
+  const int it = S.itp[p], mode = S.modep[p];
+  int iu, ipos, inext;
+  bro_slots(it, S.M, iu, ipos, inext);
+  if (mode != BRO_BROYDEN) iu = 0;
+  const long long o = (long long)p * S.N;
+  __shared__ float2 g[64];
+  if (mode == BRO_BROYDEN && (int)threadIdx.x < iu) g[threadIdx.x] = pair_split(gamma[(long long)p * 64 + threadIdx.x]);
+  __syncthreads();
+  const float2* up = S.u + (long long)p * S.M * S.N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < S.N; e += (long long)gridDim.x * blockDim.x) {
+    const double v = S.vout[o + e];
+    if (mode == BRO_NOMIX) { S.vin[o + e] += v; continue; }
+    if (mode == BRO_LINEAR) { S.vin[o + e] += S.alpha * v; continue; }
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int k = 0; k < iu; ++k) pair_fma(acc, up[(long long)k * S.N + e], g[k]);
+    const double old = S.vin[o + e];
+    S.lastf[o + e] = v;
+    S.lastv[o + e] = old;
+    S.vin[o + e] = old + (S.alpha * v - pair_value(acc));
+  }
+}
+
 // per-point vector operations, [P][n] layout:
 // op 0: dst = src; op 1: dst += src; op 2: dst = 0; op 3: dst = a*src
 __global__ void k_vecop(int op, double a, double* __restrict__ dst, const double* __restrict__ src, long long n,
