@@ -155,10 +155,8 @@ def cpu_sample(case, omegas, iters):
 
 
 def dist_init(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from pynfam_gb300 import replicas
+    return replicas.env()
 
 
 def solver_kw(case, precision, eps):
@@ -287,11 +285,10 @@ def run_reference(args):
 
 def run_gpu(args):
     import torch
+    from pynfam_gb300 import replicas
     world, rank, local = dist_init(args)
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    replicas.init("nccl")
     cases, omegas = workload(args.points)
     P = len(omegas)
     R = args.requests
@@ -300,9 +297,7 @@ def run_gpu(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier("cuda")
 
     # ---- the mixed serving form: warm-up, then K timed serving runs ----
     slots = args.slots or P
@@ -313,25 +308,24 @@ def run_gpu(args):
     barrier()
     walls, lat, launches = [], [], 0
     counts = None
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        ev0.record()
         out, st, profs = mixed.run()
-        torch.cuda.synchronize()
-        walls.append(time.perf_counter() - t0)
+        torch.cuda.synchronize()   # every engine's stream has finished
+        ev1.record()
+        ev1.synchronize()
+        walls.append(ev0.elapsed_time(ev1) / 1e3)
         lat += st.latencies
         launches += sum(n for _, n in profs.values())
         counts = score(out, ref, R)
     barrier()
     ck = clocks.stop()
-    step_s = statistics.mean(walls)
-    if world > 1:
-        t = torch.tensor([step_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_s = float(t.item())
+    step_s = replicas.max_over_ranks(statistics.mean(walls), "cuda")
     conv, ok, worst = counts
-    value = world * ok / step_s
+    value = replicas.job_rate(ok, step_s, world)
     # ---- per-stage device time of one more run (events between stages) ----
     out_t, st_t, profs_t = mixed.run(timed=True)
     mixed.close()
@@ -393,6 +387,8 @@ def run_gpu(args):
                        "points_per_step": npts, "nghl": int(hf.nghl), "nxy": [int(c.F.mat.nelem) for c in cases],
                        "form": f"mixed, epsilon {MIXED_EPS}", "engines": len(OPERATORS), "slots_per_engine": slots,
                        "l2": "256 MB buffer written between timed steps",
+                       "timing": "CUDA events around each serving run, the device synchronized on both sides "
+                                 "(the engines run on their own streams)",
                        "parallelism": f"replicas{world}"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)) * 1e3, "p99": float(np.percentile(lat, 99)) * 1e3,
                            "note": "per point, from request arrival (start of the step) to its result"},
@@ -421,8 +417,7 @@ def run_gpu(args):
                                           f"workload, scaled by the FP64 form's {mi:.2f} iterations/point"}
     if rank == 0:
         print(json.dumps(line, default=_plain), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish()
 
 
 def run_serve_stream(args):
