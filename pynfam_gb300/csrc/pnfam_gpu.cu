@@ -193,6 +193,7 @@ struct pnfam_ctx {
   int cap_P = 0, cap_M = 0;
   DBuf<double> d_state, d_vout, d_T, d_rsp, d_hsp, d_hqp, d_dpart, d_mf;
   DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
+  DBuf<double> d_gfn;   // [P][Re | Im][2nxy] Green's function of each slot's omega
   DBuf<int> d_active, d_act32, d_act64;
   DBuf<int> d_pint;      // [6][P]: Broyden iteration, Broyden mode, increment step, anchor step,
                          // zero field (first evaluation), newly admitted
@@ -253,7 +254,7 @@ struct pnfam_ctx {
     DBuf<double>* dbs[] = {&d_up, &d_vp, &d_un, &d_vn, &d_ep, &d_en, &d_phi, &d_wd, &d_crho, &d_cs,
                            &d_cpair, &d_cspair, &d_fops, &d_state, &d_vout, &d_T, &d_rsp, &d_hsp,
                            &d_hqp, &d_dpart, &d_mf, &d_df, &d_dv, &d_bpart, &d_si, &d_norm,
-                           &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim};
+                           &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim, &d_gfn};
     for (auto* b : dbs) b->release();
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
     d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
@@ -535,6 +536,7 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   CK(dalloc(c->d_cpart, (size_t)P * c->nchunk_c * 2 * c->nops));
   CK(dalloc(c->d_wre, (size_t)P));
   CK(dalloc(c->d_wim, (size_t)P));
+  CK(dalloc(c->d_gfn, (size_t)P * 4 * nxy));
   CK(dalloc(c->d_active, (size_t)P));
   CK(dalloc(c->d_pint, (size_t)6 * P));
   CK(dalloc(c->d_actlist, (size_t)P));
@@ -1186,9 +1188,14 @@ static int engine_launch(pnfam_engine* e) {
     CK(cudaMemcpyAsync(c->d_wim.p, e->wim.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
     e->dirty_w = false;
   }
-  if (nfresh) {  // newly admitted slots start from X = 0
+  const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
+  const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
+  if (nfresh) {  // newly admitted slots start from X = 0, with their Green's function
     k_vecop<<<vgrid, 256, 0, c->stream>>>(2, 0.0, c->d_state.p, nullptr, N, d_fresh);
-    c->launches++;
+    const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
+    k_green_prep<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, c->d_erow.p, c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
+                                                     c->d_gfn.p, d_fresh);
+    c->launches += 2;
   }
   const int* act = c->d_active.p;
   int rc;
@@ -1216,20 +1223,17 @@ static int engine_launch(pnfam_engine* e) {
         k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
                                                c->d_dmax.p);
         if ((rc = residual_t<float>(c, P, n32, c->d_act32.p, timed, c->stream))) return rc;
-        k_to_f64<<<vgrid, 256, 0, c->stream>>>(c->d_hqp32.p, c->d_hqp.p, N, N, c->d_act32.p);
-        c->launches += 2;
+        c->launches++;
         CK(cudaGetLastError());
       }
     }
   }
   if (split) CK(cudaStreamWaitEvent(c->stream, c->evf[1], 0));
-  const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
-  const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
   tic();
   {
     const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
-    k_green<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, P, e->no_res ? nullptr : c->d_hqp.p, c->d_fops.p, c->d_erow.p,
-                                                c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
+    k_green<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, P, e->no_res ? nullptr : c->d_hqp.p,
+                                                e->mixed ? c->d_hqp32.p : nullptr, c->d_fops.p, c->d_gfn.p,
                                                 e->o.quench_residual_int, c->d_vout.p, act,
                                                 e->mixed ? d_incr : nullptr, c->d_radd.p, d_zero);
     c->launches++;

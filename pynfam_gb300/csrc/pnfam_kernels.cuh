@@ -628,9 +628,9 @@ __global__ void __launch_bounds__(256, sizeof(T) >= 8 ? 1 : 2) k_density(DevBasi
 // ---------------------------------------------------------------------------
 // FP64 densities (the drop-in form and the anchors of the mixed form): a CTA of
 // 32 mesh points x 8 column lanes; each lane accumulates W for one column b over
-// chunks of DAK rows and folds it into the densities with shuffle reductions over
-// the 8 lanes.  FP64 is bound by the DFMA rate, so the tiles follow the blocks
-// closely (8 columns per chunk, rows exact).
+// chunks of DAK rows and folds it into its own 28 complex densities (registers),
+// which are summed over the 8 lanes once, at the end.  FP64 is bound by the DFMA
+// rate, so the tiles follow the blocks closely (8 columns per chunk, rows exact).
 // ---------------------------------------------------------------------------
 #define DBC 8    // b columns per chunk
 #define DAK 16   // a rows per chunk
@@ -644,7 +644,7 @@ __device__ __forceinline__ double red8(double v) {
 
 // grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT r x DBC b
 // dpart: [P][2][G][2*ND][nghl]
-__global__ void __launch_bounds__(256) k_density_fp64(DevBasis B, DensCall c0, DensCall c1, int G,
+__global__ void __launch_bounds__(256, 1) k_density_fp64(DevBasis B, DensCall c0, DensCall c1, int G,
                                                       double* __restrict__ dpart, const int* __restrict__ active) {
   using T = double;
   const int p = blockIdx.z >> 1, call = blockIdx.z & 1;
@@ -656,19 +656,15 @@ __global__ void __launch_bounds__(256) k_density_fp64(DevBasis B, DensCall c0, D
   const int nghl = B.nghl;
   const int r = r0 + rl;
   const bool rok = r < nghl;
-  __shared__ T acc[2 * ND][DRT];
-  __shared__ T sphi[4][DAK][DRT];  // static smem: ~33 KB
+  __shared__ T sphi[4][DAK][DRT];  // static smem: ~20 KB
   __shared__ T srho[2][DAK][DBC];
-  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) (&acc[0][0])[e] = 0;
-  __syncthreads();
+  T al[2 * ND];   // this lane's densities at mesh point r
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) al[k] = 0;
   const long long ps = (long long)B.dqp * nghl;
   const T h5 = (T)0.5, two = (T)2;
 
-#define ACC(k, re, im)                                   \
-  {                                                      \
-    const T vr_ = red8(re), vi_ = red8(im);       \
-    if (bl == 0) { acc[2 * (k)][rl] += vr_; acc[2 * (k) + 1][rl] += vi_; } \
-  }
+#define ACC(k, re, im) { al[2 * (k)] += (re); al[2 * (k) + 1] += (im); }
 
   // ---------------- normal densities ----------------
   for (int ix = g; ix < B.nb; ix += G) {
@@ -857,11 +853,11 @@ __global__ void __launch_bounds__(256) k_density_fp64(DevBasis B, DensCall c0, D
     }
   }
 #undef ACC
-  __syncthreads();
   T* out = dpart + (((long long)p * 2 + call) * G + g) * (2 * ND) * nghl;
-  for (int e = threadIdx.x; e < 2 * ND * DRT; e += 256) {
-    const int k = e / DRT, rr = e % DRT;
-    if (r0 + rr < nghl) out[(long long)k * nghl + r0 + rr] = acc[k][rr];
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) {
+    const T v = red8(al[k]);
+    if (bl == 0 && rok) out[(long long)k * nghl + r] = v;
   }
 }
 
@@ -1912,34 +1908,51 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
 // ---------------------------------------------------------------------------
 // Green's function update: vout = G o (q*H + F); layout [P][Re X|Y, Im X|Y]
 // ---------------------------------------------------------------------------
-// corr[p] != 0 (increment step of the mixed form, H evaluated from X - X_anchor):
-// vout = G o (q*H) + radd[p], radd = g(X_anchor) evaluated in FP64
-__global__ void k_green(long long nxy, int P, const double* __restrict__ hqp, const double* __restrict__ fqp,
-                        const int* __restrict__ erow, const int* __restrict__ ecol,
-                        const double* __restrict__ E1, const double* __restrict__ E2,
-                        const double* __restrict__ wre, const double* __restrict__ wim, double quench,
+// the Green's function of the points flagged in mask, once per point (omega is fixed):
+// G = -1/(E1 + E2 -/+ w), X (e < nxy) with -w, Y with +w; gfn: [P][Re | Im][2*nxy]
+__global__ void k_green_prep(long long nxy, const int* __restrict__ erow, const int* __restrict__ ecol,
+                             const double* __restrict__ E1, const double* __restrict__ E2,
+                             const double* __restrict__ wre, const double* __restrict__ wim,
+                             double* __restrict__ gfn, const int* __restrict__ mask) {
+  const int p = blockIdx.y;
+  if (!mask[p]) return;
+  const long long n2 = 2 * nxy;
+  const double wr = wre[p], wi = wim[p];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n2; e += (long long)gridDim.x * blockDim.x) {
+    const double sgn = e < nxy ? -1.0 : 1.0;
+    const double dr = E1[erow[e]] + E2[ecol[e]] + sgn * wr, di = sgn * wi;
+    const double den = dr * dr + di * di;
+    gfn[(long long)p * 2 * n2 + e] = -dr / den;
+    gfn[(long long)p * 2 * n2 + n2 + e] = di / den;
+  }
+}
+
+// vout = G o (q*H + F), G from k_green_prep.  corr[p] != 0 (increment evaluation of the
+// mixed form): H is the FP32 field of X - X_anchor (hqp32) and vout = G o (q*H) + radd[p],
+// radd = g(X_anchor) evaluated in FP64
+__global__ void k_green(long long nxy, int P, const double* __restrict__ hqp, const float* __restrict__ hqp32,
+                        const double* __restrict__ fqp, const double* __restrict__ gfn, double quench,
                         double* __restrict__ vout, const int* __restrict__ active,
                         const int* __restrict__ corr, const double* __restrict__ radd,
                         const int* __restrict__ zeroh) {
   const int p = blockIdx.y;
   if (!active[p]) return;
   const long long n2 = 2 * nxy;
-  const double wr = wre[p], wi = wim[p];
   const bool cstep = corr && corr[p];
   const bool useh = hqp && !(zeroh && zeroh[p]);  // zeroh: H = 0 (the field of X = 0)
+  const long long o = (long long)p * 2 * n2;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n2; e += (long long)gridDim.x * blockDim.x) {
     double hr = 0.0, hi = 0.0;
-    if (useh) { hr = quench * hqp[(long long)p * 2 * n2 + e]; hi = quench * hqp[(long long)p * 2 * n2 + n2 + e]; }
+    if (useh) {
+      if (cstep) { hr = quench * (double)hqp32[o + e]; hi = quench * (double)hqp32[o + n2 + e]; }
+      else { hr = quench * hqp[o + e]; hi = quench * hqp[o + n2 + e]; }
+    }
     if (!cstep) hr += fqp[e];
-    // G = -1/(E1 + E2 -/+ w): X (e < nxy) uses -w, Y uses +w
-    const double sgn = e < nxy ? -1.0 : 1.0;
-    const double dr = E1[erow[e]] + E2[ecol[e]] + sgn * wr, di = sgn * wi;
-    const double den = dr * dr + di * di;
-    const double gr = -dr / den, gi = di / den;
+    const double gr = gfn[o + e], gi = gfn[o + n2 + e];
     double vr = gr * hr - gi * hi, vi = gr * hi + gi * hr;
-    if (cstep) { vr += radd[(long long)p * 2 * n2 + e]; vi += radd[(long long)p * 2 * n2 + n2 + e]; }
-    vout[(long long)p * 2 * n2 + e] = vr;
-    vout[(long long)p * 2 * n2 + n2 + e] = vi;
+    if (cstep) { vr += radd[o + e]; vi += radd[o + n2 + e]; }
+    vout[o + e] = vr;
+    vout[o + n2 + e] = vi;
   }
 }
 

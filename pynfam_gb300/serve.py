@@ -64,7 +64,7 @@ class ServeStats:
 
 def slot_bytes(nxy: int, broyden_m: int, mixed: bool) -> int:
     """Device memory of one solve slot (the per-point buffers of pnfam_gpu.cu)."""
-    f64 = 4 + 4 + 16 + 8 + 8 + 4 + 2 * 4 * max(broyden_m, 1)   # state, vout, T, rsp, hsp, hqp, df+dv
+    f64 = 4 + 4 + 16 + 8 + 8 + 4 + 4 + 2 * 4 * max(broyden_m, 1)   # state, vout, T, rsp, hsp, hqp, G, df+dv
     if mixed:
         f64 += 4 + 4 + 4 * 4                                     # anchor, its image; Broyden raw vectors
     f32 = (4 + 16 + 8 + 8 + 4) if mixed else 0
