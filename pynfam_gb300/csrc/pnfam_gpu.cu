@@ -149,6 +149,28 @@ static GemmTerm mkterm(const MatRef& A, const MatRef& B, double a_re, double a_i
 
 }  // namespace
 
+// pinned host memory: a copy between the device and pageable host memory makes the
+// host wait (device to pageable host returns only when the stream has reached it),
+// which would keep the engines of different contexts from overlapping on the GPU
+template <class T>
+struct PinBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t m) {
+    if (p && n >= m) return cudaSuccess;
+    release();
+    const cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&p), std::max<size_t>(m, 1) * sizeof(T));
+    if (e == cudaSuccess) n = m; else p = nullptr;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~PinBuf() { release(); }
+};
+
 struct pnfam_engine;
 struct pnfam_ctx {
   int dev = 0;
@@ -1010,6 +1032,11 @@ struct pnfam_engine {
   std::vector<int> pint, act32, act64, actlist;
   int herr = 0;
   std::vector<double> hsi, cpart;
+  // pinned staging of the per-evaluation copies: ints [active P | pint 6P | act64 P |
+  // act32 P | actlist P | err 1], doubles [wre P | wim P | si P | cpart], dmax [P]
+  PinBuf<int> pin_i;
+  PinBuf<double> pin_d;
+  PinBuf<unsigned long long> pin_u;
   double* hist = nullptr;   // optional [P][max_iter+1][3] (batch solve only)
   bool dirty_w = true;
   int pending = 0;          // an evaluation is in flight
@@ -1065,6 +1092,9 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->best.assign(P, 1e300); e->wre.assign(P, 0.0); e->wim.assign(P, 0.0); e->hdmax.assign(P, 0);
   e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
   e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
+  CK(e->pin_i.ensure((size_t)10 * P + 1));
+  CK(e->pin_d.ensure((size_t)3 * P + e->cpart.size()));
+  CK(e->pin_u.ensure((size_t)P));
   for (int k = 0; k < 8; ++k) c->stage_ms[k] = 0.0;
   for (int k = 0; k < 5; ++k) c->stage32_ms[k] = 0.0;
   c->pit64 = 0; c->pit32 = 0; c->launches = 0;
@@ -1181,11 +1211,19 @@ static int engine_launch(pnfam_engine* e) {
   int* d_zero = c->d_pint.p + 4 * P;
   int* d_fresh = c->d_pint.p + 5 * P;
   const dim3 vgrid((unsigned)std::min<long long>(2048, (N + 255) / 256), P);
-  CK(cudaMemcpyAsync(c->d_active.p, e->active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->d_pint.p, e->pint.data(), sizeof(int) * 6 * P, cudaMemcpyHostToDevice, c->stream));
+  // host-to-device copies through pinned staging (nothing of the previous evaluation
+  // is in flight: engine_finish waited for it)
+  int* pi_ = e->pin_i.p;
+  double* pd_ = e->pin_d.p;
+  std::memcpy(pi_, e->active.data(), sizeof(int) * P);
+  std::memcpy(pi_ + P, e->pint.data(), sizeof(int) * 6 * P);
+  CK(cudaMemcpyAsync(c->d_active.p, pi_, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_pint.p, pi_ + P, sizeof(int) * 6 * P, cudaMemcpyHostToDevice, c->stream));
   if (e->dirty_w) {
-    CK(cudaMemcpyAsync(c->d_wre.p, e->wre.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_wim.p, e->wim.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+    std::memcpy(pd_, e->wre.data(), sizeof(double) * P);
+    std::memcpy(pd_ + P, e->wim.data(), sizeof(double) * P);
+    CK(cudaMemcpyAsync(c->d_wre.p, pd_, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_wim.p, pd_ + P, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
     e->dirty_w = false;
   }
   const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
@@ -1201,7 +1239,8 @@ static int engine_launch(pnfam_engine* e) {
   int rc;
   bool split = false;
   if (!e->no_res) {
-    CK(cudaMemcpyAsync(c->d_act64.p, e->act64.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+    std::memcpy(pi_ + 7 * P, e->act64.data(), sizeof(int) * P);
+    CK(cudaMemcpyAsync(c->d_act64.p, pi_ + 7 * P, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
     // FP64 (anchor) evaluations of some points and FP32 increment evaluations of the
     // others use disjoint scratch and write disjoint rows of hqp: the FP64 ones run
     // on the second stream, joined before the Green's function (not when stages are timed)
@@ -1213,12 +1252,14 @@ static int engine_launch(pnfam_engine* e) {
     if (n64 && (rc = residual_t<double>(c, P, n64, c->d_act64.p, timed, split ? c->stream64 : c->stream))) return rc;
     if (split) CK(cudaEventRecord(c->evf[1], c->stream64));
     if (e->mixed) {
-      CK(cudaMemcpyAsync(c->d_act32.p, e->act32.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+      std::memcpy(pi_ + 8 * P, e->act32.data(), sizeof(int) * P);
+      CK(cudaMemcpyAsync(c->d_act32.p, pi_ + 8 * P, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
       if (n32) {
         e->actlist.clear();
         for (int p = 0; p < P; ++p)
           if (e->act32[p]) e->actlist.push_back(p);
-        CK(cudaMemcpyAsync(c->d_actlist.p, e->actlist.data(), sizeof(int) * n32, cudaMemcpyHostToDevice, c->stream));
+        std::memcpy(pi_ + 9 * P, e->actlist.data(), sizeof(int) * n32);
+        CK(cudaMemcpyAsync(c->d_actlist.p, pi_ + 9 * P, sizeof(int) * n32, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
         k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
                                                c->d_dmax.p);
@@ -1256,13 +1297,15 @@ static int engine_launch(pnfam_engine* e) {
     c->launches++;
     CK(cudaGetLastError());
   }
-  CK(cudaMemcpyAsync(e->hsi.data(), c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+  // device-to-host copies into pinned staging: the call returns at once and
+  // engine_finish picks the values up after its wait
+  CK(cudaMemcpyAsync(pd_ + 2 * P, c->d_si.p, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
   if (e->mixed)
-    CK(cudaMemcpyAsync(e->hdmax.data(), c->d_dmax.p, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost,
+    CK(cudaMemcpyAsync(e->pin_u.p, c->d_dmax.p, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost,
                        c->stream));
-  CK(cudaMemcpyAsync(e->cpart.data(), c->d_cpart.p, sizeof(double) * e->cpart.size(), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(pd_ + 3 * P, c->d_cpart.p, sizeof(double) * e->cpart.size(), cudaMemcpyDeviceToHost,
                      c->stream));
-  CK(cudaMemcpyAsync(&e->herr, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(pi_ + 10 * P, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   if (timed) toc(7);
   e->pending = 1;
   return PNFAM_OK;
@@ -1275,6 +1318,13 @@ static int engine_finish(pnfam_engine* e) {
   pnfam_ctx* c = e->c;
   CK(cudaStreamSynchronize(c->stream));
   e->pending = 0;
+  {
+    const int P = e->P;
+    std::memcpy(e->hsi.data(), e->pin_d.p + 2 * P, sizeof(double) * P);
+    std::memcpy(e->cpart.data(), e->pin_d.p + 3 * P, sizeof(double) * e->cpart.size());
+    if (e->mixed) std::memcpy(e->hdmax.data(), e->pin_u.p, sizeof(unsigned long long) * P);
+    e->herr = e->pin_i.p[10 * P];
+  }
   if (e->herr) {
     cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream);
     e->herr = 0;
