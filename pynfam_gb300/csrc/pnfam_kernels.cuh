@@ -1689,7 +1689,7 @@ struct HTaskTC {
   long long ooff;
   long long tphi;  // floats: the pre-split row basis functions of rows a0..a0+na of block ix
 };
-enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 4, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
+enum { HTC_K = 32, HTC_MAXB = 64, HTC_MAXN = 128, HTC_MAXPG = 8, HTC_PROD = 256, HTC_THREADS = HTC_PROD + 32 };
 // pre-split B operand of one row tile (rows a0..a0+na of block ix): for component q
 // and mesh chunk rc (32 points), [hi | lo][np x 32] at off + (q * nrc + rc) * 64 * np
 struct HPTile { int ix, a0, na, np; long long off; };
@@ -1712,10 +1712,10 @@ __global__ void __launch_bounds__(256) k_hproj_bsplit(DevBasisT<float> B, const 
 }
 
 // dynamic shared memory for tiles of at most npmax output rows: two stages of
-// A (128 x 32, hi and lo) and B (npmax x 32, hi and lo), then the field tensor of
-// two chunks [2][pg][2 sb][5 iz][2 re/im][32 r]
+// A (128 x 32, hi and lo) and B (npmax x 32, hi and lo), then the field tensor
+// of the current chunk [pg][2 sb][5 iz][2 re/im][32 r]
 __host__ __device__ constexpr size_t hproj_tc_smem_bytes(int npmax) {
-  return (size_t)(2 * (2 * 128 * HTC_K + 2 * npmax * HTC_K) + 2 * HTC_MAXPG * 2 * 5 * 2 * HTC_K) * sizeof(float);
+  return (size_t)(2 * (2 * 128 * HTC_K + 2 * npmax * HTC_K) + HTC_MAXPG * 2 * 5 * 2 * HTC_K) * sizeof(float);
 }
 
 // grid (ntasks, point groups); HTC_THREADS threads; dynamic smem hproj_tc_smem_bytes(npmax)
@@ -1733,7 +1733,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
   extern __shared__ __align__(16) unsigned char smraw[];
   float* stage_base = reinterpret_cast<float*>(smraw);
   const int stage_floats = 2 * 128 * HTC_K + 2 * npmax * HTC_K;
-  float* sMF = stage_base + 2 * stage_floats;   // [2 chunks][pg][2 sb][5 iz][2 re/im][32 r]
+  float* sMF = stage_base + 2 * stage_floats;   // [pg][2 sb][5 iz][2 re/im][32 r]
   __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -1781,30 +1781,6 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
       a_oim[it] = tc::cm_off(64 + j, 4 * r4, 128);
     }
     int lc0 = -1, lc1 = -1;   // thread 0: last chunk copied into stage 0, stage 1
-    // the field tensor of a chunk (component q, 32 mesh points) of every point of the
-    // group, shared by all rows: copied with cp.async into one of two buffers while
-    // the previous chunk's rows are generated
-    const bool mf_vec = (nghl & 3) == 0;   // 16-byte rows; otherwise plain loads
-    auto stage_mf = [&](int cn) {
-      const int qn = cn % nc, rn = (cn / nc) * HTC_K;
-      float* dst = sMF + (cn & 1) * HTC_MAXPG * 2 * 5 * 2 * HTC_K;
-      for (int e = tid; e < npg * 160; e += HTC_PROD) {
-        const int r4 = e & 7, ri = (e >> 3) & 1, iz = (e >> 4) % 5, sbi = (e / 80) & 1, pi = e / 160;
-        float* d = &dst[((((pi * 2 + sbi) * 5 + iz) * 2 + ri) * HTC_K) + 4 * r4];
-        const int sb = sbi == 0 ? 1 : -1;
-        const int slot = Th.mode == 0 ? mfslot(qn, iz < nc ? iz : 0, Th.sa, sb) : 100 + (Th.sa < 0 ? 2 : 0) + sbi;
-        const float* src = mfbase + (long long)spt[pi] * 2 * NMF * 2 * nghl + ((long long)slot * 2 + ri) * nghl +
-                           rn + 4 * r4;
-        const bool in = iz < nc && rn + 4 * r4 < nghl;
-        if (mf_vec) {
-          tc::cp_async16(d, in ? src : mfbase, in ? 16u : 0u);
-        } else {
-          *reinterpret_cast<float4*>(d) = ld_row4(src - (rn + 4 * r4), rn + 4 * r4, nghl, iz < nc);
-        }
-      }
-      tc::cp_async_commit();
-    };
-    stage_mf(0);
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !abort_flag && !tc::mbar_wait(&empty_bar[st], ((c >> 1) - 1) & 1)) abort_flag = 1;
@@ -1822,12 +1798,22 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
         issued = true;
         if (st == 0) lc0 = c; else lc1 = c;
       }
-      // this thread's copies of chunk c's field have landed; after the barrier all of
-      // them are visible, and every thread is done with the other buffer (chunk c - 1)
-      tc::cp_async_wait_all();
+      // the field tensor of this chunk (component q, mesh points r0..r0+31) of every
+      // point of the group, shared by all rows; the barriers keep one chunk's copy
+      // from being overwritten while another chunk's rows are generated
       asm volatile("bar.sync 1, %0;" ::"r"(HTC_PROD) : "memory");
-      if (c + 1 < nchunk) stage_mf(c + 1);
-      const float* sMFc = sMF + (c & 1) * HTC_MAXPG * 2 * 5 * 2 * HTC_K;
+      for (int e = tid; e < npg * 2 * 5 * 2 * 8; e += HTC_PROD) {
+        const int r4 = e & 7, ri = (e >> 3) & 1, iz = (e >> 4) % 5, sbi = (e / 80) & 1, pi = e / 160;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (iz < nc) {
+          const int sb = sbi == 0 ? 1 : -1;
+          const int slot = Th.mode == 0 ? mfslot(q, iz, Th.sa, sb) : 100 + (Th.sa < 0 ? 2 : 0) + sbi;
+          const float* mp = mfbase + (long long)spt[pi] * 2 * NMF * 2 * nghl;
+          v = ld_row4(mp + ((long long)slot * 2 + ri) * nghl, r0 + 4 * r4, nghl, true);
+        }
+        *reinterpret_cast<float4*>(&sMF[((((pi * 2 + sbi) * 5 + iz) * 2 + ri) * HTC_K) + 4 * r4]) = v;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(HTC_PROD) : "memory");
       if (!abort_flag) {
         // A: hpsi rows, Re at j, Im at 64 + j, four mesh points per item
 #pragma unroll
@@ -1840,7 +1826,7 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
               for (int iz = 0; iz < 5; ++iz)
                 if (iz < nc) fz[it][iz] = ld_row4(B.phi + iz * ps + (long long)a_row[it] * nghl, r, nghl, true);
             }
-            const float* m = &sMFc[a_m[it]];
+            const float* m = &sMF[a_m[it]];
 #pragma unroll
             for (int iz = 0; iz < 5; ++iz)
               if (iz < nc) {
@@ -1855,7 +1841,6 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
       tc::fence_async_smem();
       if (!issued) tc::mbar_arrive(&full_bar[st]);
     }
-    tc::cp_async_wait_all();
     // no copy may still be landing when the memory is reused (the last two chunks
     // are the only ones that can be in flight)
     if (tid == 0) {

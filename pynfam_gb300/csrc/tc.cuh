@@ -142,15 +142,6 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float (&va)
   for (int i = 0; i < 8; ++i) { va[i] = __uint_as_float(r[i]); vb[i] = __uint_as_float(q[i]); }
 }
 
-// 16-byte asynchronous copy global -> shared (both 16-byte aligned); src_bytes = 0
-// fills the destination with zeros
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 }  // namespace tc
 
 // operand staging helpers: four consecutive floats of one row (mesh points r..r+3 of
