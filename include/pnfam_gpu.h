@@ -152,6 +152,9 @@ int pnfam_gpu_engine_launch(pnfam_engine_t* engine);
 int pnfam_gpu_engine_finish(pnfam_engine_t* engine, int maxout, long long* tags, double* re_S,
                             double* im_S, int* iters, double* si, int* nout);
 int pnfam_gpu_engine_active(const pnfam_engine_t* engine);
+/* 1 when pnfam_gpu_engine_finish would not wait (no evaluation in flight, or the
+ * one in flight has completed), 0 while it runs, minus an error code */
+int pnfam_gpu_engine_ready(const pnfam_engine_t* engine);
 void pnfam_gpu_engine_free(pnfam_engine_t* engine);
 
 /*

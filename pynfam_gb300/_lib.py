@@ -16,7 +16,7 @@ LIBPATH = os.path.join(HERE, "libpnfam_gb300.so")
 EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam_gpu_calc_hamiltonian",
            "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error",
            "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
-           "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_free",
+           "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_ready", "pnfam_gpu_engine_free",
            "pnfam_gpu_calc_hamiltonian_mixed")
 
 ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENONFINITE", 5: "ESTATE"}
@@ -88,6 +88,8 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_engine_finish.restype = C.c_int
     lib.pnfam_gpu_engine_active.argtypes = [C.c_void_p]
     lib.pnfam_gpu_engine_active.restype = C.c_int
+    lib.pnfam_gpu_engine_ready.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_engine_ready.restype = C.c_int
     lib.pnfam_gpu_engine_free.argtypes = [C.c_void_p]
     lib.pnfam_gpu_engine_free.restype = None
     _lib = lib

@@ -252,6 +252,7 @@ struct pnfam_ctx {
   cudaEvent_t evt[2] = {nullptr, nullptr};   // whole-solve device time
   cudaStream_t stream64 = nullptr;           // FP64 anchor evaluations beside the FP32 increments
   cudaEvent_t evf[2] = {nullptr, nullptr};   // fork to / join from stream64
+  cudaEvent_t evd = nullptr;                 // end of the engine's evaluation in flight
   double stage_ms[8] = {0};     // FP64 evaluations (0-4) and the common stages (5-7)
   double stage32_ms[5] = {0};   // FP32 evaluations of the mixed form
   double total_ms = 0.0;
@@ -292,6 +293,7 @@ struct pnfam_ctx {
     if (evt[1]) cudaEventDestroy(evt[1]);
     if (evf[0]) cudaEventDestroy(evf[0]);
     if (evf[1]) cudaEventDestroy(evf[1]);
+    if (evd) cudaEventDestroy(evd);
     if (stream64) cudaStreamDestroy(stream64);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -875,7 +877,8 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
       cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream64, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->evf[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: stream/event creation failed");
   }
@@ -1306,6 +1309,7 @@ static int engine_launch(pnfam_engine* e) {
   CK(cudaMemcpyAsync(pd_ + 3 * P, c->d_cpart.p, sizeof(double) * e->cpart.size(), cudaMemcpyDeviceToHost,
                      c->stream));
   CK(cudaMemcpyAsync(pi_ + 10 * P, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaEventRecord(c->evd, c->stream));
   if (timed) toc(7);
   e->pending = 1;
   return PNFAM_OK;
@@ -1473,6 +1477,15 @@ extern "C" int pnfam_gpu_engine_finish(pnfam_engine_t* e, int maxout, long long*
 }
 
 extern "C" int pnfam_gpu_engine_active(const pnfam_engine_t* e) { return e ? engine_nactive(e) : 0; }
+
+extern "C" int pnfam_gpu_engine_ready(const pnfam_engine_t* e) {
+  if (!e || !e->c) return -PNFAM_EINVAL;
+  if (!e->pending) return 1;
+  const cudaError_t q = cudaEventQuery(e->c->evd);
+  if (q == cudaSuccess) return 1;
+  if (q == cudaErrorNotReady) return 0;
+  return -PNFAM_ECUDA;
+}
 
 extern "C" void pnfam_gpu_engine_free(pnfam_engine_t* e) {
   if (!e) return;

@@ -10,9 +10,13 @@ engines together so that their work overlaps on the GPU.  Engines are created
 while their estimated device memory fits the budget and released when their
 queue is empty and another pair needs the memory.
 
-The scheduler only talks to objects with the Engine interface
-(``slots``, ``active``, ``admit``, ``launch``, ``finish``, ``close``), so it is
-tested on the host with a fake engine.
+Each engine steps at its own pace: ``launch`` only enqueues an evaluation, and the
+loop takes an engine's results as soon as ``ready`` says they are there, admits new
+points into its free slots and launches it again, so an engine with a few slow
+points left is not held to the pace of a busy one, and the engines' work overlaps on
+the GPU.  The scheduler only talks to objects with the Engine interface (``slots``,
+``active``, ``admit``, ``launch``, ``ready``, ``finish``, ``close``), so it is tested
+on the host with a fake engine.
 """
 from __future__ import annotations
 
@@ -53,7 +57,7 @@ class ServeStats:
     points: int = 0
     converged: int = 0
     wall: float = 0.0
-    steps: int = 0
+    steps: int = 0             # evaluations launched (all engines)
     peak_engines: int = 0
     peak_bytes: int = 0
     latencies: list = field(default_factory=list)
@@ -72,16 +76,18 @@ def slot_bytes(nxy: int, broyden_m: int, mixed: bool) -> int:
 
 
 class Server:
-    """engine_factory(key, slots) -> Engine; engine_bytes(key, slots) -> int."""
+    """engine_factory(key, slots) -> Engine; engine_bytes(key, slots) -> int; poll: the
+    wait (s) between looks at the engines in flight when none has finished."""
 
     def __init__(self, engine_factory, engine_bytes, slots: int, budget_bytes: int,
-                 clock=time.perf_counter, sleep=time.sleep):
+                 clock=time.perf_counter, sleep=time.sleep, poll: float = 5e-5):
         self.factory = engine_factory
         self.bytes = engine_bytes
         self.slots = int(slots)
         self.budget = int(budget_bytes)
         self.clock = clock
         self.sleep = sleep
+        self.poll = float(poll)
 
     def run(self, requests):
         reqs = sorted(requests, key=lambda r: r.arrival)
@@ -89,11 +95,20 @@ class Server:
         queues = collections.OrderedDict()     # key -> deque of (rid, index, omega, arrival)
         engines = collections.OrderedDict()    # key -> engine
         used = {}                              # key -> bytes
+        inflight = collections.OrderedDict()   # key -> engine with an evaluation in flight
         meta = {}                              # tag -> (rid, index, omega, arrival, admitted)
         outcomes = []
         stats = ServeStats(points=sum(len(r.omegas) for r in reqs))
         tag = 0
         t0 = self.clock()
+
+        def collect(key):
+            eng = inflight.pop(key)
+            for res in eng.finish():
+                rid, idx, w, arr, adm = meta.pop(res.tag)
+                done = self.clock() - t0
+                outcomes.append(PointOutcome(rid, idx, w, res.S, res.iters, res.si, arr, adm, done))
+
         while True:
             now = self.clock() - t0
             while arrivals and arrivals[0].arrival <= now:
@@ -101,6 +116,10 @@ class Server:
                 q = queues.setdefault(r.key, collections.deque())
                 for i, w in enumerate(np.atleast_1d(r.omegas)):
                     q.append((r.rid, i, complex(w), r.arrival))
+            # every engine steps at its own pace: results of the evaluations that have
+            # completed are taken as they come, without waiting for the other engines
+            for key in [k for k, e in inflight.items() if e.ready()]:
+                collect(key)
             # engines for queued keys, within the memory budget (idle engines make room)
             for key, q in queues.items():
                 if not q or key in engines:
@@ -109,7 +128,7 @@ class Server:
                 for k2 in list(engines):
                     if sum(used.values()) + need <= self.budget:
                         break
-                    if engines[k2].active == 0 and not queues.get(k2):
+                    if k2 not in inflight and engines[k2].active == 0 and not queues.get(k2):
                         engines.pop(k2).close()
                         used.pop(k2)
                 if sum(used.values()) + need <= self.budget or not engines:
@@ -117,36 +136,34 @@ class Server:
                     used[key] = need
             stats.peak_engines = max(stats.peak_engines, len(engines))
             stats.peak_bytes = max(stats.peak_bytes, sum(used.values()))
-            # admit into free slots
+            # admit into the free slots of the idle engines, and launch them
             for key, eng in engines.items():
+                if key in inflight:
+                    continue
                 q = queues.get(key)
                 free = eng.slots - eng.active
-                if not q or free <= 0:
-                    continue
-                batch = [q.popleft() for _ in range(min(free, len(q)))]
-                tags = np.arange(tag, tag + len(batch), dtype=np.int64)
-                adm = self.clock() - t0
-                for t, b in zip(tags, batch):
-                    meta[int(t)] = b + (adm,)
-                tag += len(batch)
-                n = eng.admit(np.array([b[2] for b in batch]), tags)
-                if n != len(batch):
-                    raise RuntimeError(f"engine admitted {n} of {len(batch)} points")
-            running = [eng for eng in engines.values() if eng.active > 0]
-            if not running:
+                if q and free > 0:
+                    batch = [q.popleft() for _ in range(min(free, len(q)))]
+                    tags = np.arange(tag, tag + len(batch), dtype=np.int64)
+                    adm = self.clock() - t0
+                    for t, b in zip(tags, batch):
+                        meta[int(t)] = b + (adm,)
+                    tag += len(batch)
+                    n = eng.admit(np.array([b[2] for b in batch]), tags)
+                    if n != len(batch):
+                        raise RuntimeError(f"engine admitted {n} of {len(batch)} points")
+                if eng.active > 0:
+                    eng.launch()       # enqueues one evaluation and returns
+                    inflight[key] = eng
+                    stats.steps += 1
+            if not inflight:
                 if not arrivals and not any(queues.values()):
                     break
                 if arrivals and not any(queues.values()):
                     self.sleep(max(0.0, arrivals[0].arrival - (self.clock() - t0)))
                 continue
-            for eng in running:          # enqueue one iteration on every engine, then wait for all
-                eng.launch()
-            stats.steps += 1
-            for eng in running:
-                for res in eng.finish():
-                    rid, idx, w, arr, adm = meta.pop(res.tag)
-                    done = self.clock() - t0
-                    outcomes.append(PointOutcome(rid, idx, w, res.S, res.iters, res.si, arr, adm, done))
+            if not any(e.ready() for e in inflight.values()):
+                self.sleep(self.poll)   # nothing to take yet
         stats.wall = self.clock() - t0
         stats.converged = sum(1 for o in outcomes if o.iters >= 0)
         stats.latencies = [o.latency for o in outcomes]

@@ -204,6 +204,13 @@ class Engine:
     def launch(self):
         _lib.check(self.lib.pnfam_gpu_engine_launch(self.eng))
 
+    def ready(self) -> bool:
+        """True when finish() would not wait for the device."""
+        r = int(self.lib.pnfam_gpu_engine_ready(self.eng))
+        if r < 0:
+            _lib.check(-r)
+        return r == 1
+
     def finish(self):
         out = []
         while True:

@@ -60,6 +60,9 @@ class FakeEngine:
         assert not self.launched and self.pts
         self.launched = True
 
+    def ready(self):
+        return True
+
     def finish(self):
         assert self.launched
         self.launched = False
@@ -136,12 +139,52 @@ def test_memory_budget_limits_resident_engines():
     assert order == ["create", "close", "create", "close", "create", "close"]
 
 
-def test_two_engines_step_together_within_budget():
+def test_two_engines_are_resident_within_budget():
     clock, log = FakeClock(), []
     reqs = [Request(0, "a", np.array([4.5, 4.5]) + 0.1j), Request(1, "b", np.array([4.5, 4.5]) + 0.1j)]
     out, st = make_server(2, 10, 5, clock, log).run(reqs)
     assert st.peak_engines == 2
-    assert st.steps == fake_iters(4.5 + 0.1j)   # both engines advance in the same steps
+    assert st.steps == 2 * fake_iters(4.5 + 0.1j)   # evaluations launched, both engines
+    assert len(out) == 4
+
+
+class TimedEngine(FakeEngine):
+    """An evaluation takes dt of (fake) device time after its launch: ready() is false
+    until then, and finish() waits for it."""
+
+    def launch(self):
+        super().launch()
+        self.t_launch = self.clock.t
+
+    def ready(self):
+        return not self.launched or self.clock.t >= self.t_launch + self.dt
+
+    def finish(self):
+        assert self.launched
+        self.launched = False
+        self.clock.t = max(self.clock.t, self.t_launch + self.dt)
+        out = []
+        for sl in list(self.pts):
+            pt = self.pts[sl]
+            pt[2] -= 1
+            if pt[2] == 0:
+                out.append(Res(pt[0], fake_result(self.key, pt[1]), fake_iters(pt[1]), 1e-9))
+                del self.pts[sl]
+        return out
+
+
+def test_engines_step_at_their_own_pace():
+    """A point on a fast engine is not held to the pace of a slow one."""
+    clock, log = FakeClock(), []
+    dts = {"slow": 1.0, "fast": 0.1}
+    srv = Server(lambda key, n: TimedEngine(key, n, clock, log, dt=dts[key]), lambda key, n: 1, slots=2,
+                 budget_bytes=10, clock=clock, sleep=clock.sleep, poll=0.01)
+    w = np.array([2.0 + 0.1j])   # fake_iters = 5 evaluations
+    out, st = srv.run([Request(0, "slow", w), Request(1, "fast", w)])
+    by = {o.rid: o for o in out}
+    assert by[1].done == pytest.approx(5 * 0.1, abs=0.05)
+    assert by[0].done == pytest.approx(5 * 1.0, abs=0.05)
+    assert by[1].iters == by[0].iters == 5
 
 
 def test_slot_bytes_grow_with_history_and_precision():
