@@ -1448,7 +1448,13 @@ extern "C" int pnfam_gpu_engine_launch(pnfam_engine_t* e) {
   if (!e->c) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: the context was freed");
   if (e->pending) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: an evaluation is in flight");
   const int rc = engine_launch(e);
-  if (rc) { cudaStreamSynchronize(e->c->stream); e->pending = 0; g_err = "pnfam_gpu_engine_launch: " + g_err; }
+  if (rc) {
+    // nothing of a failed launch may stay in flight (the FP64 anchors' stream included)
+    cudaStreamSynchronize(e->c->stream64);
+    cudaStreamSynchronize(e->c->stream);
+    e->pending = 0;
+    g_err = "pnfam_gpu_engine_launch: " + g_err;
+  }
   return rc;
 }
 
