@@ -52,6 +52,9 @@ INTERACTION = {"interaction_name": "SKOP", "require_self_consistency": True, "re
 SOLVER = {"max_iter": 300, "convergence_epsilon": 1e-7, "broyden_history_size": 50}
 OPERATORS = (("GT", 0), ("GT", 1))
 MIXED_EPS = 1e-9
+# DRAM traffic of the FP32 stages per point-evaluation, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum of one 8-point launch / 8)
+TRAFFIC_PER_POINT = {"field_projection_fp32": 14.6e6, "density_fp32": 16.3e6}
 REL = 1e-6
 METRIC = "converged FAM omega-points/s at N_sh=16 within 1e-6 rel err; p50/p99 point latency"
 
@@ -404,7 +407,11 @@ def run_gpu(args):
             "gpu_launches": launches,
             "stages_ms": {k: round(v, 3) for k, v in stages.items()},
             "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None, "peak_source": src,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": TRAFFIC_PER_POINT.get(dom),
+                         "traffic_unit": "DRAM bytes read + written per point-evaluation, from one ncu capture of "
+                                         "an 8-point launch (profiles/k_density_tc2_k_hproj_tc_nsh16.md)",
+                         "peak_source": src,
                          "note": "achieved = algorithmic FLOPs of the stage over its FP32 point-evaluations / "
                                  "stage device time; 3xTF32 issues three MMAs per product"},
             "clocks": ck}
