@@ -94,10 +94,10 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, gpu_index):
+        import tempfile
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"pnfam_gb300_clocks_{os.getpid()}.csv")
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={gpu_index}",
@@ -173,10 +173,10 @@ def signature(P, operators=OPERATORS):
             "interaction": INTERACTION}
 
 
-def fixed_point(cases, omegas, P):
+def fixed_point(cases, omegas, P, out_dir="."):
     """FP64 fixed point (epsilon 1e-12) of every (operator, omega): from the
     committed file when it matches this workload, else computed here (untimed)
-    and written to gpurun_out/ for committing."""
+    and written to out_dir (--out-dir) for committing."""
     sig = signature(P)
     try:
         with open(FIXED_POINT) as fh:
@@ -200,8 +200,8 @@ def fixed_point(cases, omegas, P):
         out[(name, k)] = S
         rec.append({"operator": [name, k], "S": [[float(z.real), float(z.imag)] for z in S],
                     "iters": r.iters.tolist()})
-    path = os.path.join(ROOT, "gpurun_out", os.path.basename(FIXED_POINT))
-    os.makedirs(os.path.dirname(path), exist_ok=True)
+    path = os.path.join(out_dir, os.path.basename(FIXED_POINT))
+    os.makedirs(out_dir, exist_ok=True)
     with open(path, "w") as fh:
         json.dump({"signature": sig, "how": "FP64 form, epsilon 1e-12, max_iter 1000 (bench.py)",
                    "results": rec}, fh)
@@ -296,7 +296,7 @@ def run_gpu(args):
     P = len(omegas)
     R = args.requests
     npts = P * len(OPERATORS) * R
-    ref, ref_src = fixed_point(cases, omegas, args.points)
+    ref, ref_src = fixed_point(cases, omegas, args.points, args.out_dir)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
@@ -428,7 +428,7 @@ def run_gpu(args):
 
 
 def run_serve_stream(args):
-    """Serving stream (the BASELINE serving configuration, scaled by --stream-scale):
+    """Serving stream (the serving configuration of many nuclei and bases, scaled by --stream-scale):
     nuclei drawn (seeded) from the three recorded ground states (40S, 116Kr, 162Gd)
     re-diagonalised in a basis of N_sh drawn from --nsh, each requesting GT- K = 0
     and K = 1 strengths on a CIRCLE contour of 40-200 points (times the scale);
@@ -549,6 +549,7 @@ def main():
     ap.add_argument("--stream-slots", type=int, default=32, help="serve-stream: slots per engine")
     ap.add_argument("--stream-seed", type=int, default=0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--out-dir", default=".", help="where a newly computed FP64 fixed point is written")
     ap.add_argument("--solve-only", action="store_true",
                     help="one operator, batch solves only (no serving, e2e or CPU legs); used for kernel profiling")
     args = ap.parse_args()
