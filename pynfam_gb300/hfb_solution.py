@@ -328,21 +328,46 @@ def diagonalise(h: HelData, hd, it: str, tz: float) -> QPSolution:
                       [e[3] for e in eig], final_ala)
 
 
-def local_density(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float) -> np.ndarray:
-    """rho(r) of one isospin from the final quasiparticles (DENSIT, T=0)."""
-    tro = np.zeros(h.ngh * h.ngl)
+def local_densities(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float):
+    """rho(r), tau(r) and the Laplacian of rho(r) of one isospin from the final
+    quasiparticles: DENSIT at T = 0 without blocking (hfbtho_solver.f90:4318-4734).
+    Per block and pairing-window quasiparticle k, with f_up/down = sum_i V_ik phi_i
+    over the spin-up/down basis states and Lambda_up/down = Omega -/+ 1/2:
+    rho ~ f_u^2 + f_d^2; tau ~ (Lambda_u y f_u)^2 + (Lambda_d y f_d)^2 + |grad f|^2;
+    Laplacian ~ 2 (f_u Lap f_u + f_d Lap f_d + |grad f|^2).  The sums are
+    normalised to the particle number and freed of the quadrature weights."""
+    nghl = h.ngh * h.ngl
+    tro = np.zeros(nghl); ttau = np.zeros(nghl); tdro = np.zeros(nghl)
+    y2 = mb.y * mb.y
     start = 0
     for ib, nd in enumerate(h.ID):
         nd = int(nd)
         ns = h.ns[start:start + nd]
-        q = mb.qhla[start:start + nd]
+        up, dn = ns > 0, ns < 0
         V = qp.V[ib][:, qp.active[ib]]
-        fu = V[ns > 0].T @ q[ns > 0]
-        fd = V[ns < 0].T @ q[ns < 0]
+        Vu, Vd = V[up].T, V[dn].T
+        sl = slice(start, start + nd)
+
+        def comp(a):
+            a = a[sl]
+            return Vu @ a[up], Vd @ a[dn]
+        fu, fd = comp(mb.qhla)
+        fur, fdr = comp(mb.fi1r)
+        fuz, fdz = comp(mb.fi1z)
+        fu2, fd2 = comp(mb.fi2d)
+        tw = np.sum(fur * fur + fdr * fdr + fuz * fuz + fdz * fdz, axis=0)
         tro += np.sum(fu * fu + fd * fd, axis=0)
+        ttau += mb.xlam[ib] ** 2 * y2 * np.sum(fu * fu, axis=0) + mb.xlap[ib] ** 2 * y2 * np.sum(fd * fd, axis=0) + tw
+        tdro += np.sum(fu * fu2 + fd * fd2, axis=0) + tw
         start += nd
     s = 2.0 * tro.sum()
-    return tro * mb.wdcori * (2.0 * tz / s)
+    wgt = mb.wdcori * (2.0 * tz / s)
+    return tro * wgt, ttau * wgt, tdro * (2.0 * wgt)
+
+
+def local_density(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float) -> np.ndarray:
+    """rho(r) of one isospin from the final quasiparticles (DENSIT, T=0)."""
+    return local_densities(h, mb, qp, tz)[0]
 
 
 # ----------------------------------------------------------------------------
@@ -388,6 +413,10 @@ class HFBSolution:
     rho_n: np.ndarray       # [nghl] local densities (for couplings)
     rho_p: np.ndarray
     hel: HelData
+    tau_n: np.ndarray = None    # [nghl] kinetic densities (two-body-current fields)
+    tau_p: np.ndarray = None
+    d2rho_n: np.ndarray = None  # [nghl] Laplacian of the densities
+    d2rho_p: np.ndarray = None
 
     @property
     def dqp(self) -> int:
@@ -412,8 +441,8 @@ def load_hfb_solution(path) -> HFBSolution:
 def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution) -> HFBSolution:
     """The pnFAM view of Omega>0 quasiparticles (hfbtho_solution.f90:164-459): TR
     doubling, spin sort inside each block, pairing window."""
-    rho_n = local_density(h, mb, qpn, float(h.N))
-    rho_p = local_density(h, mb, qpp, float(h.Z))
+    rho_n, tau_n, d2rho_n = local_densities(h, mb, qpn, float(h.N))
+    rho_p, tau_p, d2rho_p = local_densities(h, mb, qpp, float(h.Z))
 
     nbh = len(h.ID)
     nb = 2 * nbh
@@ -471,4 +500,4 @@ def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution) -> HFB
     En, Un, Vn = doubled(qpn)
     return HFBSolution(h.Z, h.N, h.n00, nb, db, isstart, nr, nz, nl, ns, npar, num_up,
                        h.ngh * h.ngl, wf, wfdr, wfdz, wfdp, wfd2_all, y, mb.z, mb.wdcori,
-                       Ep, En, Up, Vp, Un, Vn, rho_n, rho_p, h)
+                       Ep, En, Up, Vp, Un, Vn, rho_n, rho_p, h, tau_n, tau_p, d2rho_n, d2rho_p)

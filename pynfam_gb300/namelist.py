@@ -11,6 +11,8 @@ from __future__ import annotations
 
 import re
 
+import numpy as np
+
 GROUPS = ("general", "ext_field", "interaction", "solver")
 
 
@@ -26,7 +28,8 @@ def defaults() -> dict:
         "ext_field": {"beta_type": "-", "operator_k": 0, "operator_name": "F",
                       "compute_crossterms": False, "two_body_current_mode": 0,
                       "two_body_current_usep": False,
-                      "two_body_current_lecs": [-3.4, 5.4, 0.0]},
+                      # default-real literals in the reference (pnfam_setup.f90:189-191)
+                      "two_body_current_lecs": [float(np.float32(-3.4)), float(np.float32(5.4)), 0.0]},
         "solver": {"broyden_history_size": 50, "convergence_epsilon": 1.0e-7, "max_iter": 200,
                    "energy_shift_prot": 0.0, "energy_shift_neut": 0.0,
                    "quench_residual_int": 1.0},

@@ -5,7 +5,8 @@ Usage (what pynfam's fortProcess runs, pynfam/fortran/pnfam_run.py:140-167):
     pnfam_main.x [namelist]        # default: pnfam_NAMELIST.dat
 
 Reads the namelist (&general &ext_field &interaction &solver,
-pnfam_setup.f90:232-268) and ``hfbtho_output.hel`` from the working
+pnfam_setup.f90:232-268), ``hfbtho_output.hel`` and, for the finite-range
+two-body-current modes, ``<fam_output_filename>.tbc`` from the working
 directory, solves the point on the GPU and writes ``<fam_output_filename>.dat``
 (pnfam_txtoutput.f90).  On any error it writes the message to the log and to
 stderr, writes no result table and exits with status 1; pynfam treats
@@ -37,7 +38,8 @@ def load_ground_state(hel_path: str):
     key = None
     if cdir:
         with open(hel_path, "rb") as fh:
-            key = hashlib.sha256(fh.read()).hexdigest()
+            # the tag changes whenever the cached HFBSolution gains fields
+            key = hashlib.sha256(b"hfb-solution-2\0" + fh.read()).hexdigest()
         p = os.path.join(cdir, key + ".pkl")
         if os.path.exists(p):
             try:

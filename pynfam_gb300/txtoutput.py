@@ -69,6 +69,11 @@ def header(log: Log, nml: dict, case, nshells: int):
     log.write(" " + _center("pnFAM solver details", w))
     log.write(" " + "-" * w)
     log.write(f" Operator:                        {e['operator_name']}{e['beta_type']}  K={e['operator_k']:2d}")
+    mode = int(e.get("two_body_current_mode", 0) or 0)
+    log.write(f" Two-body current mode (use_p):   {mode} ({1 if e.get('two_body_current_usep') else 0})")
+    if mode != 0:
+        lecs = " ".join(f"{float(x):+8.4f}" for x in e["two_body_current_lecs"])
+        log.write(f"   LECs (c3, c4, cd):             {lecs}")
     xt = ", ".join(x.label for x in case.G) if case.G else "None"
     log.write(f" Compute cross-terms:             {'Yes' if e['compute_crossterms'] else 'No'}")
     log.write(f"   Cross-terms computed:          {xt}")

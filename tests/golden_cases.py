@@ -29,6 +29,11 @@ def namelist_for(case, point):
     p = point["namelist"]
     for k in ("operator_name", "operator_k", "beta_type", "compute_crossterms"):
         nml["ext_field"][k] = p[k]
+    for k in ("two_body_current_mode", "two_body_current_usep", "two_body_current_lecs"):
+        if k in p:
+            nml["ext_field"][k] = p[k]
+    if "fam_output_filename" in p:
+        nml["general"]["fam_output_filename"] = p["fam_output_filename"]
     for k in ("max_iter", "convergence_epsilon", "broyden_history_size", "quench_residual_int"):
         nml["solver"][k] = p[k]
     nml["general"]["real_eqrpa"] = p["real_eqrpa"]
@@ -37,8 +42,14 @@ def namelist_for(case, point):
 
 
 def case_for(case, op, index=0):
-    pt = golden(case)["operators"][op][index]
-    return setup_case(namelist_for(case, pt), None, hfb=hfb(case)), pt
+    """Solver inputs of a recorded point; two-body-current cases read their
+    cached finite-range fields from tests/golden/<case>/ and apply the
+    constants of the reference revision that recorded them."""
+    g = golden(case)
+    pt = g["operators"][op][index]
+    tbc_dir = os.path.join(GOLDEN, g["tbc_dir"]) if g.get("tbc_dir") else GOLDEN
+    return setup_case(namelist_for(case, pt), None, hfb=hfb(case), tbc_dir=tbc_dir,
+                      twobc_revision=g.get("revision") or None), pt
 
 
 def recorded_values(point, labels):

@@ -15,8 +15,13 @@ pytestmark = pytest.mark.gpu
 
 REL = 1e-6
 
+# two-body-current operators (GT with the cached finite-range field, GT with the DME
+# exchange function, P/PS0 with the nuclear-matter and DME corrections)
+TWO_BODY_OPS = [(case, op) for case in ("S40_2bc_fam", "S40_2bc_dme", "S40_2bc_ps0", "Gd162_2bc_p",
+                                         "S40_2bc_p_dme", "S40_2bc_ps0_dme")
+                for op in sorted(golden(case)["operators"])]
 ALL_OPS = [("S40", op) for op in sorted(golden("S40")["operators"])] + \
-          [("Gd162", "GT-K0"), ("Gd162", "GT-K1"), ("Kr116", "P-K0")]
+          [("Gd162", "GT-K0"), ("Gd162", "GT-K1"), ("Kr116", "P-K0")] + TWO_BODY_OPS
 
 
 @pytest.fixture(scope="module")

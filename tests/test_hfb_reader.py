@@ -43,6 +43,19 @@ def test_quasiparticle_energies_match_hfbtho():
     assert abs(np.sum(rn / mb.wdcori) - 24.0) < 1e-9
 
 
+def test_kinetic_density_and_laplacian():
+    """tau and Laplacian rho of the rebuilt solution (the DME inputs): the kinetic
+    energies hbar^2/2m int tau against HFBTHO's printed values (thoout.dat :618 of
+    the same run), and int Laplacian rho = 0."""
+    s = hfb("S40")
+    mb = build_mesh_basis(s.hel)
+    hb = s.hel.hbzero
+    assert abs(hb * np.sum(s.tau_n / mb.wdcori) - 447.846356) < 1.5e-6
+    assert abs(hb * np.sum(s.tau_p / mb.wdcori) - 265.730132) < 1.5e-6
+    for d2 in (s.d2rho_n, s.d2rho_p):
+        assert abs(np.sum(d2 / mb.wdcori)) < 1e-12
+
+
 def test_doubled_solution_is_unitary():
     s = hfb("S40")
     nb, half = s.nb, s.nb // 2

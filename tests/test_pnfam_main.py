@@ -16,6 +16,8 @@ EXE = os.path.join(ROOT, "pynfam_gb300", "bin", "pnfam_main.x")
 
 def write_in(path, pt, interaction, name):
     n = pt["namelist"]
+    mode = n.get("two_body_current_mode", 0)
+    lecs = ", ".join(repr(float(x)) for x in n.get("two_body_current_lecs", [-3.1962, 3.1962, 0]))
     txt = f"""&general
     fam_output_filename = '{name}'
     print_stdout = .false.
@@ -29,9 +31,9 @@ def write_in(path, pt, interaction, name):
     operator_name = '{n['operator_name']}'
     operator_k = {n['operator_k']}
     compute_crossterms = {'.true.' if n['compute_crossterms'] else '.false.'}
-    two_body_current_mode = 0
+    two_body_current_mode = {mode}
     two_body_current_usep = .false.
-    two_body_current_lecs = -3.1962, 3.1962, 0
+    two_body_current_lecs = {lecs}
 /
 
 {interaction}
@@ -72,6 +74,19 @@ def test_cli_reports_missing_ground_state(tmp_path):
     assert "ERROR" in out and "Strength" not in out
 
 
+def test_cli_two_body_current_needs_its_tbc_file(tmp_path):
+    """Mode 111100 reads the finite-range field from <fam_output_filename>.tbc;
+    without it the run fails with a message and no result table."""
+    g = golden("S40_2bc_fam")
+    write_in(tmp_path / "GT-K0.in", g["operators"]["GT-K0"][0], g["interaction"], "GT-K0")
+    shutil.copyfile(os.path.join(GOLDEN, "S40_2bc_fam.hel"), tmp_path / "hfbtho_output.hel")
+    env = dict(os.environ, PNFAM_GB300_CACHE="off")
+    p = subprocess.run([sys.executable, EXE, "GT-K0.in"], cwd=tmp_path, capture_output=True, text=True, env=env)
+    assert p.returncode == 1 and "GT-K0.tbc" in p.stderr
+    out = open(tmp_path / "GT-K0.dat").read()
+    assert "GT-K0.tbc" in out and "Strength" not in out
+
+
 def test_cli_rejects_two_arguments(tmp_path):
     p = subprocess.run([sys.executable, EXE, "a", "b"], cwd=tmp_path, capture_output=True, text=True)
     assert p.returncode == 1 and "More than one" in p.stderr
@@ -89,6 +104,26 @@ def test_cli_point_matches_recorded(tmp_path, op, idx):
     assert p.returncode == 0 and p.stderr.strip() == "", p.stderr
     version, conv, t, rows = parse_dat(tmp_path / f"{op}.dat")
     assert conv == "Yes" and t >= 0.0 and version
+    for lab, (re_, im_) in pt["result"].items():
+        got = rows[lab]
+        assert abs(got[0] - re_) <= 1e-6 * abs(re_) + 1e-15, (lab, got, re_)
+        assert abs(got[1] - im_) <= 1e-6 * abs(im_) + 1e-15, (lab, got, im_)
+
+
+@pytest.mark.gpu
+def test_cli_two_body_current_point_matches_recorded(tmp_path):
+    """GT with the two-body current (one-body part with the Park sign plus the
+    cached finite-range field of GT-K0.tbc in the working directory)."""
+    g = golden("S40_2bc_fam")
+    pt = g["operators"]["GT-K0"][0]
+    write_in(tmp_path / "GT-K0.in", pt, g["interaction"], "GT-K0")
+    shutil.copyfile(os.path.join(GOLDEN, "S40_2bc_fam.hel"), tmp_path / "hfbtho_output.hel")
+    shutil.copyfile(os.path.join(GOLDEN, "S40_2bc_fam", "GT-K0.tbc"), tmp_path / "GT-K0.tbc")
+    env = dict(os.environ, PNFAM_GB300_CACHE="off")
+    p = subprocess.run([sys.executable, EXE, "GT-K0.in"], cwd=tmp_path, capture_output=True, text=True, env=env)
+    assert p.returncode == 0 and p.stderr.strip() == "", p.stderr
+    version, conv, t, rows = parse_dat(tmp_path / "GT-K0.dat")
+    assert conv == "Yes"
     for lab, (re_, im_) in pt["result"].items():
         got = rows[lab]
         assert abs(got[0] - re_) <= 1e-6 * abs(re_) + 1e-15, (lab, got, re_)
