@@ -603,9 +603,17 @@ def _bm(m: BlockMatrix, sgn=1.0):
 
 
 class FAMOracle:
-    """pnfam_solve for one (operator, omega) on a prepared HFB solution."""
+    """pnfam_solve for one (operator, omega) on a prepared HFB solution.
 
-    def __init__(self, hfb, couplings, F, G=(), quench=1.0, alpha_mix=float(np.float32(0.7))):
+    ``occupations`` = (f_p, f_n), quasiparticle occupations [dqp] of the doubled
+    basis, switches on the statistical FAM (finite temperature or EFA blocking,
+    pnfam_solver.f90:248-254,425-458): the diagonal quadrants P (m11) and Q (m22)
+    join X and Y, with Green's functions -1/(E1 - E2 -/+ w) and the occupation
+    factors 1 - f1 - f2 (X, Y) and f2 - f1 (P, Q) applied after the Green's
+    function; the Broyden vector is [Re X, Re Y, Im X, Im Y, Re P, Re Q, Im P, Im Q]
+    (pnfam_broyden.f90:26-61)."""
+
+    def __init__(self, hfb, couplings, F, G=(), quench=1.0, alpha_mix=float(np.float32(0.7)), occupations=None):
         # alpha_mix: pnfam_broyden.f90:20 sets 0.7 from a single-precision literal
         self.hfb, self.cp, self.quench, self.alpha = hfb, couplings, quench, alpha_mix
         nb, db = hfb.nb, hfb.db
@@ -619,8 +627,14 @@ class FAMOracle:
         self.Wn, self.Wp = mk(Un, Vn), mk(Up, Vp)
         self.W1, self.W2 = (self.Wp, self.Wn) if self.bminus else (self.Wn, self.Wp)
         self.E1, self.E2 = (hfb.Ep, hfb.En) if self.bminus else (hfb.En, hfb.Ep)
+        self.stat = occupations is not None
+        if self.stat:
+            fp, fn = (np.asarray(x, dtype=np.float64) for x in occupations)
+            self.f1, self.f2 = (fp, fn) if self.bminus else (fn, fp)
+        self.quads = (12, 21, 11, 22) if self.stat else (12, 21)
+        d = True if self.stat else None
         Fsp = BBM(q={11: F.mat, 12: None, 21: None, 22: None})
-        qp = BBM(q={11: None, 12: True, 21: True, 22: None}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0})
+        qp = BBM(q={11: d, 12: True, 21: True, 22: d}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0})
         self.Fqp = triprod_bbm("t", self.W1, "n", Fsp, "n", self.W2, qp, nb, db)
         self.Gqp = [triprod_bbm("t", self.W1, "n", BBM(q={11: g.mat, 12: None, 21: None, 22: None}),
                                 "n", self.W2, qp, nb, db) for g in G]
@@ -628,62 +642,76 @@ class FAMOracle:
         self.fmat = F.mat
         self.nxy = F.mat.nelem
 
-    def _green(self, quad, ree, ime):
-        """matrix_2qp(-1,+1,+1,-1, ree, ime, E1, E2) on the block structure of quad."""
+    def _map2qp(self, quad, f):
+        """f(i, j) on the blocks of Fqp quadrant ``quad`` (row/column states)."""
         m = self.Fqp.q[quad]
         st = self.hfb.isstart
         blocks = []
         for i, j in enumerate(m.cols):
             if j < 0:
                 blocks.append(None); continue
-            e1 = self.E1[st[i]:st[i] + self.db[i]]
-            e2 = self.E2[st[j]:st[j] + self.db[j]]
-            blocks.append(-1.0 / (e1[:, None] + e2[None, :] + complex(ree, ime)))
+            blocks.append(f(slice(st[i], st[i] + self.db[i]), slice(st[j], st[j] + self.db[j])))
         return blocks
+
+    def _green(self, quad, ree, ime, c=1.0):
+        """matrix_2qp(-1,+1,c,-1, ree, ime, E1, E2) on the block structure of quad."""
+        return self._map2qp(quad, lambda r, k: -1.0 / (self.E1[r][:, None] + c * self.E2[k][None, :] + complex(ree, ime)))
+
+    def _occupation(self, quad):
+        """matrix_2qp(+1,-1,-1,+1, 1, 0) on X/Y and (+1,-1,+1,+1, 0, 0) on P/Q
+        (pnfam_solver.f90:445-458)."""
+        if quad in (12, 21):
+            return self._map2qp(quad, lambda r, k: (-self.f1[r][:, None] - self.f2[k][None, :]) + 1.0)
+        return self._map2qp(quad, lambda r, k: (-self.f1[r][:, None] + self.f2[k][None, :]) + 0.0)
 
     def solve(self, omega: complex, max_iter=300, eps=1e-7, broyden_m=50, keep_solution=False):
         t0 = time.perf_counter()
         nb, db, hfb = self.nb, self.db, self.hfb
         quench = self.quench
         Fq = self.Fqp
-        # Green's functions X (12) and Y (21), complex
-        GX = self._green(12, -omega.real, -omega.imag)
-        GY = self._green(21, omega.real, omega.imag)
-        colsX, colsY = Fq.q[12].cols, Fq.q[21].cols
+        quads = self.quads
+        # Green's functions X (12), Y (21) and, statistical, P (11), Q (22); complex
+        Gf = {12: self._green(12, -omega.real, -omega.imag), 21: self._green(21, omega.real, omega.imag)}
+        Tq = {}
+        if self.stat:
+            Gf[11] = self._green(11, -omega.real, -omega.imag, -1.0)
+            Gf[22] = self._green(22, omega.real, omega.imag, -1.0)
+            Tq = {q: self._occupation(q) for q in quads}
+        cols = {q: Fq.q[q].cols for q in quads}
+        colsX, colsY = cols[12], cols[21]
         nx = Fq.q[12].nelem
-        # dR_qp (stored X, Y) as complex blocks
-        X = [None if c < 0 else np.zeros((db[i], db[c]), dtype=complex) for i, c in enumerate(colsX)]
-        Y = [None if c < 0 else np.zeros((db[i], db[c]), dtype=complex) for i, c in enumerate(colsY)]
+        R = {q: [None if c < 0 else np.zeros((db[i], db[c]), dtype=complex) for i, c in enumerate(cols[q])]
+             for q in quads}
         if abs(quench) < 1e-10:
             broyden_m = -1
-        bro = Broyden(4 * nx, broyden_m, self.alpha)
+        bro = Broyden(len(quads) * 2 * nx, broyden_m, self.alpha)
         flat = lambda blks: np.concatenate([b.reshape(-1, order="F") for b in blks if b is not None])
+        # Broyden layout: (quadrant pair, Re|Im) groups of pnfam_broyden.f90:47-60
+        groups = [(12, 21)] + ([(11, 22)] if self.stat else [])
 
-        def pack(Xb, Yb):
-            fx, fy = flat(Xb), flat(Yb)
-            return np.concatenate([fx.real, fy.real, fx.imag, fy.imag])
+        def pack(Rd):
+            parts = []
+            for qa, qb in groups:
+                fa, fb = flat(Rd[qa]), flat(Rd[qb])
+                parts += [fa.real, fb.real, fa.imag, fb.imag]
+            return np.concatenate(parts)
 
         def unpack(v):
-            out = []
-            p = 0
-            for blks in (X, Y):
-                nb_ = []
-                for b in blks:
-                    nb_.append(None if b is None else np.zeros(b.shape, dtype=complex))
-                out.append(nb_)
-            n = nx
-            vals = {}
-            for part, blks, off_re, off_im in ((0, out[0], 0, 2 * n), (1, out[1], n, 3 * n)):
-                p = 0
-                for k, b in enumerate(blks):
-                    if b is None:
-                        continue
-                    s = b.size
-                    b[...] = (v[off_re + p:off_re + p + s] + 1j * v[off_im + p:off_im + p + s]).reshape(b.shape, order="F")
-                    p += s
-            return out[0], out[1]
+            out = {q: [None if b is None else np.zeros(b.shape, dtype=complex) for b in R[q]] for q in quads}
+            base = 0
+            for qa, qb in groups:
+                for q, off_re, off_im in ((qa, base, base + 2 * nx), (qb, base + nx, base + 3 * nx)):
+                    p = 0
+                    for b in out[q]:
+                        if b is None:
+                            continue
+                        n = b.size
+                        b[...] = (v[off_re + p:off_re + p + n] + 1j * v[off_im + p:off_im + p + n]).reshape(b.shape, order="F")
+                        p += n
+                base += 4 * nx
+            return out
 
-        vin = pack(X, Y)
+        vin = pack(R)
         si = 1.0
         flag = "N"
         nxt = len(self.Gqp)
@@ -693,6 +721,16 @@ class FAMOracle:
         # SP-basis structures of the H/rho quadrants
         h_cols = {"h_pn": self.fmat.cols, "h_np": self.fmat.cols, "dp": colsX, "dm": colsY}
         basis = _Basis(hfb)
+
+        def contract(op, Rd):
+            # contract_bbm (pnfam_type_bbm.f90:393-421): quadrants 11, 12, 21, 22 in order
+            sr = si_ = 0.0
+            for q in (11, 12, 21, 22):
+                if q in Rd:
+                    f = op.q[q].flatten(); x = flat(Rd[q])
+                    sr = sr + float(np.dot(f, x.real)); si_ = si_ + float(np.dot(f, x.imag))
+            return -sr / PI, -si_ / PI
+
         for it in range(0, max_iter + 1):
             history.append((it, flag, si, re_str[0], im_str[0], re_str[1:].copy(), im_str[1:].copy()))
             if si < eps:
@@ -702,40 +740,35 @@ class FAMOracle:
                 iter_conv = -1
                 break
             if abs(quench) < 1e-10:
-                HX = [None if b is None else np.zeros_like(b) for b in X]
-                HY = [None if b is None else np.zeros_like(b) for b in Y]
+                H = {q: [None if b is None else np.zeros_like(b) for b in R[q]] for q in quads}
             else:
-                HX, HY = self._residual(X, Y, colsX, colsY, h_cols, basis)
-                HX = [None if b is None else quench * b for b in HX]
-                HY = [None if b is None else quench * b for b in HY]
-            HX = [None if b is None else b + Fq.q[12].blocks[i] for i, b in enumerate(HX)]
-            HY = [None if b is None else b + Fq.q[21].blocks[i] for i, b in enumerate(HY)]
-            Xo = [None if b is None else GX[i] * b for i, b in enumerate(HX)]
-            Yo = [None if b is None else GY[i] * b for i, b in enumerate(HY)]
-            vout = pack(Xo, Yo)
+                H = self._residual(R, cols, h_cols, basis)
+                H = {q: [None if b is None else quench * b for b in H[q]] for q in quads}
+            Ro = {}
+            for q in quads:
+                Hq = [None if b is None else b + Fq.q[q].blocks[i] for i, b in enumerate(H[q])]
+                Ro[q] = [None if b is None else Gf[q][i] * b for i, b in enumerate(Hq)]
+                if self.stat:
+                    Ro[q] = [None if b is None else Tq[q][i] * b for i, b in enumerate(Ro[q])]
+            vout = pack(Ro)
             vin, si, flag = bro.step(vout, vin, it)
-            X, Y = unpack(vin)
-            fx = flat(X); fy = flat(Y)
-            f12 = Fq.q[12].flatten(); f21 = Fq.q[21].flatten()
-            re_str[0] = -(np.dot(f12, fx.real) + np.dot(f21, fy.real)) / PI
-            im_str[0] = -(np.dot(f12, fx.imag) + np.dot(f21, fy.imag)) / PI
+            R = unpack(vin)
+            re_str[0], im_str[0] = contract(Fq, R)
             for k, g in enumerate(self.Gqp):
-                g12 = g.q[12].flatten(); g21 = g.q[21].flatten()
-                re_str[1 + k] = -(np.dot(g12, fx.real) + np.dot(g21, fy.real)) / PI
-                im_str[1 + k] = -(np.dot(g12, fx.imag) + np.dot(g21, fy.imag)) / PI
+                re_str[1 + k], im_str[1 + k] = contract(g, R)
         res = OracleResult(re_str.copy(), im_str.copy(), iter_conv, si, history, time.perf_counter() - t0)
         if keep_solution:
-            fx = flat(X); fy = flat(Y)
+            fx = flat(R[12]); fy = flat(R[21])
             res.X_re, res.X_im, res.Y_re, res.Y_im = fx.real.copy(), fx.imag.copy(), fy.real.copy(), fy.imag.copy()
         return res
 
-    def _residual(self, X, Y, colsX, colsY, h_cols, basis):
-        """dH_qp (stored X/Y quadrants, complex) from dR_qp, via the SP basis."""
+    def _residual(self, R, cols, h_cols, basis):
+        """dH_qp (stored quadrants, complex) from dR_qp, via the SP basis."""
         nb, db = self.nb, self.db
-        mkq = lambda cols, blks, part: BlockMatrix(cols, [None if b is None else getattr(b, part).copy() for b in blks])
+        mkq = lambda q, part: BlockMatrix(cols[q], [None if b is None else getattr(b, part).copy() for b in R[q]])
         dRq = {}
         for part, im in (("real", False), ("imag", True)):
-            dRq[part] = BBM(q={11: None, 12: mkq(colsX, X, part), 21: mkq(colsY, Y, part), 22: None},
+            dRq[part] = BBM(q={q: (mkq(q, part) if q in R else None) for q in (11, 12, 21, 22)},
                             s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0}, imag=im)
         sp_re = BBM(q={11: True, 12: True, 21: True, 22: True}, s={11: 1.0, 12: -1.0, 21: 1.0, 22: -1.0},
                     t={11: "n", 12: "t", 21: "t", 22: "t"})
@@ -753,10 +786,10 @@ class FAMOracle:
         Him = BBM(q={11: mk(h_cols["h_pn"], out["h_pn"], "imag"), 12: mk(h_cols["dp"], out["dp"], "imag"),
                      21: mk(h_cols["dm"], out["dm"], "imag"), 22: mk(h_cols["h_np"], out["h_np"], "imag")},
                   s={11: 1.0, 12: 1.0, 21: 1.0, 22: -1.0}, t={11: "n", 12: "n", 21: "n", 22: "t"}, imag=True)
-        qp_re = BBM(q={11: None, 12: True, 21: True, 22: None}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0})
-        qp_im = BBM(q={11: None, 12: True, 21: True, 22: None}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0}, imag=True)
+        d = True if self.stat else None
+        qp_re = BBM(q={11: d, 12: True, 21: True, 22: d}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0})
+        qp_im = BBM(q={11: d, 12: True, 21: True, 22: d}, s={11: 1.0, 12: 1.0, 21: -1.0, 22: -1.0}, imag=True)
         Hq_re = triprod_bbm("t", self.W1, "n", Hre, "n", self.W2, qp_re, nb, db)
         Hq_im = triprod_bbm("t", self.W1, "n", Him, "n", self.W2, qp_im, nb, db)
-        HX = [None if b is None else b + 1j * Hq_im.q[12].blocks[i] for i, b in enumerate(Hq_re.q[12].blocks)]
-        HY = [None if b is None else b + 1j * Hq_im.q[21].blocks[i] for i, b in enumerate(Hq_re.q[21].blocks)]
-        return HX, HY
+        return {q: [None if b is None else b + 1j * Hq_im.q[q].blocks[i] for i, b in enumerate(Hq_re.q[q].blocks)]
+                for q in self.quads}
