@@ -111,6 +111,20 @@ int pnfam_gpu_set_operator(pnfam_ctx_t* ctx, int beta_minus, const int* fcols,
                            const double* Fsp, int n_xterms, const double* const* Gsp);
 
 /*
+ * Statistical FAM: quasiparticle occupations of a finite-temperature or an
+ * EFA-blocked ground state (setup_hfb_solution, pnfam_setup.f90:324-381; the
+ * use_diagonal_blocks branch of init_pnfam_solver, pnfam_solver.f90:248-254,
+ * 425-458).  With occupations the QP state carries the quadrants P and Q besides
+ * X and Y, the Green's function of P/Q is -1/(E1 - E2 -/+ w) and the response is
+ * weighted by 1 - f1 - f2 (X, Y) and f2 - f1 (P, Q); the Broyden vector doubles.
+ *   fp, fn   [dqp] proton / neutron occupations in [0, 1] (the doubled basis),
+ *            both NULL to return to the zero-temperature form
+ * Call before pnfam_gpu_set_operator (it clears the operator).  Solved in the
+ * FP64 form only (precision 0).
+ */
+int pnfam_gpu_set_occupations(pnfam_ctx_t* ctx, const double* fp, const double* fn);
+
+/*
  * Solve npts omega points (ifam, pnfam_solver.f90:93-221) as one batch.
  *   re_w, im_w    [npts] complex energies
  *   re_S, im_S    [npts*(1+n_xterms)] strength and cross terms (-1/pi contraction)
@@ -227,6 +241,28 @@ int pnfam_gpu_calc_hamiltonian_noalloc(const pnfam_basis_t* basis, const double*
                                        const double* d_wdcori, const pnfam_coupl_t* d_coupl,
                                        const int* fcols, const double* const* d_in,
                                        double* const* d_out, void* stream);
+
+/*
+ * Host-only introspection, no device needed: the block-GEMM task tables that
+ * pnfam_gpu_set_operator builds for the QP <-> SP transforms of a basis and an
+ * operator structure (the triprod_bbm products of pnfam_solver.f90:144-166), for
+ * verification against a CPU restatement.
+ *   stage       0/1: dR_sp = W1 dR_qp W2^T (T = op(B) op(C), then out = sum a op(A) T);
+ *               2/3: dH_qp = W1^T dH_sp W2 (same two steps)
+ *   out         [cap][PNFAM_TASK_RECORD] per task: M, N, K, nterm, cbuf, coff, ldc,
+ *               then per term (PNFAM_TASK_TERMS): abuf, aoff, lda, tA, bbuf, boff,
+ *               ldb, tB, alpha_re, alpha_im  (buffer ids: 0 UP, 1 VP, 2 UN, 3 VN,
+ *               4 QP state, 5 scratch, 6 dR_sp, 7 dH_sp, 8 dH_qp; offsets within a
+ *               Re or Im plane; the state and dH_qp hold X, Y[, P, Q] nxy apart, the
+ *               SP buffers rho_pn, kappa+, kappa-, rho_np)
+ *   ntask       number of tasks (all of them, even beyond cap)
+ *   nxy, scratch elements per QP quadrant and per scratch plane
+ */
+#define PNFAM_TASK_TERMS 4
+#define PNFAM_TASK_RECORD (7 + 10 * PNFAM_TASK_TERMS)
+int pnfam_gpu_task_tables(int nb, const int* db, const int* num_spin_up, int beta_minus,
+                          const int* fcols, int statistical, int stage, double* out, int cap,
+                          int* ntask, long long* nxy, long long* scratch);
 
 /* Number of non-trivial FAM matrix elements nxy (valid after set_operator). */
 long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);

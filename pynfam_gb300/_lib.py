@@ -17,7 +17,10 @@ EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam
            "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error",
            "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
            "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_ready", "pnfam_gpu_engine_free",
-           "pnfam_gpu_calc_hamiltonian_mixed")
+           "pnfam_gpu_calc_hamiltonian_mixed", "pnfam_gpu_set_occupations", "pnfam_gpu_task_tables")
+
+TASK_TERMS = 4
+TASK_RECORD = 7 + 10 * TASK_TERMS
 
 ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENONFINITE", 5: "ESTATE"}
 
@@ -92,6 +95,10 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_engine_ready.restype = C.c_int
     lib.pnfam_gpu_engine_free.argtypes = [C.c_void_p]
     lib.pnfam_gpu_engine_free.restype = None
+    lib.pnfam_gpu_set_occupations.argtypes = [C.c_void_p, dp, dp]
+    lib.pnfam_gpu_set_occupations.restype = C.c_int
+    lib.pnfam_gpu_task_tables.argtypes = [C.c_int, ip, ip, C.c_int, ip, C.c_int, C.c_int, dp, C.c_int, ip, lp, lp]
+    lib.pnfam_gpu_task_tables.restype = C.c_int
     _lib = lib
     return lib
 
@@ -110,3 +117,21 @@ def dptr(a: np.ndarray):
 def iptr(a: np.ndarray):
     assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def task_tables(db, num_spin_up, fcols, beta_minus: bool, statistical: bool, stage: int):
+    """The block-GEMM tasks of one stage (host only, no device): (records [n, TASK_RECORD],
+    nxy, scratch elements per plane); see pnfam_gpu_task_tables."""
+    lib = load()
+    db = np.ascontiguousarray(db, dtype=np.int32)
+    nup = np.ascontiguousarray(num_spin_up, dtype=np.int32)
+    fc = np.ascontiguousarray(fcols, dtype=np.int32)
+    n = C.c_int(); nxy = C.c_longlong(); scr = C.c_longlong()
+    check(lib.pnfam_gpu_task_tables(len(db), iptr(db), iptr(nup), int(bool(beta_minus)), iptr(fc),
+                                    int(bool(statistical)), int(stage), None, 0, C.byref(n), C.byref(nxy),
+                                    C.byref(scr)))
+    out = np.zeros((max(n.value, 1), TASK_RECORD))
+    check(lib.pnfam_gpu_task_tables(len(db), iptr(db), iptr(nup), int(bool(beta_minus)), iptr(fc),
+                                    int(bool(statistical)), int(stage), dptr(out), n.value, C.byref(n),
+                                    C.byref(nxy), C.byref(scr)))
+    return out[:n.value], int(nxy.value), int(scr.value)

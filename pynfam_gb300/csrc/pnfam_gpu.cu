@@ -191,6 +191,13 @@ struct pnfam_ctx {
   int nops = 1;
   std::vector<int> fc, xc, yc, xtc, ytc;
   std::vector<long long> foff, xoff, yoff, xtoff, ytoff;
+  // statistical FAM (finite temperature, EFA blocking): the diagonal quadrants P
+  // (m11) and Q (m22) join X and Y; nq = quadrants of the QP state
+  int nq = 2;
+  std::vector<int> pc, qc;
+  std::vector<long long> poff, qoff;
+  DBuf<double> d_fp, d_fn;   // [dqp] quasiparticle occupations
+  long long tplane = 0;      // elements per plane of the GEMM scratch (B_T)
   DBuf<int> d_fc, d_xtc, d_ytc, d_erow, d_ecol;
   DBuf<long long> d_foff, d_xtoff, d_ytoff;
   DBuf<double> d_fops;   // [nops][2*nxy] operator and cross terms in the QP basis
@@ -277,7 +284,7 @@ struct pnfam_ctx {
     DBuf<double>* dbs[] = {&d_up, &d_vp, &d_un, &d_vn, &d_ep, &d_en, &d_phi, &d_wd, &d_crho, &d_cs,
                            &d_cpair, &d_cspair, &d_fops, &d_state, &d_vout, &d_T, &d_rsp, &d_hsp,
                            &d_hqp, &d_dpart, &d_mf, &d_df, &d_dv, &d_bpart, &d_si, &d_norm,
-                           &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim, &d_gfn};
+                           &d_beta, &d_gamma, &d_cpart, &d_wre, &d_wim, &d_gfn, &d_fp, &d_fn};
     for (auto* b : dbs) b->release();
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
     d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
@@ -358,41 +365,61 @@ static void build_tasks(pnfam_ctx* c) {
   const int UL = c->left_u(), VL = c->left_v(), UR = c->right_u(), VR = c->right_v();
   auto X = [&](int i, int tr_) { return MatRef{B_STATE, c->xoff[i], c->db[i], c->db[c->xc[i]], tr_}; };
   auto Y = [&](int i, int tr_) { return MatRef{B_STATE, nxy + c->yoff[i], c->db[i], c->db[c->yc[i]], tr_}; };
+  // statistical FAM: P and Q follow X and Y in the state (and in hqp)
+  auto Pq = [&](int i, int tr_) { return MatRef{B_STATE, 2 * nxy + c->poff[i], c->db[i], c->db[c->pc[i]], tr_}; };
+  auto Qq = [&](int i, int tr_) { return MatRef{B_STATE, 3 * nxy + c->qoff[i], c->db[i], c->db[c->qc[i]], tr_}; };
+  const bool stat = c->nq == 4;
   c->k1a.clear(); c->k1b.clear(); c->k2a.clear(); c->k2b.clear();
   long long toff = 0;
   // ---- K1: dR_sp = W1 dR_qp W2^T (pnfam_solver.f90:144-150) ----
+  // represented dR_qp = [P X; -Y -Q], W = [U V; V U]; stored quadrants of dR_sp
+  // carry the signs and transposes of pnfam_solver.f90:357-363
   for (int i = 0; i < nb; ++i) {
     if (c->fc[i] < 0) continue;
     const int j = c->fc[i], x = c->xc[i], t = c->tr[i];
-    // rho_pn = UL_i X_i VR_j^T - VL_i Y_t UR_j^T      (F structure, row i)
-    emit_triple(c->k1a, c->k1b, toff,
-                {{{1.0, 1.0}, c->ublk(UL, i, 0), X(i, 0), c->vblk(VR, j, 1)},
-                 {{-1.0, -1.0}, c->vblk(VL, i, 0), Y(t, 0), c->ublk(UR, j, 1)}},
-                B_RSP, 0 * nxy + c->foff[i], c->db[i], c->db[j]);
-    // kappa(+) stored = -UR_x X_i^T UL_i^T + VR_x Y_t^T VL_i^T   (XT structure, row x)
-    emit_triple(c->k1a, c->k1b, toff,
-                {{{-1.0, -1.0}, c->ublk(UR, x, 0), X(i, 1), c->ublk(UL, i, 1)},
-                 {{1.0, 1.0}, c->vblk(VR, x, 0), Y(t, 1), c->vblk(VL, i, 1)}},
-                B_RSP, 1 * nxy + c->xtoff[x], c->db[x], c->db[i]);
+    // rho_pn = UL_i X_i VR_j^T - VL_i Y_t UR_j^T [+ UL_i P_i UR_j^T - VL_i Q_t VR_j^T]   (F structure, row i)
+    std::vector<TripleTerm> r = {{{1.0, 1.0}, c->ublk(UL, i, 0), X(i, 0), c->vblk(VR, j, 1)},
+                                 {{-1.0, -1.0}, c->vblk(VL, i, 0), Y(t, 0), c->ublk(UR, j, 1)}};
+    if (stat) {
+      r.push_back({{1.0, 1.0}, c->ublk(UL, i, 0), Pq(i, 0), c->ublk(UR, j, 1)});
+      r.push_back({{-1.0, -1.0}, c->vblk(VL, i, 0), Qq(t, 0), c->vblk(VR, j, 1)});
+    }
+    emit_triple(c->k1a, c->k1b, toff, r, B_RSP, 0 * nxy + c->foff[i], c->db[i], c->db[j]);
+    // kappa(+) stored = -UR_x X_i^T UL_i^T + VR_x Y_t^T VL_i^T [- VR_x P_i^T UL_i^T + UR_x Q_t^T VL_i^T]  (XT, row x)
+    std::vector<TripleTerm> k = {{{-1.0, -1.0}, c->ublk(UR, x, 0), X(i, 1), c->ublk(UL, i, 1)},
+                                 {{1.0, 1.0}, c->vblk(VR, x, 0), Y(t, 1), c->vblk(VL, i, 1)}};
+    if (stat) {
+      k.push_back({{-1.0, -1.0}, c->vblk(VR, x, 0), Pq(i, 1), c->ublk(UL, i, 1)});
+      k.push_back({{1.0, 1.0}, c->ublk(UR, x, 0), Qq(t, 1), c->vblk(VL, i, 1)});
+    }
+    emit_triple(c->k1a, c->k1b, toff, k, B_RSP, 1 * nxy + c->xtoff[x], c->db[x], c->db[i]);
   }
   for (int i = 0; i < nb; ++i) {
     if (c->yc[i] < 0) continue;
     const int y = c->yc[i], t = c->tr[i];
-    // kappa(-) stored = s (VR_y X_t^T VL_i^T - UR_y Y_i^T UL_i^T), s = +1 Re, -1 Im  (YT, row y)
-    emit_triple(c->k1a, c->k1b, toff,
-                {{{1.0, -1.0}, c->vblk(VR, y, 0), X(t, 1), c->vblk(VL, i, 1)},
-                 {{-1.0, 1.0}, c->ublk(UR, y, 0), Y(i, 1), c->ublk(UL, i, 1)}},
-                B_RSP, 2 * nxy + c->ytoff[y], c->db[y], c->db[i]);
+    // kappa(-) stored = s (VR_y X_t^T VL_i^T - UR_y Y_i^T UL_i^T [+ UR_y P_t^T VL_i^T - VR_y Q_i^T UL_i^T]),
+    // s = +1 Re, -1 Im  (YT, row y)
+    std::vector<TripleTerm> k = {{{1.0, -1.0}, c->vblk(VR, y, 0), X(t, 1), c->vblk(VL, i, 1)},
+                                 {{-1.0, 1.0}, c->ublk(UR, y, 0), Y(i, 1), c->ublk(UL, i, 1)}};
+    if (stat) {
+      k.push_back({{1.0, -1.0}, c->ublk(UR, y, 0), Pq(t, 1), c->vblk(VL, i, 1)});
+      k.push_back({{-1.0, 1.0}, c->vblk(VR, y, 0), Qq(i, 1), c->ublk(UL, i, 1)});
+    }
+    emit_triple(c->k1a, c->k1b, toff, k, B_RSP, 2 * nxy + c->ytoff[y], c->db[y], c->db[i]);
   }
   for (int j = 0; j < nb; ++j) {
     if (c->fc[j] < 0) continue;
     const int i = c->fc[j], t = c->tr[i];
-    // rho_np stored = -UR_j X_t^T VL_i^T + VR_j Y_i^T UL_i^T      (F structure, row j)
-    emit_triple(c->k1a, c->k1b, toff,
-                {{{-1.0, -1.0}, c->ublk(UR, j, 0), X(t, 1), c->vblk(VL, i, 1)},
-                 {{1.0, 1.0}, c->vblk(VR, j, 0), Y(i, 1), c->ublk(UL, i, 1)}},
-                B_RSP, 3 * nxy + c->foff[j], c->db[j], c->db[i]);
+    // rho_np stored = -UR_j X_t^T VL_i^T + VR_j Y_i^T UL_i^T [- VR_j P_t^T VL_i^T + UR_j Q_i^T UL_i^T]  (F, row j)
+    std::vector<TripleTerm> r = {{{-1.0, -1.0}, c->ublk(UR, j, 0), X(t, 1), c->vblk(VL, i, 1)},
+                                 {{1.0, 1.0}, c->vblk(VR, j, 0), Y(i, 1), c->ublk(UL, i, 1)}};
+    if (stat) {
+      r.push_back({{-1.0, -1.0}, c->vblk(VR, j, 0), Pq(t, 1), c->vblk(VL, i, 1)});
+      r.push_back({{1.0, 1.0}, c->ublk(UR, j, 0), Qq(i, 1), c->ublk(UL, i, 1)});
+    }
+    emit_triple(c->k1a, c->k1b, toff, r, B_RSP, 3 * nxy + c->foff[j], c->db[j], c->db[i]);
   }
+  c->tplane = toff;
   // ---- K2: dH_qp = W1^T dH_sp W2 (pnfam_solver.f90:160-166) ----
   auto H = [&](int q, int row, const std::vector<long long>& off, const std::vector<int>& cols, int tr_) {
     return MatRef{B_HSP, q * nxy + off[row], c->db[row], c->db[cols[row]], tr_};
@@ -420,6 +447,31 @@ static void build_tasks(pnfam_ctx* c) {
                  {{1.0, 1.0}, c->ublk(UL, i, 1), H(3, j, c->foff, c->fc, 1), c->vblk(VR, j, 0)}},
                 B_HQP, nxy + c->yoff[i], c->db[i], c->db[y]);
   }
+  if (stat) {
+    for (int i = 0; i < nb; ++i) {
+      if (c->pc[i] < 0) continue;
+      const int j = c->pc[i], x = c->xc[i], t = c->tr[i];
+      // H11_i = UL_i^T h11_i UR_j + UL_i^T h12_i VR_x + s VL_t^T m21_t UR_j - VL_t^T m22_x^T VR_x
+      emit_triple(c->k2a, c->k2b, toff,
+                  {{{1.0, 1.0}, c->ublk(UL, i, 1), H(0, i, c->foff, c->fc, 0), c->ublk(UR, j, 0)},
+                   {{1.0, 1.0}, c->ublk(UL, i, 1), H(1, i, c->xoff, c->xc, 0), c->vblk(VR, x, 0)},
+                   {{-1.0, 1.0}, c->vblk(VL, t, 1), H(2, t, c->yoff, c->yc, 0), c->ublk(UR, j, 0)},
+                   {{-1.0, -1.0}, c->vblk(VL, t, 1), H(3, x, c->foff, c->fc, 1), c->vblk(VR, x, 0)}},
+                  B_HQP, 2 * nxy + c->poff[i], c->db[i], c->db[j]);
+    }
+    for (int i = 0; i < nb; ++i) {
+      if (c->qc[i] < 0) continue;
+      const int y = c->yc[i], q = c->qc[i], t = c->tr[i];
+      // H11t_i = -VL_t^T h11_t VR_y - VL_t^T h12_t UR_q - s UL_i^T m21_i VR_y + UL_i^T m22_q^T UR_q
+      emit_triple(c->k2a, c->k2b, toff,
+                  {{{-1.0, -1.0}, c->vblk(VL, t, 1), H(0, t, c->foff, c->fc, 0), c->vblk(VR, y, 0)},
+                   {{-1.0, -1.0}, c->vblk(VL, t, 1), H(1, t, c->xoff, c->xc, 0), c->ublk(UR, q, 0)},
+                   {{1.0, -1.0}, c->ublk(UL, i, 1), H(2, i, c->yoff, c->yc, 0), c->vblk(VR, y, 0)},
+                   {{1.0, 1.0}, c->ublk(UL, i, 1), H(3, q, c->foff, c->fc, 1), c->ublk(UR, q, 0)}},
+                  B_HQP, 3 * nxy + c->qoff[i], c->db[i], c->db[q]);
+    }
+  }
+  c->tplane = std::max(c->tplane, toff);
   // ---- FP64 field projection tasks: spin-uniform 32 x 32 tiles ----
   c->htasks.clear();
   auto cdiv = [](int a, int b) { return (a + b - 1) / b; };
@@ -541,17 +593,19 @@ static void build_tasks(pnfam_ctx* c) {
 // ---------------------------------------------------------------------------
 static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   const long long nxy = c->nxy;
-  CK(dalloc(c->d_state, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_vout, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_T, (size_t)P * 16 * nxy));
+  const long long nv = 2 * c->nq * nxy;   // Re and Im of the QP state (X, Y[, P, Q])
+  const long long tpl = std::max(c->tplane, 8 * nxy);
+  CK(dalloc(c->d_state, (size_t)P * nv));
+  CK(dalloc(c->d_vout, (size_t)P * nv));
+  CK(dalloc(c->d_T, (size_t)P * 2 * tpl));
   CK(dalloc(c->d_rsp, (size_t)P * 8 * nxy));
   CK(dalloc(c->d_hsp, (size_t)P * 8 * nxy));
-  CK(dalloc(c->d_hqp, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_hqp, (size_t)P * nv));
   CK(dalloc(c->d_dpart, (size_t)P * 2 * c->G * 2 * ND * c->nghl));
   CK(dalloc(c->d_mf, (size_t)P * 2 * NMF * 2 * c->nghl));
   const int Mh = std::max(M, 1);
-  CK(dalloc(c->d_df, (size_t)P * Mh * 4 * nxy));
-  CK(dalloc(c->d_dv, (size_t)P * Mh * 4 * nxy));
+  CK(dalloc(c->d_df, (size_t)P * Mh * nv));
+  CK(dalloc(c->d_dv, (size_t)P * Mh * nv));
   CK(dalloc(c->d_bpart, (size_t)P * c->nchunk_bro * BRO_NPART));
   CK(dalloc(c->d_si, (size_t)P));
   CK(dalloc(c->d_norm, (size_t)P));
@@ -560,7 +614,7 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   CK(dalloc(c->d_cpart, (size_t)P * c->nchunk_c * 2 * c->nops));
   CK(dalloc(c->d_wre, (size_t)P));
   CK(dalloc(c->d_wim, (size_t)P));
-  CK(dalloc(c->d_gfn, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_gfn, (size_t)P * nv));
   CK(dalloc(c->d_active, (size_t)P));
   CK(dalloc(c->d_pint, (size_t)6 * P));
   CK(dalloc(c->d_actlist, (size_t)P));
@@ -575,11 +629,11 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   bd[B_VP] = {c->d_vp.p, 0, 0};
   bd[B_UN] = {c->d_un.p, 0, 0};
   bd[B_VN] = {c->d_vn.p, 0, 0};
-  bd[B_STATE] = {c->d_state.p, 4 * nxy, 2 * nxy};
-  bd[B_T] = {c->d_T.p, 16 * nxy, 8 * nxy};
+  bd[B_STATE] = {c->d_state.p, nv, nv / 2};
+  bd[B_T] = {c->d_T.p, 2 * tpl, tpl};
   bd[B_RSP] = {c->d_rsp.p, 8 * nxy, 4 * nxy};
   bd[B_HSP] = {c->d_hsp.p, 8 * nxy, 4 * nxy};
-  bd[B_HQP] = {c->d_hqp.p, 4 * nxy, 2 * nxy};
+  bd[B_HQP] = {c->d_hqp.p, nv, nv / 2};
   CK(upload(c->d_bufs, bd, NBUF));
   return PNFAM_OK;
 }
@@ -810,6 +864,32 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// host half of the basis set-up: block sizes, starts, TR partners, U/V offsets
+static int host_basis(pnfam_ctx* c, int nb, int nghl, const int* db, const int* nup) {
+  if (nb <= 0 || nb % 2 || nghl <= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_init: nb must be positive and even, nghl positive");
+  c->nb = nb;
+  c->nghl = nghl;
+  c->db.assign(db, db + nb);
+  c->maxdb = *std::max_element(c->db.begin(), c->db.end());
+  c->nup.assign(nup, nup + nb);
+  c->st.resize(nb);
+  c->tr.resize(nb);
+  c->uoff.resize(nb);
+  long long mo = 0;
+  int s = 0;
+  for (int i = 0; i < nb; ++i) {
+    if (c->db[i] < 0 || c->nup[i] < 0 || c->nup[i] > c->db[i])
+      return fail(PNFAM_EINVAL, "pnfam_gpu_init: bad block size or spin count");
+    c->st[i] = s; s += c->db[i];
+    c->uoff[i] = mo; mo += (long long)c->db[i] * c->db[i];
+    c->tr[i] = i < nb / 2 ? i + nb / 2 : i - nb / 2;
+  }
+  for (int i = 0; i < nb; ++i)
+    if (c->db[i] != c->db[c->tr[i]]) return fail(PNFAM_EINVAL, "pnfam_gpu_init: TR partner blocks differ in size");
+  c->dqp = s;
+  return PNFAM_OK;
+}
+
 extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, const double* En,
                               const double* Up, const double* Vp, const double* Un, const double* Vn,
                               const double* phi, const double* wdcori, const pnfam_coupl_t* coupl,
@@ -825,33 +905,17 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: no CUDA device available");
   pnfam_ctx* c = new pnfam_ctx();
   cudaGetDevice(&c->dev);
-  c->nb = basis->nb;
-  c->nghl = basis->nghl;
-  c->db.assign(basis->db, basis->db + c->nb);
-  c->maxdb = c->nb > 0 ? *std::max_element(c->db.begin(), c->db.end()) : 0;
+  {
+    const int rcb = host_basis(c, basis->nb, basis->nghl, basis->db, basis->num_spin_up);
+    if (rcb) { delete c; return rcb; }
+  }
   {
     // FP32 densities on the tensor cores unless PNFAM_GB300_TC_DENSITY=0 (SIMT kernel)
     const char* v = std::getenv("PNFAM_GB300_TC_DENSITY");
     c->tc_density = !(v && v[0] == '0');
   }
-  c->nup.assign(basis->num_spin_up, basis->num_spin_up + c->nb);
-  c->st.resize(c->nb);
-  c->tr.resize(c->nb);
-  c->uoff.resize(c->nb);
-  long long mo = 0;
-  int s = 0;
-  for (int i = 0; i < c->nb; ++i) {
-    if (c->db[i] < 0 || c->nup[i] < 0 || c->nup[i] > c->db[i]) {
-      delete c;
-      return fail(PNFAM_EINVAL, "pnfam_gpu_init: bad block size or spin count");
-    }
-    c->st[i] = s; s += c->db[i];
-    c->uoff[i] = mo; mo += (long long)c->db[i] * c->db[i];
-    c->tr[i] = i < c->nb / 2 ? i + c->nb / 2 : i - c->nb / 2;
-  }
-  for (int i = 0; i < c->nb; ++i)
-    if (c->db[i] != c->db[c->tr[i]]) { delete c; return fail(PNFAM_EINVAL, "pnfam_gpu_init: TR partner blocks differ in size"); }
-  c->dqp = s;
+  const int s = c->dqp;
+  const long long mo = c->uoff.back() + (long long)c->db.back() * c->db.back();
   c->ns.resize(s);
   for (int k = 0; k < s; ++k) {
     if (basis->ns[k] != 1 && basis->ns[k] != -1) { delete c; return fail(PNFAM_EINVAL, "pnfam_gpu_init: ns must be +-1"); }
@@ -897,34 +961,57 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
   return PNFAM_OK;
 }
 
-extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int* fcols, const double* Fsp,
-                                      int n_xterms, const double* const* Gsp) {
-  g_err.clear();
-  if (!c || !fcols || !Fsp || n_xterms < 0 || (n_xterms > 0 && !Gsp))
-    return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: bad argument");
+// block structures of the QP quadrants from F's block map (host): X = U1^T F V2
+// (row i -> tr fc i), Y = V1^T F U2 (i -> fc tr i) and, statistical, P = U1^T F U2
+// (i -> fc i), Q = V1^T F V2 (i -> tr fc tr i); all hold nxy elements
+static int host_structure(pnfam_ctx* c, int beta_minus, const int* fcols) {
   const int nb = c->nb;
   c->beta_minus = beta_minus ? 1 : 0;
   c->fc.assign(fcols, fcols + nb);
   for (int i = 0; i < nb; ++i)
     if (c->fc[i] < -1 || c->fc[i] >= nb) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: fcols out of range");
   c->xc.assign(nb, -1); c->yc.assign(nb, -1); c->xtc.assign(nb, -1); c->ytc.assign(nb, -1);
+  c->pc.assign(nb, -1); c->qc.assign(nb, -1);
   for (int i = 0; i < nb; ++i) {
     if (c->fc[i] >= 0) c->xc[i] = c->tr[c->fc[i]];
     c->yc[i] = c->fc[c->tr[i]];
+    c->pc[i] = c->fc[i];
+    if (c->yc[i] >= 0) c->qc[i] = c->tr[c->yc[i]];
   }
   for (int i = 0; i < nb; ++i) {
     if (c->xc[i] >= 0) { if (c->xtc[c->xc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: F is not one block per column"); c->xtc[c->xc[i]] = i; }
     if (c->yc[i] >= 0) { if (c->ytc[c->yc[i]] >= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: F is not one block per column"); c->ytc[c->yc[i]] = i; }
   }
-  long long nf, nx, ny, nxt, nyt;
+  long long nf, nx, ny, nxt, nyt, np_, nq_;
   c->foff = offsets(c->fc, c->db, &nf);
   c->xoff = offsets(c->xc, c->db, &nx);
   c->yoff = offsets(c->yc, c->db, &ny);
   c->xtoff = offsets(c->xtc, c->db, &nxt);
   c->ytoff = offsets(c->ytc, c->db, &nyt);
-  if (nf != nx || nf != ny || nf != nxt || nf != nyt || nf == 0)
+  c->poff = offsets(c->pc, c->db, &np_);
+  c->qoff = offsets(c->qc, c->db, &nq_);
+  if (nf != nx || nf != ny || nf != nxt || nf != nyt || nf != np_ || nf != nq_ || nf == 0)
     return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: inconsistent block structure");
+  // the statistical quadrants keep the symmetry fc[tr fc[i]] = tr i that their tasks use
+  if (c->nq == 4)
+    for (int i = 0; i < nb; ++i)
+      if (c->fc[i] >= 0 && c->fc[c->tr[c->fc[i]]] != c->tr[i])
+        return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: F block map is not symmetric under time reversal");
   c->nxy = nf;
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int* fcols, const double* Fsp,
+                                      int n_xterms, const double* const* Gsp) {
+  g_err.clear();
+  if (!c || !fcols || !Fsp || n_xterms < 0 || (n_xterms > 0 && !Gsp))
+    return fail(PNFAM_EINVAL, "pnfam_gpu_set_operator: bad argument");
+  const int nb = c->nb;
+  {
+    const int rcs = host_structure(c, beta_minus, fcols);
+    if (rcs) return rcs;
+  }
+  const long long nf = c->nxy;
   c->nops = 1 + n_xterms;
   CK(upload(c->d_fc, c->fc.data(), nb));
   CK(upload(c->d_xtc, c->xtc.data(), nb));
@@ -932,11 +1019,12 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   CK(upload(c->d_foff, c->foff.data(), nb));
   CK(upload(c->d_xtoff, c->xtoff.data(), nb));
   CK(upload(c->d_ytoff, c->ytoff.data(), nb));
-  // element -> (row state, column state) for the X|Y layout (Green's function)
-  std::vector<int> erow(2 * nf), ecol(2 * nf);
-  for (int part = 0; part < 2; ++part) {
-    const std::vector<int>& cols = part == 0 ? c->xc : c->yc;
-    const std::vector<long long>& off = part == 0 ? c->xoff : c->yoff;
+  // element -> (row state, column state) for the X|Y[|P|Q] layout (Green's function)
+  const int nq = c->nq;
+  std::vector<int> erow(nq * nf), ecol(nq * nf);
+  for (int part = 0; part < nq; ++part) {
+    const std::vector<int>& cols = part == 0 ? c->xc : part == 1 ? c->yc : part == 2 ? c->pc : c->qc;
+    const std::vector<long long>& off = part == 0 ? c->xoff : part == 1 ? c->yoff : part == 2 ? c->poff : c->qoff;
     for (int i = 0; i < nb; ++i) {
       if (cols[i] < 0) continue;
       const int d = c->db[i], dc = c->db[cols[i]];
@@ -960,8 +1048,8 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
     for (int i = 0; i < nb; ++i) nrows += c->fc[i] >= 0;
     c->G = std::max(1, std::min(nrows, (2 * std::max(nsm, 1) + ntr - 1) / ntr));
   }
-  c->nchunk_bro = (int)((4 * nf + BRO_CHUNK - 1) / BRO_CHUNK);
-  c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (2 * nf) / 4096));
+  c->nchunk_bro = (int)((2 * nq * nf + BRO_CHUNK - 1) / BRO_CHUNK);
+  c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (nq * nf) / 4096));
   build_tasks(c);
   CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
   {
@@ -992,7 +1080,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   if (rc) return rc;
   c->cap_P = std::max(1, c->cap_P); c->cap_M = std::max(1, c->cap_M);
   // F_qp and cross terms: K2 applied to dH_sp = (F, 0, 0, 0) (pnfam_solver.f90:368-381)
-  CK(dalloc(c->d_fops, (size_t)c->nops * 2 * nf));
+  CK(dalloc(c->d_fops, (size_t)c->nops * nq * nf));
   std::vector<int> one = {1};
   CK(upload(c->d_active, one.data(), 1));
   for (int k = 0; k < c->nops; ++k) {
@@ -1001,7 +1089,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
     CK(cudaMemcpyAsync(c->d_hsp.p, src, sizeof(double) * nf, cudaMemcpyHostToDevice, c->stream));
     if ((rc = launch_gemm(c, c->k2a, 1, c->d_active.p))) return rc;
     if ((rc = launch_gemm(c, c->k2b, 1, c->d_active.p))) return rc;
-    CK(cudaMemcpyAsync(c->d_fops.p + (long long)k * 2 * nf, c->d_hqp.p, sizeof(double) * 2 * nf,
+    CK(cudaMemcpyAsync(c->d_fops.p + (long long)k * nq * nf, c->d_hqp.p, sizeof(double) * nq * nf,
                        cudaMemcpyDeviceToDevice, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -1068,7 +1156,9 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->M = e->no_res ? -1 : o->broyden_history_size;
   if (e->M > 64) return fail(PNFAM_EINVAL, "broyden_history_size > 64 is not supported");
   e->bmode = e->M < 0 ? BRO_NOMIX : e->M == 0 ? BRO_LINEAR : BRO_BROYDEN;
-  e->nxy = c->nxy; e->N = (int)(4 * c->nxy); e->nops = c->nops;
+  e->nxy = c->nxy; e->N = (int)(2 * c->nq * c->nxy); e->nops = c->nops;
+  if (o->precision == 1 && c->nq != 2)
+    return fail(PNFAM_EINVAL, "the statistical FAM (occupations set) is solved in the FP64 form (precision 0)");
   int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(e->M, 1), c->cap_M));
   if (rc) return rc;
   c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(e->M, 1), c->cap_M);
@@ -1231,11 +1321,14 @@ static int engine_launch(pnfam_engine* e) {
   }
   const double* E1 = c->beta_minus ? c->d_ep.p : c->d_en.p;
   const double* E2 = c->beta_minus ? c->d_en.p : c->d_ep.p;
+  const int nq = c->nq;
   if (nfresh) {  // newly admitted slots start from X = 0, with their Green's function
     k_vecop<<<vgrid, 256, 0, c->stream>>>(2, 0.0, c->d_state.p, nullptr, N, d_fresh);
-    const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
-    k_green_prep<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, c->d_erow.p, c->d_ecol.p, E1, E2, c->d_wre.p, c->d_wim.p,
-                                                     c->d_gfn.p, d_fresh);
+    const int gx = (int)std::min<long long>(4096, (nq * nxy + 255) / 256);
+    const double* f1 = nq == 4 ? (c->beta_minus ? c->d_fp.p : c->d_fn.p) : nullptr;
+    const double* f2 = nq == 4 ? (c->beta_minus ? c->d_fn.p : c->d_fp.p) : nullptr;
+    k_green_prep<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, nq, c->d_erow.p, c->d_ecol.p, E1, E2, f1, f2, c->d_wre.p,
+                                                     c->d_wim.p, c->d_gfn.p, d_fresh);
     c->launches += 2;
   }
   const int* act = c->d_active.p;
@@ -1275,8 +1368,8 @@ static int engine_launch(pnfam_engine* e) {
   if (split) CK(cudaStreamWaitEvent(c->stream, c->evf[1], 0));
   tic();
   {
-    const int gx = (int)std::min<long long>(4096, (2 * nxy + 255) / 256);
-    k_green<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, P, e->no_res ? nullptr : c->d_hqp.p,
+    const int gx = (int)std::min<long long>(4096, (nq * nxy + 255) / 256);
+    k_green<<<dim3(gx, P), 256, 0, c->stream>>>(nxy, nq, P, e->no_res ? nullptr : c->d_hqp.p,
                                                 e->mixed ? c->d_hqp32.p : nullptr, c->d_fops.p, c->d_gfn.p,
                                                 e->o.quench_residual_int, c->d_vout.p, act,
                                                 e->mixed ? d_incr : nullptr, c->d_radd.p, d_zero);
@@ -1296,7 +1389,8 @@ static int engine_launch(pnfam_engine* e) {
   tic();
   {
     dim3 grid(c->nchunk_c, P);
-    k_contract<<<grid, 256, 0, c->stream>>>(nxy, e->nops, c->d_fops.p, c->d_state.p, c->nchunk_c, c->d_cpart.p, act);
+    k_contract<<<grid, 256, 0, c->stream>>>(nxy, nq, e->nops, c->d_fops.p, c->d_state.p, c->nchunk_c, c->d_cpart.p,
+                                            act);
     c->launches++;
     CK(cudaGetLastError());
   }
@@ -1612,6 +1706,57 @@ extern "C" int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* c, const double* re
   if (herr) {
     cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream);
     return fail(PNFAM_ECUDA, "pnfam_gpu_calc_hamiltonian_mixed: a wait on the tensor cores gave up");
+  }
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_set_occupations(pnfam_ctx_t* c, const double* fp, const double* fn) {
+  g_err.clear();
+  if (!c || (!fp) != (!fn)) return fail(PNFAM_EINVAL, "pnfam_gpu_set_occupations: pass both occupation arrays or neither");
+  if (c->engine) return fail(PNFAM_ESTATE, "pnfam_gpu_set_occupations: an engine is using this context");
+  if (!fp) {
+    c->nq = 2;
+  } else {
+    for (int k = 0; k < c->dqp; ++k)
+      if (!(fp[k] >= 0.0 && fp[k] <= 1.0 && fn[k] >= 0.0 && fn[k] <= 1.0))
+        return fail(PNFAM_EINVAL, "pnfam_gpu_set_occupations: occupations must lie in [0, 1]");
+    CK(upload(c->d_fp, fp, (size_t)c->dqp));
+    CK(upload(c->d_fn, fn, (size_t)c->dqp));
+    c->nq = 4;
+  }
+  c->have_op = false;   // the quadrant set changed: the operator is set again
+  return PNFAM_OK;
+}
+
+static_assert(PNFAM_TASK_TERMS == PNFAM_MAXTERM, "task record layout");
+extern "C" int pnfam_gpu_task_tables(int nb, const int* db, const int* num_spin_up, int beta_minus,
+                                     const int* fcols, int statistical, int stage, double* out, int cap,
+                                     int* ntask, long long* nxy, long long* scratch) {
+  g_err.clear();
+  if (!db || !num_spin_up || !fcols || !ntask || stage < 0 || stage > 3 || cap < 0 || (cap > 0 && !out))
+    return fail(PNFAM_EINVAL, "pnfam_gpu_task_tables: bad argument");
+  pnfam_ctx c;
+  int rc = host_basis(&c, nb, 1, db, num_spin_up);
+  if (rc) return rc;
+  c.nq = statistical ? 4 : 2;
+  if ((rc = host_structure(&c, beta_minus, fcols))) return rc;
+  build_tasks(&c);
+  const TaskList& tl = stage == 0 ? c.k1a : stage == 1 ? c.k1b : stage == 2 ? c.k2a : c.k2b;
+  *ntask = (int)tl.tasks.size();
+  if (nxy) *nxy = c.nxy;
+  if (scratch) *scratch = c.tplane;
+  const int n = std::min(cap, *ntask);
+  for (int k = 0; k < n; ++k) {
+    const GemmTask& t = tl.tasks[k];
+    double* r = out + (size_t)k * PNFAM_TASK_RECORD;
+    r[0] = t.M; r[1] = t.N; r[2] = t.K; r[3] = t.nterm; r[4] = t.cbuf; r[5] = (double)t.coff; r[6] = t.ldc;
+    for (int i = 0; i < PNFAM_MAXTERM; ++i) {
+      const GemmTerm& g = t.t[i];
+      double* q = r + 7 + 10 * i;
+      q[0] = g.abuf; q[1] = (double)g.aoff; q[2] = g.lda; q[3] = g.tA;
+      q[4] = g.bbuf; q[5] = (double)g.boff; q[6] = g.ldb; q[7] = g.tB;
+      q[8] = g.alpha[0]; q[9] = g.alpha[1];
+    }
   }
   return PNFAM_OK;
 }

@@ -1664,10 +1664,6 @@ __global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __r
 }
 
 // ---------------------------------------------------------------------------
-// Green's function update: vout = G o (q*H + F); layout [P][Re X|Y, Im X|Y]
-// ---------------------------------------------------------------------------
-
-// ---------------------------------------------------------------------------
 // field projection on the tensor cores (FP32 data, 3xTF32 products).
 // One CTA computes, for one (block pair, spin segment of the rows) and up to pg
 // points, D[m][n] = sum_k hpsi[k][m] phi[k][n] with
@@ -1906,38 +1902,50 @@ __global__ void __launch_bounds__(HTC_THREADS, 2) k_hproj_tc(DevBasisT<float> B,
 }
 
 // ---------------------------------------------------------------------------
-// Green's function update: vout = G o (q*H + F); layout [P][Re X|Y, Im X|Y]
+// Green's function update: vout = G o (q*H + F); layout [P][Re X|Y[|P|Q], Im ...]
 // ---------------------------------------------------------------------------
 // the Green's function of the points flagged in mask, once per point (omega is fixed):
-// G = -1/(E1 + E2 -/+ w), X (e < nxy) with -w, Y with +w; gfn: [P][Re | Im][2*nxy]
-__global__ void k_green_prep(long long nxy, const int* __restrict__ erow, const int* __restrict__ ecol,
+// G = -1/(E1 + E2 -/+ w) on X (quadrant 0, -w) and Y (1, +w) and, in the statistical
+// FAM (nq = 4), G = -1/(E1 - E2 -/+ w) on P (2) and Q (3) (pnfam_solver.f90:420-442),
+// times the occupation factor 1 - f1 - f2 (X, Y) or f2 - f1 (P, Q) (:445-458), which
+// the reference applies to G o H; gfn: [P][Re | Im][nq*nxy]
+__global__ void k_green_prep(long long nxy, int nq, const int* __restrict__ erow, const int* __restrict__ ecol,
                              const double* __restrict__ E1, const double* __restrict__ E2,
+                             const double* __restrict__ f1, const double* __restrict__ f2,
                              const double* __restrict__ wre, const double* __restrict__ wim,
                              double* __restrict__ gfn, const int* __restrict__ mask) {
   const int p = blockIdx.y;
   if (!mask[p]) return;
-  const long long n2 = 2 * nxy;
+  const long long n2 = nq * nxy;
   const double wr = wre[p], wi = wim[p];
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n2; e += (long long)gridDim.x * blockDim.x) {
-    const double sgn = e < nxy ? -1.0 : 1.0;
-    const double dr = E1[erow[e]] + E2[ecol[e]] + sgn * wr, di = sgn * wi;
+    const int q = (int)(e / nxy);
+    const double sgn = (q & 1) ? 1.0 : -1.0;
+    const double c2 = q < 2 ? 1.0 : -1.0;
+    const int r = erow[e], k = ecol[e];
+    const double dr = E1[r] + c2 * E2[k] + sgn * wr, di = sgn * wi;
     const double den = dr * dr + di * di;
-    gfn[(long long)p * 2 * n2 + e] = -dr / den;
-    gfn[(long long)p * 2 * n2 + n2 + e] = di / den;
+    double gr = -dr / den, gi = di / den;
+    if (f1) {
+      const double t = q < 2 ? (-f1[r] - f2[k]) + 1.0 : (-f1[r] + f2[k]) + 0.0;
+      gr *= t; gi *= t;
+    }
+    gfn[(long long)p * 2 * n2 + e] = gr;
+    gfn[(long long)p * 2 * n2 + n2 + e] = gi;
   }
 }
 
 // vout = G o (q*H + F), G from k_green_prep.  corr[p] != 0 (increment evaluation of the
 // mixed form): H is the FP32 field of X - X_anchor (hqp32) and vout = G o (q*H) + radd[p],
 // radd = g(X_anchor) evaluated in FP64
-__global__ void k_green(long long nxy, int P, const double* __restrict__ hqp, const float* __restrict__ hqp32,
+__global__ void k_green(long long nxy, int nq, int P, const double* __restrict__ hqp, const float* __restrict__ hqp32,
                         const double* __restrict__ fqp, const double* __restrict__ gfn, double quench,
                         double* __restrict__ vout, const int* __restrict__ active,
                         const int* __restrict__ corr, const double* __restrict__ radd,
                         const int* __restrict__ zeroh) {
   const int p = blockIdx.y;
   if (!active[p]) return;
-  const long long n2 = 2 * nxy;
+  const long long n2 = nq * nxy;
   const bool cstep = corr && corr[p];
   const bool useh = hqp && !(zeroh && zeroh[p]);  // zeroh: H = 0 (the field of X = 0)
   const long long o = (long long)p * 2 * n2;
@@ -2429,14 +2437,14 @@ __global__ void k_vecop(int op, double a, double* __restrict__ dst, const double
 }
 
 // S_k = -1/pi * (F_k . Re, F_k . Im) for the operator (k=0) and cross terms
-// fops: [nops][2*nxy]; part: [P][nchunk][2*nops]
-__global__ void __launch_bounds__(256) k_contract(long long nxy, int nops, const double* __restrict__ fops,
+// fops: [nops][nq*nxy]; part: [P][nchunk][2*nops]
+__global__ void __launch_bounds__(256) k_contract(long long nxy, int nq, int nops, const double* __restrict__ fops,
                                                   const double* __restrict__ vin, int nchunk,
                                                   double* __restrict__ part, const int* __restrict__ active) {
   const int p = blockIdx.y;
   if (!active[p]) return;
   __shared__ double sh[32];
-  const long long n2 = 2 * nxy;
+  const long long n2 = nq * nxy;
   const double* v = vin + (long long)p * 2 * n2;
   const long long chunk = (n2 + nchunk - 1) / nchunk;
   const long long e0 = blockIdx.x * chunk, e1 = min(n2, e0 + chunk);

@@ -89,6 +89,7 @@ class HelData:
     aka: np.ndarray = None
     fields: dict = field(default_factory=dict)   # 'n'/'p' -> dict of mesh arrays
     set_temperature: bool = False
+    temperature: float = 0.0     # Temperat: HFBTHO's temper (MeV)
     has_blocking_request: bool = False
 
 
@@ -168,6 +169,7 @@ def read_hel(path: str) -> HelData:
         elif key == "Blk-rest":
             i += 1
         elif key == "Temperat":
+            h.temperature = float(f8(recs[i])[0])
             i += 4
         elif key == "Regular.":
             i += 3

@@ -431,6 +431,13 @@ def load_hfb_solution(path) -> HFBSolution:
     """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file
     (a path, or an already decoded :class:`HelData`)."""
     h = path if isinstance(path, HelData) else read_hel(path)
+    if h.set_temperature and h.temperature > 0.0:
+        # the reference then runs the statistical FAM on the thermal quasiparticles;
+        # rebuilding them needs HFBTHO's finite-temperature particle-number and density
+        # equations, which this reader does not restate
+        raise ValueError(f"the .hel ground state is at T = {h.temperature} MeV: rebuilding finite-temperature "
+                         "solutions is not supported (pass occupations from pynfam_gb300.statistics to GPUSolver "
+                         "to run the statistical FAM on a zero-temperature basis)")
     mb = build_mesh_basis(h)
     hd = hfb_matrices(h, mb)
     qpn = diagonalise(h, hd, "n", float(h.N))

@@ -35,7 +35,9 @@ def _flat_blocks(blocks) -> np.ndarray:
 class GPUSolver:
     """One nucleus resident on the current CUDA device."""
 
-    def __init__(self, hfb, couplings):
+    def __init__(self, hfb, couplings, occupations=None):
+        """occupations: (f_p, f_n) quasiparticle occupations [dqp] of a finite-temperature
+        or EFA-blocked ground state (pynfam_gb300.statistics), for the statistical FAM."""
         self.lib = _lib.load()
         self.hfb = hfb
         self.nb = int(hfb.nb)
@@ -60,6 +62,24 @@ class GPUSolver:
                                            _lib.dptr(wd), C.byref(cp), C.byref(ctx)))
         self.ctx = ctx
         self.nops = 1
+        self.F = None
+        if occupations is not None:
+            self.set_occupations(*occupations)
+
+    def set_occupations(self, fp=None, fn=None):
+        """Statistical FAM with these occupations (None, None: zero temperature); the
+        operator must be set afterwards."""
+        if (fp is None) != (fn is None):
+            raise ValueError("give both occupation arrays or neither")
+        if fp is None:
+            _lib.check(self.lib.pnfam_gpu_set_occupations(self.ctx, None, None))
+            self.occupations = None
+            return
+        a = np.ascontiguousarray(fp, dtype=np.float64); b = np.ascontiguousarray(fn, dtype=np.float64)
+        if a.shape != (int(self.hfb.dqp),) or b.shape != a.shape:
+            raise ValueError("occupations must have dqp entries")
+        _lib.check(self.lib.pnfam_gpu_set_occupations(self.ctx, _lib.dptr(a), _lib.dptr(b)))
+        self.occupations = (a, b)
         self.F = None
 
     def set_operator(self, F, G=()):

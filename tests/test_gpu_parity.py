@@ -355,3 +355,75 @@ def test_tensor_core_density_mixed_solve(monkeypatch, case, op):
     worst = float(np.max(np.abs(g - w) / np.abs(w)))
     print(f"{case} {op} mixed form, tensor-core densities: worst rel err vs FP64 fixed point {worst:.2e}")
     assert worst <= REL
+
+
+# ---------------------------------------------------------------------------
+# statistical FAM (finite temperature, EFA blocking): quadrants P and Q
+# ---------------------------------------------------------------------------
+def _stat_cases():
+    from pynfam_gb300.statistics import blocking_occupations, thermal_occupations
+    out = []
+    for case, op, idx, kind in (("S40", "GT-K0", 5, 1.0), ("S40", "RS1-K1", 3, 2.0), ("Kr116", "P-K0", 4, "block")):
+        c, _ = case_for(case, op, idx)
+        if kind == "block":
+            # one neutron quasiparticle inside the pairing window blocked (EFA)
+            k = int(np.flatnonzero(c.hfb.En > 0)[3])
+            occ = blocking_occupations(c.hfb, iqp_n=k)
+        else:
+            occ = thermal_occupations(c.hfb, kind)
+        out.append((f"{case} {op} {kind}", c, occ))
+    return out
+
+
+def test_statistical_fam_matches_oracle():
+    """GPU statistical FAM against the oracle: the whole iteration history (1e-9)
+    and the final strength and cross terms (1e-10)."""
+    from pynfam_gb300.solver import GPUSolver
+    for name, c, occ in _stat_cases():
+        gpu = GPUSolver(c.hfb, c.couplings, occupations=occ)
+        gpu.set_operator(c.F, c.G)
+        s = c.nml["solver"]
+        r = gpu.solve([c.omega], max_iter=s["max_iter"], eps=s["convergence_epsilon"],
+                      broyden_m=s["broyden_history_size"], quench=c.quench, history=True)
+        gpu.close()
+        orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench, occupations=occ)
+        ref = orc.solve(c.omega, max_iter=s["max_iter"], eps=s["convergence_epsilon"],
+                        broyden_m=s["broyden_history_size"])
+        assert ref.iter_conv > 0 and r.iters[0] == ref.iter_conv, (name, r.iters[0], ref.iter_conv)
+        for h in ref.history:
+            g = r.hist[0, h[0]]
+            assert abs(g[0] - h[2]) <= 1e-9 * max(abs(h[2]), 1e-3), (name, h, g)
+            assert abs(g[1] - h[3]) <= 1e-9 * abs(ref.re_str[0]), (name, h, g)
+            assert abs(g[2] - h[4]) <= 1e-9 * abs(ref.im_str[0]) + 1e-15, (name, h, g)
+        for k in range(len(ref.re_str)):
+            assert abs(r.re_S[0, k] - ref.re_str[k]) <= 1e-10 * abs(ref.re_str[k]) + 1e-15, (name, k)
+            assert abs(r.im_S[0, k] - ref.im_str[k]) <= 1e-10 * abs(ref.im_str[k]) + 1e-15, (name, k)
+        print(f"{name}: statistical FAM, {ref.iter_conv} iterations, S = {r.re_S[0, 0]:.12e} "
+              f"{r.im_S[0, 0]:+.12e}i")
+
+
+def test_statistical_fam_zero_occupations_is_ground_state_form(solvers):
+    """All occupations zero: P = Q = 0 and the T factors are 1, so a contour solved in the
+    statistical form equals the zero-temperature form (rounding level)."""
+    from pynfam_gb300 import _lib
+    from pynfam_gb300.solver import GPUSolver
+    pts = golden("S40")["operators"]["GT-K1"][:6]
+    c, _ = case_for("S40", "GT-K1", 0)
+    omegas = [complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"]) for p in pts]
+    r0 = _solve(solvers("S40", c), c, omegas)
+    z = np.zeros(c.hfb.dqp)
+    gpu = GPUSolver(c.hfb, c.couplings, occupations=(z, z))
+    gpu.set_operator(c.F, c.G)
+    r1 = _solve(gpu, c, omegas)
+    assert np.array_equal(r0.iters, r1.iters)
+    np.testing.assert_allclose(r1.re_S, r0.re_S, rtol=1e-11, atol=1e-15)
+    np.testing.assert_allclose(r1.im_S, r0.im_S, rtol=1e-11, atol=1e-15)
+    # the statistical form is FP64 only; clearing the occupations needs the operator again
+    with pytest.raises(_lib.PnfamGPUError) as e:
+        _solve(gpu, c, omegas[:1], precision=1)
+    assert e.value.code == 1
+    gpu.set_occupations(None, None)
+    with pytest.raises(_lib.PnfamGPUError) as e:
+        gpu.solve(omegas[:1])
+    assert e.value.code == 5
+    gpu.close()
