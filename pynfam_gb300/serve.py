@@ -66,9 +66,11 @@ class ServeStats:
         return float(np.percentile(self.latencies, q)) if self.latencies else float("nan")
 
 
-def slot_bytes(nxy: int, broyden_m: int, mixed: bool) -> int:
-    """Device memory of one solve slot (the per-point buffers of pnfam_gpu.cu)."""
-    f64 = 4 + 4 + 16 + 8 + 8 + 4 + 4 + 2 * 4 * max(broyden_m, 1)   # state, vout, T, rsp, hsp, hqp, G, df+dv
+def slot_bytes(nxy: int, broyden_m: int, mixed: bool, statistical: bool = False) -> int:
+    """Device memory of one solve slot (the per-point buffers of pnfam_gpu.cu); the
+    statistical FAM doubles the QP-state arrays (quadrants P and Q) and the scratch."""
+    q = 2 if statistical else 1
+    f64 = q * (4 + 4 + 16 + 4 + 4 + 2 * 4 * max(broyden_m, 1)) + 8 + 8   # state, vout, T, hqp, G, df+dv; rsp, hsp
     if mixed:
         f64 += 4 + 4 + 4 * 4                                     # anchor, its image; Broyden raw vectors
     f32 = (4 + 16 + 8 + 8 + 4) if mixed else 0

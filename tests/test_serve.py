@@ -190,6 +190,8 @@ def test_engines_step_at_their_own_pace():
 def test_slot_bytes_grow_with_history_and_precision():
     assert slot_bytes(1000, 50, True) > slot_bytes(1000, 50, False) > slot_bytes(1000, 5, False)
     assert slot_bytes(94482, 50, True) < 400e6
+    # the statistical FAM (P, Q quadrants) doubles the QP-state arrays
+    assert 1.9 < slot_bytes(1000, 50, False, True) / slot_bytes(1000, 50, False) < 2.0
 
 
 def test_poisson_arrivals():
