@@ -438,6 +438,12 @@ def load_hfb_solution(path) -> HFBSolution:
         raise ValueError(f"the .hel ground state is at T = {h.temperature} MeV: rebuilding finite-temperature "
                          "solutions is not supported (pass occupations from pynfam_gb300.statistics to GPUSolver "
                          "to run the statistical FAM on a zero-temperature basis)")
+    if int(h.N) % 2 or int(h.Z) % 2:
+        # an odd nucleus is an HFBTHO solution with a blocked quasiparticle, whose
+        # reconstruction (blocked hfbdiag/ALambda/DENSIT) this reader does not restate
+        raise ValueError(f"the .hel ground state has N = {h.N}, Z = {h.Z}: rebuilding blocked odd-nucleus solutions "
+                         "is not supported (pass EFA occupations from pynfam_gb300.statistics to GPUSolver to run "
+                         "the statistical FAM on an even-even basis)")
     mb = build_mesh_basis(h)
     hd = hfb_matrices(h, mb)
     qpn = diagonalise(h, hd, "n", float(h.N))

@@ -81,3 +81,18 @@ def test_corrupt_file_rejected(tmp_path):
     bad.write_bytes(b"\x04\x00\x00\x00\x07\x00\x00\x00\x04\x00\x00\x00")
     with pytest.raises(HelFormatError):
         read_hel(str(bad))
+
+
+@pytest.mark.parametrize("what", ["temperature", "odd"])
+def test_unsupported_ground_states_are_refused(what):
+    """Finite-temperature and blocked (odd-nucleus) solutions need HFBTHO equations this
+    reader does not restate: loading one stops with a message instead of a wrong state."""
+    import copy
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    h = copy.copy(read_hel(HEL))
+    if what == "temperature":
+        h.set_temperature, h.temperature = True, 1.0
+    else:
+        h.N = h.N + 1
+    with pytest.raises(ValueError, match="not supported"):
+        load_hfb_solution(h)
