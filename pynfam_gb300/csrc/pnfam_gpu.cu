@@ -222,7 +222,7 @@ struct pnfam_ctx {
   int cap_P = 0, cap_M = 0;
   DBuf<double> d_state, d_vout, d_T, d_rsp, d_hsp, d_hqp, d_dpart, d_mf;
   DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
-  DBuf<double> d_gfn;   // [P][Re | Im][2nxy] Green's function of each slot's omega
+  DBuf<double> d_gfn;   // [P][Re | Im][nq*nxy] Green's function of each slot's omega
   DBuf<int> d_active, d_act32, d_act64;
   DBuf<int> d_pint;      // [6][P]: Broyden iteration, Broyden mode, increment step, anchor step,
                          // zero field (first evaluation), newly admitted
@@ -664,8 +664,8 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active) {
   return launch_gemm<double>(c, tl, P, active, c->d_bufs.p, c->stream);
 }
 
-// residual interaction of the points flagged in `act`: state (X, Y) -> hqp
-// (H20, H02 stored), computed in precision T (the FP32 form reads the FP32
+// residual interaction of the points flagged in `act`: state (X, Y[, P, Q]) -> hqp
+// (H20, H02[, H11, H11t] stored), computed in precision T (the FP32 form reads the FP32
 // copy of the state and writes the FP32 hqp)
 template <class T>
 // P: batch size (grid extent), nact: points active in this evaluation

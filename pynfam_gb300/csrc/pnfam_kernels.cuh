@@ -1971,7 +1971,7 @@ __global__ void k_green(long long nxy, int nq, int P, const double* __restrict__
 // ---------------------------------------------------------------------------
 enum { BRO_BROYDEN = 0, BRO_LINEAR = 1, BRO_NOMIX = 2 };
 struct BroState {
-  int N;            // vector length (4*nxy)
+  int N;            // vector length (2*nq*nxy: Re and Im of the QP quadrants)
   int M;            // history size
   double alpha;
   double* vin;      // [P][N]
