@@ -149,8 +149,14 @@ def build_mesh_basis(h: HelData) -> MeshBasis:
 def hfb_matrices(h: HelData, mb: MeshBasis):
     """Per block: dict it -> (h_block, delta_block), full symmetric matrices.
 
-    Restates gamdel (hfbtho_solver.f90:5190-5302) for one block at a time with
-    the mesh sum vectorised; h/Delta for neutrons ('n') and protons ('p').
+    Restates gamdel (hfbtho_solver.f90:5190-5302) for one block at a time.  Every
+    matrix element there is a mesh sum of products of two basis functions (or their
+    derivatives) weighted by a field, so each group of terms is one GEMM
+    (A w) B^T over the mesh: same-spin terms with the weights
+    w1 = v + 2 Lyam vSFIZ + L^2y^2 (2 vd + vhb), w2 = 2 vd + vhb, w3 = vr +/- Ly vs
+    (L = Lambda of the spin, +/- for up/down), and the spin-flip terms of
+    J_{r phi}, J_{phi r}, J_{z phi} and nabla.J.  The reference fills n2 <= n1 and
+    mirrors; the lower triangle is taken the same way here.
     """
     out = {"n": [], "p": []}
     start = 0
@@ -167,59 +173,37 @@ def hfb_matrices(h: HelData, mb: MeshBasis):
         xlamy2 = xlam * xlam * y * y; xlapy2 = xlap * xlap * y * y
         FU, FUR, FUZ, FUD2 = q * up, r1 * up, z1 * up, (d2 - xlamy2 * q) * up
         FD, FDR, FDZ, FDD2 = q * dn, r1 * dn, z1 * dn, (d2 - xlapy2 * q) * dn
+        flip_du = (ns[:, None] < 0) & (ns[None, :] > 0)   # a down, b up
+        flip_ud = (ns[:, None] > 0) & (ns[None, :] < 0)   # a up, b down
+
+        def G(A, w, B):
+            return (A * w) @ B.T
+
+        def sym2(A, w, B):
+            m = G(A, w, B)
+            return m + m.T
         for t in ("n", "p"):
             f = h.fields[t]
-            hm = np.zeros((nd, nd)); dm = np.zeros((nd, nd))
-            # spin up-up
-            vh = FU[:, None, :] * FU[None, :, :]
-            hbh = vh * xlamy2 + FUR[:, None] * FUR[None, :] + FUZ[:, None] * FUZ[None, :]
-            vdh = 2 * hbh + FU[:, None] * FUD2[None, :] + FU[None, :] * FUD2[:, None]
-            snr = FUR[:, None] * FU[None, :] + FUR[None, :] * FU[:, None]
-            snz = FUZ[:, None] * FU[None, :] + FUZ[None, :] * FU[:, None]
-            vsh = snr * xlamy
-            sfiz = 2 * vh * xlamy
-            # spin down-down
-            vhd = FD[:, None, :] * FD[None, :, :]
-            hbhd = vhd * xlapy2 + FDR[:, None] * FDR[None, :] + FDZ[:, None] * FDZ[None, :]
-            vdhd = 2 * hbhd + FD[:, None] * FDD2[None, :] + FD[None, :] * FDD2[:, None]
-            snrd = FDR[:, None] * FD[None, :] + FDR[None, :] * FD[:, None]
-            snzd = FDZ[:, None] * FD[None, :] + FDZ[None, :] * FD[:, None]
-            vshd = -snrd * xlapy
-            sfizd = -2 * vhd * xlapy
-            vh = vh + vhd; hbh = hbh + hbhd; vdh = vdh + vdhd
-            snr = snr + snrd; snz = snz + snzd; vsh = vsh + vshd; sfiz = sfiz + sfizd
-            hm += (sfiz * f["vSFIZ"] + vh * f["v"] + snr * f["vr"] + snz * f["vz"]
-                   + vdh * f["vd"] + vsh * f["vs"] + hbh * f["vhb"]).sum(-1)
-            dm += (vh * f["dv"]).sum(-1)
-            # spin-flip: (a=n1 down, b=n2 up) and (a=n1 up, b=n2 down); the
-            # reference fills only n2<=n1, mirrored here to the full matrix.
-            # a down, b up
-            fitw3 = -FDZ[:, None] * FU[None, :]
-            fitw4 = FUZ[None, :] * FD[:, None]
-            vshx = -FDR[:, None] * FUZ[None, :] + FUR[None, :] * FDZ[:, None] + fitw3 * xlamy - fitw4 * xlapy
-            srfi = -FDR[:, None] * FU[None, :] + FUR[None, :] * FD[:, None]
-            sfir = FD[:, None] * FU[None, :] * xlampy
-            szfi = fitw3 + fitw4
-            du = (vshx * f["vs"] + f["vSRFI"] * srfi + f["vSFIR"] * sfir + f["vSZFI"] * szfi).sum(-1)
-            # a up, b down
-            fitw3 = -FDZ[None, :] * FU[:, None]
-            fitw4 = FUZ[:, None] * FD[None, :]
-            vshx = FUR[:, None] * FDZ[None, :] - FDR[None, :] * FUZ[:, None] - fitw4 * xlapy + fitw3 * xlamy
-            srfi = FUR[:, None] * FD[None, :] - FDR[None, :] * FU[:, None]
-            sfir = FU[:, None] * FD[None, :] * xlampy
-            szfi = fitw3 + fitw4
-            ud = (vshx * f["vs"] + f["vSRFI"] * srfi + f["vSFIR"] * sfir + f["vSZFI"] * szfi).sum(-1)
-            nsab = ns[:, None] + ns[None, :]
-            flip = (nsab == 0)
-            a_dn_b_up = flip & (ns[None, :] > 0)
-            a_up_b_dn = flip & (ns[None, :] < 0)
-            hm = np.where(a_dn_b_up, du, hm)
-            hm = np.where(a_up_b_dn, ud, hm)
+            v, vd, vhb, vs, vr, vz = f["v"], f["vd"], f["vhb"], f["vs"], f["vr"], f["vz"]
+            vsfiz, vsrfi, vsfir, vszfi = f["vSFIZ"], f["vSRFI"], f["vSFIR"], f["vSZFI"]
+            w2 = 2.0 * vd + vhb
+            hm = (G(FU, v + 2.0 * xlamy * vsfiz + xlamy2 * w2, FU) + G(FUR, w2, FUR) + G(FUZ, w2, FUZ)
+                  + sym2(FU, vd, FUD2) + sym2(FUR, vr + xlamy * vs, FU) + sym2(FUZ, vz, FU))
+            hm += (G(FD, v - 2.0 * xlapy * vsfiz + xlapy2 * w2, FD) + G(FDR, w2, FDR) + G(FDZ, w2, FDZ)
+                   + sym2(FD, vd, FDD2) + sym2(FDR, vr - xlapy * vs, FD) + sym2(FDZ, vz, FD))
+            dm = G(FU, f["dv"], FU) + G(FD, f["dv"], FD)
+            # spin flip, a down / b up, and a up / b down
+            du = (G(FDR, -vs, FUZ) + G(FDZ, vs, FUR) + G(FDZ, -xlamy * vs - vszfi, FU)
+                  + G(FD, -xlapy * vs + vszfi, FUZ) + G(FDR, -vsrfi, FU) + G(FD, vsrfi, FUR)
+                  + G(FD, xlampy * vsfir, FU))
+            ud = (G(FUR, vs, FDZ) + G(FUZ, -vs, FDR) + G(FUZ, -xlapy * vs + vszfi, FD)
+                  + G(FU, -xlamy * vs - vszfi, FDZ) + G(FUR, vsrfi, FD) + G(FU, -vsrfi, FDR)
+                  + G(FU, xlampy * vsfir, FD))
+            hm = np.where(flip_du, du, hm)
+            hm = np.where(flip_ud, ud, hm)
             # the reference computes element (n1, n2<=n1) and uses it for both
-            lo = np.tril(hm)
-            hm = lo + np.tril(hm, -1).T
-            lo = np.tril(dm)
-            dm = lo + np.tril(dm, -1).T
+            hm = np.tril(hm) + np.tril(hm, -1).T
+            dm = np.tril(dm) + np.tril(dm, -1).T
             out[t].append((hm, dm))
         start += nd
     return out
