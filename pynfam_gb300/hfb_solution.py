@@ -212,14 +212,21 @@ def hfb_matrices(h: HelData, mb: MeshBasis):
 # ----------------------------------------------------------------------------
 # 3. Diagonalisation with the particle-number loop (hfbdiag + ALambda)
 # ----------------------------------------------------------------------------
-def _alambda(al, erhfb, drhfb, tz, cpv0_zero):
-    """Fermi energy from the BCS-like particle number (hfbtho_solver.f90:1977-2075)."""
+def _alambda(al, erhfb, drhfb, tz, cpv0_zero, temper=0.0):
+    """Fermi energy from the BCS-like particle number (hfbtho_solver.f90:1977-2075);
+    at temperature T each pairing-window state adds 2 (1 - 2 v^2) f with
+    f = (1 - tanh(b / 2T)) / 2, b = sqrt((e - lambda)^2 + Delta^2).  Returns
+    (lambda, f of the last particle-number evaluation, in pairing-window order)."""
     if cpv0_zero:
+        if temper > 0.0:
+            raise HFBReconstructionError("finite-temperature solutions without pairing are not supported")
         ntz = int(tz + 0.1) // 2
         d = np.sort(erhfb)
         if ntz < len(d):
-            return 0.5 * (d[ntz - 1] + d[ntz])
-        return d[ntz - 1] + 0.001
+            return 0.5 * (d[ntz - 1] + d[ntz]), None
+        return d[ntz - 1] + 0.001, None
+    thermal = temper > 1e-12
+    fT = None
     xinf, xsup = -1000.0, 1000.0
     for lit in range(1, 501):
         y = erhfb - al
@@ -230,8 +237,15 @@ def _alambda(al, erhfb, drhfb, tz, cpv0_zero):
             dvh = np.where(b > 0, 0.5 * drhfb ** 2 / (a * b), 0.0)
         vh = np.where(vh < 1e-12, 0.0, vh)
         vh = np.where((vh - 1.0) > 1e-12, 1.0, vh)
-        sn = float(np.sum(2.0 * vh))
-        dez = float(np.sum(2.0 * dvh))
+        if thermal:
+            fT = 0.5 * (1.0 - np.tanh(0.5 * b / temper))
+            with np.errstate(divide="ignore", invalid="ignore"):
+                dfT = y / b / temper * fT * (1.0 - fT)
+            sn = float(np.sum(2.0 * vh + 2.0 * (1.0 - 2.0 * vh) * fT))
+            dez = float(np.sum(2.0 * (1.0 - 2.0 * fT) * dvh)) + float(np.sum(2.0 * (1.0 - 2.0 * vh) * dfT))
+        else:
+            sn = float(np.sum(2.0 * vh))
+            dez = float(np.sum(2.0 * dvh))
         ez = sn - tz
         absez = abs(ez) / tz
         if ez < 0:
@@ -245,8 +259,8 @@ def _alambda(al, erhfb, drhfb, tz, cpv0_zero):
         if al < xinf or al > xsup:
             al = 0.5 * (xinf + xsup)
         if absez <= 1e-10:
-            return al
-    return al
+            return al, fT
+    return al, fT
 
 
 @dataclass
@@ -257,10 +271,13 @@ class QPSolution:
     V: list
     active: list   # per block: [nd] bool, below the pairing window
     ala: float
+    fwin: list = None   # finite temperature: per block, f of the active quasiparticles (DENSIT)
 
 
-def diagonalise(h: HelData, hd, it: str, tz: float) -> QPSolution:
-    """hfbdiag(it, icanon) restricted to what pnFAM reads (no blocking, T=0)."""
+def diagonalise(h: HelData, hd, it: str, tz: float, temper: float = 0.0) -> QPSolution:
+    """hfbdiag(it, icanon) restricted to what pnFAM reads (no blocking); at
+    temperature T the particle number of each pairing-window state is
+    2 v^2 + 2 (1 - 2 v^2) f(E) (hfbtho_solver.f90:1750-1774)."""
     k = 0 if it == "n" else 1
     ala = float(h.ala[k])
     pwi = h.pwi
@@ -299,27 +316,38 @@ def diagonalise(h: HelData, hd, it: str, tz: float) -> QPSolution:
                 expo = np.where(np.abs(arg) < math.log(np.finfo(float).max), np.exp(np.minimum(arg, 700.0)), np.inf)
             act = (enb <= pwi) | (np.abs(1.0 / (1.0 + expo)) > CUTOFF_TOL)
             erhfb.append(enb[act]); drhfb.append(ekb[act])
-            nsum += float(np.sum(2.0 * pn[act]))
+            if temper > 1e-12:
+                fe = 0.5 * (1.0 - np.tanh(0.5 * Eq[act] / temper))
+                nsum += float(np.sum(2.0 * pn[act] + 2.0 * (1.0 - 2.0 * pn[act]) * fe))
+            else:
+                nsum += float(np.sum(2.0 * pn[act]))
             eig.append((Eq, Ub, Vb, act))
         erhfb = np.concatenate(erhfb); drhfb = np.concatenate(drhfb)
         if len(erhfb) == 0:
             raise HFBReconstructionError("no states below the pairing window")
         sumnz = nsum - tz
-        al = _alambda(al, erhfb, drhfb, tz, cpv0_zero)
+        al, fwin = _alambda(al, erhfb, drhfb, tz, cpv0_zero, temper)
         final_ala = ala
         ala = al
+    per_block = None
+    if fwin is not None:
+        # ALambda's occupations, in the pairing-window numbering, are what DENSIT reads
+        counts = [int(np.sum(e[3])) for e in eig]
+        per_block = np.split(fwin, np.cumsum(counts)[:-1])
     return QPSolution([e[0] for e in eig], [e[1] for e in eig], [e[2] for e in eig],
-                      [e[3] for e in eig], final_ala)
+                      [e[3] for e in eig], final_ala, per_block)
 
 
 def local_densities(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float):
     """rho(r), tau(r) and the Laplacian of rho(r) of one isospin from the final
-    quasiparticles: DENSIT at T = 0 without blocking (hfbtho_solver.f90:4318-4734).
+    quasiparticles: DENSIT without blocking (hfbtho_solver.f90:4318-4734).
     Per block and pairing-window quasiparticle k, with f_up/down = sum_i V_ik phi_i
     over the spin-up/down basis states and Lambda_up/down = Omega -/+ 1/2:
     rho ~ f_u^2 + f_d^2; tau ~ (Lambda_u y f_u)^2 + (Lambda_d y f_d)^2 + |grad f|^2;
-    Laplacian ~ 2 (f_u Lap f_u + f_d Lap f_d + |grad f|^2).  The sums are
-    normalised to the particle number and freed of the quadrature weights."""
+    Laplacian ~ 2 (f_u Lap f_u + f_d Lap f_d + |grad f|^2).  At finite temperature
+    every term is (1 - f_k) (its V form) + f_k (the same with U), f_k the thermal
+    occupation of ALambda.  The sums are normalised to the particle number and
+    freed of the quadrature weights."""
     nghl = h.ngh * h.ngl
     tro = np.zeros(nghl); ttau = np.zeros(nghl); tdro = np.zeros(nghl)
     y2 = mb.y * mb.y
@@ -328,21 +356,27 @@ def local_densities(h: HelData, mb: MeshBasis, qp: QPSolution, tz: float):
         nd = int(nd)
         ns = h.ns[start:start + nd]
         up, dn = ns > 0, ns < 0
-        V = qp.V[ib][:, qp.active[ib]]
-        Vu, Vd = V[up].T, V[dn].T
         sl = slice(start, start + nd)
+        xl2, xp2 = mb.xlam[ib] ** 2 * y2, mb.xlap[ib] ** 2 * y2
+        thermal = qp.fwin is not None
+        parts = [(qp.V[ib][:, qp.active[ib]], 1.0 - qp.fwin[ib] if thermal else None)]
+        if thermal:
+            parts.append((qp.U[ib][:, qp.active[ib]], qp.fwin[ib]))
+        for W, wk in parts:
+            Wu, Wd = W[up].T, W[dn].T
 
-        def comp(a):
-            a = a[sl]
-            return Vu @ a[up], Vd @ a[dn]
-        fu, fd = comp(mb.qhla)
-        fur, fdr = comp(mb.fi1r)
-        fuz, fdz = comp(mb.fi1z)
-        fu2, fd2 = comp(mb.fi2d)
-        tw = np.sum(fur * fur + fdr * fdr + fuz * fuz + fdz * fdz, axis=0)
-        tro += np.sum(fu * fu + fd * fd, axis=0)
-        ttau += mb.xlam[ib] ** 2 * y2 * np.sum(fu * fu, axis=0) + mb.xlap[ib] ** 2 * y2 * np.sum(fd * fd, axis=0) + tw
-        tdro += np.sum(fu * fu2 + fd * fd2, axis=0) + tw
+            def comp(a):
+                a = a[sl]
+                return Wu @ a[up], Wd @ a[dn]
+            fu, fd = comp(mb.qhla)
+            fur, fdr = comp(mb.fi1r)
+            fuz, fdz = comp(mb.fi1z)
+            fu2, fd2 = comp(mb.fi2d)
+            kw = (lambda x: x) if wk is None else (lambda x: x * wk[:, None])
+            tw = np.sum(kw(fur * fur + fdr * fdr + fuz * fuz + fdz * fdz), axis=0)
+            tro += np.sum(kw(fu * fu + fd * fd), axis=0)
+            ttau += np.sum(kw(xl2 * fu * fu + xp2 * fd * fd), axis=0) + tw
+            tdro += np.sum(kw(fu * fu2 + fd * fd2), axis=0) + tw
         start += nd
     s = 2.0 * tro.sum()
     wgt = mb.wdcori * (2.0 * tz / s)
@@ -401,6 +435,14 @@ class HFBSolution:
     tau_p: np.ndarray = None
     d2rho_n: np.ndarray = None  # [nghl] Laplacian of the densities
     d2rho_p: np.ndarray = None
+    temperature: float = 0.0    # MeV; > 0: the statistical FAM with occupations fp, fn
+    fp: np.ndarray = None       # [dqp] thermal quasiparticle occupations
+    fn: np.ndarray = None
+
+    @property
+    def occupations(self):
+        """(fp, fn) of a finite-temperature solution, None at T = 0."""
+        return None if self.fp is None else (self.fp, self.fn)
 
     @property
     def dqp(self) -> int:
@@ -413,26 +455,29 @@ class HFBSolution:
 
 def load_hfb_solution(path) -> HFBSolution:
     """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file
-    (a path, or an already decoded :class:`HelData`)."""
+    (a path, or an already decoded :class:`HelData`).  A finite-temperature
+    solution is rebuilt with HFBTHO's thermal particle number and densities and
+    carries the quasiparticle occupations of the statistical FAM."""
     h = path if isinstance(path, HelData) else read_hel(path)
-    if h.set_temperature and h.temperature > 0.0:
-        # the reference then runs the statistical FAM on the thermal quasiparticles;
-        # rebuilding them needs HFBTHO's finite-temperature particle-number and density
-        # equations, which this reader does not restate
-        raise ValueError(f"the .hel ground state is at T = {h.temperature} MeV: rebuilding finite-temperature "
-                         "solutions is not supported (pass occupations from pynfam_gb300.statistics to GPUSolver "
-                         "to run the statistical FAM on a zero-temperature basis)")
     if int(h.N) % 2 or int(h.Z) % 2:
         # an odd nucleus is an HFBTHO solution with a blocked quasiparticle, whose
         # reconstruction (blocked hfbdiag/ALambda/DENSIT) this reader does not restate
         raise ValueError(f"the .hel ground state has N = {h.N}, Z = {h.Z}: rebuilding blocked odd-nucleus solutions "
                          "is not supported (pass EFA occupations from pynfam_gb300.statistics to GPUSolver to run "
                          "the statistical FAM on an even-even basis)")
+    temper = h.temperature if h.set_temperature else 0.0
     mb = build_mesh_basis(h)
     hd = hfb_matrices(h, mb)
-    qpn = diagonalise(h, hd, "n", float(h.N))
-    qpp = diagonalise(h, hd, "p", float(h.Z))
-    return assemble(h, mb, qpn, qpp)
+    qpn = diagonalise(h, hd, "n", float(h.N), temper)
+    qpp = diagonalise(h, hd, "p", float(h.Z), temper)
+    hfb = assemble(h, mb, qpn, qpp)
+    if temper > 1e-12:
+        # the statistical FAM's occupations from the final quasiparticle energies,
+        # 0 above the pairing window (hfbtho_solution.f90:376-389, 426, 446)
+        from .statistics import thermal_occupations
+        hfb.temperature = temper
+        hfb.fp, hfb.fn = thermal_occupations(hfb, temper)
+    return hfb
 
 
 def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution) -> HFBSolution:

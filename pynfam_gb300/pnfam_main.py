@@ -39,7 +39,7 @@ def load_ground_state(hel_path: str):
     if cdir:
         with open(hel_path, "rb") as fh:
             # the tag changes whenever the cached HFBSolution gains fields
-            key = hashlib.sha256(b"hfb-solution-2\0" + fh.read()).hexdigest()
+            key = hashlib.sha256(b"hfb-solution-3\0" + fh.read()).hexdigest()
         p = os.path.join(cdir, key + ".pkl")
         if os.path.exists(p):
             try:
@@ -82,7 +82,7 @@ def main(argv=None) -> int:
         case = setup_case(nml, None, hfb=hfb)
         txtoutput.header(log, nml, case, int(hfb.n00))
         s = nml["solver"]
-        gpu = GPUSolver(case.hfb, case.couplings)
+        gpu = GPUSolver(case.hfb, case.couplings, occupations=case.hfb.occupations)
         gpu.set_operator(case.F, case.G)
         t0 = time.perf_counter()
         res = gpu.solve([case.omega], max_iter=int(s["max_iter"]), eps=float(s["convergence_epsilon"]),

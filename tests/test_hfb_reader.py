@@ -83,16 +83,37 @@ def test_corrupt_file_rejected(tmp_path):
         read_hel(str(bad))
 
 
-@pytest.mark.parametrize("what", ["temperature", "odd"])
-def test_unsupported_ground_states_are_refused(what):
-    """Finite-temperature and blocked (odd-nucleus) solutions need HFBTHO equations this
+def test_unsupported_ground_states_are_refused():
+    """A blocked (odd-nucleus) solution needs HFBTHO's blocking equations, which this
     reader does not restate: loading one stops with a message instead of a wrong state."""
     import copy
     from pynfam_gb300.hfb_solution import load_hfb_solution
     h = copy.copy(read_hel(HEL))
-    if what == "temperature":
-        h.set_temperature, h.temperature = True, 1.0
-    else:
-        h.N = h.N + 1
+    h.N = h.N + 1
     with pytest.raises(ValueError, match="not supported"):
         load_hfb_solution(h)
+
+
+def test_finite_temperature_reconstruction():
+    """The 40S fields rebuilt at finite temperature (thermal hfbdiag/ALambda/DENSIT):
+    the particle numbers hold, T -> 0 gives the zero-temperature state, and the
+    statistical FAM's occupations follow f = (1 - tanh(E/2T))/2, 0 above the window."""
+    import copy
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    cold = hfb("S40")
+    mb = build_mesh_basis(cold.hel)
+    assert cold.occupations is None
+    for T, close in ((1e-3, True), (1.5, False)):
+        h = copy.copy(read_hel(HEL))
+        h.set_temperature, h.temperature = True, T
+        s = load_hfb_solution(h)
+        fp, fn = s.occupations
+        assert s.temperature == T and fp.shape == (s.dqp,)
+        np.testing.assert_allclose(fn, np.where(s.En == 0, 0.0, 0.5 * (1 - np.tanh(0.5 * s.En / T))), rtol=0, atol=0)
+        assert abs(np.sum(s.rho_n / mb.wdcori) - 24.0) < 1e-9 and abs(np.sum(s.rho_p / mb.wdcori) - 16.0) < 1e-9
+        d = max(np.max(np.abs(s.rho_n - cold.rho_n)), np.max(np.abs(s.tau_p - cold.tau_p)),
+                np.max(np.abs(s.En - cold.En)))
+        if close:
+            assert d < 1e-10, d
+        else:
+            assert d > 1e-4 and np.max(fn) > 0.05

@@ -61,3 +61,23 @@ def test_occupations():
     assert bn[3] == 0.5 and bn[qp_t_reverse(h, 3)] == 0.5 and bn.sum() == 1.0 and not bp.any()
     with pytest.raises(ValueError):
         blocking_occupations(h, iqp_p=h.dqp)
+
+
+def test_finite_temperature_ground_state_solves():
+    """A finite-temperature ground state (the 40S fields rebuilt at T = 1 MeV) carries
+    its occupations into the statistical FAM, which converges; pnfam_main passes the
+    same occupations to the GPU solver."""
+    import copy
+    import os
+    from golden_cases import GOLDEN, golden, namelist_for
+    from pynfam_gb300.hel import read_hel
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    from pynfam_gb300.pnfam_setup import setup_case
+    h = copy.copy(read_hel(os.path.join(GOLDEN, "S40.hel")))
+    h.set_temperature, h.temperature = True, 1.0
+    hot = load_hfb_solution(h)
+    pt = golden("S40")["operators"]["GT-K0"][5]
+    c = setup_case(namelist_for("S40", pt), None, hfb=hot)
+    assert c.hfb.occupations is not None
+    r = _solve(c, c.hfb.occupations)
+    assert r.iter_conv > 0 and np.isfinite(r.re_str[0])
