@@ -51,12 +51,24 @@ def _flat_u(blocks):
 
 @pytest.mark.parametrize("case,op,idx,statistical,bminus", [
     ("S40", "GT-K0", 0, False, True), ("S40", "GT-K1", 0, True, True), ("S40", "RS1-K1", 0, True, True),
-    ("Kr116", "P-K0", 0, True, True), ("S40", "GT-K1", 0, True, False), ("S40", "RS2-K2", 0, False, False)])
+    ("Kr116", "P-K0", 0, True, True), ("S40", "GT-K1", 0, True, False), ("S40", "RS2-K2", 0, False, False),
+    ("synthetic12", "GT-K1", 0, True, True)])
 def test_task_tables_match_oracle_products(case, op, idx, statistical, bminus):
     import copy
     from pynfam_gb300 import _lib, build
     build.build()
-    c, _ = case_for(case, op, idx)
+    if case == "synthetic12":
+        # Omega-only blocks up to 91 (N_sh = 12): the multi-tile block shapes
+        import os
+        from golden_cases import GOLDEN, golden, namelist_for
+        from pynfam_gb300.pnfam_setup import setup_case
+        from pynfam_gb300.synthetic import bogoliubov_nucleus
+        hs = bogoliubov_nucleus(os.path.join(GOLDEN, "Gd162.hel"), 12, seed=1, parity=False)
+        nml = namelist_for("Gd162", golden("Gd162")["operators"][op][0])
+        nml["interaction"]["require_self_consistency"] = False
+        c = setup_case(nml, None, hfb=hs)
+    else:
+        c, _ = case_for(case, op, idx)
     h = c.hfb
     c.F = copy.copy(c.F)
     c.F.beta_minus = bminus
