@@ -14,7 +14,11 @@ non-empty stderr or a missing result as a failed point.
 
 The HFB reconstruction is cached per ``.hel`` content (directory from
 $PNFAM_GB300_CACHE, default ~/.cache/pynfam_gb300; set it to "off" to
-disable), so the points of one contour pay it once.
+disable), so the points of one contour pay it once.  With
+$PNFAM_GB300_SERVER naming the socket of a running point server
+(``python -m pynfam_gb300.pointserver <socket>``), the point is handed to that
+resident process, which batches the points of concurrent runs on the GPU; if
+no server answers there, the point runs here.
 """
 from __future__ import annotations
 
@@ -22,6 +26,7 @@ import hashlib
 import os
 import pickle
 import sys
+import threading
 import time
 
 HEL_NAME = "hfbtho_output.hel"
@@ -32,76 +37,134 @@ def _cache_dir():
     return None if d.lower() == "off" else d
 
 
+_MEMO = {}                  # ground states rebuilt in this process, by .hel content
+_MEMO_LOCK = threading.Lock()
+
+
 def load_ground_state(hel_path: str):
+    """The rebuilt ground state of a ``.hel`` file: from this process's memo, the
+    on-disk cache or a fresh reconstruction (each by the file's content)."""
     from .hfb_solution import load_hfb_solution
+    with open(hel_path, "rb") as fh:
+        # the tag changes whenever the cached HFBSolution gains fields
+        key = hashlib.sha256(b"hfb-solution-3\0" + fh.read()).hexdigest()
+    with _MEMO_LOCK:
+        if key in _MEMO:
+            return _MEMO[key]
     cdir = _cache_dir()
-    key = None
+    hfb = None
     if cdir:
-        with open(hel_path, "rb") as fh:
-            # the tag changes whenever the cached HFBSolution gains fields
-            key = hashlib.sha256(b"hfb-solution-3\0" + fh.read()).hexdigest()
         p = os.path.join(cdir, key + ".pkl")
         if os.path.exists(p):
             try:
                 with open(p, "rb") as fh:
-                    return pickle.load(fh)
+                    hfb = pickle.load(fh)
             except Exception:
+                hfb = None
+    if hfb is None:
+        hfb = load_hfb_solution(hel_path)
+        if cdir:
+            try:
+                os.makedirs(cdir, exist_ok=True)
+                tmp = os.path.join(cdir, f"{key}.{os.getpid()}.{threading.get_ident()}.tmp")
+                with open(tmp, "wb") as fh:
+                    pickle.dump(hfb, fh, protocol=pickle.HIGHEST_PROTOCOL)
+                os.replace(tmp, os.path.join(cdir, key + ".pkl"))
+            except OSError:
                 pass
-    hfb = load_hfb_solution(hel_path)
-    if cdir and key:
-        try:
-            os.makedirs(cdir, exist_ok=True)
-            tmp = os.path.join(cdir, f"{key}.{os.getpid()}.tmp")
-            with open(tmp, "wb") as fh:
-                pickle.dump(hfb, fh, protocol=pickle.HIGHEST_PROTOCOL)
-            os.replace(tmp, os.path.join(cdir, key + ".pkl"))
-        except OSError:
-            pass
+    with _MEMO_LOCK:
+        _MEMO[key] = hfb
     return hfb
 
 
-def main(argv=None) -> int:
+class Point:
+    """One pnfam_main run: its namelist, output log and solver inputs."""
+
+    def __init__(self, nml, log, case):
+        self.nml, self.log, self.case = nml, log, case
+
+    @property
+    def solve_kwargs(self) -> dict:
+        s = self.nml["solver"]
+        return dict(max_iter=int(s["max_iter"]), eps=float(s["convergence_epsilon"]),
+                    broyden_m=int(s["broyden_history_size"]), quench=self.case.quench)
+
+
+def prepare(nml_path: str, cwd: str = ".", sink=None) -> Point:
+    """Read the namelist and the ground state of the run directory ``cwd``, set up
+    the operator and write the header of ``<fam_output_filename>.dat``.  ``sink``
+    (a list) collects the lines the run would print instead of printing them."""
     from . import txtoutput
     from .namelist import read_pnfam_namelist
+    from .pnfam_setup import setup_case
+    log = None
+    try:
+        nml = read_pnfam_namelist(os.path.join(cwd, nml_path))
+        g = nml["general"]
+        name = str(g["fam_output_filename"]).strip()
+        log = txtoutput.Log(os.path.join(cwd, name + ".dat") if name else "", bool(g["print_stdout"]) or not name,
+                            sink=sink)
+        if int(g["use_fam_storage"]) != 0:
+            log.write(" Note: use_fam_storage is not supported; running without restart storage")
+        hfb = load_ground_state(os.path.join(cwd, HEL_NAME))
+        case = setup_case(nml, None, hfb=hfb, tbc_dir=cwd)
+        txtoutput.header(log, nml, case, int(hfb.n00))
+        return Point(nml, log, case)
+    except Exception as e:
+        if log is not None:
+            e.pnfam_log = log
+        raise
+
+
+def finish(pt: Point, res, index: int, seconds: float) -> None:
+    """The iteration table and the result table of point ``index`` of ``res``."""
+    from . import txtoutput
+    s = pt.nml["solver"]
+    it_conv = int(res.iters[index])
+    last = it_conv if it_conv >= 0 else int(s["max_iter"])
+    hist = [tuple(res.hist[index, i]) for i in range(last + 1)]
+    labels = [x.label for x in pt.case.G]
+    txtoutput.iterations(pt.log, hist, it_conv, float(res.si[index]), labels)
+    txtoutput.result(pt.log, seconds, pt.case.omega, res.re_S[index], res.im_S[index], labels)
+    pt.log.close()
+
+
+def fail(err: Exception, log=None) -> str:
+    """The reference aborts with a message and no result table."""
+    msg = f" ERROR: {type(err).__name__}: {err}"
+    log = log or getattr(err, "pnfam_log", None)
+    if log is not None:
+        log.write(msg)
+        log.close()
+    return msg.strip() + "\n"
+
+
+def main(argv=None) -> int:
     argv = sys.argv[1:] if argv is None else argv
     if len(argv) > 1:
         sys.stderr.write("More than one command-line argument! Aborting.\n")
         return 1
     nml_path = argv[0] if argv else "pnfam_NAMELIST.dat"
-    log = None
+    server = os.environ.get("PNFAM_GB300_SERVER", "")
+    if server:
+        from .pointserver import submit
+        rc = submit(server, os.getcwd(), nml_path)
+        if rc is not None:
+            return rc
+    pt = None
     try:
-        nml = read_pnfam_namelist(nml_path)
-        g = nml["general"]
-        name = str(g["fam_output_filename"]).strip()
-        log = txtoutput.Log(name + ".dat" if name else "", bool(g["print_stdout"]) or not name)
-        if int(g["use_fam_storage"]) != 0:
-            log.write(" Note: use_fam_storage is not supported; running without restart storage")
-        from .pnfam_setup import setup_case
+        pt = prepare(nml_path)
         from .solver import GPUSolver
-        hfb = load_ground_state(HEL_NAME)
-        case = setup_case(nml, None, hfb=hfb)
-        txtoutput.header(log, nml, case, int(hfb.n00))
-        s = nml["solver"]
-        gpu = GPUSolver(case.hfb, case.couplings, occupations=case.hfb.occupations)
-        gpu.set_operator(case.F, case.G)
+        gpu = GPUSolver(pt.case.hfb, pt.case.couplings, occupations=pt.case.hfb.occupations)
+        gpu.set_operator(pt.case.F, pt.case.G)
         t0 = time.perf_counter()
-        res = gpu.solve([case.omega], max_iter=int(s["max_iter"]), eps=float(s["convergence_epsilon"]),
-                        broyden_m=int(s["broyden_history_size"]), quench=case.quench, history=True)
+        res = gpu.solve([pt.case.omega], history=True, **pt.solve_kwargs)
         dt = time.perf_counter() - t0
         gpu.close()
-        it_conv = int(res.iters[0])
-        last = it_conv if it_conv >= 0 else int(s["max_iter"])
-        hist = [tuple(res.hist[0, i]) for i in range(last + 1)]
-        txtoutput.iterations(log, hist, it_conv, float(res.si[0]), [x.label for x in case.G])
-        txtoutput.result(log, dt, case.omega, res.re_S[0], res.im_S[0], [x.label for x in case.G])
-        log.close()
+        finish(pt, res, 0, dt)
         return 0
-    except Exception as e:  # the reference aborts with a message and no result table
-        msg = f" ERROR: {type(e).__name__}: {e}"
-        if log is not None:
-            log.write(msg)
-            log.close()
-        sys.stderr.write(msg.strip() + "\n")
+    except Exception as e:
+        sys.stderr.write(fail(e, pt.log if pt else None))
         return 1
 
 

@@ -16,9 +16,13 @@ VERSION = "2.00-gb300"
 
 
 class Log:
-    def __init__(self, path: str, to_stdout: bool):
+    """``sink``: a list that takes the printed lines instead of stdout (a run served
+    by another process returns them to its caller)."""
+
+    def __init__(self, path: str, to_stdout: bool, sink=None):
         self.fh = open(path, "w") if path else None
         self.to_stdout = to_stdout
+        self.sink = sink
 
     def write(self, s: str = "", comment: bool = True):
         line = ("#" + s) if comment else (" " + s)
@@ -26,7 +30,10 @@ class Log:
         if self.fh:
             self.fh.write(line + "\n")
         if self.to_stdout:
-            sys.stdout.write(line + "\n")
+            if self.sink is not None:
+                self.sink.append(line)
+            else:
+                sys.stdout.write(line + "\n")
 
     def close(self):
         if self.fh:

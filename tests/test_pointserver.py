@@ -1,0 +1,107 @@
+"""The point server: pnfam_main runs handed to a resident process and batched.
+
+Runs on the CPU with a fake device solver: each client is a pnfam_main run in its
+own run directory (namelist + .hel, as pynfam prepares them); the server prepares
+the points with the real host code, batches the concurrent points of one key into
+one solve, and every run directory gets the .dat a standalone run writes.
+"""
+import json
+import os
+import shutil
+import threading
+
+import numpy as np
+import pytest
+
+from golden_cases import GOLDEN, golden
+from pynfam_gb300 import pnfam_main
+from pynfam_gb300.pointserver import PointServer, submit
+from pynfam_gb300.solver import SolveResult
+from test_pnfam_main import parse_dat, write_in
+
+
+class FakeSolver:
+    """Strength = (Re w, Im w) of each point; the iteration table converges at 2."""
+
+    def __init__(self, pt, log):
+        self.nops = 1 + len(pt.case.G)
+        self.log = log
+
+    def solve(self, omegas, history=True, max_iter=300, **kw):
+        w = np.asarray(omegas, dtype=complex)
+        P = len(w)
+        self.log.append(P)
+        re = np.repeat(w.real[:, None], self.nops, axis=1)
+        im = np.repeat(w.imag[:, None], self.nops, axis=1)
+        hist = np.full((P, max_iter + 1, 3), np.nan)
+        hist[:, 0] = (1.0, 0.0, 0.0)
+        hist[:, 1] = (1e-3, 0.5, 0.5)
+        hist[:, 2] = (1e-9, 1.0, 1.0)
+        return SolveResult(re, im, np.full(P, 2, dtype=np.int32), np.full(P, 1e-9), hist, 0.0)
+
+    def close(self):
+        pass
+
+
+def _run_dir(tmp_path, name, pt, interaction, op):
+    d = tmp_path / name
+    d.mkdir()
+    write_in(d / f"{op}.in", pt, interaction, op)
+    shutil.copyfile(os.path.join(GOLDEN, "S40.hel"), d / "hfbtho_output.hel")
+    return d
+
+
+def test_concurrent_runs_share_one_batch(tmp_path, monkeypatch):
+    monkeypatch.setenv("PNFAM_GB300_CACHE", "off")
+    g = golden("S40")
+    pts = g["operators"]["GT-K0"][:3]
+    log = []
+    sock = str(tmp_path / "pnfam.sock")
+    srv = PointServer(sock, solver_factory=lambda pt: FakeSolver(pt, log), window=1.0).start()
+    try:
+        dirs = [_run_dir(tmp_path, f"run{i}", p, g["interaction"], "GT-K0") for i, p in enumerate(pts)]
+        rcs = [None] * len(dirs)
+
+        def client(i):
+            rcs[i] = submit(sock, str(dirs[i]), "GT-K0.in")
+        th = [threading.Thread(target=client, args=(i,)) for i in range(len(dirs))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join(timeout=60)
+        assert rcs == [0, 0, 0]
+        assert log == [3]   # one batch of the three points
+        for d, p in zip(dirs, pts):
+            version, conv, t, rows = parse_dat(d / "GT-K0.dat")
+            assert conv == "Yes" and version
+            w = complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"])
+            assert rows["Strength"] == pytest.approx((w.real, w.imag), rel=1e-15)
+            assert "Two-body current mode" in open(d / "GT-K0.dat").read()
+        # another operator is another key: its own batch and context
+        d = _run_dir(tmp_path, "other", g["operators"]["GT-K1"][0], g["interaction"], "GT-K1")
+        assert submit(sock, str(d), "GT-K1.in") == 0
+        assert log == [3, 1] and len(srv.solvers) == 2
+    finally:
+        srv.stop()
+    assert not os.path.exists(sock)
+
+
+def test_server_reports_errors_like_a_run(tmp_path, monkeypatch, capsys):
+    monkeypatch.setenv("PNFAM_GB300_CACHE", "off")
+    g = golden("S40")
+    sock = str(tmp_path / "pnfam.sock")
+    srv = PointServer(sock, solver_factory=lambda pt: FakeSolver(pt, []), window=0.0).start()
+    try:
+        d = tmp_path / "nohel"
+        d.mkdir()
+        write_in(d / "GT-K0.in", g["operators"]["GT-K0"][0], g["interaction"], "GT-K0")
+        assert submit(sock, str(d), "GT-K0.in") == 1
+        err = capsys.readouterr().err
+        assert "hfbtho_output.hel" in err
+        assert "Strength" not in open(d / "GT-K0.dat").read()
+    finally:
+        srv.stop()
+
+
+def test_client_without_server_runs_the_point_itself(tmp_path):
+    assert submit(str(tmp_path / "absent.sock"), str(tmp_path), "x.in") is None
