@@ -105,3 +105,35 @@ def test_server_reports_errors_like_a_run(tmp_path, monkeypatch, capsys):
 
 def test_client_without_server_runs_the_point_itself(tmp_path):
     assert submit(str(tmp_path / "absent.sock"), str(tmp_path), "x.in") is None
+
+
+@pytest.mark.gpu
+def test_point_server_on_the_gpu(tmp_path, monkeypatch):
+    """Three concurrent runs of recorded points through the server's device batch:
+    the recorded strengths (1e-6), one batch, one context."""
+    monkeypatch.setenv("PNFAM_GB300_CACHE", "off")
+    g = golden("S40")
+    pts = g["operators"]["GT-K0"][:3]
+    sock = str(tmp_path / "pnfam.sock")
+    srv = PointServer(sock, window=2.0).start()
+    try:
+        dirs = [_run_dir(tmp_path, f"run{i}", p, g["interaction"], "GT-K0") for i, p in enumerate(pts)]
+        rcs = [None] * len(dirs)
+
+        def client(i):
+            rcs[i] = submit(sock, str(dirs[i]), "GT-K0.in")
+        th = [threading.Thread(target=client, args=(i,)) for i in range(len(dirs))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join(timeout=120)
+        assert rcs == [0, 0, 0] and srv.batches == [3] and len(srv.solvers) == 1
+        for d, p in zip(dirs, pts):
+            _, conv, _, rows = parse_dat(d / "GT-K0.dat")
+            assert conv == "Yes"
+            for lab, (re_, im_) in p["result"].items():
+                got = rows[lab]
+                assert abs(got[0] - re_) <= 1e-6 * abs(re_) + 1e-15, (lab, got, re_)
+                assert abs(got[1] - im_) <= 1e-6 * abs(im_) + 1e-15, (lab, got, im_)
+    finally:
+        srv.stop()
