@@ -23,19 +23,64 @@ class InteractionError(RuntimeError):
     pass
 
 
-# name -> (t0, t1, t2, t3, x0, x1, x2, x3, b4, b4p, alpha, tte, tto, uses_j2)
-# SkO': P.-G. Reinhard et al., Phys. Rev. C 60, 014316 (1999)
+# name -> (label, t0, t1, t2, t3, x0, x1, x2, x3, b4, b4p, alpha, tte, tto, uses_j2); the
+# parameter sets the reference tabulates (pnfam_interaction.f90:339-667), with the spin-orbit
+# b4 = b4' = W0/2 where a set gives W0.  The same numbers are needed to give the same
+# couplings; the papers are those the reference cites:
+# SIII: M. Beiner et al., Nucl. Phys. A 238, 29 (1975) (HFBTHO v2 alpha and x3)
+# SGII: N. V. Giai, H. Sagawa, Phys. Lett. B 106, 379 (1981)
 # SkM*: J. Bartel et al., Nucl. Phys. A 386, 79 (1982)
-# SLy4: E. Chabanat et al., Nucl. Phys. A 635, 231 (1998) (HFBTHO's rounding)
+# SkO, SkO': P.-G. Reinhard et al., Phys. Rev. C 60, 014316 (1999)
+# SLy4, SLy5: E. Chabanat et al., Nucl. Phys. A 635, 231 (1998) (HFBTHO's rounding, and the
+#   published values as SLY4PUB / SLY5PUB)
+# T43: T. Lesinski et al., Phys. Rev. C 76, 014312 (2007)
+# SV-min: P. Kluepfel et al., Phys. Rev. C 79, 034310 (2009)
+# UNEDF0/1/2: M. Kortelainen et al., Phys. Rev. C 89, 054314 (2014) supplement (tensor terms
+#   dropped for UNEDF0/1, as in the reference); UNEDF1-HFB: N. Schunck et al., J. Phys. G 42,
+#   034024 (2015) (time-odd tensor terms dropped)
 _SKYRME = {
-    "SKOP": ("SkO'", -2099.419, 301.531, 154.781, 13526.464, -0.029503, -1.325732,
-             -2.323439, -0.147404, 143.895, -82.8888, 0.25, 0.0, 0.0, True),
+    "SIII": ("SIII", -1128.75, 395.0, -95.0, 14000.0, 0.45, 0.0, 0.0, 1.0,
+             120.0 / 2.0, 120.0 / 2.0, 1.0, 0.0, 0.0, False),
+    "SGII": ("SGII", -2645.0, 340.0, -41.9, 15595.0, 0.09, -0.0588, 1.425, 0.06044,
+             105.0 / 2.0, 105.0 / 2.0, 1.0 / 6.0, 0.0, 0.0, False),
     "SKM*": ("SkM*", -2645.0, 410.0, -135.0, 15595.0, 0.09, 0.0, 0.0, 0.0,
              65.0, 65.0, 1.0 / 6.0, 0.0, 0.0, False),
+    "SKO": ("SkO", -2103.653, 303.352, 791.674, 13553.252, -0.210701, -2.810752, -1.461595,
+            -0.429881, 176.578, -198.7490, 1.0 / 4.0, 0.0, 0.0, False),
+    "SKOP": ("SkO'", -2099.419, 301.531, 154.781, 13526.464, -0.029503, -1.325732,
+             -2.323439, -0.147404, 143.895, -82.8888, 0.25, 0.0, 0.0, True),
     "SLY4": ("SLy4", -2488.913, 486.818, -546.395, 13777.0, 0.834, -0.344, -1.0, 1.354,
              61.5, 61.5, 1.0 / 6.0, 0.0, 0.0, False),
+    "SLY4PUB": ("SLy4 (published)", -2488.91, 486.820, -546.390, 13777.0, 0.834, -0.344, -1.000, 1.354,
+                123.0 / 2.0, 123.0 / 2.0, 1.0 / 6.0, 0.0, 0.0, False),
+    "SLY5": ("SLy5 (HFBTHO)", -2483.45, 484.23, -556.69, 13757.00, 0.776, -0.317, -1.000, 1.263,
+             125.0 / 2.0, 125.0 / 2.0, 1.0 / 6.0, 0.0, 0.0, True),
+    "SLY5PUB": ("SLy5 (published)", -2484.88, 483.13, -549.40, 13763.00, 0.778, -0.328, -1.000, 1.267,
+                126.0 / 2.0, 126.0 / 2.0, 1.0 / 6.0, 0.0, 0.0, True),
+    "T43": ("T43", -2490.275, 494.608, -255.534, 13847.12, 0.698702, -0.781655, -0.646302, 1.135795,
+            153.103 / 2.0, 153.103 / 2.0, 1.0 / 6.0, 196.868, -49.160, True),
+    "SVMIN": ("SV-min", -2112.248, 295.781, 142.268, 13988.567, 0.243886, -1.434926, -2.625899,
+              0.258070, 111.291 / 2.0, 45.93615, 0.255368, 0.0, 0.0, False),
+    "UNEDF0": ("UNEDF0", -1883.68781034247695, 277.500212238931113, 608.430905591534383,
+               13901.9483446343256, 0.00974374651612197606, -1.77784394560870229,
+               -1.67699034528797575, -0.380790414633100260, 125.161, -91.2604,
+               0.321955989588264435, 0.0, 0.0, False),
+    "UNEDF1": ("UNEDF1", -2078.32802325564080, 239.400812041522045, 1575.11954189757989,
+               14263.6462470775950, 0.0537569206858470316, -5.07723238187693671,
+               -1.36650561394298609, -0.162491168089956339, 38.3680720616682009, 71.3165222295833985,
+               0.270018011502707600, 0.0, 0.0, False),
+    "UNEDF2": ("UNEDF2", -1735.45685190850349, 262.814456235313969, 1183.31263243304011,
+               12293.2432941125371, 0.172247227624101162, -3.76692685046941023,
+               -1.38349812677880979, 0.0528642727436126059, 25.6586677306483040, 77.3003893702710059,
+               0.351455132555483607, -240.140598215558754, -266.930662318713644, True),
+    "UNEDF1-HFB": ("UNEDF1-HFB", -1666.40609652204898, 255.225795498529067, 1521.27603913447047,
+                   12072.5070586946749, 0.146079699879160696, -4.82248258717499834,
+                   -1.35211044158474336, 0.00431668727902556615, 22.0338399999999979, 103.825096000000002,
+                   0.376580313583912030, 0.0, 0.0, False),
 }
-_ALIASES = {"SKO'": "SKOP"}
+_ALIASES = {"SKO'": "SKOP", "S3": "SIII", "SG2": "SGII", "SV-MIN": "SVMIN", "UNE0": "UNEDF0",
+            "UNE1": "UNEDF1", "UNE2": "UNEDF2", "UNEDF1HFB": "UNEDF1-HFB", "UNE1HFB": "UNEDF1-HFB",
+            "UNE1-HFB": "UNEDF1-HFB", "HFB1": "UNEDF1-HFB"}
 
 
 @dataclass

@@ -62,3 +62,20 @@ def test_missing_file():
 def test_unterminated_group():
     with pytest.raises(NamelistError):
         parse_namelist_text("&solver\n max_iter = 3\n")
+
+
+def test_every_tabulated_functional_gives_couplings():
+    """Each Skyrme set the reference tabulates (and its aliases) builds finite couplings on a
+    recorded ground state (pnfam_interaction.f90:339-690); the tensor-free relation
+    CJ0 = 2/3 CJ1, CJ2 = 2 CJ1 holds (:704-708)."""
+    import numpy as np
+    from golden_cases import hfb
+    from pynfam_gb300.interaction import _ALIASES, _SKYRME, init_interaction
+    h = hfb("S40")
+    for name in list(_SKYRME) + list(_ALIASES):
+        nml = {"interaction_name": name, "require_self_consistency": False, "require_gauge_invariance": False,
+               "force_j2_terms": False}
+        c = init_interaction(nml, h, h.rho_n + h.rho_p)
+        assert not c.skip_residual_interaction
+        assert np.all(np.isfinite(c.crho)) and np.all(np.isfinite(c.scalars()))
+        assert abs(c.ctj0 - 2.0 / 3.0 * c.ctj1) < 1e-12 and abs(c.ctj2 - 2.0 * c.ctj1) < 1e-12
