@@ -468,12 +468,8 @@ def load_hfb_solution(path) -> HFBSolution:
     temper = h.temperature if h.set_temperature else 0.0
     mb = build_mesh_basis(h)
     hd = hfb_matrices(h, mb)
-    # the two isospins are independent (LAPACK runs without the interpreter lock)
-    from concurrent.futures import ThreadPoolExecutor
-    with ThreadPoolExecutor(2) as ex:
-        fn = ex.submit(diagonalise, h, hd, "n", float(h.N), temper)
-        fp = ex.submit(diagonalise, h, hd, "p", float(h.Z), temper)
-        qpn, qpp = fn.result(), fp.result()
+    qpn = diagonalise(h, hd, "n", float(h.N), temper)
+    qpp = diagonalise(h, hd, "p", float(h.Z), temper)
     hfb = assemble(h, mb, qpn, qpp)
     if temper > 1e-12:
         # the statistical FAM's occupations from the final quasiparticle energies,
