@@ -44,13 +44,17 @@ _MEMO_LOCK = threading.Lock()
 def load_ground_state(hel_path: str):
     """The rebuilt ground state of a ``.hel`` file: from this process's memo, the
     on-disk cache or a fresh reconstruction (each by the file's content)."""
-    from .hfb_solution import load_hfb_solution
     with open(hel_path, "rb") as fh:
         # the tag changes whenever the cached HFBSolution gains fields
         key = hashlib.sha256(b"hfb-solution-3\0" + fh.read()).hexdigest()
-    with _MEMO_LOCK:
-        if key in _MEMO:
-            return _MEMO[key]
+    with _MEMO_LOCK:   # one reconstruction per .hel content, even for concurrent callers
+        if key not in _MEMO:
+            _MEMO[key] = _load_uncached(hel_path, key)
+        return _MEMO[key]
+
+
+def _load_uncached(hel_path: str, key: str):
+    from .hfb_solution import load_hfb_solution
     cdir = _cache_dir()
     hfb = None
     if cdir:
@@ -72,8 +76,6 @@ def load_ground_state(hel_path: str):
                 os.replace(tmp, os.path.join(cdir, key + ".pkl"))
             except OSError:
                 pass
-    with _MEMO_LOCK:
-        _MEMO[key] = hfb
     return hfb
 
 
