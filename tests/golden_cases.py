@@ -56,3 +56,33 @@ def recorded_values(point, labels):
     """Recorded (re, im) per output row, in solver order [Strength, cross terms...]."""
     res = point["result"]
     return [res[l] for l in labels]
+
+
+@functools.lru_cache(maxsize=None)
+def oracle_counts():
+    """The oracle's convergence step and first near-threshold iteration of every
+    recorded point (tests/golden/make_oracle_counts.py)."""
+    with open(os.path.join(GOLDEN, "oracle_counts.json")) as fh:
+        return json.load(fh)
+
+
+def count_window(point, oracle):
+    """(expected iteration count, allowance) of a recorded point.
+
+    The FAM stops at the first iteration with si < eps (`pnfam_solver.f90:127`).  Two
+    correct FP64 implementations stop at the same step where si falls through eps
+    decisively; where si lingers within 5 eps of the threshold for several iterations
+    before crossing it (¹⁶²Gd GT-K0 at omega = 2.746 + 0.1i: iterations 52 to 62 of
+    the recorded run), rounding differences pick another iteration of that stretch.
+    The expected count is the oracle's on the same inputs; the allowance is 2 plus
+    the longer of the two near-threshold stretches (the recorded run's and the
+    oracle's) beyond two iterations, plus the spread between the recorded run and the
+    oracle themselves."""
+    near = oracle["near"]
+    eps = point["namelist"]["convergence_epsilon"]
+    rec = point["converged"]
+    orc_conv, orc_first = oracle["point"]
+    rec_near = [h[0] for h in point["history"] if h[0] < rec and h[2] < near * eps]
+    stretch = max(rec - rec_near[0] if rec_near else 0,
+                  orc_conv - orc_first if orc_first is not None and orc_conv >= 0 else 0)
+    return orc_conv, 2 + max(0, stretch - 2) + abs(rec - orc_conv)

@@ -7,7 +7,7 @@ Tolerance: 1e-6 relative per Re/Im strength value (plus 1e-12 of the largest
 import numpy as np
 import pytest
 
-from golden_cases import case_for, golden, hfb
+from golden_cases import case_for, count_window, golden, hfb, oracle_counts
 from oracle.fam_oracle import FAMOracle, _Basis, calc_hamiltonian
 from pynfam_gb300.blockmatrix import BlockMatrix
 
@@ -56,10 +56,11 @@ def test_contour_batch_matches_recorded(case, op, solvers):
     scale = max(abs(complex(*p["result"]["Strength"])) for p in pts)
     worst = 0.0
     moved = 0
+    counts = oracle_counts()
     for i, p in enumerate(pts):
-        # near the 1e-7 threshold rounding differences grow over the last iterations and can
-        # move the convergence step (the FP64 oracle shows the same spread: up to 6 of 62)
-        assert abs(int(r.iters[i]) - p["converged"]) <= max(3, p["converged"] // 8), (i, r.iters[i], p["converged"])
+        assert r.iters[i] >= 0, (i, r.si[i])
+        want, slack = count_window(p, {"near": counts["near"], "point": counts["counts"][case][op][i]})
+        assert abs(int(r.iters[i]) - want) <= slack, (i, r.iters[i], want, p["converged"], slack)
         moved += int(r.iters[i]) != p["converged"]
         for k, lab in enumerate(labels):
             want = p["result"][lab]

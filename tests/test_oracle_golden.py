@@ -40,3 +40,34 @@ def test_oracle_matches_recorded(case, op, idx):
         assert abs(si - h[2]) < 1.5e-10 * max(1.0, abs(si)) + 6e-11
         assert abs(re - h[3]) < 6e-11 + 1e-9 * abs(re)
         assert abs(im - h[4]) < 6e-11 + 1e-9 * abs(im)
+
+
+def _counts():
+    from golden_cases import oracle_counts
+    return oracle_counts()
+
+
+def test_oracle_iteration_counts_match_recorded_runs():
+    """The oracle stops at the recorded iteration on all but a handful of the 594
+    recorded points; those few lie inside the window the GPU test allows for
+    rounding-sensitive stopping steps (tests/golden/oracle_counts.json, made by
+    tests/golden/make_oracle_counts.py)."""
+    from golden_cases import count_window, golden
+    d = _counts()
+    total = same = 0
+    for case, ops in d["counts"].items():
+        for op, lst in ops.items():
+            pts = golden(case)["operators"][op]
+            assert len(lst) == len(pts)
+            for p, o in zip(pts, lst):
+                total += 1
+                same += o[0] == p["converged"]
+                want, slack = count_window(p, {"near": d["near"], "point": o})
+                assert want >= 0 and abs(p["converged"] - want) <= slack
+    assert total == 594 and same >= 580, (total, same)
+
+
+@pytest.mark.parametrize("case,op,idx", [("S40", "GT-K0", 27), ("S40", "PS0-K0", 3), ("Kr116", "P-K0", 10)])
+def test_oracle_counts_fixture_is_the_oracle(case, op, idx):
+    _, pt, _, r = run(case, op, idx)
+    assert _counts()["counts"][case][op][idx][0] == r.iter_conv
