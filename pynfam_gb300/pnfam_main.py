@@ -41,12 +41,26 @@ _MEMO = {}                  # ground states rebuilt in this process, by .hel con
 _MEMO_LOCK = threading.Lock()
 
 
+# the modules whose code decides what a reconstruction produces: a change to any of
+# them gives new cache keys, so a stale reconstruction is never loaded
+_RECONSTRUCTION_SOURCES = ("hfb_solution.py", "hel.py", "interaction.py", "synthetic.py")
+
+
+def _code_digest() -> bytes:
+    h = hashlib.sha256(b"hfb-solution\0")
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name in _RECONSTRUCTION_SOURCES:
+        with open(os.path.join(here, name), "rb") as fh:
+            h.update(name.encode() + b"\0" + fh.read())
+    return h.digest()
+
+
 def load_ground_state(hel_path: str):
     """The rebuilt ground state of a ``.hel`` file: from this process's memo, the
-    on-disk cache or a fresh reconstruction (each by the file's content)."""
+    on-disk cache or a fresh reconstruction (each by the file's content and the
+    reconstruction code's own digest)."""
     with open(hel_path, "rb") as fh:
-        # the tag changes whenever the cached HFBSolution gains fields
-        key = hashlib.sha256(b"hfb-solution-3\0" + fh.read()).hexdigest()
+        key = hashlib.sha256(_code_digest() + fh.read()).hexdigest()
     with _MEMO_LOCK:   # one reconstruction per .hel content, even for concurrent callers
         if key not in _MEMO:
             _MEMO[key] = _load_uncached(hel_path, key)
@@ -59,7 +73,7 @@ def _load_uncached(hel_path: str, key: str):
     hfb = None
     if cdir:
         p = os.path.join(cdir, key + ".pkl")
-        if os.path.exists(p):
+        if os.path.exists(p) and _private(cdir) and _private(p):
             try:
                 with open(p, "rb") as fh:
                     hfb = pickle.load(fh)
@@ -69,7 +83,7 @@ def _load_uncached(hel_path: str, key: str):
         hfb = load_hfb_solution(hel_path)
         if cdir:
             try:
-                os.makedirs(cdir, exist_ok=True)
+                os.makedirs(cdir, mode=0o700, exist_ok=True)
                 tmp = os.path.join(cdir, f"{key}.{os.getpid()}.{threading.get_ident()}.tmp")
                 with open(tmp, "wb") as fh:
                     pickle.dump(hfb, fh, protocol=pickle.HIGHEST_PROTOCOL)
@@ -77,6 +91,16 @@ def _load_uncached(hel_path: str, key: str):
             except OSError:
                 pass
     return hfb
+
+
+def _private(path: str) -> bool:
+    """True if ``path`` belongs to this user and nobody else can write to it: a cached
+    reconstruction is unpickled only from such a file in such a directory."""
+    try:
+        st = os.stat(path)
+    except OSError:
+        return False
+    return st.st_uid == os.getuid() and not (st.st_mode & 0o022)
 
 
 class Point:

@@ -31,24 +31,38 @@ import time
 from . import pnfam_main
 
 
+# how long a client waits for its point (seconds; $PNFAM_GB300_SERVER_TIMEOUT overrides):
+# a server that stops answering fails the point instead of holding pynfam's worker
+DEFAULT_TIMEOUT = 3600.0
+
+
 def submit(path: str, cwd: str, nml_path: str, timeout: float = None):
     """Client side: run the point through the server at ``path``.  Returns the run's
-    exit status, or None if no server answers there (the caller runs the point)."""
+    exit status (1 if no reply came within ``timeout`` seconds), or None if no server
+    answers there (the caller runs the point)."""
+    if timeout is None:
+        timeout = float(os.environ.get("PNFAM_GB300_SERVER_TIMEOUT", DEFAULT_TIMEOUT))
     try:
         s = socket.socket(socket.AF_UNIX, socket.SOCK_STREAM)
         s.connect(path)
     except OSError:
         return None
+    buf = b""
     with s:
-        if timeout is not None:
-            s.settimeout(timeout)
-        s.sendall((json.dumps({"cwd": os.path.abspath(cwd), "namelist": nml_path}) + "\n").encode())
-        buf = b""
-        while not buf.endswith(b"\n"):
-            chunk = s.recv(65536)
-            if not chunk:
-                break
-            buf += chunk
+        s.settimeout(timeout)
+        try:
+            s.sendall((json.dumps({"cwd": os.path.abspath(cwd), "namelist": nml_path}) + "\n").encode())
+            while not buf.endswith(b"\n"):
+                chunk = s.recv(65536)
+                if not chunk:
+                    break
+                buf += chunk
+        except socket.timeout:
+            sys.stderr.write(f"pnfam point server: no reply within {timeout:g} s\n")
+            return 1
+        except OSError as e:
+            sys.stderr.write(f"pnfam point server: {e}\n")
+            return 1
     try:
         rep = json.loads(buf.decode())
     except ValueError:
@@ -94,8 +108,9 @@ class PointServer:
     first out)."""
 
     def __init__(self, path: str, solver_factory=gpu_solver, window: float = 0.05, max_batch: int = 256,
-                 max_contexts: int = 8):
+                 max_contexts: int = 8, point_timeout: float = DEFAULT_TIMEOUT):
         self.path = path
+        self.point_timeout = float(point_timeout)
         self.factory = solver_factory
         self.window = float(window)
         self.max_batch = int(max_batch)
@@ -124,8 +139,11 @@ class PointServer:
                 pt = pnfam_main.prepare(req["namelist"], req["cwd"], sink=sink)
                 done = threading.Event()
                 box = {}
+                if self._stop.is_set():
+                    raise RuntimeError("the point server is shutting down")
                 self.pending.put((point_key(pt), pt, done, box))
-                done.wait()
+                if not done.wait(self.point_timeout):
+                    raise RuntimeError(f"no result within {self.point_timeout:g} s")
                 if "error" in box:
                     raise box["error"]
                 pnfam_main.finish(pt, box["res"], box["index"], box["seconds"])
@@ -197,6 +215,17 @@ class PointServer:
                 for _, _, done, box in items:
                     box["error"] = e
                     done.set()
+        self._fail_pending()
+
+    def _fail_pending(self):
+        """Points queued after the batch loop has stopped get an error, not a wait."""
+        while True:
+            try:
+                _, _, done, box = self.pending.get_nowait()
+            except queue.Empty:
+                return
+            box["error"] = RuntimeError("the point server stopped before solving this point")
+            done.set()
 
     # -- lifecycle ------------------------------------------------------------
     def start(self):
@@ -220,6 +249,7 @@ class PointServer:
             self._sock.close()
         if os.path.exists(self.path):
             os.unlink(self.path)
+        self._fail_pending()
         for s in self.solvers.values():
             s.close()
         self.solvers.clear()

@@ -103,6 +103,54 @@ def test_server_reports_errors_like_a_run(tmp_path, monkeypatch, capsys):
         srv.stop()
 
 
+class StuckSolver(FakeSolver):
+    """A device solve that does not come back until the test releases it."""
+
+    def __init__(self, pt, release):
+        super().__init__(pt, [])
+        self.release = release
+
+    def solve(self, omegas, **kw):
+        self.release.wait(30)
+        return super().solve(omegas, **kw)
+
+
+def test_a_point_that_gets_no_result_fails_instead_of_waiting(tmp_path, monkeypatch, capsys):
+    """The server gives up on a point after point_timeout, the client after its own
+    timeout; both report a failed run (exit status 1, message on stderr)."""
+    monkeypatch.setenv("PNFAM_GB300_CACHE", "off")
+    g = golden("S40")
+    pt = g["operators"]["GT-K0"][0]
+    release = threading.Event()
+    sock = str(tmp_path / "pnfam.sock")
+    srv = PointServer(sock, solver_factory=lambda p: StuckSolver(p, release), window=0.0,
+                      point_timeout=0.5).start()
+    try:
+        d = _run_dir(tmp_path, "server_gives_up", pt, g["interaction"], "GT-K0")
+        assert submit(sock, str(d), "GT-K0.in", timeout=20) == 1
+        assert "no result within" in capsys.readouterr().err
+        srv.point_timeout = 60.0
+        d = _run_dir(tmp_path, "client_gives_up", pt, g["interaction"], "GT-K0")
+        assert submit(sock, str(d), "GT-K0.in", timeout=0.5) == 1
+        assert "no reply within" in capsys.readouterr().err
+    finally:
+        release.set()
+        srv.stop()
+
+
+def test_points_queued_at_stop_are_failed(tmp_path, monkeypatch):
+    monkeypatch.setenv("PNFAM_GB300_CACHE", "off")
+    g = golden("S40")
+    sock = str(tmp_path / "pnfam.sock")
+    srv = PointServer(sock, solver_factory=lambda p: FakeSolver(p, []), window=0.0)
+    pt = pnfam_main.prepare("GT-K0.in", str(_run_dir(tmp_path, "late", g["operators"]["GT-K0"][0],
+                                                          g["interaction"], "GT-K0")), sink=[])
+    done, box = threading.Event(), {}
+    srv.pending.put(("key", pt, done, box))
+    srv.stop()          # never started: the queued point is answered with an error
+    assert done.is_set() and isinstance(box["error"], RuntimeError)
+
+
 def test_client_without_server_runs_the_point_itself(tmp_path):
     assert submit(str(tmp_path / "absent.sock"), str(tmp_path), "x.in") is None
 
