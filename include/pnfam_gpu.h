@@ -74,7 +74,15 @@ typedef struct {
                                  is accepted only on that anchor.  Every evaluation counts
                                  against max_iter.  Broyden, Green's function and strength
                                  are FP64 in both modes. */
-  int reserved[7];            /* [0]: per-stage event timing on/off; [1]: see precision */
+  int reserved[7];            /* [0]: per-stage event timing on/off; [1]: see precision;
+                                 [2]: live timing of the FP32 density and field-projection
+                                 launches (an event pair around each launch on its own
+                                 stream, read after the engine's wait; no serialisation);
+                                 [3] = n > 0: convergence also asks every strength value
+                                 (Re and Im of the strength and each cross term) to have
+                                 settled, |S - S_previous| <= 10^-n |S| + 1e-13 max|S|, for
+                                 at most 20 iterations beyond si < epsilon (0: the
+                                 reference's test si < epsilon alone) */
 } pnfam_solver_opts_t;
 
 /*
@@ -273,8 +281,10 @@ long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
  * nstage > 8, the whole solve's device time (CUDA events on the solver's
  * stream), if nstage > 10 the FP64 and FP32 point-iterations of the solve,
  * then (entries 11-15) the first five stages of the FP32 evaluations of the
- * mixed form (entries 0-4 then hold the FP64 evaluations only), and the number
- * of kernel launches.  An engine's figures accumulate from its creation. */
+ * mixed form (entries 0-4 then hold the FP64 evaluations only), then (entries
+ * 16-19, with opts.reserved[2] != 0) the number and total device ms of the FP32
+ * density launches and of the FP32 field-projection launches, and the number of
+ * kernel launches.  An engine's figures accumulate from its creation. */
 int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
                            long long* launches);
 

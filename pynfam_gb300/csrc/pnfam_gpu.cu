@@ -7,6 +7,7 @@
 // the reference's per-process ifam loop (pnfam_solver.f90:114-209) does.
 #include "../../include/pnfam_gpu.h"
 #include "pnfam_kernels.cuh"
+#include "pair_gemm.cuh"
 
 #include <cuda_runtime.h>
 
@@ -253,6 +254,26 @@ struct pnfam_ctx {
   // FP32 densities on the tensor cores (k_density_tc2, the default) or on the SIMT
   // cores (k_density<float>, PNFAM_GB300_TC_DENSITY=0 at context creation)
   bool tc_density = true;
+  // FP32 densities and field projection as GEMMs against the operator's pair tensor
+  // (pair_gemm.cuh): PNFAM_GB300_PAIR_GEMM=0 at context creation keeps the kernels
+  // above; the pair tensor is formed only while it fits PNFAM_GB300_PAIR_GEMM_GB
+  // (default 16 GB), and used for evaluations of at least pg_min points
+  int pg_mode = 1;
+  double pg_budget = 16e9;
+  int pg_min = 4;
+  bool pg_on = false, pg_built = false;
+  std::vector<PGProb> pg_probs;
+  std::vector<PGElem> pg_elems;
+  std::vector<PGTask> pg_tproj, pg_tdens;
+  std::vector<PGBChunk> pg_bproj, pg_bdens;
+  std::vector<PGAChunk> pg_ach;
+  PGFold pg_fold{};
+  long long pg_nachunk = 0, pg_nbchunk = 0, pg_dfloats = 0;
+  DBuf<PGProb> d_pg_probs;
+  DBuf<PGElem> d_pg_elems;
+  DBuf<PGTask> d_pg_tproj, d_pg_tdens;
+  DBuf<PGBChunk> d_pg_bproj, d_pg_bdens;
+  DBuf<float> d_pg_a, d_pg_b, d_pg_d;
   int nchunk_bro = 1, nchunk_c = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -262,6 +283,15 @@ struct pnfam_ctx {
   cudaEvent_t evd = nullptr;                 // end of the engine's evaluation in flight
   double stage_ms[8] = {0};     // FP64 evaluations (0-4) and the common stages (5-7)
   double stage32_ms[5] = {0};   // FP32 evaluations of the mixed form
+  // live timing of the FP32 density and field-projection launches (opts.reserved[2]):
+  // an event pair around each launch on its own stream, read once the engine has
+  // waited for the evaluation, so nothing is serialised or synchronised for it
+  bool live = false;
+  std::vector<cudaEvent_t> lev;   // [2 * pairs]
+  std::vector<int> lkind;         // stage of each pair: 0 density, 1 field projection
+  int nlev = 0;
+  double live_ms[2] = {0.0, 0.0};
+  long long live_n[2] = {0, 0};
   double total_ms = 0.0;
   long long launches = 0;
   pnfam_engine* engine = nullptr;   // the engine using this context's solve buffers
@@ -289,6 +319,8 @@ struct pnfam_ctx {
     d_foff.release(); d_xtoff.release(); d_ytoff.release();
     d_htasks.release(); d_bufs.release(); d_htasks_tc.release(); d_actlist.release(); d_err.release();
     d_gsplit.release(); d_hptiles.release(); d_hphi.release();
+    d_pg_probs.release(); d_pg_elems.release(); d_pg_tproj.release(); d_pg_tdens.release();
+    d_pg_bproj.release(); d_pg_bdens.release(); d_pg_a.release(); d_pg_b.release(); d_pg_d.release();
     k1a.d_tasks.release(); k1a.d_tile2task.release();
     k1b.d_tasks.release(); k1b.d_tile2task.release();
     k2a.d_tasks.release(); k2a.d_tile2task.release();
@@ -301,6 +333,7 @@ struct pnfam_ctx {
     if (evf[0]) cudaEventDestroy(evf[0]);
     if (evf[1]) cudaEventDestroy(evf[1]);
     if (evd) cudaEventDestroy(evd);
+    for (cudaEvent_t e : lev) cudaEventDestroy(e);
     if (stream64) cudaStreamDestroy(stream64);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -591,6 +624,209 @@ static void build_tasks(pnfam_ctx* c) {
 // ---------------------------------------------------------------------------
 // buffers for a batch of P points
 // ---------------------------------------------------------------------------
+// live kernel timing: the event index of a launch about to be enqueued on st (-1 when
+// live timing is off or an event could not be made)
+static int live_begin(pnfam_ctx* c, cudaStream_t st) {
+  if (!c->live) return -1;
+  while ((int)c->lev.size() < c->nlev + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    c->lev.push_back(e);
+  }
+  const int i = c->nlev;
+  if (cudaEventRecord(c->lev[i], st) != cudaSuccess) return -1;
+  c->nlev += 2;
+  c->lkind.resize(c->nlev / 2);
+  c->lkind[i / 2] = -1;
+  return i;
+}
+
+static void live_end(pnfam_ctx* c, int i, int kind, cudaStream_t st) {
+  if (i < 0) return;
+  if (cudaEventRecord(c->lev[i + 1], st) == cudaSuccess) c->lkind[i / 2] = kind;
+}
+
+// after the stream of the timed launches has been waited for
+static void live_collect(pnfam_ctx* c) {
+  for (int i = 0; i + 1 < c->nlev; i += 2) {
+    const int k = c->lkind[i / 2];
+    float ms = 0.f;
+    if (k >= 0 && cudaEventElapsedTime(&ms, c->lev[i], c->lev[i + 1]) == cudaSuccess) {
+      c->live_ms[k] += ms;
+      c->live_n[k] += 1;
+    }
+  }
+  c->nlev = 0;
+}
+
+// ---------------------------------------------------------------------------
+// pair-tensor GEMMs (pair_gemm.cuh): problems, element lists, tasks
+// ---------------------------------------------------------------------------
+static constexpr int PG_SMEM = 220 * 1024;   // dynamic shared memory of k_pg_gemm
+
+// stages of k_pg_gemm for B slots of bslot floats
+static int pg_stages(int bslot) {
+  const int per = (int)((PG_ACHUNK + bslot) * sizeof(float));
+  return std::max(2, std::min((int)PG_MAXSTAGE, PG_SMEM / per));
+}
+
+static void pg_setup(pnfam_ctx* c) {
+  c->pg_on = false;
+  c->pg_built = false;
+  c->pg_probs.clear(); c->pg_elems.clear(); c->pg_tproj.clear(); c->pg_tdens.clear();
+  c->pg_bproj.clear(); c->pg_bdens.clear(); c->pg_ach.clear();
+  for (int k = 0; k < 12; ++k) c->pg_fold.dens[k] = -1;
+  if (!c->pg_mode || c->nq != 2) return;
+  const int nghl = c->nghl, nb = c->nb;
+  auto cdiv = [](long long a, long long b) { return (a + b - 1) / b; };
+  // element lists of one structure, per class, in (block row, column, row) order
+  auto elements = [&](const std::vector<int>& cols, const std::vector<long long>& offs,
+                      std::vector<PGElem> (&out)[4]) {
+    for (int ix = 0; ix < nb; ++ix) {
+      const int iy = cols[ix];
+      if (iy < 0) continue;
+      const int d = c->db[ix], dc = c->db[iy];
+      for (int b = 0; b < dc; ++b)
+        for (int a = 0; a < d; ++a) {
+          const int ja = c->st[ix] + a, jb = c->st[iy] + b;
+          const int k = 2 * (c->ns[ja] < 0) + (c->ns[jb] < 0);
+          out[k].push_back(PGElem{ja, jb, offs[ix] + a + (long long)b * d});
+        }
+    }
+  };
+  long long a0 = 0, b0 = 0, d0 = 0;
+  auto add = [&](int kind, int pairing, int ncombo, int cls, int ncol, int call, const std::vector<PGElem>& el) {
+    if (el.empty()) return -1;
+    PGProb pr{};
+    pr.kind = kind; pr.pairing = pairing; pr.ncombo = ncombo; pr.cls = cls; pr.ncol = ncol; pr.call = call;
+    pr.e0 = (long long)c->pg_elems.size(); pr.ne = (int)el.size();
+    c->pg_elems.insert(c->pg_elems.end(), el.begin(), el.end());
+    if (kind == 0) { pr.mrows = pr.ne; pr.kdim = ncombo * nghl; }
+    else { pr.mrows = ncombo * nghl; pr.kdim = pr.ne; }
+    pr.nkc = (int)cdiv(pr.kdim, PG_K);
+    pr.ntile = (int)cdiv(pr.mrows, PG_M);
+    pr.nsplit = kind == 1 ? (int)std::max(1LL, cdiv(pr.nkc, 192)) : 1;
+    pr.a0 = a0; a0 += (long long)pr.ntile * pr.nkc;
+    pr.b0 = b0; b0 += pr.nkc;
+    pr.d0 = 0;
+    if (kind == 1) { pr.d0 = d0; d0 += (long long)pr.nsplit * ncol * PG_MAXPTS * pr.mrows; }
+    const int id = (int)c->pg_probs.size();
+    c->pg_probs.push_back(pr);
+    for (int t = 0; t < pr.ntile; ++t)
+      for (int s = 0; s < pr.nsplit; ++s) {
+        const int k0 = (int)((long long)pr.nkc * s / pr.nsplit), k1 = (int)((long long)pr.nkc * (s + 1) / pr.nsplit);
+        if (k1 <= k0) continue;
+        (kind == 0 ? c->pg_tproj : c->pg_tdens).push_back(PGTask{id, t, k0, k1 - k0, s, 0});
+      }
+    for (int kc = 0; kc < pr.nkc; ++kc) (kind == 0 ? c->pg_bproj : c->pg_bdens).push_back(PGBChunk{id, kc});
+    return id;
+  };
+  std::vector<PGElem> ef[4], ex[4], ey[4], ext[4], eyt[4];
+  elements(c->fc, c->foff, ef);
+  elements(c->xc, c->xoff, ex);
+  elements(c->yc, c->yoff, ey);
+  elements(c->xtc, c->xtoff, ext);
+  elements(c->ytc, c->ytoff, eyt);
+  for (int k = 0; k < 4; ++k) {
+    add(0, 0, 18, k, 4, -1, ef[k]);
+    add(0, 1, 1, k, 2, 0, ex[k]);
+    add(0, 1, 1, k, 2, 1, ey[k]);
+    c->pg_fold.dens[k] = add(1, 0, 16, k, 4, -1, ef[k]);
+    c->pg_fold.dens[4 + k] = add(1, 1, 1, k, 2, 0, ext[k]);
+    c->pg_fold.dens[8 + k] = add(1, 1, 1, k, 2, 1, eyt[k]);
+  }
+  c->pg_nachunk = a0;
+  c->pg_nbchunk = b0;
+  c->pg_dfloats = d0;
+  // the largest tasks first: the long projection tiles, then the density splits
+  std::stable_sort(c->pg_tproj.begin(), c->pg_tproj.end(),
+                   [](const PGTask& x, const PGTask& y) { return x.nkc > y.nkc; });
+  std::stable_sort(c->pg_tdens.begin(), c->pg_tdens.end(),
+                   [](const PGTask& x, const PGTask& y) { return x.nkc > y.nkc; });
+  const double bytes = (double)a0 * PG_ACHUNK * sizeof(float) + (double)b0 * PG_BCHUNK * sizeof(float) +
+                       (double)d0 * sizeof(float);
+  c->pg_on = bytes <= c->pg_budget;
+  if (!c->pg_on) return;
+  for (int id = 0; id < (int)c->pg_probs.size(); ++id) {
+    const PGProb& pr = c->pg_probs[id];
+    for (int t = 0; t < pr.ntile; ++t)
+      for (int kc = 0; kc < pr.nkc; ++kc) c->pg_ach.push_back(PGAChunk{id, t, kc, 0});
+  }
+}
+
+// device tables and the pair tensor (once per operator)
+static int pg_build(pnfam_ctx* c) {
+  if (!c->pg_on || c->pg_built) return PNFAM_OK;
+  CK(upload(c->d_pg_probs, c->pg_probs.data(), c->pg_probs.size()));
+  CK(upload(c->d_pg_elems, c->pg_elems.data(), c->pg_elems.size()));
+  CK(upload(c->d_pg_tproj, c->pg_tproj.data(), c->pg_tproj.size()));
+  CK(upload(c->d_pg_tdens, c->pg_tdens.data(), c->pg_tdens.size()));
+  CK(upload(c->d_pg_bproj, c->pg_bproj.data(), c->pg_bproj.size()));
+  CK(upload(c->d_pg_bdens, c->pg_bdens.data(), c->pg_bdens.size()));
+  CK(dalloc(c->d_pg_a, (size_t)c->pg_nachunk * PG_ACHUNK));
+  CK(dalloc(c->d_pg_b, (size_t)c->pg_nbchunk * PG_BCHUNK));
+  CK(dalloc(c->d_pg_d, (size_t)std::max(1LL, c->pg_dfloats)));
+  DBuf<PGAChunk> d_ach;
+  const cudaError_t e = upload(d_ach, c->pg_ach.data(), c->pg_ach.size());
+  if (e != cudaSuccess) { d_ach.release(); CK(e); }
+  const long long n = (long long)c->pg_ach.size();
+  for (long long i0 = 0; i0 < n; i0 += 1 << 20) {
+    const unsigned g = (unsigned)std::min<long long>(1 << 20, n - i0);
+    k_pg_build<<<g, 256, 0, c->stream>>>(c->d_phi32.p, c->dqp, c->nghl, c->d_pg_probs.p, c->d_pg_elems.p,
+                                         d_ach.p + i0, c->d_pg_a.p);
+  }
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t se = cudaStreamSynchronize(c->stream);
+  d_ach.release();
+  CK(le);
+  CK(se);
+  std::vector<PGAChunk>().swap(c->pg_ach);
+  c->pg_built = true;
+  return PNFAM_OK;
+}
+
+// densities of the points in c->d_actlist (nact of them) into dpart [P][2][1][2 ND][nghl]
+static int pg_density(pnfam_ctx* c, int nact, const float* rsp, float* dpart, cudaStream_t st) {
+  for (int g0 = 0; g0 < nact; g0 += PG_MAXPTS) {
+    const int na = std::min((int)PG_MAXPTS, nact - g0);
+    const int* al = c->d_actlist.p + g0;
+    const int bslot = ((4 * na + 15) / 16 * 16) * PG_K * 2;
+    const int ns = pg_stages(bslot);
+    k_pg_pack_rho<<<(unsigned)c->pg_bdens.size(), 256, 0, st>>>(c->d_pg_probs.p, c->d_pg_elems.p, c->d_pg_bdens.p,
+                                                                 al, na, rsp, c->nxy, c->d_pg_b.p);
+    const int lv = live_begin(c, st);
+    k_pg_gemm<<<(unsigned)c->pg_tdens.size(), PG_THREADS, pg_smem_bytes(ns, bslot), st>>>(
+        c->d_pg_probs.p, c->d_pg_tdens.p, c->d_pg_elems.p, c->d_pg_a.p, c->d_pg_b.p, na, al, ns, bslot, nullptr,
+        c->nxy, c->d_pg_d.p, c->d_err.p);
+    live_end(c, lv, 0, st);
+    k_pg_fold<<<dim3((unsigned)((c->nghl + 127) / 128), (unsigned)na, 2), 128, 0, st>>>(
+        c->d_pg_probs.p, c->pg_fold, c->d_pg_d.p, al, c->nghl, dpart);
+    c->launches += 3;
+    CK(cudaGetLastError());
+  }
+  return PNFAM_OK;
+}
+
+// field projection of the points in c->d_actlist into hsp [P][2][4][nxy]
+static int pg_projection(pnfam_ctx* c, int nact, const float* mf, float* hsp, cudaStream_t st) {
+  for (int g0 = 0; g0 < nact; g0 += PG_MAXPTS) {
+    const int na = std::min((int)PG_MAXPTS, nact - g0);
+    const int* al = c->d_actlist.p + g0;
+    const int bslot = ((4 * na + 15) / 16 * 16) * PG_K * 2;
+    const int ns = pg_stages(bslot);
+    k_pg_pack_field<<<(unsigned)c->pg_bproj.size(), 256, 0, st>>>(c->d_pg_probs.p, c->d_pg_bproj.p, al, na, mf,
+                                                                   c->nghl, c->d_pg_b.p);
+    const int lv = live_begin(c, st);
+    k_pg_gemm<<<(unsigned)c->pg_tproj.size(), PG_THREADS, pg_smem_bytes(ns, bslot), st>>>(
+        c->d_pg_probs.p, c->d_pg_tproj.p, c->d_pg_elems.p, c->d_pg_a.p, c->d_pg_b.p, na, al, ns, bslot, hsp,
+        c->nxy, nullptr, c->d_err.p);
+    live_end(c, lv, 1, st);
+    c->launches += 2;
+    CK(cudaGetLastError());
+  }
+  return PNFAM_OK;
+}
+
 static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   const long long nxy = c->nxy;
   const long long nv = 2 * c->nq * nxy;   // Re and Im of the QP state (X, Y[, P, Q])
@@ -716,15 +952,22 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
   const int G = f32 ? std::max(1, std::min(c->G, (2 * c->nsm + ntr * 2 * na - 1) / (ntr * 2 * na))) : c->G;
   int Gm = G;   // block-row groups of the partial densities
   bool dens_done = false;
+  // pair-tensor GEMMs for evaluations of enough points (one partial group)
+  const bool pair = f32 && c->pg_on && c->pg_built && nact >= c->pg_min;
   tic();
   if constexpr (f32) {
-    if (c->tc_density) {
+    if (pair) {
+      if ((rc = pg_density(c, nact, rsp, dpart, st))) return rc;
+      Gm = 1;
+      dens_done = true;
+    } else if (c->tc_density) {
       // tensor cores: c->d_actlist holds the nact points of this evaluation; their
       // densities are split and laid out first, then the units run on the tensor cores
       DensTCArgs t0{d0.rho, d0.rho_sp, d0.rho_spl, d0.rcols, d0.roffs, d0.kap, d0.kap_sp, d0.kap_spl, d0.kcols, d0.koffs};
       DensTCArgs t1{d1.rho, d1.rho_sp, d1.rho_spl, d1.rcols, d1.roffs, d1.kap, d1.kap_sp, d1.kap_spl, d1.kcols, d1.koffs};
       const int ntr32 = (c->nghl + 31) / 32;
       Gm = std::max(1, std::min(c->G, (2 * c->nsm + ntr32 * 2 * na - 1) / (ntr32 * 2 * na)));
+      const int lv = live_begin(c, st);
       if (!c->bchunks.empty()) {
         k_dens_bsplit<<<dim3((unsigned)c->bchunks.size(), (unsigned)na), 256, 0, st>>>(
             B, t0, t1, c->d_bchunks.p, c->d_actlist.p, c->d_bsplit.p, c->bstride);
@@ -733,6 +976,7 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
       k_density_tc2<<<dim3(ntr32, Gm, 2 * na), DTC2_THREADS, density_tc2_smem_bytes(), st>>>(
           B, c->d_dunits0.p, (int)c->dunits[0].size(), c->d_dunits1.p, (int)c->dunits[1].size(), c->d_aphi.p,
           (int)c->achunks.size(), c->d_bsplit.p, c->bstride, Gm, c->d_actlist.p, dpart, c->d_err.p);
+      live_end(c, lv, 0, st);
       c->launches++;
       CK(cudaGetLastError());
       dens_done = true;
@@ -756,12 +1000,18 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
   toc(2);
   tic();
   if constexpr (f32) {
-    // tensor cores: c->d_actlist holds the nact points of this evaluation
-    dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
-    k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), st>>>(
-        B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, c->d_hphi.p, hsp, nxy, c->d_err.p);
-    c->launches++;
-    CK(cudaGetLastError());
+    if (pair) {
+      if ((rc = pg_projection(c, nact, mf, hsp, st))) return rc;
+    } else {
+      // tensor cores: c->d_actlist holds the nact points of this evaluation
+      dim3 grid((unsigned)c->htasks_tc.size(), (unsigned)std::max(nact, 1));
+      const int lv = live_begin(c, st);
+      k_hproj_tc<<<grid, HTC_THREADS, hproj_tc_smem_bytes(c->tc_npmax), st>>>(
+          B, c->d_htasks_tc.p, c->d_actlist.p, nact, c->tc_npmax, mf, c->d_hphi.p, hsp, nxy, c->d_err.p);
+      live_end(c, lv, 1, st);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
   } else {
     dim3 grid((unsigned)c->htasks.size(), P);
     k_hproj_fp64<<<grid, 256, hproj_fp64_smem_bytes(), st>>>(B, c->d_htasks.p, mf, hsp, nxy, act);
@@ -858,6 +1108,10 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
     }
     c->have_gsplit = true;
   }
+  {
+    const int rc = pg_build(c);
+    if (rc) return rc;
+  }
   return PNFAM_OK;
 }
 
@@ -913,6 +1167,12 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     // FP32 densities on the tensor cores unless PNFAM_GB300_TC_DENSITY=0 (SIMT kernel)
     const char* v = std::getenv("PNFAM_GB300_TC_DENSITY");
     c->tc_density = !(v && v[0] == '0');
+    v = std::getenv("PNFAM_GB300_PAIR_GEMM");
+    c->pg_mode = (v && v[0] == '0') ? 0 : 1;
+    v = std::getenv("PNFAM_GB300_PAIR_GEMM_GB");
+    if (v && std::atof(v) > 0) c->pg_budget = std::atof(v) * 1e9;
+    v = std::getenv("PNFAM_GB300_PAIR_MIN");
+    if (v && std::atoi(v) > 0) c->pg_min = std::atoi(v);
   }
   const int s = c->dqp;
   const long long mo = c->uoff.back() + (long long)c->db.back() * c->db.back();
@@ -953,7 +1213,8 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
       cudaFuncSetAttribute(k_density_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)density_tc2_smem_bytes()) != cudaSuccess ||
       cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)gemm_tc_smem_bytes()) != cudaSuccess) {
+                           (int)gemm_tc_smem_bytes()) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pg_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, PG_SMEM) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
   }
@@ -1051,6 +1312,7 @@ extern "C" int pnfam_gpu_set_operator(pnfam_ctx_t* c, int beta_minus, const int*
   c->nchunk_bro = (int)((2 * nq * nf + BRO_CHUNK - 1) / BRO_CHUNK);
   c->nchunk_c = (int)std::min<long long>(32, std::max<long long>(1, (nq * nf) / 4096));
   build_tasks(c);
+  pg_setup(c);
   CK(c->k1a.finalize()); CK(c->k1b.finalize()); CK(c->k2a.finalize()); CK(c->k2b.finalize());
   {
     TaskList* src[4] = {&c->k1a, &c->k1b, &c->k2a, &c->k2b};
@@ -1110,6 +1372,11 @@ struct pnfam_engine {
   long long nxy = 0;
   bool no_res = false, mixed = false, timed = false;
   double switch_si = 0.0;
+  // opts.reserved[3] > 0: convergence also asks every strength value to have settled,
+  // |S - S_prev| <= s_rel |S| + 1e-13 max|S| on Re and Im of each value (at most
+  // EXTRA iterations beyond si < epsilon)
+  double s_rel = 0.0;
+  static constexpr int EXTRA = 20;
   static constexpr double NEAR = 1000.0;
   // a stall of the increment iteration counts as the FP32 noise floor (and takes an
   // anchor) only while si <= FLOOR * max|d|: far above that, FP32 rounding of the
@@ -1118,7 +1385,8 @@ struct pnfam_engine {
   // per slot (host)
   std::vector<int> active, it, anchor, since_best, nstall, fresh;
   std::vector<long long> tag;
-  std::vector<double> si, sre, sim, best, wre, wim;
+  std::vector<double> si, sre, sim, best, wre, wim, pre, pim;
+  std::vector<int> extra;
   std::vector<unsigned long long> hdmax;
   std::vector<int> pint, act32, act64, actlist;
   int herr = 0;
@@ -1178,10 +1446,16 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   // noise floor (si <= FLOOR*max|d|).  Every evaluation counts against max_iter.
   e->switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
   e->timed = o->reserved[0] != 0;
+  e->s_rel = o->reserved[3] > 0 ? std::pow(10.0, -o->reserved[3]) : 0.0;
+  c->live = o->reserved[2] != 0;
+  c->nlev = 0;
+  c->live_ms[0] = c->live_ms[1] = 0.0;
+  c->live_n[0] = c->live_n[1] = 0;
   const int nops = e->nops;
   e->active.assign(P, 0); e->it.assign(P, 0); e->anchor.assign(P, 1); e->since_best.assign(P, 0);
   e->nstall.assign(P, 0); e->fresh.assign(P, 0); e->tag.assign(P, -1);
   e->si.assign(P, 1.0); e->sre.assign((size_t)P * nops, 0.0); e->sim.assign((size_t)P * nops, 0.0);
+  e->pre.assign((size_t)P * nops, 0.0); e->pim.assign((size_t)P * nops, 0.0); e->extra.assign(P, 0);
   e->best.assign(P, 1e300); e->wre.assign(P, 0.0); e->wim.assign(P, 0.0); e->hdmax.assign(P, 0);
   e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
   e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
@@ -1215,7 +1489,7 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
   for (int p = 0; p < e->P && k < n; ++p) {
     if (e->active[p]) continue;
     e->active[p] = 1; e->it[p] = 0; e->anchor[p] = 1; e->since_best[p] = 0; e->nstall[p] = 0;
-    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1;
+    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1; e->extra[p] = 0;
     for (int q = 0; q < e->nops; ++q) { e->sre[(size_t)p * e->nops + q] = 0.0; e->sim[(size_t)p * e->nops + q] = 0.0; }
     e->wre[p] = re_w[k]; e->wim[p] = im_w[k];
     e->tag[p] = tags ? tags[k] : k;
@@ -1416,6 +1690,7 @@ static int engine_finish(pnfam_engine* e) {
   pnfam_ctx* c = e->c;
   CK(cudaStreamSynchronize(c->stream));
   e->pending = 0;
+  live_collect(c);
   {
     const int P = e->P;
     std::memcpy(e->hsi.data(), e->pin_d.p + 2 * P, sizeof(double) * P);
@@ -1436,26 +1711,41 @@ static int engine_finish(pnfam_engine* e) {
     const bool was_anchor = !e->mixed || e->anchor[p] || e->it[p] == 0;
     e->si[p] = e->hsi[p];
     if (!std::isfinite(e->si[p])) return fail(PNFAM_ENONFINITE, "non-finite residual");
+    double smax = 0.0;
     for (int k = 0; k < nops; ++k) {
       double a = 0.0, b = 0.0;
       for (int ch = 0; ch < c->nchunk_c; ++ch) {
         a += e->cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k];
         b += e->cpart[((size_t)p * c->nchunk_c + ch) * 2 * nops + 2 * k + 1];
       }
-      e->sre[(size_t)p * nops + k] = -a / pi;
-      e->sim[(size_t)p * nops + k] = -b / pi;
+      const size_t i = (size_t)p * nops + k;
+      e->pre[i] = e->sre[i]; e->pim[i] = e->sim[i];
+      e->sre[i] = -a / pi;
+      e->sim[i] = -b / pi;
+      smax = std::max(smax, std::max(std::fabs(e->sre[i]), std::fabs(e->sim[i])));
+    }
+    // every strength value settled (always, unless opts.reserved[3] asks for it)
+    bool settled = true;
+    if (e->s_rel > 0.0) {
+      for (int k = 0; k < nops && settled; ++k) {
+        const size_t i = (size_t)p * nops + k;
+        settled = std::fabs(e->sre[i] - e->pre[i]) <= e->s_rel * std::fabs(e->sre[i]) + 1e-13 * smax &&
+                  std::fabs(e->sim[i] - e->pim[i]) <= e->s_rel * std::fabs(e->sim[i]) + 1e-13 * smax;
+      }
     }
     const int it = ++e->it[p];
     engine_hist(e, p);
     const double si = e->si[p];
+    // convergence (si < epsilon), held back while a strength value still moves
+    auto accept = [&]() { return settled || ++e->extra[p] > pnfam_engine::EXTRA; };
     if (was_anchor) {
-      if (si < o.convergence_epsilon) { engine_retire(e, p, it); continue; }
+      if (si < o.convergence_epsilon && accept()) { engine_retire(e, p, it); continue; }
       if (e->mixed) { e->anchor[p] = 0; e->best[p] = si; e->since_best[p] = 0; }
     } else {
       double dm;
       std::memcpy(&dm, &e->hdmax[p], sizeof dm);
       const bool near = dm <= pnfam_engine::NEAR * o.convergence_epsilon;
-      if (si < o.convergence_epsilon && near) { engine_retire(e, p, it); continue; }
+      if (si < o.convergence_epsilon && near && accept()) { engine_retire(e, p, it); continue; }
       if (si < e->best[p] * 0.5) { e->best[p] = si; e->since_best[p] = 0; } else { ++e->since_best[p]; }
       // the stagnation window doubles with every anchor it has triggered
       const bool stalled = e->since_best[p] >= (5 << std::min(e->nstall[p], 4)) &&
@@ -1769,6 +2059,8 @@ extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, in
   if (nstage > 8) stage_ms[8] = c->total_ms;
   if (nstage > 10) { stage_ms[9] = (double)c->pit64; stage_ms[10] = (double)c->pit32; }
   for (int k = 11; k < nstage && k < 16; ++k) stage_ms[k] = c->stage32_ms[k - 11];
+  const double live[4] = {(double)c->live_n[0], c->live_ms[0], (double)c->live_n[1], c->live_ms[1]};
+  for (int k = 16; k < nstage && k < 20; ++k) stage_ms[k] = live[k - 16];
   if (launches) *launches = c->launches;
   return PNFAM_OK;
 }

@@ -101,7 +101,7 @@ class GPUSolver:
 
     @staticmethod
     def options(max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None, timed=False, precision=0,
-                switch_exp=0):
+                switch_exp=0, live=False, settle=0):
         if alpha_mix is None:
             from .pnfam_setup import ALPHA_MIX as alpha_mix
         o = _lib.SolverOpts()
@@ -110,6 +110,8 @@ class GPUSolver:
         o.quench_residual_int = float(quench); o.precision = int(precision)
         o.reserved[0] = 1 if timed else 0
         o.reserved[1] = int(switch_exp)
+        o.reserved[2] = 1 if live else 0
+        o.reserved[3] = int(settle)
         return o
 
     def engine(self, slots, owns_solver=False, **opts) -> "Engine":
@@ -118,13 +120,14 @@ class GPUSolver:
         return Engine(self, slots, self.options(**opts), owns_solver)
 
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
-              history=False, timed=False, precision=0, switch_exp=0) -> SolveResult:
+              history=False, timed=False, precision=0, switch_exp=0, settle=0) -> SolveResult:
         """precision 0: FP64 throughout (the reference's arithmetic and iteration
         trajectory).  precision 1: defect correction -- the field is evaluated in
         FP32 on the increment from an FP64 anchor; within 1000*eps of the anchor
         convergence is accepted on an FP32 increment evaluation, farther out an
         FP64 anchor evaluation is taken when si < 10**-switch_exp (default
-        100*eps) or si stops falling."""
+        100*eps) or si stops falling.  settle = n > 0: convergence also waits until
+        every strength value moved by at most 10**-n of itself in the last iteration."""
         import time
         w = np.atleast_1d(np.asarray(omegas, dtype=complex))
         P = len(w)
@@ -132,7 +135,8 @@ class GPUSolver:
         reS = np.zeros(P * self.nops); imS = np.zeros(P * self.nops)
         iters = np.zeros(P, dtype=np.int32); si = np.zeros(P)
         hist = np.full(P * (max_iter + 1) * 3, np.nan) if history else None
-        o = self.options(max_iter, eps, broyden_m, quench, alpha_mix, timed, precision, switch_exp)
+        o = self.options(max_iter, eps, broyden_m, quench, alpha_mix, timed, precision, switch_exp,
+                         settle=settle)
         t0 = time.perf_counter()
         _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
                                             _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
@@ -144,11 +148,12 @@ class GPUSolver:
     def last_profile(self):
         """Per-stage device ms of the last solve (or of this context's engine so far);
         the *_fp32 entries are the FP32 evaluations of the mixed form."""
-        ms = np.zeros(16); n = C.c_longlong()
-        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 16, C.byref(n)))
+        ms = np.zeros(20); n = C.c_longlong()
+        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 20, C.byref(n)))
         names = ("k1_blockgemm", "density", "meanfield", "field_projection", "k2_blockgemm", "green", "broyden",
                  "strength", "total", "point_iterations_fp64", "point_iterations_fp32", "k1_blockgemm_fp32",
-                 "density_fp32", "meanfield_fp32", "field_projection_fp32", "k2_blockgemm_fp32")
+                 "density_fp32", "meanfield_fp32", "field_projection_fp32", "k2_blockgemm_fp32",
+                 "live_density_launches", "live_density_ms", "live_projection_launches", "live_projection_ms")
         return dict(zip(names, ms.tolist())), int(n.value)
 
     def calc_hamiltonian(self, rho_pn, kp, rho_np, km, mixed=False):

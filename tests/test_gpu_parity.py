@@ -75,6 +75,8 @@ def test_contour_batch_matches_recorded(case, op, solvers):
 
 TIGHT = 1e-12      # FP64 convergence used as the exact fixed point
 MIXED_EPS = 1e-10  # convergence asked of the mixed form
+SETTLE = 8         # ... with every strength value settled to 1e-8 of itself (small cross
+                   # terms of a contour sit three orders below its largest strength)
 
 
 @pytest.mark.parametrize("case,op", ALL_OPS)
@@ -96,7 +98,7 @@ def test_mixed_precision_contour_matches_fp64(case, op, solvers):
     kw = dict(broyden_m=s["broyden_history_size"], quench=c.quench)
     exact = gpu.solve(omegas, max_iter=1500, eps=TIGHT, **kw)
     assert np.all(exact.iters >= 0), exact.si
-    r = gpu.solve(omegas, max_iter=1500, eps=MIXED_EPS, precision=1, **kw)
+    r = gpu.solve(omegas, max_iter=1500, eps=MIXED_EPS, precision=1, settle=SETTLE, **kw)
     prof, _ = gpu.last_profile()
     assert np.all(r.iters >= 0), r.si
     scale = np.max(np.abs(exact.re_S[:, 0] + 1j * exact.im_S[:, 0]))
@@ -318,6 +320,52 @@ def test_mixed_field_matches_fp64(case, op, monkeypatch):
     assert worst <= 1e-5
 
 
+@pytest.mark.parametrize("case,op", [("S40", "RS1-K1"), ("S40", "GT-K0"), ("Kr116", "P-K0"), ("Gd162", "GT-K1")])
+def test_pair_gemm_field_matches_fp64(case, op, monkeypatch):
+    """The mixed field evaluation through the pair-tensor GEMMs (densities and field
+    projection as 3xTF32 GEMMs against the operator's pair tensor; taken for a one-point
+    evaluation with PNFAM_GB300_PAIR_MIN=1 when the context is created) against the
+    FP64 field."""
+    monkeypatch.setenv("PNFAM_GB300_PAIR_GEMM", "1")
+    monkeypatch.setenv("PNFAM_GB300_PAIR_MIN", "1")
+    c, _ = case_for(case, op, 0)
+    worst = _mixed_vs_fp64(c, 6)
+    print(f"{case} {op}: pair-tensor GEMM field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
+
+
+def test_large_basis_pair_gemm_field_matches_fp64(large_case, monkeypatch):
+    monkeypatch.setenv("PNFAM_GB300_PAIR_GEMM", "1")
+    monkeypatch.setenv("PNFAM_GB300_PAIR_MIN", "1")
+    worst = _mixed_vs_fp64(large_case, 7)
+    print(f"N_sh=12 162Gd GT-K1: pair-tensor GEMM field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
+
+
+def test_pair_gemm_and_kernel_paths_agree_in_a_batch(monkeypatch):
+    """A contour solved in the mixed form with the pair-tensor GEMMs (the default for
+    evaluations of 4 or more points) and with the projection and density kernels
+    (PNFAM_GB300_PAIR_GEMM=0): the same fixed point within 1e-6."""
+    from pynfam_gb300.solver import GPUSolver
+    pts = golden("S40")["operators"]["RS1-K1"]
+    c, _ = case_for("S40", "RS1-K1", 0)
+    omegas = [complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"]) for p in pts]
+    kw = dict(broyden_m=c.nml["solver"]["broyden_history_size"], quench=c.quench, max_iter=1500,
+              eps=MIXED_EPS, precision=1, settle=SETTLE)
+    res = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("PNFAM_GB300_PAIR_GEMM", mode)
+        gpu = GPUSolver(c.hfb, c.couplings)
+        gpu.set_operator(c.F, c.G)
+        res[mode] = gpu.solve(omegas, **kw)
+        gpu.close()
+    a, b = res["1"], res["0"]
+    assert np.all(a.iters >= 0) and np.all(b.iters >= 0)
+    scale = np.max(np.abs(b.re_S[:, 0] + 1j * b.im_S[:, 0]))
+    for x, y in ((a.re_S, b.re_S), (a.im_S, b.im_S)):
+        assert np.all(np.abs(x - y) <= REL * np.abs(y) + 1e-12 * scale)
+
+
 def test_large_basis_mixed_field_matches_fp64(large_case):
     worst = _mixed_vs_fp64(large_case, 4)
     print(f"N_sh=12 162Gd GT-K1: mixed field worst relative error {worst:.2e}")
@@ -348,7 +396,7 @@ def test_tensor_core_density_mixed_solve(monkeypatch, case, op):
     gpu = GPUSolver(c.hfb, c.couplings)
     gpu.set_operator(c.F, c.G)
     exact = gpu.solve(omegas, max_iter=1500, eps=TIGHT, **kw)
-    r = gpu.solve(omegas, max_iter=1500, eps=MIXED_EPS, precision=1, **kw)
+    r = gpu.solve(omegas, max_iter=1500, eps=MIXED_EPS, precision=1, settle=SETTLE, **kw)
     gpu.close()
     assert np.all(exact.iters >= 0) and np.all(r.iters >= 0), r.si
     w = exact.re_S[:, 0] + 1j * exact.im_S[:, 0]
