@@ -1,32 +1,40 @@
 """Benchmark: converged FAM omega-points per second at N_sh = 16 within 1e-6
 relative error, with p50/p99 point latency.
 
-Workload (one "step" = one serving run to completion):
+Workload (one "step" = one serving run of 600 solves to completion):
   ground state  the recorded 162Gd SkO' solution (tests/golden/Gd162.hel)
                 re-diagonalised in the full N_sh = 16 axial HO basis
                 (969 Omega>0 states, 33 parity blocks, 1938 states with
                 time-reversed partners, largest block 81), 20 x 20 Gauss mesh
-  operators     Gamow-Teller beta-, K = 0 and K = 1 (one resident context each)
-  requests      R requests per operator (default 2), each the P points of pynfam's
-                CIRCLE contour (centre 10 MeV, radius 25 MeV, Gauss-Legendre
-                angles, 2P points, first P used), all arriving at the start of
-                the step; each engine has P slots (--slots), so the second
-                request's points enter as the first request's points retire
-  solver        max_iter 300, Broyden history 50, SkO' residual interaction
+  operators     beta-: Gamow-Teller K = 0 and K = 1, and the first-forbidden
+                operators RS1 K = 0, RS1 K = 1 (each with its cross terms R, RS1, P)
+                and RS2 K = 2: one resident context each
+  requests      one request per operator per step, each the 120 points of
+                pynfam's CIRCLE contour (centre 10 MeV, radius 25 MeV,
+                Gauss-Legendre angles, 240 points, first 120 used), all arriving
+                at the start of the step; each engine has 64 slots (--slots), so
+                the points enter as earlier points retire
+  solver        the reference's defaults: max_iter 200, Broyden history 50; SkO'
+                residual interaction
   form          the mixed form (FP32 increment evaluations with 3xTF32 tensor-core
-                GEMMs, FP64 anchors, FP64 Broyden) converged to 1e-9, served by
+                GEMMs, FP64 anchors -- the last ones the defect correction that
+                certifies convergence -- FP64 Broyden solve and residual) converged
+                to 1e-9 with every strength value settled to 1e-8, served by
                 continuous-batching engines, one per operator, overlapping on the GPU
-A point counts when it converged and its strength is within 1e-6 (relative) of
-the FP64 fixed point of the same equations (the FP64 form converged to 1e-12,
-computed once and kept in tests/golden/bench_fixed_point_nsh16.json).  The plain
-FP64 form (the drop-in: the reference's arithmetic and trajectory, epsilon 1e-7)
-is measured on the same stream and reported beside it.
+A point counts when it converged and its strength and every cross term are
+within 1e-6 (relative) of the FP64 fixed point of the same equations (the FP64
+form converged to 1e-12, computed once and kept in
+tests/golden/bench_fixed_point_nsh16.json).  The plain FP64 form (the drop-in:
+the reference's arithmetic and trajectory, epsilon 1e-7) is measured on the
+same stream and reported beside it.
 
 Arms:
   default           this repository's GB300 solver through its C ABI
   --impl reference  the reference algorithm on the host CPU cores (the FP64
                     numpy restatement, the only CPU implementation runnable
-                    on these machines), timed on a bounded sample
+                    on these machines), timed on a bounded sample: single FAM
+                    iterations of points of every operator plus one whole
+                    converged point, scaled by the workload's iteration count
 """
 from __future__ import annotations
 
@@ -49,28 +57,43 @@ FIXED_POINT = os.path.join(ROOT, "tests", "golden", "bench_fixed_point_nsh16.jso
 INTERACTION = {"interaction_name": "SKOP", "require_self_consistency": True, "require_gauge_invariance": True,
                "force_j2_terms": False, "vpair_t0": -346.352, "override_cs0": 128.279, "override_csr": 0.0,
                "override_cds": 0.0}
-SOLVER = {"max_iter": 300, "convergence_epsilon": 1e-7, "broyden_history_size": 50}
-OPERATORS = (("GT", 0), ("GT", 1))
+# the reference's solver defaults (pnfam_setup.f90:191-195)
+SOLVER = {"max_iter": 200, "convergence_epsilon": 1e-7, "broyden_history_size": 50}
+# Gamow-Teller K = 0, 1 and first-forbidden K = 0, 1, 2
+OPERATORS = (("GT", 0), ("GT", 1), ("RS1", 0), ("RS1", 1), ("RS2", 2))
+POINTS = 120
+SLOTS = 64
 MIXED_EPS = 1e-9
+# the mixed form also waits until every strength value has settled to 1e-8 of itself
+SETTLE = 8
+TIGHT = 1e-12
 # DRAM traffic of the FP32 stages per point-evaluation, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum of one 8-point launch / 8)
+# (dram__bytes_read.sum + dram__bytes_write.sum of one launch / its points)
 TRAFFIC_PER_POINT = {"field_projection_fp32": 14.6e6, "density_fp32": 16.3e6}
+TRAFFIC_SOURCE = "profiles/k_density_tc2_k_hproj_tc_nsh16.md"
 REL = 1e-6
 METRIC = "converged FAM omega-points/s at N_sh=16 within 1e-6 rel err; p50/p99 point latency"
+WORKLOAD = (f"162Gd SkO' N_sh={NSH} full basis (1938 states, 66 blocks, max 81), 20x20 mesh; beta- GT K=0,1 and "
+            f"first-forbidden RS1 K=0,1 (cross terms R, RS1, P) and RS2 K=2; {POINTS} CIRCLE-contour points per "
+            f"operator = {POINTS * len(OPERATORS)} solves per step, served")
 
 
-def workload(P, operators=OPERATORS):
+def opname(op):
+    return f"{op[0]}-K{op[1]}"
+
+
+def workload(P=POINTS, operators=OPERATORS, nsh=NSH):
     """Cases (one per operator, sharing the ground state) and the omega points."""
     from pynfam_gb300.contour import circle
     from pynfam_gb300.namelist import defaults
     from pynfam_gb300.pnfam_setup import setup_case
     from pynfam_gb300.synthetic import ground_state
-    hfb = ground_state(HEL, NSH)
+    hfb = ground_state(HEL, nsh)
     cases = []
     for name, k in operators:
         nml = defaults()
         nml["interaction"].update(INTERACTION)
-        nml["ext_field"].update(operator_name=name, operator_k=k, beta_type="-", compute_crossterms=False)
+        nml["ext_field"].update(operator_name=name, operator_k=k, beta_type="-", compute_crossterms=True)
         nml["solver"].update(SOLVER)
         cases.append(setup_case(nml, None, hfb=hfb))
     omegas = circle(-15.0, 35.0, 2 * P)
@@ -147,74 +170,80 @@ def measured_peaks():
         return {}
 
 
-def cpu_sample(case, omegas, iters):
-    """The FP64 restatement on the host cores: `iters` FAM iterations of one
-    point of the workload; returns seconds per iteration."""
-    from oracle.fam_oracle import FAMOracle
-    orc = FAMOracle(case.hfb, case.couplings, case.F, case.G, quench=case.quench)
-    t0 = time.perf_counter()
-    orc.solve(complex(omegas[len(omegas) // 2]), max_iter=iters, eps=1e-7, broyden_m=SOLVER["broyden_history_size"])
-    return (time.perf_counter() - t0) / iters
-
-
 def dist_init(args):
     from pynfam_gb300 import replicas
     return replicas.env()
 
 
-def solver_kw(case, precision, eps):
+def solver_kw(case, precision, eps, **extra):
     s = case.nml["solver"]
-    return dict(max_iter=s["max_iter"], eps=eps, broyden_m=s["broyden_history_size"], quench=case.quench,
-                precision=precision)
+    kw = dict(max_iter=s["max_iter"], eps=eps, broyden_m=s["broyden_history_size"], quench=case.quench,
+              precision=precision)
+    kw.update(extra)
+    return kw
 
 
-def signature(P, operators=OPERATORS):
+def signature(P=POINTS, operators=OPERATORS):
     return {"nsh": NSH, "points": P, "operators": [list(o) for o in operators], "solver": SOLVER,
-            "interaction": INTERACTION}
+            "interaction": INTERACTION, "crossterms": True}
 
 
-def fixed_point(cases, omegas, P, out_dir="."):
-    """FP64 fixed point (epsilon 1e-12) of every (operator, omega): from the
-    committed file when it matches this workload, else computed here (untimed)
-    and written to out_dir (--out-dir) for committing."""
-    sig = signature(P)
+def load_fixed_point(P=POINTS, operators=OPERATORS):
+    """The committed fixed point of this workload, or None if the file is for another one."""
     try:
         with open(FIXED_POINT) as fh:
             d = json.load(fh)
-        if d.get("signature") == sig:
-            return {tuple(k): np.array([complex(*v) for v in vals]) for k, vals in
-                    ((tuple(x["operator"]), x["S"]) for x in d["results"])}, "file"
-    except (OSError, ValueError, KeyError):
-        pass
+    except (OSError, ValueError):
+        return None
+    if d.get("signature") != signature(P, operators):
+        return None
+    return {tuple(x["operator"]): x for x in d["results"]}
+
+
+def fixed_point(cases, omegas, P=POINTS, out_dir="."):
+    """Per operator: the FP64 fixed point (epsilon 1e-12) of every omega, and the FP64
+    form's own run (epsilon 1e-7, the reference's trajectory) with its iteration
+    counts: from the committed file when it matches this workload, else computed here
+    (untimed) and written to out_dir (--out-dir) for committing."""
+    fp = load_fixed_point(P)
+    if fp is not None:
+        return fp, "file"
     from pynfam_gb300.solver import GPUSolver
-    out, rec = {}, []
-    for (name, k), c in zip(OPERATORS, cases):
+    rec = []
+    for op, c in zip(OPERATORS, cases):
         g = GPUSolver(c.hfb, c.couplings)
         g.set_operator(c.F, c.G)
-        kw = solver_kw(c, 0, 1e-12)
-        kw["max_iter"] = 1000
-        r = g.solve(omegas, **kw)
+        kw = solver_kw(c, 0, TIGHT)
+        kw["max_iter"] = 600
+        ex = g.solve(omegas, **kw)
+        ref = g.solve(omegas, **solver_kw(c, 0, SOLVER["convergence_epsilon"]))
         g.close()
-        S = r.re_S[:, 0] + 1j * r.im_S[:, 0]
-        S[r.iters < 0] = np.nan
-        out[(name, k)] = S
-        rec.append({"operator": [name, k], "S": [[float(z.real), float(z.imag)] for z in S],
-                    "iters": r.iters.tolist()})
+        S = ex.re_S + 1j * ex.im_S
+        rec.append({"operator": list(op), "labels": ["Strength"] + [x.label for x in c.G],
+                    "S": [[[float(z.real), float(z.imag)] for z in row] if it >= 0 else None
+                          for row, it in zip(S, ex.iters)],
+                    "iters": ex.iters.tolist(), "iters_ref": ref.iters.tolist(),
+                    "S_ref": [[float(z.real), float(z.imag)] for z in ref.re_S[:, 0] + 1j * ref.im_S[:, 0]]})
+        print(f"fixed point {opname(op)}: {int(np.sum(ex.iters >= 0))} of {len(omegas)} at {TIGHT}, "
+              f"{int(np.sum(ref.iters >= 0))} at {SOLVER['convergence_epsilon']}", file=sys.stderr, flush=True)
     path = os.path.join(out_dir, os.path.basename(FIXED_POINT))
     os.makedirs(out_dir, exist_ok=True)
     with open(path, "w") as fh:
-        json.dump({"signature": sig, "how": "FP64 form, epsilon 1e-12, max_iter 1000 (bench.py)",
-                   "results": rec}, fh)
-    return out, "computed"
+        json.dump({"signature": signature(P), "omegas": [[float(w.real), float(w.imag)] for w in omegas],
+                   "how": f"FP64 form, epsilon {TIGHT}, max_iter 600 (S, iters); FP64 form with the "
+                          f"reference's settings (iters_ref, S_ref); bench.py", "results": rec},
+                  fh, separators=(",", ":"))
+    return {tuple(x["operator"]): x for x in rec}, "computed"
 
 
 class Stream:
     """One serving run of the workload's requests on resident contexts."""
 
-    def __init__(self, cases, omegas, precision, eps, nreq, slots=None):
+    def __init__(self, cases, omegas, precision, eps, nreq, slots, live=False):
         from pynfam_gb300.solver import GPUSolver
         self.cases, self.omegas, self.precision, self.eps, self.nreq = cases, omegas, precision, eps, nreq
-        self.slots = slots or len(omegas)
+        self.slots = slots
+        self.live = live
         self.solvers = {}
         for op, c in zip(OPERATORS, cases):
             g = GPUSolver(c.hfb, c.couplings)
@@ -223,7 +252,9 @@ class Stream:
 
     def run(self, timed=False):
         from pynfam_gb300.serve import Request, Server
-        kws = {op: solver_kw(c, self.precision, self.eps) for op, c in zip(OPERATORS, self.cases)}
+        kws = {op: solver_kw(c, self.precision, self.eps, live=self.live and not timed,
+                             settle=SETTLE if self.precision == 1 else 0)
+               for op, c in zip(OPERATORS, self.cases)}
 
         def factory(key, slots):
             return self.solvers[key].engine(slots, timed=timed, **kws[key])
@@ -239,51 +270,114 @@ class Stream:
             g.close()
 
 
-def score(out, ref, nreq):
-    """(converged, converged within REL of the fixed point, worst relative error)."""
-    conv = ok = 0
-    worst = 0.0
+def score(out, fp, nreq):
+    """Per operator and overall: points converged, converged with the strength and
+    every cross term within REL of the fixed point, worst relative error."""
+    per = {op: {"converged": 0, "within_1e-6": 0, "worst_rel_err": 0.0} for op in OPERATORS}
     for o in out:
+        op = OPERATORS[o.rid // nreq]
         if o.iters < 0:
             continue
-        conv += 1
-        w = ref[OPERATORS[o.rid // nreq]][o.index]
-        if not np.isfinite(w):
+        d = per[op]
+        d["converged"] += 1
+        w = fp[op]["S"][o.index]
+        if w is None:
             continue
-        err = abs(o.S[0] - w) / abs(w)
-        worst = max(worst, err)
-        ok += err <= REL
-    return conv, ok, worst
+        w = np.array([complex(*x) for x in w])
+        scale = max(abs(complex(*x[0])) for x in fp[op]["S"] if x is not None)
+        good = True
+        for g, v in zip(o.S, w):
+            for a, b in ((g.real, v.real), (g.imag, v.imag)):
+                err = abs(a - b)
+                good &= err <= REL * abs(b) + 1e-12 * scale
+                if abs(b) > 1e-9 * scale:
+                    d["worst_rel_err"] = max(d["worst_rel_err"], err / abs(b))
+        d["within_1e-6"] += int(good)
+    tot = {k: sum(d[k] for d in per.values()) for k in ("converged", "within_1e-6")}
+    tot["worst_rel_err"] = max(d["worst_rel_err"] for d in per.values())
+    return tot, {opname(op): d for op, d in per.items()}
+
+
+def cpu_iteration_sample(cases, omegas, n_per_op=1):
+    """The FP64 restatement on the host cores: single FAM iterations of a mid-contour
+    point of every operator; returns the mean seconds per iteration."""
+    from oracle.fam_oracle import FAMOracle
+    ts = []
+    for c in cases:
+        orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench)
+        for _ in range(n_per_op):
+            t0 = time.perf_counter()
+            orc.solve(complex(omegas[len(omegas) // 2]), max_iter=1, eps=1e-7,
+                      broyden_m=SOLVER["broyden_history_size"])
+            ts.append(time.perf_counter() - t0)
+    return float(np.mean(ts))
+
+
+def cpu_full_point(cases, omegas, fp):
+    """One whole converged point on the host cores (GT K = 0, mid-contour, the
+    reference's settings): seconds and iterations, with the iteration count the FP64
+    GPU form took for the same point."""
+    from oracle.fam_oracle import FAMOracle
+    c = cases[0]
+    i = len(omegas) // 2
+    orc = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench)
+    t0 = time.perf_counter()
+    r = orc.solve(complex(omegas[i]), max_iter=SOLVER["max_iter"], eps=SOLVER["convergence_epsilon"],
+                  broyden_m=SOLVER["broyden_history_size"])
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "iterations": int(r.iter_conv),
+            "gpu_fp64_form_iterations": int(fp[OPERATORS[0]]["iters_ref"][i]) if fp else None,
+            "point": f"{opname(OPERATORS[0])} omega = {complex(omegas[i]):.4f}"}
+
+
+def workload_iterations(fp):
+    """FAM iterations of the whole workload in the reference's form (a point that does
+    not converge runs to max_iter) and the number of converged points, from the FP64
+    form's own run of every point."""
+    total, conv = 0, 0
+    for op in OPERATORS:
+        for it in fp[op]["iters_ref"]:
+            total += it if it >= 0 else SOLVER["max_iter"]
+            conv += it >= 0
+    return total, conv
 
 
 def run_reference(args):
     world, rank, local = dist_init(args)
     if rank != 0:
         return
-    cases, omegas = workload(args.points)
-    case = cases[0]
+    cases, omegas = workload()
+    fp = load_fixed_point()
+    if fp is None:
+        print(json.dumps({"impl": "reference", "unavailable": "the workload's iteration counts "
+                          "(tests/golden/bench_fixed_point_nsh16.json) do not match this workload"}), flush=True)
+        return
     cores = os.cpu_count()
     per_iter = []
     for s in range(args.warmup + args.steps):
-        dt = cpu_sample(case, omegas, 1)
+        c = cases[s % len(cases)]
+        dt = cpu_iteration_sample([c], omegas)
         if s >= args.warmup:
             per_iter.append(dt)
     t_iter = statistics.mean(per_iter)
-    # mean FAM iterations per converged point of this workload (FP64 form, the
-    # reference's trajectory), measured on the GPU form that follows it exactly
-    iters_per_point = 20.5
-    value = 1.0 / (t_iter * iters_per_point)
-    sample = (f"{args.steps} timed samples of one FAM iteration of one omega point of the workload "
-              f"({t_iter:.3f} s each), scaled by {iters_per_point} iterations per converged point")
+    full = cpu_full_point(cases, omegas, fp)
+    total, conv = workload_iterations(fp)
+    value = conv / (t_iter * total)
+    sample = (f"{args.steps} timed single FAM iterations of mid-contour points, rotating over the {len(cases)} "
+              f"operators ({t_iter:.3f} s each), scaled by the workload's {total} FAM iterations for {conv} "
+              f"converged points (the FP64 form's run of every point, max_iter for the ones that do not "
+              f"converge); one whole converged point took {full['seconds']:.1f} s, {full['iterations']} "
+              f"iterations ({full['point']}; the FP64 GPU form: {full['gpu_fp64_form_iterations']})")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic inputs from a recorded ground state",
-            "config": {"workload": f"162Gd SkO' N_sh={NSH} full basis, GT- K=0, CIRCLE contour",
-                       "points_per_step": 1, "nghl": case.hfb.nghl, "nxy": case.F.mat.nelem},
+            "config": {"workload": WORKLOAD, "points_per_step": POINTS * len(OPERATORS), "nghl": cases[0].hfb.nghl,
+                       "nxy": [int(c.F.mat.nelem) for c in cases]},
+            "full_point": full,
             "cpu_baseline": {"value": value, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_plain), flush=True)
 
 
 def run_gpu(args):
@@ -296,21 +390,23 @@ def run_gpu(args):
     P = len(omegas)
     R = args.requests
     npts = P * len(OPERATORS) * R
-    ref, ref_src = fixed_point(cases, omegas, args.points, args.out_dir)
+    fp, fp_src = fixed_point(cases, omegas, args.points, args.out_dir)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
         replicas.barrier("cuda")
 
     # ---- the mixed serving form: warm-up, then K timed serving runs ----
-    slots = args.slots or P
-    mixed = Stream(cases, omegas, 1, MIXED_EPS, R, slots)
+    slots = args.slots
+    mixed = Stream(cases, omegas, 1, MIXED_EPS, R, slots, live=True)
     for _ in range(args.warmup):
         mixed.run()
     clocks = Clocks(local)
     barrier()
     walls, lat, launches = [], [], 0
     counts = None
+    live = {"density_fp32": [0, 0.0], "field_projection_fp32": [0, 0.0]}
+    pit32 = 0.0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(args.steps):
         flush.zero_()
@@ -322,106 +418,120 @@ def run_gpu(args):
         ev1.synchronize()
         walls.append(ev0.elapsed_time(ev1) / 1e3)
         lat += st.latencies
-        launches += sum(n for _, n in profs.values())
-        counts = score(out, ref, R)
+        for prof, n in profs.values():
+            launches += n
+            live["density_fp32"][0] += prof["live_density_launches"]
+            live["density_fp32"][1] += prof["live_density_ms"]
+            live["field_projection_fp32"][0] += prof["live_projection_launches"]
+            live["field_projection_fp32"][1] += prof["live_projection_ms"]
+            pit32 += prof["point_iterations_fp32"]
+        counts = score(out, fp, R)
     barrier()
     ck = clocks.stop()
     step_s = replicas.max_over_ranks(statistics.mean(walls), "cuda")
-    conv, ok, worst = counts
-    value = replicas.job_rate(ok, step_s, world)
-    # ---- per-stage device time of one more run (events between stages) ----
+    (tot, per_op) = counts
+    value = replicas.job_rate(tot["within_1e-6"], step_s, world)
+    # ---- per-stage device time of one more run (events between stages, serialised) ----
     out_t, st_t, profs_t = mixed.run(timed=True)
     mixed.close()
     # ---- the plain FP64 form (the drop-in) on the same stream ----
     fp64 = Stream(cases, omegas, 0, SOLVER["convergence_epsilon"], R, slots)
-    fp64.run()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     out64, st64, profs64 = fp64.run()
     torch.cuda.synchronize()
     wall64 = time.perf_counter() - t0
     fp64.close()
-    conv64, ok64, worst64 = score(out64, ref, R)
+    tot64, per64 = score(out64, fp, R)
     iters64 = [o.iters for o in out64 if o.iters >= 0]
     # ---- end to end through the public API from host buffers ----
-    e2e_wall = []
-    for _ in range(2):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s2 = Stream(cases, omegas, 1, MIXED_EPS, R, slots)
-        out2, st2, _ = s2.run()
-        s2.close()
-        e2e_wall.append(time.perf_counter() - t0)
-    e2e_ok = score(out2, ref, R)[1]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2 = Stream(cases, omegas, 1, MIXED_EPS, R, slots)
+    out2, st2, _ = s2.run()
+    s2.close()
+    e2e_wall = time.perf_counter() - t0
+    e2e_ok = score(out2, fp, R)[0]["within_1e-6"]
     hf = cases[0].hfb
     h2d_ctx = 8 * (5 * hf.dqp * hf.nghl + 4 * sum(int(b.size) for b in hf.Up) + 2 * hf.dqp + 5 * hf.nghl) \
         + 4 * (2 * hf.nb + hf.dqp)
-    h2d = len(OPERATORS) * h2d_ctx + sum(8 * c.F.mat.nelem for c in cases) + 16 * npts
-    d2h = npts * (16 + 4 + 8 + 8)
-    e2e_value = world * e2e_ok / min(e2e_wall)
-    # ---- roofline of the dominant FP32 kernel (stage times of the timed run) ----
+    h2d = len(OPERATORS) * h2d_ctx + sum(8 * c.F.mat.nelem * (1 + len(c.G)) for c in cases) + 16 * npts
+    d2h = sum(npts // len(OPERATORS) * (16 * (1 + len(c.G)) + 4 + 8 + 8) for c in cases)
+    e2e_value = world * e2e_ok / e2e_wall
+    # ---- roofline of the dominant FP32 kernel ----
     fl = flops_per_iteration(cases[0])
     stages = {}
     for prof, _ in profs_t.values():
         for k, v in prof.items():
-            if k != "total":   # per-solve wall time, not kept by the engines
+            if k != "total" and not k.startswith("live_"):
                 stages[k] = stages.get(k, 0.0) + v
-    pit32 = stages["point_iterations_fp32"]
-    stage_fl = {"field_projection_fp32": fl["field_projection"], "density_fp32": fl["density"],
-                "k1_blockgemm_fp32": fl["block_gemm"] / 2, "k2_blockgemm_fp32": fl["block_gemm"] / 2}
-    dom = max(stage_fl, key=lambda k: stages[k])
-    achieved = stage_fl[dom] * pit32 / (stages[dom] / 1e3) / 1e12
+    stage_fl = {"field_projection_fp32": fl["field_projection"], "density_fp32": fl["density"]}
+    dom = max(live, key=lambda k: live[k][1])
+    nl, ms = live[dom]
+    pts_per_launch = pit32 / max(nl, 1)
+    launch_ms = ms / max(nl, 1)
+    achieved = stage_fl[dom] * pts_per_launch / (launch_ms / 1e3) / 1e12
+    pit32_t = max(stages.get("point_iterations_fp32", 0.0), 1.0)
+    achieved_alone = stage_fl[dom] * pit32_t / max(stages.get(dom, 0.0) / 1e3, 1e-12) / 1e12
     peaks = measured_peaks()
-    if dom == "density_fp32":
-        mhz = peaks.get("sm_max_mhz", 2070.0)
-        bound, peak, src = "fp32", 152 * 128 * 2 * mhz * 1e6 / 1e12, "nominal FP32 SIMT rate at the maximum SM clock"
-    else:
-        bf16 = peaks.get("bf16_tflops", 1900.0)
-        bound, peak = "tensor", bf16 / 2
-        src = ("TF32 dense = half of the measured bf16 dense peak" if "bf16_tflops" in peaks
-               else "TF32 dense = half of the fallback bf16 peak")
+    bf16 = peaks.get("bf16_tflops_sustained")
+    src = "TF32 dense = half of the measured sustained bf16 dense peak (kernel timed inside a long step)"
+    if bf16 is None:
+        bf16 = 1700.0
+        src = "TF32 dense = half of the fallback sustained bf16 peak (1.7 PFLOP/s)"
+    peak = bf16 / 2
     line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 (3xTF32 tensor cores) increments + fp64 anchors and Broyden",
             "data": "synthetic inputs from a recorded ground state",
-            "config": {"workload": f"162Gd SkO' N_sh={NSH} full basis (1938 states, 66 blocks, max 81), "
-                                   f"GT- K=0 and K=1, {R} requests of {P} CIRCLE-contour points each per "
-                                   f"operator per step, served",
-                       "points_per_step": npts, "nghl": int(hf.nghl), "nxy": [int(c.F.mat.nelem) for c in cases],
-                       "form": f"mixed, epsilon {MIXED_EPS}", "engines": len(OPERATORS), "slots_per_engine": slots,
+            "config": {"workload": WORKLOAD, "points_per_step": npts, "nghl": int(hf.nghl),
+                       "nxy": {opname(op): int(c.F.mat.nelem) for op, c in zip(OPERATORS, cases)},
+                       "solver": SOLVER,
+                       "form": f"mixed, epsilon {MIXED_EPS}, strength values settled to 1e-{SETTLE}",
+                       "engines": len(OPERATORS), "slots_per_engine": slots,
                        "l2": "256 MB buffer written between timed steps",
                        "timing": "CUDA events around each serving run, the device synchronized on both sides "
                                  "(the engines run on their own streams)",
                        "parallelism": f"replicas{world}"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)) * 1e3, "p99": float(np.percentile(lat, 99)) * 1e3,
                            "note": "per point, from request arrival (start of the step) to its result"},
-            "accuracy": {"converged": conv, "within_1e-6": ok, "worst_rel_err": worst,
-                         "reference": f"FP64 fixed point (epsilon 1e-12), {ref_src}"},
-            "fp64_form": {"value": world * ok64 / wall64, "unit": "points/s", "wall_s": wall64,
-                          "converged": conv64, "within_1e-6": ok64, "worst_rel_err": worst64,
+            "accuracy": dict(tot, reference=f"FP64 fixed point (epsilon {TIGHT}), {fp_src}", per_operator=per_op),
+            "fp64_form": {"value": world * tot64["within_1e-6"] / wall64, "unit": "points/s", "wall_s": wall64,
+                          "converged_per_s": world * tot64["converged"] / wall64,
+                          "converged": tot64["converged"], "within_1e-6": tot64["within_1e-6"],
+                          "worst_rel_err": tot64["worst_rel_err"],
                           "mean_iterations": float(np.mean(iters64)) if iters64 else None,
+                          "per_operator": per64,
                           "note": "the drop-in: FP64 throughout, epsilon 1e-7, same serving stream"},
             "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "note": "context creation (ground state and operator upload) + serving run + results"},
             "gpu_launches": launches,
             "stages_ms": {k: round(v, 3) for k, v in stages.items()},
-            "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
+            "stages_note": "one extra serialised run with events between stages (not the timed steps)",
+            "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": TRAFFIC_PER_POINT.get(dom),
-                         "traffic_unit": "DRAM bytes read + written per point-evaluation, from one ncu capture of "
-                                         "an 8-point launch (profiles/k_density_tc2_k_hproj_tc_nsh16.md)",
+                         "traffic": TRAFFIC_PER_POINT.get(dom, 0.0) * pts_per_launch or None,
+                         "traffic_unit": f"DRAM bytes read + written per launch ({pts_per_launch:.1f} points), "
+                                         f"scaled from one ncu capture ({TRAFFIC_SOURCE})",
+                         "launches": nl, "mean_launch_ms": launch_ms, "points_per_launch": pts_per_launch,
+                         "achieved_alone": achieved_alone, "frac_alone": achieved_alone / peak,
                          "peak_source": src,
-                         "note": "achieved = algorithmic FLOPs of the stage over its FP32 point-evaluations / "
-                                 "stage device time; 3xTF32 issues three MMAs per product"},
+                         "note": "achieved = algorithmic FLOPs per launch (reference operation count x points) / "
+                                 "mean launch time, CUDA events around every launch of the kernel on its own "
+                                 "stream in the timed steps, where the engines' kernels share the GPU; "
+                                 "achieved_alone: the same from the serialised stage run; 3xTF32 issues "
+                                 "three MMAs per product"},
             "clocks": ck}
     if rank == 0 and world == 1:
-        t_iter = cpu_sample(cases[0], omegas, 2)
-        mi = float(np.mean(iters64)) if iters64 else 20.0
-        cv = 1.0 / (t_iter * mi)
+        t_iter = cpu_iteration_sample(cases, omegas)
+        total, conv = workload_iterations(fp)
+        cv = conv / (t_iter * total)
         line["cpu_baseline"] = {"value": cv, "unit": "points/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"2 FAM iterations of one point ({t_iter:.3f} s each) of the same "
-                                          f"workload, scaled by the FP64 form's {mi:.2f} iterations/point"}
+                                "sample": f"one FAM iteration of a mid-contour point of each operator "
+                                          f"({t_iter:.3f} s each), scaled by the workload's {total} FAM "
+                                          f"iterations for {conv} converged points (FP64 form, reference "
+                                          f"settings)"}
     if rank == 0:
         print(json.dumps(line, default=_plain), flush=True)
     replicas.finish()
@@ -433,7 +543,7 @@ def run_serve_stream(args):
     re-diagonalised in a basis of N_sh drawn from --nsh, each requesting GT- K = 0
     and K = 1 strengths on a CIRCLE contour of 40-200 points (times the scale);
     Poisson arrivals at each rate of --rates; engines admitted within a device-memory
-    budget (--budget-gb, 150 GB); mixed form to 1e-9.  (The synthetic Bogoliubov
+    budget (--budget-gb, 150 GB); mixed form to 1e-9, values settled to 1e-8.  (The synthetic Bogoliubov
     states of the batching configuration give a FAM iteration that does not converge,
     so they cannot stand in for converged throughput.)  One JSON line per rate."""
     import torch
@@ -474,7 +584,7 @@ def run_serve_stream(args):
         c = cases[key]
         g = GPUSolver(c.hfb, c.couplings)
         g.set_operator(c.F, c.G)
-        return g.engine(n, owns_solver=True, **solver_kw(c, 1, MIXED_EPS))
+        return g.engine(n, owns_solver=True, **solver_kw(c, 1, MIXED_EPS, settle=SETTLE))
 
     keys = list(cases)
     npts = {key: max(4, int(round(rng.integers(40, 201) * args.stream_scale))) for key in keys}
@@ -492,19 +602,21 @@ def run_serve_stream(args):
                 "wall_s": st.wall, "points_per_s": st.points / st.wall, "converged_per_s": st.converged / st.wall,
                 "latency_ms": {"p50": st.percentile(50) * 1e3, "p99": st.percentile(99) * 1e3},
                 "peak_engines": st.peak_engines, "peak_gb": st.peak_bytes / 1e9, "slots_per_engine": slots,
-                "setup_s": setup_s, "form": f"mixed, epsilon {MIXED_EPS}",
+                "setup_s": setup_s, "form": f"mixed, epsilon {MIXED_EPS}, settled to 1e-{SETTLE}",
                 "data": "recorded ground states re-diagonalised in larger bases"}
         print(json.dumps(line, default=_plain), flush=True)
 
 
 def run_solve_only(args):
     from pynfam_gb300.solver import GPUSolver
-    cases, omegas = workload(args.points, OPERATORS[:1])
+    ops = tuple(OPERATORS[i] for i in (int(x) for x in args.operators.split(",")))
+    cases, omegas = workload(args.points, ops, args.nsh_solve)
     case = cases[0]
     s = case.nml["solver"]
     kw = dict(max_iter=args.max_iter or s["max_iter"], eps=args.eps or s["convergence_epsilon"],
               broyden_m=s["broyden_history_size"] if args.broyden_m is None else args.broyden_m,
-              quench=case.quench, precision=args.precision, switch_exp=args.switch_exp)
+              quench=case.quench, precision=args.precision, switch_exp=args.switch_exp,
+              settle=SETTLE if args.precision == 1 else 0)
     gpu = GPUSolver(case.hfb, case.couplings)
     gpu.set_operator(case.F, case.G)
     for _ in range(args.warmup):
@@ -528,9 +640,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--points", type=int, default=32, help="omega points per request")
-    ap.add_argument("--requests", type=int, default=2, help="requests per operator per step")
-    ap.add_argument("--slots", type=int, default=0, help="slots per engine (default: points per request)")
+    ap.add_argument("--points", type=int, default=POINTS, help="omega points per request")
+    ap.add_argument("--requests", type=int, default=1, help="requests per operator per step")
+    ap.add_argument("--slots", type=int, default=SLOTS, help="slots per engine")
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--precision", type=int, default=0, choices=(0, 1),
                     help="solve-only: 0 FP64 throughout; 1 mixed form")
@@ -550,6 +662,9 @@ def main():
     ap.add_argument("--stream-seed", type=int, default=0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--out-dir", default=".", help="where a newly computed FP64 fixed point is written")
+    ap.add_argument("--nsh-solve", type=int, default=NSH, help="solve-only: N_sh of the basis")
+    ap.add_argument("--operators", default="0",
+                    help="solve-only: indices into the workload's operator list (first: the one solved)")
     ap.add_argument("--solve-only", action="store_true",
                     help="one operator, batch solves only (no serving, e2e or CPU legs); used for kernel profiling")
     args = ap.parse_args()
