@@ -82,7 +82,9 @@ typedef struct {
                                  (Re and Im of the strength and each cross term) to have
                                  settled, |S - S_previous| <= 10^-n |S| + 1e-13 max|S|, for
                                  at most 20 iterations beyond si < epsilon (0: the
-                                 reference's test si < epsilon alone) */
+                                 reference's test si < epsilon alone);
+                                 [4] = n > 0: the mixed form's "near its anchor" bound is
+                                 10^n epsilon instead of 1000 epsilon */
 } pnfam_solver_opts_t;
 
 /*

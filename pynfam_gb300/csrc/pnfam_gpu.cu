@@ -1377,7 +1377,9 @@ struct pnfam_engine {
   // EXTRA iterations beyond si < epsilon)
   double s_rel = 0.0;
   static constexpr int EXTRA = 20;
-  static constexpr double NEAR = 1000.0;
+  // "near" its anchor: max|X - X_a| <= near * epsilon (opts.reserved[4] = n > 0: 10^n;
+  // default 1000), where the FP32 error of an increment evaluation is far below epsilon
+  double near = 1000.0;
   // a stall of the increment iteration counts as the FP32 noise floor (and takes an
   // anchor) only while si <= FLOOR * max|d|: far above that, FP32 rounding of the
   // increment cannot be what holds the residual up, and an anchor would not help
@@ -1447,6 +1449,7 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->switch_si = o->reserved[1] > 0 ? std::pow(10.0, -o->reserved[1]) : 100.0 * o->convergence_epsilon;
   e->timed = o->reserved[0] != 0;
   e->s_rel = o->reserved[3] > 0 ? std::pow(10.0, -o->reserved[3]) : 0.0;
+  e->near = o->reserved[4] > 0 ? std::pow(10.0, o->reserved[4]) : 1000.0;
   c->live = o->reserved[2] != 0;
   c->nlev = 0;
   c->live_ms[0] = c->live_ms[1] = 0.0;
@@ -1744,7 +1747,7 @@ static int engine_finish(pnfam_engine* e) {
     } else {
       double dm;
       std::memcpy(&dm, &e->hdmax[p], sizeof dm);
-      const bool near = dm <= pnfam_engine::NEAR * o.convergence_epsilon;
+      const bool near = dm <= e->near * o.convergence_epsilon;
       if (si < o.convergence_epsilon && near && accept()) { engine_retire(e, p, it); continue; }
       if (si < e->best[p] * 0.5) { e->best[p] = si; e->since_best[p] = 0; } else { ++e->since_best[p]; }
       // the stagnation window doubles with every anchor it has triggered

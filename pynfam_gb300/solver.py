@@ -101,7 +101,7 @@ class GPUSolver:
 
     @staticmethod
     def options(max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None, timed=False, precision=0,
-                switch_exp=0, live=False, settle=0):
+                switch_exp=0, live=False, settle=0, near_exp=0):
         if alpha_mix is None:
             from .pnfam_setup import ALPHA_MIX as alpha_mix
         o = _lib.SolverOpts()
@@ -112,6 +112,7 @@ class GPUSolver:
         o.reserved[1] = int(switch_exp)
         o.reserved[2] = 1 if live else 0
         o.reserved[3] = int(settle)
+        o.reserved[4] = int(near_exp)
         return o
 
     def engine(self, slots, owns_solver=False, **opts) -> "Engine":
