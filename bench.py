@@ -67,10 +67,13 @@ MIXED_EPS = 1e-9
 # the mixed form also waits until every strength value has settled to 1e-8 of itself
 SETTLE = 8
 TIGHT = 1e-12
-# DRAM traffic of the FP32 stages per point-evaluation, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum of one launch / its points)
-TRAFFIC_PER_POINT = {"field_projection_fp32": 14.6e6, "density_fp32": 16.3e6}
-TRAFFIC_SOURCE = "profiles/k_density_tc2_k_hproj_tc_nsh16.md"
+# the mixed form's "near its anchor" bound: 10^4 epsilon (the FP32 error of an increment
+# evaluation there is ~1e-6 of 1e-5, far below epsilon)
+NEAR_EXP = 4
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) over the algorithmic bytes of
+# one pair-tensor GEMM launch, from one ncu capture (N_sh = 12, 16 points)
+TRAFFIC_RATIO = {"density_fp32": 1.646e9 / 1.578e9, "field_projection_fp32": 1.790e9 / 1.739e9}
+TRAFFIC_SOURCE = "profiles/k_pg_gemm_nsh12.md"
 REL = 1e-6
 METRIC = "converged FAM omega-points/s at N_sh=16 within 1e-6 rel err; p50/p99 point latency"
 WORKLOAD = (f"162Gd SkO' N_sh={NSH} full basis (1938 states, 66 blocks, max 81), 20x20 mesh; beta- GT K=0,1 and "
@@ -253,7 +256,8 @@ class Stream:
     def run(self, timed=False):
         from pynfam_gb300.serve import Request, Server
         kws = {op: solver_kw(c, self.precision, self.eps, live=self.live and not timed,
-                             settle=SETTLE if self.precision == 1 else 0)
+                             settle=SETTLE if self.precision == 1 else 0,
+                             near_exp=NEAR_EXP if self.precision == 1 else 0)
                for op, c in zip(OPERATORS, self.cases)}
 
         def factory(key, slots):
@@ -296,6 +300,17 @@ def score(out, fp, nreq):
     tot = {k: sum(d[k] for d in per.values()) for k in ("converged", "within_1e-6")}
     tot["worst_rel_err"] = max(d["worst_rel_err"] for d in per.values())
     return tot, {opname(op): d for op, d in per.items()}
+
+
+def pair_bytes(case, stage, npts):
+    """Algorithmic bytes of one pair-tensor GEMM launch of npts points: the pair tensor
+    (TF32 hi + lo: 16 density pairs or 18 projection pairs per element and mesh point,
+    plus the pairing parts), the points' operands and results."""
+    S2 = flops_per_iteration(case)["S2"]
+    n = case.hfb.nghl
+    if stage == "density_fp32":
+        return (16 + 2) * n * S2 * 8 + npts * 8 * S2 * 8 + npts * 4 * 18 * n * 4
+    return (18 + 2) * n * S2 * 8 + npts * (4 * 18 + 4) * n * 8 + npts * 8 * S2 * 4
 
 
 def cpu_iteration_sample(cases, omegas, n_per_op=1):
@@ -458,7 +473,7 @@ def run_gpu(args):
     h2d = len(OPERATORS) * h2d_ctx + sum(8 * c.F.mat.nelem * (1 + len(c.G)) for c in cases) + 16 * npts
     d2h = sum(npts // len(OPERATORS) * (16 * (1 + len(c.G)) + 4 + 8 + 8) for c in cases)
     e2e_value = world * e2e_ok / e2e_wall
-    # ---- roofline of the dominant FP32 kernel ----
+    # ---- roofline of the dominant FP32 kernel (the pair-tensor GEMMs: HBM-bound) ----
     fl = flops_per_iteration(cases[0])
     stages = {}
     for prof, _ in profs_t.values():
@@ -470,16 +485,19 @@ def run_gpu(args):
     nl, ms = live[dom]
     pts_per_launch = pit32 / max(nl, 1)
     launch_ms = ms / max(nl, 1)
-    achieved = stage_fl[dom] * pts_per_launch / (launch_ms / 1e3) / 1e12
+    alg = pair_bytes(cases[0], dom, pts_per_launch)
+    achieved = alg / (launch_ms / 1e3) / 1e9
+    # the same launches alone on the GPU: the serialised stage run
     pit32_t = max(stages.get("point_iterations_fp32", 0.0), 1.0)
-    achieved_alone = stage_fl[dom] * pit32_t / max(stages.get(dom, 0.0) / 1e3, 1e-12) / 1e12
+    alone_ms = stages.get(dom, 0.0) / pit32_t * pts_per_launch
+    achieved_alone = alg / max(alone_ms / 1e3, 1e-12) / 1e9
     peaks = measured_peaks()
-    bf16 = peaks.get("bf16_tflops_sustained")
-    src = "TF32 dense = half of the measured sustained bf16 dense peak (kernel timed inside a long step)"
-    if bf16 is None:
-        bf16 = 1700.0
-        src = "TF32 dense = half of the fallback sustained bf16 peak (1.7 PFLOP/s)"
-    peak = bf16 / 2
+    peak = peaks.get("hbm_gbs")
+    src = "measured STREAM-style copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+    if peak is None:
+        peak = 6800.0
+        src = "fallback HBM copy bandwidth 6.8 TB/s"
+    bf16 = peaks.get("bf16_tflops_sustained", 1700.0)
     line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 (3xTF32 tensor cores) increments + fp64 anchors and Broyden",
@@ -509,19 +527,25 @@ def run_gpu(args):
             "gpu_launches": launches,
             "stages_ms": {k: round(v, 3) for k, v in stages.items()},
             "stages_note": "one extra serialised run with events between stages (not the timed steps)",
-            "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": TRAFFIC_PER_POINT.get(dom, 0.0) * pts_per_launch or None,
-                         "traffic_unit": f"DRAM bytes read + written per launch ({pts_per_launch:.1f} points), "
-                                         f"scaled from one ncu capture ({TRAFFIC_SOURCE})",
-                         "launches": nl, "mean_launch_ms": launch_ms, "points_per_launch": pts_per_launch,
+            "roofline": {"bound": "hbm", "kernel": f"k_pg_gemm ({dom})", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": alg * TRAFFIC_RATIO[dom],
+                         "traffic_unit": f"DRAM bytes read + written per launch ({pts_per_launch:.1f} points): "
+                                         f"algorithmic bytes x the DRAM/algorithmic ratio of one ncu capture "
+                                         f"({TRAFFIC_SOURCE}); the pair tensor grows with S2, so the ratio carries",
+                         "algorithmic_bytes": alg, "launches": nl, "mean_launch_ms": launch_ms,
+                         "points_per_launch": pts_per_launch,
                          "achieved_alone": achieved_alone, "frac_alone": achieved_alone / peak,
+                         "mean_launch_ms_alone": alone_ms,
+                         "reference_tflops": stage_fl[dom] * pts_per_launch / (launch_ms / 1e3) / 1e12,
+                         "reference_tflops_alone": stage_fl[dom] * pts_per_launch / max(alone_ms / 1e3, 1e-12) / 1e12,
+                         "tf32_peak_tflops": bf16 / 2,
                          "peak_source": src,
-                         "note": "achieved = algorithmic FLOPs per launch (reference operation count x points) / "
-                                 "mean launch time, CUDA events around every launch of the kernel on its own "
-                                 "stream in the timed steps, where the engines' kernels share the GPU; "
-                                 "achieved_alone: the same from the serialised stage run; 3xTF32 issues "
-                                 "three MMAs per product"},
+                         "note": "achieved = algorithmic bytes per launch (pair tensor + the points' operands "
+                                 "and results) / mean launch time, CUDA events around every launch of the kernel "
+                                 "on its own stream in the timed steps, where the five engines' kernels share "
+                                 "the GPU; *_alone: the same launches from the serialised stage run; "
+                                 "reference_tflops: the reference's operation count of the stage at that rate"},
             "clocks": ck}
     if rank == 0 and world == 1:
         t_iter = cpu_iteration_sample(cases, omegas)
@@ -584,7 +608,7 @@ def run_serve_stream(args):
         c = cases[key]
         g = GPUSolver(c.hfb, c.couplings)
         g.set_operator(c.F, c.G)
-        return g.engine(n, owns_solver=True, **solver_kw(c, 1, MIXED_EPS, settle=SETTLE))
+        return g.engine(n, owns_solver=True, **solver_kw(c, 1, MIXED_EPS, settle=SETTLE, near_exp=NEAR_EXP))
 
     keys = list(cases)
     npts = {key: max(4, int(round(rng.integers(40, 201) * args.stream_scale))) for key in keys}
@@ -616,7 +640,7 @@ def run_solve_only(args):
     kw = dict(max_iter=args.max_iter or s["max_iter"], eps=args.eps or s["convergence_epsilon"],
               broyden_m=s["broyden_history_size"] if args.broyden_m is None else args.broyden_m,
               quench=case.quench, precision=args.precision, switch_exp=args.switch_exp,
-              settle=SETTLE if args.precision == 1 else 0)
+              settle=SETTLE if args.precision == 1 else 0, near_exp=NEAR_EXP if args.precision == 1 else 0)
     gpu = GPUSolver(case.hfb, case.couplings)
     gpu.set_operator(case.F, case.G)
     for _ in range(args.warmup):

@@ -412,49 +412,60 @@ __device__ __forceinline__ float pg_dsum(const float* __restrict__ dsum, const P
   return s;
 }
 
-__global__ void __launch_bounds__(128) k_pg_fold(const PGProb* __restrict__ probs, PGFold F,
-                                                 const float* __restrict__ dsum, const int* __restrict__ actlist,
-                                                 int nghl, float* __restrict__ dpart) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+// one thread per (mesh point, class): the class's terms go into shared memory and are
+// added over the four classes in a fixed order.  grid (ceil(nghl / PG_FOLD_R), nact,
+// 2 calls), block 4 * PG_FOLD_R
+enum { PG_FOLD_R = 32 };
+
+__global__ void __launch_bounds__(4 * PG_FOLD_R) k_pg_fold(const PGProb* __restrict__ probs, PGFold F,
+                                                           const float* __restrict__ dsum,
+                                                           const int* __restrict__ actlist, int nghl,
+                                                           float* __restrict__ dpart) {
+  __shared__ float sacc[4][2 * ND][PG_FOLD_R];
+  const int rl = threadIdx.x % PG_FOLD_R, cls = threadIdx.x / PG_FOLD_R;
+  const int r = blockIdx.x * PG_FOLD_R + rl;
   const int pi = blockIdx.y, call = blockIdx.z;
-  if (r >= nghl) return;
   float acc[2 * ND];
 #pragma unroll
   for (int k = 0; k < 2 * ND; ++k) acc[k] = 0.f;
-  for (int cls = 0; cls < 4; ++cls) {
-    const float sb = (cls & 1) ? -1.f : 1.f;
-    const bool same = ((cls >> 1) & 1) == (cls & 1);
-    if (F.dens[cls] >= 0) {
-      const PGProb pr = probs[F.dens[cls]];
-      float Cr[16], Ci[16];
-      const int nre = pi * 4 + call * 2;
+  const bool rok = r < nghl;
+  const float sb = (cls & 1) ? -1.f : 1.f;
+  const bool same = ((cls >> 1) & 1) == (cls & 1);
+  if (rok && F.dens[cls] >= 0) {
+    const PGProb pr = probs[F.dens[cls]];
+    float Cr[16], Ci[16];
+    const int nre = pi * 4 + call * 2;
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        Cr[c] = pg_dsum(dsum, pr, nre, c * nghl + r);
-        Ci[c] = pg_dsum(dsum, pr, nre + 1, c * nghl + r);
-      }
-      if (same) fold_same(acc, Cr, Ci, sb);
-      else fold_opp(acc, Cr, Ci, sb < 0.f ? 1.f : -1.f);
+    for (int c = 0; c < 16; ++c) {
+      Cr[c] = pg_dsum(dsum, pr, nre, c * nghl + r);
+      Ci[c] = pg_dsum(dsum, pr, nre + 1, c * nghl + r);
     }
-    const int pp = F.dens[4 + 4 * call + cls];
-    if (pp >= 0) {
-      // pairing densities (the kind-1 terms of the density kernels)
-      const PGProb pr = probs[pp];
-      const float xr = 2.f * pg_dsum(dsum, pr, pi * 2, r), xi = 2.f * pg_dsum(dsum, pr, pi * 2 + 1, r);
-      if (same) {
-        const float sig = sb < 0.f ? 1.f : -1.f;
-        accC(acc, D_SBR, sig * xr, sig * xi);
-        accC(acc, D_SBP, xi, -xr);
-      } else {
-        accC(acc, D_RB, -sb * xr, -sb * xi);
-        accC(acc, D_SBZ, xr, xi);
-      }
+    if (same) fold_same(acc, Cr, Ci, sb);
+    else fold_opp(acc, Cr, Ci, sb < 0.f ? 1.f : -1.f);
+  }
+  const int pp = F.dens[4 + 4 * call + cls];
+  if (rok && pp >= 0) {
+    // pairing densities (the kind-1 terms of the density kernels)
+    const PGProb pr = probs[pp];
+    const float xr = 2.f * pg_dsum(dsum, pr, pi * 2, r), xi = 2.f * pg_dsum(dsum, pr, pi * 2 + 1, r);
+    if (same) {
+      const float sig = sb < 0.f ? 1.f : -1.f;
+      accC(acc, D_SBR, sig * xr, sig * xi);
+      accC(acc, D_SBP, xi, -xr);
+    } else {
+      accC(acc, D_RB, -sb * xr, -sb * xi);
+      accC(acc, D_SBZ, xr, xi);
     }
   }
+#pragma unroll
+  for (int k = 0; k < 2 * ND; ++k) sacc[cls][k][rl] = acc[k];
+  __syncthreads();
   const long long p = actlist[pi];
   float* out = dpart + (p * 2 + call) * (2LL * ND) * nghl;
-#pragma unroll
-  for (int k = 0; k < 2 * ND; ++k) out[(long long)k * nghl + r] = acc[k];
+  for (int e = threadIdx.x; e < 2 * ND * PG_FOLD_R; e += blockDim.x) {
+    const int k = e / PG_FOLD_R, q = e % PG_FOLD_R, rr = blockIdx.x * PG_FOLD_R + q;
+    if (rr < nghl) out[(long long)k * nghl + rr] = (sacc[0][k][q] + sacc[1][k][q]) + (sacc[2][k][q] + sacc[3][k][q]);
+  }
 }
 
 }  // namespace pnfam

@@ -799,7 +799,7 @@ static int pg_density(pnfam_ctx* c, int nact, const float* rsp, float* dpart, cu
         c->d_pg_probs.p, c->d_pg_tdens.p, c->d_pg_elems.p, c->d_pg_a.p, c->d_pg_b.p, na, al, ns, bslot, nullptr,
         c->nxy, c->d_pg_d.p, c->d_err.p);
     live_end(c, lv, 0, st);
-    k_pg_fold<<<dim3((unsigned)((c->nghl + 127) / 128), (unsigned)na, 2), 128, 0, st>>>(
+    k_pg_fold<<<dim3((unsigned)((c->nghl + PG_FOLD_R - 1) / PG_FOLD_R), (unsigned)na, 2), 4 * PG_FOLD_R, 0, st>>>(
         c->d_pg_probs.p, c->pg_fold, c->d_pg_d.p, al, c->nghl, dpart);
     c->launches += 3;
     CK(cudaGetLastError());

@@ -121,14 +121,15 @@ class GPUSolver:
         return Engine(self, slots, self.options(**opts), owns_solver)
 
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
-              history=False, timed=False, precision=0, switch_exp=0, settle=0) -> SolveResult:
+              history=False, timed=False, precision=0, switch_exp=0, settle=0, near_exp=0) -> SolveResult:
         """precision 0: FP64 throughout (the reference's arithmetic and iteration
         trajectory).  precision 1: defect correction -- the field is evaluated in
         FP32 on the increment from an FP64 anchor; within 1000*eps of the anchor
         convergence is accepted on an FP32 increment evaluation, farther out an
         FP64 anchor evaluation is taken when si < 10**-switch_exp (default
         100*eps) or si stops falling.  settle = n > 0: convergence also waits until
-        every strength value moved by at most 10**-n of itself in the last iteration."""
+        every strength value moved by at most 10**-n of itself in the last iteration;
+        near_exp = n > 0: a point counts as near its anchor within 10**n * eps (default 1000)."""
         import time
         w = np.atleast_1d(np.asarray(omegas, dtype=complex))
         P = len(w)
@@ -137,7 +138,7 @@ class GPUSolver:
         iters = np.zeros(P, dtype=np.int32); si = np.zeros(P)
         hist = np.full(P * (max_iter + 1) * 3, np.nan) if history else None
         o = self.options(max_iter, eps, broyden_m, quench, alpha_mix, timed, precision, switch_exp,
-                         settle=settle)
+                         settle=settle, near_exp=near_exp)
         t0 = time.perf_counter()
         _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
                                             _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
