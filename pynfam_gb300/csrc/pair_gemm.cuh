@@ -12,11 +12,11 @@
 // and column state b have the spins of class k = 2 (s_a < 0) + (s_b < 0).  The
 // products T_e(c, r) = phi(a_e, r) phi(b_e, r) depend only on the ground state and
 // the operator's block structure, so they are formed once per operator (split into
-// TF32 hi and lo, laid out in the tensor cores' canonical K-major layout, 128 x 32
+// TF32 hi and lo, laid out in the tensor cores' canonical K-major layout, 128 x 16
 // per chunk) and both stages become plain GEMMs of that constant operand against
 // the small per-evaluation operand of every active point (rho, or the field
 // tensor): D[m][n] = sum_k A[m][k] B[n][k], M = 128 rows per tile, N = the active
-// points' columns (Re, Im, both calls), K chunks of 32.  One thread streams the
+// points' columns (Re, Im, both calls), K chunks of 16.  One thread streams the
 // chunks of A and B into a ring of shared-memory stages with cp.async.bulk, one
 // thread issues the MMAs into a TMEM accumulator, four warps read it out.
 //
@@ -33,8 +33,8 @@
 
 namespace pnfam {
 
-enum { PG_K = 32, PG_M = 128, PG_MAXN = 256, PG_THREADS = 192, PG_MAXSTAGE = 8, PG_MAXPTS = 64 };
-// floats per A chunk (128 rows x 32, hi then lo) and per B chunk slot (up to 256 rows)
+enum { PG_K = 16, PG_M = 128, PG_MAXN = 256, PG_THREADS = 192, PG_MAXSTAGE = 8, PG_MAXPTS = 64 };
+// floats per A chunk (128 rows x 16, hi then lo) and per B chunk slot (up to 256 rows)
 constexpr long long PG_ACHUNK = 2LL * PG_M * PG_K;
 constexpr long long PG_BCHUNK = 2LL * PG_MAXN * PG_K;
 

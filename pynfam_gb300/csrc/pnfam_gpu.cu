@@ -662,7 +662,10 @@ static void live_collect(pnfam_ctx* c) {
 // ---------------------------------------------------------------------------
 // pair-tensor GEMMs (pair_gemm.cuh): problems, element lists, tasks
 // ---------------------------------------------------------------------------
-static constexpr int PG_SMEM = 220 * 1024;   // dynamic shared memory of k_pg_gemm
+// dynamic shared memory of k_pg_gemm: 128 KB, so that one of its CTAs leaves room on
+// the SM (100 KB) for a CTA of the FP64 anchor kernels or the block GEMMs of other
+// points or engines, whose FP64 and FP32 pipes it does not use
+static constexpr int PG_SMEM = 128 * 1024;
 
 // stages of k_pg_gemm for B slots of bslot floats
 static int pg_stages(int bslot) {
@@ -705,7 +708,7 @@ static void pg_setup(pnfam_ctx* c) {
     else { pr.mrows = ncombo * nghl; pr.kdim = pr.ne; }
     pr.nkc = (int)cdiv(pr.kdim, PG_K);
     pr.ntile = (int)cdiv(pr.mrows, PG_M);
-    pr.nsplit = kind == 1 ? (int)std::max(1LL, cdiv(pr.nkc, 192)) : 1;
+    pr.nsplit = kind == 1 ? (int)std::max(1LL, cdiv(pr.nkc, 384)) : 1;
     pr.a0 = a0; a0 += (long long)pr.ntile * pr.nkc;
     pr.b0 = b0; b0 += pr.nkc;
     pr.d0 = 0;
@@ -1196,10 +1199,17 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     delete c;
     return rc;
   }
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  // the context's main stream (FP32 increment evaluations, Broyden) at the highest
+  // priority, the FP64 anchor stream at the lowest: the block scheduler then gives SMs
+  // to the tensor-core and bandwidth-bound kernels first and fills what they leave (an
+  // SM running one pair-GEMM CTA keeps 100 KB of shared memory and most registers free)
+  // with CTAs of the FP64-pipe-bound anchor kernels
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
       cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->stream64, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->stream64, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->evf[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming) != cudaSuccess) {
