@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) k_pg_gemm(const PGProb* __restr
   const PGTask t = tasks[blockIdx.x];
   const PGProb pr = probs[t.prob];
   const int ncolu = pr.ncol * nact, npad = (ncolu + 15) & ~15;
-  extern __shared__ __align__(128) unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   float* sA = reinterpret_cast<float*>(smraw);
   float* sB = sA + (size_t)nstage * PG_ACHUNK;
   __shared__ __align__(8) uint64_t full_bar[PG_MAXSTAGE], empty_bar[PG_MAXSTAGE], done_bar;

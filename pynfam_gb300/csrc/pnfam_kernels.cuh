@@ -644,7 +644,7 @@ __device__ __forceinline__ double red8(double v) {
 
 // grid (ceil(nghl/DRT), G, P*2 calls); block 256 = DRT r x DBC b
 // dpart: [P][2][G][2*ND][nghl]
-__global__ void __launch_bounds__(256, 1) k_density_fp64(DevBasis B, DensCall c0, DensCall c1, int G,
+__global__ void __maxnreg__(192) k_density_fp64(DevBasis B, DensCall c0, DensCall c1, int G,
                                                       double* __restrict__ dpart, const int* __restrict__ active) {
   using T = double;
   const int p = blockIdx.z >> 1, call = blockIdx.z & 1;
