@@ -148,6 +148,25 @@ int pnfam_gpu_solve(pnfam_ctx_t* ctx, int npts, const double* re_w, const double
                     double* re_S, double* im_S, int* iters, double* si_out, double* hist);
 
 /*
+ * pnfam_gpu_solve with the restart storage of pnfam_solve (pnfam_solver.f90:63-81,
+ * pnfam_storage.f90:62-137): x0 (or NULL) holds a start vector per point, the
+ * Broyden vector of the reference (qrpa_broin: Re X | Re Y | Im X | Im Y, and
+ * Re P | Re Q | Im P | Im Q after them in the statistical FAM, each quadrant in
+ * block-matrix order), npts x pnfam_gpu_state_size(ctx) doubles; the first
+ * iteration then evaluates the field of that state (an FP64 anchor in the mixed
+ * form) and the Broyden history starts empty, as in the reference.  x_out (or
+ * NULL) receives the final vectors in the same layout (what the reference writes
+ * to <fam_output_filename>.bin).
+ */
+int pnfam_gpu_solve_state(pnfam_ctx_t* ctx, int npts, const double* re_w, const double* im_w,
+                          const pnfam_solver_opts_t* opts, const double* x0,
+                          double* re_S, double* im_S, int* iters, double* si_out, double* hist,
+                          double* x_out);
+
+/* Length of one point's state vector: 4 nxy, or 8 nxy in the statistical FAM. */
+long long pnfam_gpu_state_size(const pnfam_ctx_t* ctx);
+
+/*
  * Continuous batching.  No counterpart in the reference, which runs one point
  * per process (pynfam's task farm): an engine keeps `slots` omega points of
  * one (nucleus, operator) context on the device, each slot iterating on its

@@ -596,6 +596,7 @@ class OracleResult:
     Y_re: np.ndarray = None
     X_im: np.ndarray = None
     Y_im: np.ndarray = None
+    vector: np.ndarray = None   # the final Broyden vector (what the restart storage keeps)
 
 
 def _bm(m: BlockMatrix, sgn=1.0):
@@ -664,7 +665,11 @@ class FAMOracle:
             return self._map2qp(quad, lambda r, k: (-self.f1[r][:, None] - self.f2[k][None, :]) + 1.0)
         return self._map2qp(quad, lambda r, k: (-self.f1[r][:, None] + self.f2[k][None, :]) + 0.0)
 
-    def solve(self, omega: complex, max_iter=300, eps=1e-7, broyden_m=50, keep_solution=False):
+    def solve(self, omega: complex, max_iter=300, eps=1e-7, broyden_m=50, keep_solution=False, x0=None,
+              si0=1.0, s0=None):
+        """x0: a start vector in the Broyden layout (the restart storage of pnfam_solve,
+        pnfam_solver.f90:63-72), with the stored si0 and strengths s0 (complex, strength
+        then cross terms) shown at iteration 0; the result's ``vector`` is the final one."""
         t0 = time.perf_counter()
         nb, db, hfb = self.nb, self.db, self.hfb
         quench = self.quench
@@ -716,6 +721,12 @@ class FAMOracle:
         flag = "N"
         nxt = len(self.Gqp)
         re_str = np.zeros(1 + nxt); im_str = np.zeros(1 + nxt)
+        if x0 is not None:
+            vin = np.array(x0, dtype=np.float64)
+            R = unpack(vin)
+            si = float(si0)
+            if s0 is not None:
+                re_str[:] = np.real(s0); im_str[:] = np.imag(s0)
         history = []
         iter_conv = -1
         # SP-basis structures of the H/rho quadrants
@@ -757,6 +768,7 @@ class FAMOracle:
             for k, g in enumerate(self.Gqp):
                 re_str[1 + k], im_str[1 + k] = contract(g, R)
         res = OracleResult(re_str.copy(), im_str.copy(), iter_conv, si, history, time.perf_counter() - t0)
+        res.vector = vin.copy()
         if keep_solution:
             fx = flat(R[12]); fy = flat(R[21])
             res.X_re, res.X_im, res.Y_re, res.Y_im = fx.real.copy(), fx.imag.copy(), fy.real.copy(), fy.imag.copy()

@@ -17,7 +17,8 @@ EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam
            "pnfam_gpu_nxy", "pnfam_gpu_last_profile", "pnfam_gpu_free", "pnfam_gpu_last_error",
            "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
            "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_ready", "pnfam_gpu_engine_free",
-           "pnfam_gpu_calc_hamiltonian_mixed", "pnfam_gpu_set_occupations", "pnfam_gpu_task_tables")
+           "pnfam_gpu_calc_hamiltonian_mixed", "pnfam_gpu_set_occupations", "pnfam_gpu_task_tables",
+           "pnfam_gpu_solve_state", "pnfam_gpu_state_size")
 
 TASK_TERMS = 4
 TASK_RECORD = 7 + 10 * TASK_TERMS
@@ -68,6 +69,11 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_set_operator.restype = C.c_int
     lib.pnfam_gpu_solve.argtypes = [C.c_void_p, C.c_int, dp, dp, C.POINTER(SolverOpts), dp, dp, ip, dp, dp]
     lib.pnfam_gpu_solve.restype = C.c_int
+    lib.pnfam_gpu_solve_state.argtypes = [C.c_void_p, C.c_int, dp, dp, C.POINTER(SolverOpts), dp, dp, dp, ip, dp, dp,
+                                          dp]
+    lib.pnfam_gpu_solve_state.restype = C.c_int
+    lib.pnfam_gpu_state_size.argtypes = [C.c_void_p]
+    lib.pnfam_gpu_state_size.restype = C.c_longlong
     lib.pnfam_gpu_calc_hamiltonian.argtypes = [C.c_void_p] + [dp] * 16
     lib.pnfam_gpu_calc_hamiltonian.restype = C.c_int
     lib.pnfam_gpu_calc_hamiltonian_mixed.argtypes = [C.c_void_p] + [dp] * 16

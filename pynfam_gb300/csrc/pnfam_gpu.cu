@@ -1399,6 +1399,11 @@ struct pnfam_engine {
   std::vector<long long> tag;
   std::vector<double> si, sre, sim, best, wre, wim, pre, pim;
   std::vector<int> extra;
+  // restart: slots admitted with a stored state vector (their first iteration evaluates
+  // the field of that state instead of starting from X = 0) and the vectors still to be
+  // copied in at the next launch
+  std::vector<int> x0;
+  std::vector<std::pair<int, std::vector<double>>> x0q;
   std::vector<unsigned long long> hdmax;
   std::vector<int> pint, act32, act64, actlist;
   int herr = 0;
@@ -1469,6 +1474,7 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->nstall.assign(P, 0); e->fresh.assign(P, 0); e->tag.assign(P, -1);
   e->si.assign(P, 1.0); e->sre.assign((size_t)P * nops, 0.0); e->sim.assign((size_t)P * nops, 0.0);
   e->pre.assign((size_t)P * nops, 0.0); e->pim.assign((size_t)P * nops, 0.0); e->extra.assign(P, 0);
+  e->x0.assign(P, 0); e->x0q.clear();
   e->best.assign(P, 1e300); e->wre.assign(P, 0.0); e->wim.assign(P, 0.0); e->hdmax.assign(P, 0);
   e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
   e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
@@ -1502,7 +1508,7 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
   for (int p = 0; p < e->P && k < n; ++p) {
     if (e->active[p]) continue;
     e->active[p] = 1; e->it[p] = 0; e->anchor[p] = 1; e->since_best[p] = 0; e->nstall[p] = 0;
-    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1; e->extra[p] = 0;
+    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1; e->extra[p] = 0; e->x0[p] = 0;
     for (int q = 0; q < e->nops; ++q) { e->sre[(size_t)p * e->nops + q] = 0.0; e->sim[(size_t)p * e->nops + q] = 0.0; }
     e->wre[p] = re_w[k]; e->wim[p] = im_w[k];
     e->tag[p] = tags ? tags[k] : k;
@@ -1512,6 +1518,36 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
     ++k;
   }
   return k;
+}
+
+// The reference's Broyden vector (pnfam_broyden.f90:47-60) orders the parts
+// Re X, Re Y, Im X, Im Y[, Re P, Re Q, Im P, Im Q]; a slot's device state is
+// [Re X|Y[|P|Q] | Im X|Y[|P|Q]].  Both are the same for nq = 2.  Part j (nf doubles)
+// of the reference vector sits at part state_part(nq, j) of the device state.
+static inline int state_part(int nq, int j) {
+  if (nq == 2) return j;
+  static const int map4[8] = {0, 1, 4, 5, 2, 3, 6, 7};
+  return map4[j];
+}
+static void state_from_ref(int nq, long long nf, const double* ref, double* dev) {
+  for (int j = 0; j < 2 * nq; ++j)
+    std::copy(ref + j * nf, ref + (j + 1) * nf, dev + state_part(nq, j) * nf);
+}
+static void state_to_ref(int nq, long long nf, const double* dev, double* ref) {
+  for (int j = 0; j < 2 * nq; ++j)
+    std::copy(dev + state_part(nq, j) * nf, dev + (state_part(nq, j) + 1) * nf, ref + j * nf);
+}
+
+// restart: slot p (just admitted, not yet launched) starts from the state vector x
+// (N doubles in the reference's Broyden order)
+static int engine_set_state(pnfam_engine* e, int p, const double* x) {
+  if (p < 0 || p >= e->P || !e->active[p] || e->it[p] != 0)
+    return fail(PNFAM_ESTATE, "a start vector needs a slot that was just admitted");
+  e->x0[p] = 1;
+  std::vector<double> v(e->N);
+  state_from_ref((int)(e->N / (2 * e->nxy)), e->nxy, x, v.data());
+  e->x0q.emplace_back(p, std::move(v));
+  return PNFAM_OK;
 }
 
 // one Broyden step of every active slot: FP64 history (FP64 form), pair-arithmetic
@@ -1558,15 +1594,18 @@ static int engine_launch(pnfam_engine* e) {
   int nact = 0, n32 = 0, n64 = 0, nanch = 0, nfresh = 0, any_bro = 0;
   for (int p = 0; p < P; ++p) {
     const bool a = e->active[p] != 0, first = a && e->it[p] == 0;
+    // the field of X = 0 vanishes: no evaluation at the first iteration, unless the
+    // slot starts from a stored state
+    const bool zero = first && !e->x0[p];
     const bool lo = e->mixed && !e->anchor[p];
-    e->act32[p] = a && lo && !first;
-    e->act64[p] = a && !lo && !first;
+    e->act32[p] = a && lo && !zero;
+    e->act64[p] = a && !lo && !zero;
     nact += a; n32 += e->act32[p]; n64 += e->act64[p];
     e->pint[p] = e->it[p];
     e->pint[P + p] = first && e->bmode == BRO_BROYDEN ? BRO_LINEAR : e->bmode;
     e->pint[2 * P + p] = e->act32[p];
     e->pint[3 * P + p] = a && e->mixed && e->anchor[p];
-    e->pint[4 * P + p] = first;  // the field of X = 0 vanishes: no evaluation
+    e->pint[4 * P + p] = zero;
     e->pint[5 * P + p] = a && e->fresh[p];
     nanch += e->pint[3 * P + p]; nfresh += e->pint[5 * P + p];
     any_bro |= a && e->pint[P + p] == BRO_BROYDEN;
@@ -1618,6 +1657,11 @@ static int engine_launch(pnfam_engine* e) {
                                                      c->d_wim.p, c->d_gfn.p, d_fresh);
     c->launches += 2;
   }
+  // stored start vectors (restart) over the zeroed state of their slots
+  for (auto& q : e->x0q)
+    CK(cudaMemcpyAsync(c->d_state.p + (size_t)q.first * N, q.second.data(), sizeof(double) * N,
+                       cudaMemcpyHostToDevice, c->stream));
+  e->x0q.clear();
   const int* act = c->d_active.p;
   int rc;
   bool split = false;
@@ -1776,9 +1820,9 @@ static int engine_nactive(const pnfam_engine* e) {
   return n;
 }
 
-extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
-                               const pnfam_solver_opts_t* o, double* re_S, double* im_S, int* iters,
-                               double* si_out, double* hist) {
+static int solve_impl(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
+                      const pnfam_solver_opts_t* o, const double* x0, double* re_S, double* im_S, int* iters,
+                      double* si_out, double* hist, double* x_out) {
   g_err.clear();
   if (!c || !o || !re_w || !im_w || !re_S || !im_S || !iters || !si_out || P <= 0)
     return fail(PNFAM_EINVAL, "pnfam_gpu_solve: bad argument");
@@ -1789,6 +1833,10 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
   e.hist = hist;
   CK(cudaEventRecord(c->evt[0], c->stream));
   engine_admit(&e, P, re_w, im_w, nullptr);
+  if (x0) {
+    for (int p = 0; p < P; ++p)
+      if (e.active[p] && (rc = engine_set_state(&e, p, x0 + (size_t)p * e.N))) return rc;
+  }
   while (engine_nactive(&e) > 0) {
     if ((rc = engine_launch(&e)) || (rc = engine_finish(&e))) {
       cudaStreamSynchronize(c->stream);
@@ -1813,7 +1861,29 @@ extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const 
       im_S[(size_t)p * nops + q] = e.done_im[k * nops + q];
     }
   }
+  // the final state vectors (point p was admitted into slot p)
+  if (x_out) {
+    std::vector<double> v((size_t)P * e.N);
+    CK(cudaMemcpy(v.data(), c->d_state.p, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    for (int p = 0; p < P; ++p) state_to_ref(c->nq, c->nxy, v.data() + (size_t)p * e.N, x_out + (size_t)p * e.N);
+  }
   return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_solve(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
+                               const pnfam_solver_opts_t* o, double* re_S, double* im_S, int* iters,
+                               double* si_out, double* hist) {
+  return solve_impl(c, P, re_w, im_w, o, nullptr, re_S, im_S, iters, si_out, hist, nullptr);
+}
+
+extern "C" int pnfam_gpu_solve_state(pnfam_ctx_t* c, int P, const double* re_w, const double* im_w,
+                                     const pnfam_solver_opts_t* o, const double* x0, double* re_S, double* im_S,
+                                     int* iters, double* si_out, double* hist, double* x_out) {
+  return solve_impl(c, P, re_w, im_w, o, x0, re_S, im_S, iters, si_out, hist, x_out);
+}
+
+extern "C" long long pnfam_gpu_state_size(const pnfam_ctx_t* c) {
+  return c && c->have_op ? 2LL * c->nq * c->nxy : 0;
 }
 
 // ---- continuous-batching engine (C ABI) ----

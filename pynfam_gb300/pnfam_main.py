@@ -29,6 +29,8 @@ import sys
 import threading
 import time
 
+from . import storage
+
 HEL_NAME = "hfbtho_output.hel"
 
 
@@ -104,10 +106,24 @@ def _private(path: str) -> bool:
 
 
 class Point:
-    """One pnfam_main run: its namelist, output log and solver inputs."""
+    """One pnfam_main run: its namelist, output log and solver inputs; with restart
+    storage (``use_fam_storage`` != 0) the start vector read from
+    ``<fam_output_filename>.bin`` (``restart``) and whether the final vector is
+    stored there (``store``)."""
 
-    def __init__(self, nml, log, case):
+    def __init__(self, nml, log, case, restart=None, store="", nxy=0):
         self.nml, self.log, self.case = nml, log, case
+        self.restart, self.store, self.nxy = restart, store, nxy
+
+    @property
+    def x0(self):
+        return None if self.restart is None else self.restart.vector
+
+    @property
+    def done_at_start(self) -> bool:
+        """The stored state already meets the stopping test: the reference stops at
+        iteration 0 (pnfam_solver.f90:126-129) with the stored strengths."""
+        return self.x0 is not None and self.restart.si < float(self.nml["solver"]["convergence_epsilon"])
 
     @property
     def solve_kwargs(self) -> dict:
@@ -130,12 +146,18 @@ def prepare(nml_path: str, cwd: str = ".", sink=None) -> Point:
         name = str(g["fam_output_filename"]).strip()
         log = txtoutput.Log(os.path.join(cwd, name + ".dat") if name else "", bool(g["print_stdout"]) or not name,
                             sink=sink)
-        if int(g["use_fam_storage"]) != 0:
-            log.write(" Note: use_fam_storage is not supported; running without restart storage")
         hfb = load_ground_state(os.path.join(cwd, HEL_NAME))
         case = setup_case(nml, None, hfb=hfb, tbc_dir=cwd)
-        txtoutput.header(log, nml, case, int(hfb.n00))
-        return Point(nml, log, case)
+        txtoutput.main_header(log, nml, case)
+        use = int(g["use_fam_storage"]) if name else 0
+        path = storage.storage_path(nml, cwd)
+        restart = None
+        nxy = case.F.mat.nelem
+        if use != 0:
+            nq = 4 if hfb.occupations is not None else 2
+            restart = storage.read_storage(path, case, nxy, 2 * nq * nxy, log)
+        txtoutput.solver_header(log, nml, case, int(hfb.n00))
+        return Point(nml, log, case, restart, path if use == -1 else "", nxy)
     except Exception as e:
         if log is not None:
             e.pnfam_log = log
@@ -149,10 +171,29 @@ def finish(pt: Point, res, index: int, seconds: float) -> None:
     it_conv = int(res.iters[index])
     last = it_conv if it_conv >= 0 else int(s["max_iter"])
     hist = [tuple(res.hist[index, i]) for i in range(last + 1)]
+    if pt.restart is not None:
+        # iteration 0 shows the stored si (1 when the file was not taken) and strength
+        s0 = pt.restart.s0
+        hist[0] = (pt.restart.si, s0[0].real if s0 is not None else 0.0, s0[0].imag if s0 is not None else 0.0)
     labels = [x.label for x in pt.case.G]
     txtoutput.iterations(pt.log, hist, it_conv, float(res.si[index]), labels)
     txtoutput.result(pt.log, seconds, pt.case.omega, res.re_S[index], res.im_S[index], labels)
     pt.log.close()
+    if pt.store:
+        storage.write_storage(pt.store, pt.case, pt.nxy, float(res.si[index]), res.re_S[index], res.im_S[index],
+                              res.state[index])
+
+
+def stored_result(pt: Point):
+    """The result of a run whose stored state already meets the stopping test:
+    converged at iteration 0 with the stored si, strengths and vector."""
+    from .solver import SolveResult
+    import numpy as np
+    s0 = pt.restart.s0
+    hist = np.full((1, 1, 3), np.nan)
+    hist[0, 0] = (pt.restart.si, s0[0].real, s0[0].imag)
+    return SolveResult(s0.real[None, :].copy(), s0.imag[None, :].copy(), np.zeros(1, dtype=np.int32),
+                       np.array([pt.restart.si]), hist, 0.0, pt.x0[None, :].copy())
 
 
 def fail(err: Exception, log=None) -> str:
@@ -180,11 +221,15 @@ def main(argv=None) -> int:
     pt = None
     try:
         pt = prepare(nml_path)
+        if pt.done_at_start:
+            finish(pt, stored_result(pt), 0, 0.0)
+            return 0
         from .solver import GPUSolver
         gpu = GPUSolver(pt.case.hfb, pt.case.couplings, occupations=pt.case.hfb.occupations)
         gpu.set_operator(pt.case.F, pt.case.G)
         t0 = time.perf_counter()
-        res = gpu.solve([pt.case.omega], history=True, **pt.solve_kwargs)
+        x0 = None if pt.x0 is None else pt.x0[None, :]
+        res = gpu.solve([pt.case.omega], history=True, x0=x0, return_state=bool(pt.store), **pt.solve_kwargs)
         dt = time.perf_counter() - t0
         gpu.close()
         finish(pt, res, 0, dt)

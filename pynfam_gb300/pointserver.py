@@ -28,12 +28,18 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 from . import pnfam_main
 
 
 # how long a client waits for its point (seconds; $PNFAM_GB300_SERVER_TIMEOUT overrides):
 # a server that stops answering fails the point instead of holding pynfam's worker
 DEFAULT_TIMEOUT = 3600.0
+
+
+class _Answered(Exception):
+    """A point answered without the device (its stored state had converged)."""
 
 
 def submit(path: str, cwd: str, nml_path: str, timeout: float = None):
@@ -137,6 +143,10 @@ class PointServer:
             try:
                 req = json.loads(buf.decode())
                 pt = pnfam_main.prepare(req["namelist"], req["cwd"], sink=sink)
+                if pt.done_at_start:
+                    pnfam_main.finish(pt, pnfam_main.stored_result(pt), 0, 0.0)
+                    rc = 0
+                    raise _Answered()
                 done = threading.Event()
                 box = {}
                 if self._stop.is_set():
@@ -148,6 +158,8 @@ class PointServer:
                     raise box["error"]
                 pnfam_main.finish(pt, box["res"], box["index"], box["seconds"])
                 rc = 0
+            except _Answered:
+                pass
             except Exception as e:
                 err = pnfam_main.fail(e, pt.log if pt else None)
             rep = {"rc": rc, "stdout": "".join(l + "\n" for l in sink), "stderr": err}
@@ -205,7 +217,15 @@ class PointServer:
             try:
                 gpu = self._solver(key, pt0)
                 t = time.perf_counter()
-                res = gpu.solve([it[1].case.omega for it in items], history=True, **pt0.solve_kwargs)
+                kw = dict(pt0.solve_kwargs)
+                if any(it[1].x0 is not None for it in items):
+                    # points with a stored start vector; the others start from X = 0,
+                    # whose field is exactly zero, so their iterations are unchanged
+                    n = len(items[[it[1].x0 is not None for it in items].index(True)][1].x0)
+                    kw["x0"] = np.stack([it[1].x0 if it[1].x0 is not None else np.zeros(n) for it in items])
+                if any(it[1].store for it in items):
+                    kw["return_state"] = True
+                res = gpu.solve([it[1].case.omega for it in items], history=True, **kw)
                 dt = time.perf_counter() - t
                 self.batches.append(len(items))
                 for i, (_, _, done, box) in enumerate(items):

@@ -25,6 +25,7 @@ class SolveResult:
     si: np.ndarray        # [P]
     hist: np.ndarray = None  # [P, max_iter + 1, 3] (si, Re S, Im S), NaN after convergence
     seconds: float = 0.0
+    state: np.ndarray = None  # [P, state_size] final Broyden vectors (solve(..., return_state=True))
 
 
 def _flat_blocks(blocks) -> np.ndarray:
@@ -121,7 +122,8 @@ class GPUSolver:
         return Engine(self, slots, self.options(**opts), owns_solver)
 
     def solve(self, omegas, max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None,
-              history=False, timed=False, precision=0, switch_exp=0, settle=0, near_exp=0) -> SolveResult:
+              history=False, timed=False, precision=0, switch_exp=0, settle=0, near_exp=0,
+              x0=None, return_state=False) -> SolveResult:
         """precision 0: FP64 throughout (the reference's arithmetic and iteration
         trajectory).  precision 1: defect correction -- the field is evaluated in
         FP32 on the increment from an FP64 anchor; within 1000*eps of the anchor
@@ -129,7 +131,9 @@ class GPUSolver:
         FP64 anchor evaluation is taken when si < 10**-switch_exp (default
         100*eps) or si stops falling.  settle = n > 0: convergence also waits until
         every strength value moved by at most 10**-n of itself in the last iteration;
-        near_exp = n > 0: a point counts as near its anchor within 10**n * eps (default 1000)."""
+        near_exp = n > 0: a point counts as near its anchor within 10**n * eps (default 1000).
+        x0: [P, state_size] start vectors (the reference's restart storage; None: X = 0);
+        return_state: also return the final vectors (SolveResult.state)."""
         import time
         w = np.atleast_1d(np.asarray(omegas, dtype=complex))
         P = len(w)
@@ -140,12 +144,29 @@ class GPUSolver:
         o = self.options(max_iter, eps, broyden_m, quench, alpha_mix, timed, precision, switch_exp,
                          settle=settle, near_exp=near_exp)
         t0 = time.perf_counter()
-        _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
-                                            _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
-                                            _lib.dptr(hist) if hist is not None else None))
+        if x0 is None and not return_state:
+            _lib.check(self.lib.pnfam_gpu_solve(self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o),
+                                                _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
+                                                _lib.dptr(hist) if hist is not None else None))
+            xo = None
+        else:
+            n = self.state_size
+            xs = None
+            if x0 is not None:
+                xs = np.ascontiguousarray(x0, dtype=np.float64).reshape(P, n)
+            xo = np.zeros((P, n)) if return_state else None
+            _lib.check(self.lib.pnfam_gpu_solve_state(
+                self.ctx, P, _lib.dptr(wre), _lib.dptr(wim), C.byref(o), _lib.dptr(xs) if xs is not None else None,
+                _lib.dptr(reS), _lib.dptr(imS), _lib.iptr(iters), _lib.dptr(si),
+                _lib.dptr(hist) if hist is not None else None, _lib.dptr(xo) if xo is not None else None))
         dt = time.perf_counter() - t0
         return SolveResult(reS.reshape(P, self.nops), imS.reshape(P, self.nops), iters, si,
-                           hist.reshape(P, max_iter + 1, 3) if hist is not None else None, dt)
+                           hist.reshape(P, max_iter + 1, 3) if hist is not None else None, dt, xo)
+
+    @property
+    def state_size(self) -> int:
+        """Length of one point's state (Broyden) vector: 4 nxy, 8 nxy in the statistical FAM."""
+        return int(self.lib.pnfam_gpu_state_size(self.ctx))
 
     def last_profile(self):
         """Per-stage device ms of the last solve (or of this context's engine so far);

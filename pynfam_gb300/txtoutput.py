@@ -50,7 +50,14 @@ def _txtr(s, n):
 
 
 def header(log: Log, nml: dict, case, nshells: int):
-    g, e, s = nml["general"], nml["ext_field"], nml["solver"]
+    """The run header (print_main_header) and the solver and interaction details
+    (log_header); a run with restart storage reports its read between the two."""
+    main_header(log, nml, case)
+    solver_header(log, nml, case, nshells)
+
+
+def main_header(log: Log, nml: dict, case):
+    g, e = nml["general"], nml["ext_field"]
     hfb = case.hfb
     Z, N = hfb.Z, hfb.N
     bm = e["beta_type"] == "-"
@@ -72,6 +79,12 @@ def header(log: Log, nml: dict, case, nshells: int):
     log.write(" " + _center(f"Daughter nucleus: (N={nf}, Z={zf})", w))
     log.write(" " + "=" * w)
     log.write()
+
+
+def solver_header(log: Log, nml: dict, case, nshells: int):
+    g, e, s = nml["general"], nml["ext_field"], nml["solver"]
+    hfb = case.hfb
+    w = 51
     log.write(" " + "-" * w)
     log.write(" " + _center("pnFAM solver details", w))
     log.write(" " + "-" * w)
