@@ -78,6 +78,8 @@ NEAR_EXP = 4
 TRAFFIC_RATIO = {"density_fp32": 1.646e9 / 1.578e9, "field_projection_fp32": 1.790e9 / 1.739e9}
 TRAFFIC_SOURCE = "profiles/k_pg_gemm_nsh12.md"
 REL = 1e-6
+# mixed form: FP64 anchors beside FP32 increments run asynchronously (--async-anchors)
+ASYNC_ANCHORS = False
 METRIC = "converged FAM omega-points/s at N_sh=16 within 1e-6 rel err; p50/p99 point latency"
 WORKLOAD = (f"162Gd SkO' N_sh={NSH} full basis (1938 states, 66 blocks, max 81), 20x20 mesh; beta- GT K=0,1 and "
             f"first-forbidden RS1 K=0,1 (cross terms R, RS1, P) and RS2 K=2; {POINTS} CIRCLE-contour points per "
@@ -261,7 +263,8 @@ class Stream:
         kws = {op: solver_kw(c, self.precision, self.eps, live=self.live and not timed,
                              settle=SETTLE if self.precision == 1 else 0,
                              near_exp=NEAR_EXP if self.precision == 1 else 0,
-                             switch_exp=SWITCH_EXP if self.precision == 1 else 0)
+                             switch_exp=SWITCH_EXP if self.precision == 1 else 0,
+                             async_anchors=ASYNC_ANCHORS and self.precision == 1)
                for op, c in zip(OPERATORS, self.cases)}
 
         def factory(key, slots):
@@ -484,8 +487,12 @@ def run_gpu(args):
     stages = {}
     for prof, _ in profs_t.values():
         for k, v in prof.items():
-            if k != "total" and not k.startswith("live_"):
+            if k != "total" and not k.startswith("live_") and not k.startswith("tuned_") and k != "autotune_ms":
                 stages[k] = stages.get(k, 0.0) + v
+    autotune = {opname(op): {"pair_tensor_from_points": int(p["tuned_pair_min_points"]),
+                             "density_k_chunks_per_task": int(p["tuned_density_kspan"]),
+                             "ms": p["autotune_ms"]}
+                for op, (p, _) in profs_t.items()}
     stage_fl = {"field_projection_fp32": fl["field_projection"], "density_fp32": fl["density"]}
     dom = max(live, key=lambda k: live[k][1])
     nl, ms = live[dom]
@@ -511,7 +518,8 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "points_per_step": npts, "nghl": int(hf.nghl),
                        "nxy": {opname(op): int(c.F.mat.nelem) for op, c in zip(OPERATORS, cases)},
                        "solver": SOLVER,
-                       "form": f"mixed, epsilon {MIXED_EPS}, strength values settled to 1e-{SETTLE}",
+                       "form": f"mixed, epsilon {MIXED_EPS}, strength values settled to 1e-{SETTLE}"
+                       + (", asynchronous anchors" if ASYNC_ANCHORS else ""),
                        "engines": len(OPERATORS), "slots_per_engine": slots,
                        "l2": "256 MB buffer written between timed steps",
                        "timing": "CUDA events around each serving run, the device synchronized on both sides "
@@ -539,6 +547,7 @@ def run_gpu(args):
             "gpu_launches": launches,
             "stages_ms": {k: round(v, 3) for k, v in stages.items()},
             "stages_note": "one extra serialised run with events between stages (not the timed steps)",
+            "autotune": autotune,
             "roofline": {"bound": "hbm", "kernel": f"k_pg_gemm ({dom})", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": alg * TRAFFIC_RATIO[dom],
@@ -568,6 +577,8 @@ def run_gpu(args):
                                           f"({t_iter:.3f} s each), scaled by the workload's {total} FAM "
                                           f"iterations for {conv} converged points (FP64 form, reference "
                                           f"settings)"}
+    if rank == 0 and world == 1 and not args.no_config4:
+        line["config4"] = run_config4(args, emit=False)
     if rank == 0:
         print(json.dumps(line, default=_plain), flush=True)
     replicas.finish()
@@ -644,6 +655,119 @@ def run_serve_stream(args):
         print(json.dumps(line, default=_plain), flush=True)
 
 
+def config4_cases(nsh=20, seed=3):
+    """The large-basis stress configuration: the synthetic Bogoliubov state (seed 3) in
+    the full N_sh = 20 basis with Omega-only blocks (3542 states, blocks up to 231), GT-
+    K = 0 and K = 1 (no cross terms), the benchmark's interaction without the
+    self-consistency check (the random state is not self-consistent)."""
+    from pynfam_gb300.namelist import defaults
+    from pynfam_gb300.pnfam_setup import setup_case
+    from pynfam_gb300.synthetic import bogoliubov_nucleus
+    hfb = bogoliubov_nucleus(HEL, nsh, seed=seed, parity=False)
+    cases = []
+    for k in (0, 1):
+        nml = defaults()
+        nml["interaction"].update(INTERACTION)
+        nml["interaction"]["require_self_consistency"] = False
+        nml["ext_field"].update(operator_name="GT", operator_k=k, beta_type="-", compute_crossterms=False)
+        nml["solver"].update(SOLVER)
+        cases.append(setup_case(nml, None, hfb=hfb))
+    return hfb, cases
+
+
+def run_config4(args, emit=True):
+    """Large-basis stress: GT- K = 0 and K = 1 at 256 CIRCLE points each on the N_sh = 20
+    synthetic state, every point iterated a fixed number of FAM iterations (the random
+    state's iteration does not converge, so the measure is FAM point-iterations per
+    second), through one continuous-batching engine per operator, in the mixed form and
+    in the FP64 form.  A separate timed run gives the per-stage device time, from which
+    the stage rates (reference FLOP counts per TF32 or FP64 peak; HBM bytes of the
+    pair-tensor stream per measured HBM peak) follow."""
+    import torch
+    from pynfam_gb300.contour import circle
+    from pynfam_gb300.serve import Request, Server
+    from pynfam_gb300.solver import GPUSolver
+    torch.cuda.set_device(0)
+    # the pair tensors of N_sh = 20 (about 62 GB per operator) stay off: the per-block
+    # tensor-core kernels evaluate these points
+    t0 = time.perf_counter()
+    hfb, cases = config4_cases()
+    omegas = circle(-15.0, 35.0, 2 * args.c4_points)
+    iters = args.c4_iters
+    gpus = []
+    for c in cases:
+        g = GPUSolver(c.hfb, c.couplings)
+        g.set_operator(c.F, c.G)
+        gpus.append(g)
+    setup_s = time.perf_counter() - t0
+
+    def serve(precision, timed=False, npts=None):
+        def factory(key, slots):
+            c = cases[key]
+            return gpus[key].engine(slots, timed=timed, max_iter=iters, eps=1e-300,
+                                    broyden_m=c.nml["solver"]["broyden_history_size"], quench=c.quench,
+                                    precision=precision, near_exp=NEAR_EXP if precision else 0)
+        reqs = [Request(k, k, omegas[:npts], 0.0) for k in range(len(cases))]
+        server = Server(factory, lambda key, n: 1, slots=args.c4_slots, budget_bytes=len(cases))
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        out, _ = server.run(reqs)
+        torch.cuda.synchronize()
+        return time.perf_counter() - ta, out
+
+    res = {}
+    # the FP64 form (about 40 point-iterations/s here) on the first c4_fp64_points points
+    for precision, name, npts in ((1, "mixed", None), (0, "fp64", args.c4_fp64_points)):
+        if precision == 1:
+            serve(precision)                   # warm-up (FP32 scratch, autotuning)
+        wall, out = serve(precision, npts=npts)
+        npi = sum(iters if o.iters < 0 else o.iters for o in out)
+        res[name] = {"point_iterations_per_s": npi / wall, "wall_s": wall, "point_iterations": npi,
+                     "points": len(out)}
+    # stage times of the mixed form (serialised, events between stages)
+    serve(1, timed=True)
+    stages = {}
+    pit32 = pit64 = 0.0
+    for g in gpus:
+        prof = g.last_profile()[0]
+        for k, v in prof.items():
+            if isinstance(v, (int, float)):
+                stages[k] = stages.get(k, 0.0) + v
+        pit32 += prof["point_iterations_fp32"]
+        pit64 += prof["point_iterations_fp64"]
+    peaks = measured_peaks()
+    tf32 = peaks["bf16_tflops"] / 2.0
+    per_stage = {}
+    for stage, key in (("block_gemm", ("k1_blockgemm_fp32", "k2_blockgemm_fp32")),
+                       ("density", ("density_fp32",)), ("field_projection", ("field_projection_fp32",))):
+        ms = sum(stages.get(k, 0.0) for k in key)
+        flops = sum(flops_per_iteration(c)[stage] for c in cases) / len(cases) * pit32
+        d = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12 if ms > 0 else None}
+        d["tensor_frac_of_tf32_peak"] = d["tflops"] / tf32 if d["tflops"] else None
+        if stage != "block_gemm":
+            key2 = "density_fp32" if stage == "density" else "field_projection_fp32"
+            byts = sum(pair_bytes(c, key2, 0) for c in cases) / len(cases)
+            d["pair_tensor_gb"] = byts / 1e9
+        per_stage[stage] = d
+    per_stage["broyden"] = {"ms": stages.get("broyden", 0.0)}
+    line = {"config": "large-basis stress (N_sh=20 synthetic Bogoliubov seed 3, Omega-only blocks up to 231, "
+                      f"3542 states; GT- K=0,1 at {len(omegas)} CIRCLE points each, {iters} FAM iterations per "
+                      f"point, {args.c4_slots} slots per engine)",
+            "nxy": {f"GT-K{k}": int(c.F.mat.nelem) for k, c in enumerate(cases)},
+            "max_block": int(max(hfb.db)), "setup_s": setup_s,
+            "unit": "FAM point-iterations/s", "mixed": res["mixed"], "fp64_form": res["fp64"],
+            "mixed_over_fp64": res["mixed"]["point_iterations_per_s"] / res["fp64"]["point_iterations_per_s"],
+            "stages_mixed": per_stage, "stage_point_iterations": {"fp32": pit32, "fp64": pit64},
+            "note": "stage rates from one serialised run with events between stages; tensor fraction = reference "
+                    "FLOPs per second over the TF32 dense peak (half the measured bf16 peak), 3xTF32 issues three "
+                    "MMAs per product"}
+    for g in gpus:
+        g.close()
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 def run_solve_only(args):
     from pynfam_gb300.solver import GPUSolver
     ops = tuple(OPERATORS[i] for i in (int(x) for x in args.operators.split(",")))
@@ -702,10 +826,23 @@ def main():
     ap.add_argument("--nsh-solve", type=int, default=NSH, help="solve-only: N_sh of the basis")
     ap.add_argument("--operators", default="0",
                     help="solve-only: indices into the workload's operator list (first: the one solved)")
+    ap.add_argument("--config4", action="store_true",
+                    help="the large-basis stress configuration (N_sh = 20) alone, one JSON line")
+    ap.add_argument("--c4-points", type=int, default=256, help="config 4: CIRCLE points per operator")
+    ap.add_argument("--c4-iters", type=int, default=6, help="config 4: FAM iterations per point")
+    ap.add_argument("--c4-slots", type=int, default=16, help="config 4: slots per engine")
+    ap.add_argument("--c4-fp64-points", type=int, default=32, help="config 4: points per operator, FP64 form")
+    ap.add_argument("--no-config4", action="store_true", help="leave the config 4 object out of the line")
+    ap.add_argument("--async-anchors", action="store_true",
+                    help="mixed form: FP64 anchors beside FP32 increments run asynchronously")
     ap.add_argument("--solve-only", action="store_true",
                     help="one operator, batch solves only (no serving, e2e or CPU legs); used for kernel profiling")
     args = ap.parse_args()
-    if args.solve_only:
+    global ASYNC_ANCHORS
+    ASYNC_ANCHORS = args.async_anchors
+    if args.config4:
+        run_config4(args)
+    elif args.solve_only:
         run_solve_only(args)
     elif args.serve_stream:
         run_serve_stream(args)

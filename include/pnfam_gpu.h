@@ -84,7 +84,13 @@ typedef struct {
                                  at most 20 iterations beyond si < epsilon (0: the
                                  reference's test si < epsilon alone);
                                  [4] = n > 0: the mixed form's "near its anchor" bound is
-                                 10^n epsilon instead of 1000 epsilon */
+                                 10^n epsilon instead of 1000 epsilon;
+                                 [5] != 0: mixed form, asynchronous anchors: an FP64 anchor
+                                 evaluation that meets FP32 increments in one launch runs on
+                                 the context's second stream and its points wait (parked)
+                                 while the engine keeps stepping the others (same arithmetic
+                                 per point; 0: the anchor and the increments of a launch end
+                                 together) */
 } pnfam_solver_opts_t;
 
 /*
@@ -129,8 +135,8 @@ int pnfam_gpu_set_operator(pnfam_ctx_t* ctx, int beta_minus, const int* fcols,
  * weighted by 1 - f1 - f2 (X, Y) and f2 - f1 (P, Q); the Broyden vector doubles.
  *   fp, fn   [dqp] proton / neutron occupations in [0, 1] (the doubled basis),
  *            both NULL to return to the zero-temperature form
- * Call before pnfam_gpu_set_operator (it clears the operator).  Solved in the
- * FP64 form only (precision 0).
+ * Call before pnfam_gpu_set_operator (it clears the operator).  Solved in either
+ * form (precision 0 or 1).
  */
 int pnfam_gpu_set_occupations(pnfam_ctx_t* ctx, const double* fp, const double* fn);
 
@@ -304,8 +310,13 @@ long long pnfam_gpu_nxy(const pnfam_ctx_t* ctx);
  * then (entries 11-15) the first five stages of the FP32 evaluations of the
  * mixed form (entries 0-4 then hold the FP64 evaluations only), then (entries
  * 16-19, with opts.reserved[2] != 0) the number and total device ms of the FP32
- * density launches and of the FP32 field-projection launches, and the number of
- * kernel launches.  An engine's figures accumulate from its creation. */
+ * density launches and of the FP32 field-projection launches, then (entries
+ * 20-22) the autotuner's choices for the context's operator: the point count from
+ * which FP32 evaluations take the pair-tensor GEMMs (2^30: never), the K chunks per
+ * density task of those GEMMs, and the autotuner's host time in ms (0: not run; it
+ * runs once per operator when the first mixed-form engine or solve sets up its FP32
+ * buffers, unless PNFAM_GB300_AUTOTUNE=0), and the number of kernel launches.  An
+ * engine's figures accumulate from its creation. */
 int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
                            long long* launches);
 

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <deque>
 #include <map>
 #include <tuple>
 #include <type_traits>
@@ -42,6 +44,9 @@ static int fail(int code, const std::string& msg) {
   } while (0)
 
 namespace {
+
+// asynchronous FP64 anchor batches an engine keeps in flight at most
+constexpr int ANCH_RING = 8;
 
 template <class T>
 struct DBuf {
@@ -99,7 +104,16 @@ struct TaskList {
     t.M = M; t.N = N; t.K = K; t.nterm = (int)terms.size();
     for (size_t i = 0; i < terms.size(); ++i) t.t[i] = terms[i];
     t.cbuf = cbuf; t.coff = coff; t.ldc = ldc;
-    const int ntm = (M + GT - 1) / GT, ntn = (N + GT - 1) / GT;
+    // tile shape: the fewest 1024-element tiles covering M x N (32 x 32 on ties); every
+    // tile costs the same DFMAs, so this is the fewest padded outputs
+    int best = 32, bt = -1;
+    for (int tm : {32, 64, 16, 128, 8}) {
+      const int tn = 1024 / tm;
+      const int nt = ((M + tm - 1) / tm) * ((N + tn - 1) / tn);
+      if (bt < 0 || nt < bt) { bt = nt; best = tm; }
+    }
+    t.tm = best;
+    const int ntm = (M + best - 1) / best, ntn = (N + 1024 / best - 1) / (1024 / best);
     t.tile0 = ntiles; t.ntn = ntn;
     for (int k = 0; k < ntm * ntn; ++k) tile2task.push_back((int)tasks.size());
     ntiles += ntm * ntn;
@@ -225,6 +239,7 @@ struct pnfam_ctx {
   DBuf<double> d_df, d_dv, d_bpart, d_si, d_norm, d_beta, d_gamma, d_cpart, d_wre, d_wim;
   DBuf<double> d_gfn;   // [P][Re | Im][nq*nxy] Green's function of each slot's omega
   DBuf<int> d_active, d_act32, d_act64;
+  DBuf<int> d_act64r;   // [ANCH_RING][P] slot flags of the asynchronous anchor batches
   DBuf<int> d_pint;      // [6][P]: Broyden iteration, Broyden mode, increment step, anchor step,
                          // zero field (first evaluation), newly admitted
   DBuf<BufDesc> d_bufs;
@@ -262,6 +277,12 @@ struct pnfam_ctx {
   double pg_budget = 16e9;
   int pg_min = 4;
   bool pg_on = false, pg_built = false;
+  // autotuning (pg_autotune, once per operator, unless PNFAM_GB300_AUTOTUNE=0): the K
+  // chunks per density task (pg_kspan) and, unless PNFAM_GB300_PAIR_MIN fixes it,
+  // pg_min, the point count from which the pair-tensor path is the faster one
+  int pg_kspan = 384;
+  bool pg_tuned = false, pg_min_env = false, autotune = true;
+  double tune_ms = 0.0;
   std::vector<PGProb> pg_probs;
   std::vector<PGElem> pg_elems;
   std::vector<PGTask> pg_tproj, pg_tdens;
@@ -299,7 +320,7 @@ struct pnfam_ctx {
 
   ~pnfam_ctx() {
     detach_engine();
-    DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active, &d_act32, &d_act64,
+    DBuf<int>* ib[] = {&d_db, &d_st, &d_nup, &d_fc, &d_xtc, &d_ytc, &d_erow, &d_ecol, &d_active, &d_act32, &d_act64, &d_act64r,
                       &d_pint};
     DBuf<float>* fb[] = {&d_up32, &d_vp32, &d_un32, &d_vn32, &d_phi32, &d_state32, &d_T32, &d_rsp32, &d_hsp32,
                          &d_hqp32, &d_dpart32, &d_mf32};
@@ -505,21 +526,40 @@ static void build_tasks(pnfam_ctx* c) {
     }
   }
   c->tplane = std::max(c->tplane, toff);
-  // ---- FP64 field projection tasks: spin-uniform 32 x 32 tiles ----
+  // ---- FP64 field projection tasks: spin-uniform tiles of 1024 / tn rows x tn columns ----
+  // The shape of each (block pair, spin segment) is the one that issues the fewest DFMAs:
+  // per tile, tn columns x the rows up to the warp granularity of the shape (a warp holds
+  // 64 / (tn / 2) rows and skips when they are all beyond the tile), twice (Re, Im), plus
+  // the hpsi generation (10 DFMAs per column and mesh point of each component)
   c->htasks.clear();
   auto cdiv = [](int a, int b) { return (a + b - 1) / b; };
   auto add_h = [&](int ix, int iy, int mode, int call, int outq, long long ooff) {
     const int d = c->db[ix], dc = c->db[iy], nu = c->nup[ix];
     const int seg[3] = {0, nu, d};
-    for (int s = 0; s < 2; ++s)
-      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += 32)
-        for (int b0 = 0; b0 < dc; b0 += 32) {
-          HTask h;
-          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = std::min(32, seg[s + 1] - a0);
-          h.b0 = b0; h.nbc = std::min(32, dc - b0); h.sa = s == 0 ? 1 : -1;
-          h.mode = mode; h.call = call; h.outq = outq; h.ooff = ooff;
+    for (int s = 0; s < 2; ++s) {
+      const int n = seg[s + 1] - seg[s];
+      if (n <= 0) continue;
+      int best = 32;
+      long long bcost = -1;
+      for (int tn : {32, 16, 8}) {
+        const int tm = 1024 / tn, wr = 128 / tn;   // rows per tile, rows per warp
+        long long cost = 0;
+        for (int a0 = 0; a0 < n; a0 += tm) {
+          const int na = std::min(tm, n - a0);
+          cost += (long long)cdiv(dc, tn) * tn * (2LL * cdiv(na, wr) * wr + 10);
+        }
+        if (bcost < 0 || cost < bcost) { bcost = cost; best = tn; }
+      }
+      const int tm = 1024 / best;
+      for (int a0 = seg[s]; a0 < seg[s + 1]; a0 += tm)
+        for (int b0 = 0; b0 < dc; b0 += best) {
+          HTask h{};
+          h.ix = ix; h.iy = iy; h.a0 = a0; h.na = std::min(tm, seg[s + 1] - a0);
+          h.b0 = b0; h.nbc = std::min(best, dc - b0); h.sa = s == 0 ? 1 : -1;
+          h.mode = mode; h.call = call; h.outq = outq; h.tn = best; h.ooff = ooff;
           c->htasks.push_back(h);
         }
+    }
   };
   // tensor-core tiles: rows of the output block (N <= 128, padded to 16) against up to
   // 64 columns x pg points (M = 128 = Re and Im of 64 hpsi rows)
@@ -673,13 +713,41 @@ static int pg_stages(int bslot) {
   return std::max(2, std::min((int)PG_MAXSTAGE, PG_SMEM / per));
 }
 
+// K chunks per density task the autotuner tries (the finest first)
+static constexpr int PG_KSPANS[4] = {96, 192, 384, 768};
+
+// density tasks (problem, M tile, K range of at most kspan chunks) and the layout of
+// their partial sums; the largest tasks first
+static void pg_density_tasks(pnfam_ctx* c, int kspan) {
+  auto cdiv = [](long long a, long long b) { return (a + b - 1) / b; };
+  c->pg_tdens.clear();
+  long long d0 = 0;
+  for (int id = 0; id < (int)c->pg_probs.size(); ++id) {
+    PGProb& pr = c->pg_probs[id];
+    if (pr.kind != 1) continue;
+    pr.nsplit = (int)std::max(1LL, cdiv(pr.nkc, kspan));
+    pr.d0 = d0;
+    d0 += (long long)pr.nsplit * pr.ncol * PG_MAXPTS * pr.mrows;
+    for (int t = 0; t < pr.ntile; ++t)
+      for (int sp = 0; sp < pr.nsplit; ++sp) {
+        const int k0 = (int)((long long)pr.nkc * sp / pr.nsplit), k1 = (int)((long long)pr.nkc * (sp + 1) / pr.nsplit);
+        if (k1 <= k0) continue;
+        c->pg_tdens.push_back(PGTask{id, t, k0, k1 - k0, sp, 0});
+      }
+  }
+  std::stable_sort(c->pg_tdens.begin(), c->pg_tdens.end(),
+                   [](const PGTask& x, const PGTask& y) { return x.nkc > y.nkc; });
+  c->pg_dfloats = d0;
+  c->pg_kspan = kspan;
+}
+
 static void pg_setup(pnfam_ctx* c) {
   c->pg_on = false;
   c->pg_built = false;
   c->pg_probs.clear(); c->pg_elems.clear(); c->pg_tproj.clear(); c->pg_tdens.clear();
   c->pg_bproj.clear(); c->pg_bdens.clear(); c->pg_ach.clear();
   for (int k = 0; k < 12; ++k) c->pg_fold.dens[k] = -1;
-  if (!c->pg_mode || c->nq != 2) return;
+  if (!c->pg_mode) return;
   const int nghl = c->nghl, nb = c->nb;
   auto cdiv = [](long long a, long long b) { return (a + b - 1) / b; };
   // element lists of one structure, per class, in (block row, column, row) order
@@ -708,19 +776,14 @@ static void pg_setup(pnfam_ctx* c) {
     else { pr.mrows = ncombo * nghl; pr.kdim = pr.ne; }
     pr.nkc = (int)cdiv(pr.kdim, PG_K);
     pr.ntile = (int)cdiv(pr.mrows, PG_M);
-    pr.nsplit = kind == 1 ? (int)std::max(1LL, cdiv(pr.nkc, 384)) : 1;
+    pr.nsplit = 1;   // density problems: pg_density_tasks
     pr.a0 = a0; a0 += (long long)pr.ntile * pr.nkc;
     pr.b0 = b0; b0 += pr.nkc;
     pr.d0 = 0;
-    if (kind == 1) { pr.d0 = d0; d0 += (long long)pr.nsplit * ncol * PG_MAXPTS * pr.mrows; }
     const int id = (int)c->pg_probs.size();
     c->pg_probs.push_back(pr);
-    for (int t = 0; t < pr.ntile; ++t)
-      for (int s = 0; s < pr.nsplit; ++s) {
-        const int k0 = (int)((long long)pr.nkc * s / pr.nsplit), k1 = (int)((long long)pr.nkc * (s + 1) / pr.nsplit);
-        if (k1 <= k0) continue;
-        (kind == 0 ? c->pg_tproj : c->pg_tdens).push_back(PGTask{id, t, k0, k1 - k0, s, 0});
-      }
+    if (kind == 0)
+      for (int t = 0; t < pr.ntile; ++t) c->pg_tproj.push_back(PGTask{id, t, 0, pr.nkc, 0, 0});
     for (int kc = 0; kc < pr.nkc; ++kc) (kind == 0 ? c->pg_bproj : c->pg_bdens).push_back(PGBChunk{id, kc});
     return id;
   };
@@ -740,14 +803,19 @@ static void pg_setup(pnfam_ctx* c) {
   }
   c->pg_nachunk = a0;
   c->pg_nbchunk = b0;
-  c->pg_dfloats = d0;
-  // the largest tasks first: the long projection tiles, then the density splits
+  c->pg_tuned = false;
+  c->pg_kspan = 384;
+  pg_density_tasks(c, c->pg_kspan);
+  // the largest tasks first: the long projection tiles
   std::stable_sort(c->pg_tproj.begin(), c->pg_tproj.end(),
                    [](const PGTask& x, const PGTask& y) { return x.nkc > y.nkc; });
-  std::stable_sort(c->pg_tdens.begin(), c->pg_tdens.end(),
-                   [](const PGTask& x, const PGTask& y) { return x.nkc > y.nkc; });
+  // budget with the partial sums of the finest density split the autotuner may choose
+  long long dmax = 0;
+  for (const PGProb& pr : c->pg_probs)
+    if (pr.kind == 1) dmax += (long long)std::max(1LL, cdiv(pr.nkc, PG_KSPANS[0])) * pr.ncol * PG_MAXPTS * pr.mrows;
+  (void)d0;
   const double bytes = (double)a0 * PG_ACHUNK * sizeof(float) + (double)b0 * PG_BCHUNK * sizeof(float) +
-                       (double)d0 * sizeof(float);
+                       (double)dmax * sizeof(float);
   c->pg_on = bytes <= c->pg_budget;
   if (!c->pg_on) return;
   for (int id = 0; id < (int)c->pg_probs.size(); ++id) {
@@ -863,6 +931,7 @@ static int ensure_buffers(pnfam_ctx* c, int P, int M) {
   }
   CK(dalloc(c->d_act32, (size_t)P));
   CK(dalloc(c->d_act64, (size_t)P));
+  CK(dalloc(c->d_act64r, (size_t)ANCH_RING * P));
   BufDesc bd[NBUF];
   bd[B_UP] = {c->d_up.p, 0, 0};
   bd[B_VP] = {c->d_vp.p, 0, 0};
@@ -1035,6 +1104,135 @@ static int residual_t(pnfam_ctx* c, int P, int nact, const int* act, bool timed,
 }
 
 
+// ---------------------------------------------------------------------------
+// Autotuning of the FP32 evaluation, once per operator (after its pair tensor is
+// built), from the operator's block structure and timed trial evaluations:
+//  1. the K span of the density tasks of the pair-tensor GEMM.  The problem sizes
+//     (rows = component pairs x mesh points, K = the elements of a spin class, both
+//     fixed by the block-size histogram) give the task count of each candidate span,
+//     hence its number of waves on the SMs; the candidates whose last wave is at least
+//     half full, or the finest one, are timed and the fastest is kept.
+//  2. pg_min, the point count from which an evaluation takes the pair-tensor path
+//     instead of the per-block tensor-core kernels: both are timed at 1, 2, 4, ... up
+//     to 64 points (or the engine's slots) and pg_min is the smallest count from which
+//     the pair path stays the faster one (PNFAM_GB300_PAIR_MIN fixes it instead).
+// Trial evaluations run on the FP32 scratch of the context's first slots (zeroed), on
+// the context's stream, before any point is admitted.  PNFAM_GB300_AUTOTUNE=0 skips it.
+// ---------------------------------------------------------------------------
+// Choices are kept per process, keyed by what they depend on (the problem sizes of
+// the operator's pair tensor, the mesh, the trial point count, the SM count), so a
+// later context of the same operator structure takes them without trials.
+struct TuneChoice { int kspan, pg_min; };
+static std::mutex g_tune_mu;
+static std::map<unsigned long long, TuneChoice> g_tune;
+
+static unsigned long long pg_tune_key(const pnfam_ctx* c, int nmax) {
+  unsigned long long h = 1469598103934665603ULL;
+  auto mix = [&](long long v) {
+    for (int b = 0; b < 8; ++b) { h ^= (unsigned long long)((v >> (8 * b)) & 0xff); h *= 1099511628211ULL; }
+  };
+  mix(c->nghl); mix(c->nq); mix(nmax); mix(c->nsm); mix(c->dev); mix(c->pg_min_env ? c->pg_min : -1);
+  for (const PGProb& pr : c->pg_probs) { mix(pr.kind); mix(pr.ntile); mix(pr.nkc); mix(pr.ncol); }
+  return h;
+}
+
+static int pg_autotune(pnfam_ctx* c, int P) {
+  const int nmax = std::min(P, (int)PG_MAXPTS);
+  if (c->pg_tuned || !c->pg_on || !c->pg_built || !c->autotune || nmax < 2) return PNFAM_OK;
+  c->pg_tuned = true;
+  const unsigned long long key = pg_tune_key(c, nmax);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      if (it->second.kspan != c->pg_kspan) {
+        pg_density_tasks(c, it->second.kspan);
+        CK(upload(c->d_pg_probs, c->pg_probs.data(), c->pg_probs.size()));
+        CK(upload(c->d_pg_tdens, c->pg_tdens.data(), c->pg_tdens.size()));
+        CK(dalloc(c->d_pg_d, (size_t)std::max(1LL, c->pg_dfloats)));
+      }
+      c->pg_min = it->second.pg_min;
+      c->tune_ms = 0.0;
+      return PNFAM_OK;
+    }
+  }
+  cudaStream_t st = c->stream;
+  const long long nv = 2 * c->nq * c->nxy;
+  CK(cudaMemsetAsync(c->d_state32.p, 0, sizeof(float) * (size_t)nmax * nv, st));
+  std::vector<int> list(nmax), flags(P, 0);
+  for (int i = 0; i < nmax; ++i) list[i] = i;
+  CK(upload(c->d_actlist, list.data(), list.size()));
+  const int saved_min = c->pg_min;
+  auto t0 = std::chrono::steady_clock::now();
+  // device ms of one FP32 evaluation of n points (pair: the pair-tensor path or not)
+  auto trial = [&](int n, bool pair, double* ms) -> int {
+    for (int i = 0; i < P; ++i) flags[i] = i < n;
+    CK(upload(c->d_act32, flags.data(), flags.size()));
+    c->pg_min = pair ? 1 : (1 << 30);
+    int rc = residual_t<float>(c, P, n, c->d_act32.p, false, st);   // warm
+    if (rc) return rc;
+    const int reps = 2;
+    CK(cudaEventRecord(c->ev[0], st));
+    for (int r = 0; r < reps && !rc; ++r) rc = residual_t<float>(c, P, n, c->d_act32.p, false, st);
+    if (rc) return rc;
+    CK(cudaEventRecord(c->ev[1], st));
+    CK(cudaEventSynchronize(c->ev[1]));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, c->ev[0], c->ev[1]));
+    *ms = f / reps;
+    return PNFAM_OK;
+  };
+  int rc;
+  // 1. density task span
+  {
+    std::vector<int> cand;
+    for (int span : PG_KSPANS) {
+      long long tasks = 0;
+      for (const PGProb& pr : c->pg_probs)
+        if (pr.kind == 1) tasks += (long long)pr.ntile * std::max(1, (pr.nkc + span - 1) / span);
+      const double waves = (double)tasks / c->nsm;
+      const double last = waves - std::floor(waves);
+      if (last == 0.0 || last >= 0.5 || span == PG_KSPANS[0]) cand.push_back(span);
+    }
+    double best = 1e300;
+    int bspan = c->pg_kspan;
+    for (int span : cand) {
+      pg_density_tasks(c, span);
+      CK(upload(c->d_pg_probs, c->pg_probs.data(), c->pg_probs.size()));
+      CK(upload(c->d_pg_tdens, c->pg_tdens.data(), c->pg_tdens.size()));
+      CK(dalloc(c->d_pg_d, (size_t)std::max(1LL, c->pg_dfloats)));
+      double ms = 0.0;
+      if ((rc = trial(nmax, true, &ms))) return rc;
+      if (ms < best) { best = ms; bspan = span; }
+    }
+    pg_density_tasks(c, bspan);
+    CK(upload(c->d_pg_probs, c->pg_probs.data(), c->pg_probs.size()));
+    CK(upload(c->d_pg_tdens, c->pg_tdens.data(), c->pg_tdens.size()));
+    CK(dalloc(c->d_pg_d, (size_t)std::max(1LL, c->pg_dfloats)));
+  }
+  // 2. pair-tensor path from pg_min points on
+  if (!c->pg_min_env) {
+    std::vector<int> ns;
+    std::vector<bool> pair_wins;
+    for (int n = 1; n <= nmax; n *= 2) {
+      double tp = 0.0, tb = 0.0;
+      if ((rc = trial(n, true, &tp)) || (rc = trial(n, false, &tb))) return rc;
+      ns.push_back(n);
+      pair_wins.push_back(tp <= tb);
+    }
+    int m = 1 << 30;
+    for (int i = (int)ns.size() - 1; i >= 0 && pair_wins[i]; --i) m = ns[i];
+    c->pg_min = m;
+  } else {
+    c->pg_min = saved_min;
+  }
+  CK(cudaStreamSynchronize(st));
+  c->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = TuneChoice{c->pg_kspan, c->pg_min};
+  return PNFAM_OK;
+}
+
 // FP32 copies of the ground state and FP32 scratch for P points
 static int ensure_buffers32(pnfam_ctx* c, int P) {
   const long long nxy = c->nxy;
@@ -1051,20 +1249,24 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
     }
     c->have32 = true;
   }
-  CK(dalloc(c->d_state32, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_T32, (size_t)P * 16 * nxy));
+  // QP-state arrays: nv = Re and Im of X, Y (and P, Q in the statistical FAM); GEMM
+  // scratch as in the FP64 form
+  const long long nv = 2 * c->nq * nxy;
+  const long long tpl = std::max(c->tplane, 8 * nxy);
+  CK(dalloc(c->d_state32, (size_t)P * nv));
+  CK(dalloc(c->d_T32, (size_t)P * 2 * tpl));
   CK(dalloc(c->d_rsp32, (size_t)P * 8 * nxy));
   CK(dalloc(c->d_hsp32, (size_t)P * 8 * nxy));
-  CK(dalloc(c->d_hqp32, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_hqp32, (size_t)P * nv));
   CK(dalloc(c->d_dpart32, (size_t)P * 2 * c->G * 2 * ND * c->nghl));
   CK(dalloc(c->d_mf32, (size_t)P * 2 * NMF * 2 * c->nghl));
-  CK(dalloc(c->d_xsave, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_radd, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_xsave, (size_t)P * nv));
+  CK(dalloc(c->d_radd, (size_t)P * nv));
   CK(dalloc(c->d_dmax, (size_t)P));
-  CK(dalloc(c->d_lastf, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_lastv, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_tf, (size_t)P * 4 * nxy));
-  CK(dalloc(c->d_tv, (size_t)P * 4 * nxy));
+  CK(dalloc(c->d_lastf, (size_t)P * nv));
+  CK(dalloc(c->d_lastv, (size_t)P * nv));
+  CK(dalloc(c->d_tf, (size_t)P * nv));
+  CK(dalloc(c->d_tv, (size_t)P * nv));
   if (c->tc_density) {
     CK(dalloc(c->d_bsplit, (size_t)P * c->bstride));
     if (!c->have_aphi) {
@@ -1082,11 +1284,11 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
   bd[B_VP] = {c->d_vp32.p, 0, 0};
   bd[B_UN] = {c->d_un32.p, 0, 0};
   bd[B_VN] = {c->d_vn32.p, 0, 0};
-  bd[B_STATE] = {c->d_state32.p, 4 * nxy, 2 * nxy};
-  bd[B_T] = {c->d_T32.p, 16 * nxy, 8 * nxy};
+  bd[B_STATE] = {c->d_state32.p, nv, nv / 2};
+  bd[B_T] = {c->d_T32.p, 2 * tpl, tpl};
   bd[B_RSP] = {c->d_rsp32.p, 8 * nxy, 4 * nxy};
   bd[B_HSP] = {c->d_hsp32.p, 8 * nxy, 4 * nxy};
-  bd[B_HQP] = {c->d_hqp32.p, 4 * nxy, 2 * nxy};
+  bd[B_HQP] = {c->d_hqp32.p, nv, nv / 2};
   CK(upload(c->d_bufs32, bd, NBUF));
   if (!c->have_hphi) {
     const int nrc = (c->nghl + HTC_K - 1) / HTC_K;
@@ -1115,7 +1317,7 @@ static int ensure_buffers32(pnfam_ctx* c, int P) {
     const int rc = pg_build(c);
     if (rc) return rc;
   }
-  return PNFAM_OK;
+  return pg_autotune(c, P);
 }
 
 // ---------------------------------------------------------------------------
@@ -1175,7 +1377,9 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     v = std::getenv("PNFAM_GB300_PAIR_GEMM_GB");
     if (v && std::atof(v) > 0) c->pg_budget = std::atof(v) * 1e9;
     v = std::getenv("PNFAM_GB300_PAIR_MIN");
-    if (v && std::atoi(v) > 0) c->pg_min = std::atoi(v);
+    if (v && std::atoi(v) > 0) { c->pg_min = std::atoi(v); c->pg_min_env = true; }
+    v = std::getenv("PNFAM_GB300_AUTOTUNE");
+    c->autotune = !(v && v[0] == '0');
   }
   const int s = c->dqp;
   const long long mo = c->uoff.back() + (long long)c->db.back() * c->db.back();
@@ -1406,6 +1610,25 @@ struct pnfam_engine {
   std::vector<std::pair<int, std::vector<double>>> x0q;
   std::vector<unsigned long long> hdmax;
   std::vector<int> pint, act32, act64, actlist;
+  // Asynchronous anchors (mixed form): when a launch has FP32 increment evaluations,
+  // the FP64 anchor evaluations it also needs run as a batch on the context's second
+  // stream and their slots are parked (afly 1) while the engine keeps stepping its
+  // other slots; a later launch finds the batch complete (its event), and each parked
+  // slot then takes the Green's function and Broyden step of that anchor (afly 2, then
+  // 0).  A slot's arithmetic is the same as with the anchor inside one launch; only
+  // the anchor's FP64 work no longer holds up the other slots.  stepped: the slots
+  // that step in the launch in flight.
+  bool async = false;   // opts.reserved[5]
+  std::vector<int> afly, stepped;
+  struct ABatch { int ring; std::vector<int> slots; };
+  std::deque<ABatch> abatch;
+  cudaEvent_t aev[ANCH_RING] = {};
+  int aring = 0;
+  PinBuf<int> pin_a;   // [ANCH_RING][P] the batches' slot flags
+  ~pnfam_engine() {
+    for (cudaEvent_t& ev : aev)
+      if (ev) cudaEventDestroy(ev);
+  }
   int herr = 0;
   std::vector<double> hsi, cpart;
   // pinned staging of the per-evaluation copies: ints [active P | pint 6P | act64 P |
@@ -1424,6 +1647,7 @@ struct pnfam_engine {
 // a context freed before its engine leaves the engine without a context
 void pnfam_ctx::detach_engine() {
   if (engine) {
+    cudaStreamSynchronize(stream64);
     cudaStreamSynchronize(stream);
     engine->c = nullptr;
     engine->pending = 0;
@@ -1442,8 +1666,6 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   if (e->M > 64) return fail(PNFAM_EINVAL, "broyden_history_size > 64 is not supported");
   e->bmode = e->M < 0 ? BRO_NOMIX : e->M == 0 ? BRO_LINEAR : BRO_BROYDEN;
   e->nxy = c->nxy; e->N = (int)(2 * c->nq * c->nxy); e->nops = c->nops;
-  if (o->precision == 1 && c->nq != 2)
-    return fail(PNFAM_EINVAL, "the statistical FAM (occupations set) is solved in the FP64 form (precision 0)");
   int rc = ensure_buffers(c, std::max(P, c->cap_P), std::max(std::max(e->M, 1), c->cap_M));
   if (rc) return rc;
   c->cap_P = std::max(P, c->cap_P); c->cap_M = std::max(std::max(e->M, 1), c->cap_M);
@@ -1465,6 +1687,7 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->timed = o->reserved[0] != 0;
   e->s_rel = o->reserved[3] > 0 ? std::pow(10.0, -o->reserved[3]) : 0.0;
   e->near = o->reserved[4] > 0 ? std::pow(10.0, o->reserved[4]) : 1000.0;
+  e->async = o->reserved[5] != 0;
   c->live = o->reserved[2] != 0;
   c->nlev = 0;
   c->live_ms[0] = c->live_ms[1] = 0.0;
@@ -1477,6 +1700,10 @@ static int engine_setup(pnfam_engine* e, pnfam_ctx* c, int P, const pnfam_solver
   e->x0.assign(P, 0); e->x0q.clear();
   e->best.assign(P, 1e300); e->wre.assign(P, 0.0); e->wim.assign(P, 0.0); e->hdmax.assign(P, 0);
   e->pint.assign((size_t)6 * P, 0); e->act32.assign(P, 0); e->act64.assign(P, 0);
+  e->afly.assign(P, 0); e->stepped.assign(P, 0); e->abatch.clear(); e->aring = 0;
+  for (cudaEvent_t& ev : e->aev)
+    if (!ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(e->pin_a.ensure((size_t)ANCH_RING * P));
   e->hsi.assign(P, 0.0); e->cpart.assign((size_t)P * c->nchunk_c * 2 * nops, 0.0);
   CK(e->pin_i.ensure((size_t)10 * P + 1));
   CK(e->pin_d.ensure((size_t)3 * P + e->cpart.size()));
@@ -1508,7 +1735,7 @@ static int engine_admit(pnfam_engine* e, int n, const double* re_w, const double
   for (int p = 0; p < e->P && k < n; ++p) {
     if (e->active[p]) continue;
     e->active[p] = 1; e->it[p] = 0; e->anchor[p] = 1; e->since_best[p] = 0; e->nstall[p] = 0;
-    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1; e->extra[p] = 0; e->x0[p] = 0;
+    e->best[p] = 1e300; e->si[p] = 1.0; e->fresh[p] = 1; e->extra[p] = 0; e->x0[p] = 0; e->afly[p] = 0;
     for (int q = 0; q < e->nops; ++q) { e->sre[(size_t)p * e->nops + q] = 0.0; e->sim[(size_t)p * e->nops + q] = 0.0; }
     e->wre[p] = re_w[k]; e->wim[p] = im_w[k];
     e->tag[p] = tags ? tags[k] : k;
@@ -1586,34 +1813,80 @@ static int broyden_step(pnfam_ctx* c, pnfam_engine* e, int any_bro, const int* d
   return PNFAM_OK;
 }
 
-// enqueue one evaluation (and Broyden step) for every active slot
-static int engine_launch(pnfam_engine* e) {
+// enqueue one evaluation (and Broyden step) for every active slot that is not parked
+// on an anchor in flight.  block_if_idle: when every active slot is parked, wait for
+// the oldest anchor batch instead of returning with nothing launched.
+static int engine_launch(pnfam_engine* e, bool block_if_idle) {
   pnfam_ctx* c = e->c;
   const int P = e->P, N = e->N;
   const long long nxy = e->nxy;
+  const bool timed = e->timed;
+  // anchor batches that have completed: their slots step in this launch
+  std::vector<int> resumed_ev;
+  auto resume_front = [&]() {
+    const pnfam_engine::ABatch& b = e->abatch.front();
+    for (int p : b.slots) e->afly[p] = 2;
+    resumed_ev.push_back(b.ring);
+    e->abatch.pop_front();
+  };
+  while (!e->abatch.empty()) {
+    const cudaError_t q = cudaEventQuery(e->aev[e->abatch.front().ring]);
+    if (q == cudaErrorNotReady) break;
+    if (q != cudaSuccess) return fail(PNFAM_ECUDA, std::string("anchor batch: ") + cudaGetErrorString(q));
+    resume_front();
+  }
+  {
+    int nstep = 0;
+    for (int p = 0; p < P; ++p) nstep += e->active[p] && e->afly[p] != 1;
+    if (nstep == 0 && !e->abatch.empty()) {
+      if (!block_if_idle) return PNFAM_OK;   // nothing can step before an anchor completes
+      CK(cudaEventSynchronize(e->aev[e->abatch.front().ring]));
+      resume_front();
+    }
+  }
+  // a free ring entry for a new batch
+  if ((int)e->abatch.size() == ANCH_RING) {
+    CK(cudaEventSynchronize(e->aev[e->abatch.front().ring]));
+    resume_front();
+  }
   int nact = 0, n32 = 0, n64 = 0, nanch = 0, nfresh = 0, any_bro = 0;
   for (int p = 0; p < P; ++p) {
-    const bool a = e->active[p] != 0, first = a && e->it[p] == 0;
+    const bool a = e->active[p] != 0 && e->afly[p] != 1;   // steps in this launch
+    const bool resumed = a && e->afly[p] == 2;            // its anchor was evaluated earlier
+    const bool first = a && e->it[p] == 0;
     // the field of X = 0 vanishes: no evaluation at the first iteration, unless the
     // slot starts from a stored state
     const bool zero = first && !e->x0[p];
     const bool lo = e->mixed && !e->anchor[p];
     e->act32[p] = a && lo && !zero;
-    e->act64[p] = a && !lo && !zero;
-    nact += a; n32 += e->act32[p]; n64 += e->act64[p];
+    e->act64[p] = a && !lo && !zero && !resumed;
+    e->stepped[p] = a;
+    n32 += e->act32[p]; n64 += e->act64[p];
+  }
+  // FP64 anchors beside FP32 increments: asynchronous, their slots parked
+  const bool async = e->async && e->mixed && !timed && n64 > 0 && n32 > 0;
+  std::vector<int> batch;
+  if (async)
+    for (int p = 0; p < P; ++p)
+      if (e->act64[p]) { batch.push_back(p); e->stepped[p] = 0; }
+  for (int p = 0; p < P; ++p) {
+    const bool a = e->stepped[p] != 0, first = a && e->it[p] == 0;
+    if (a && e->afly[p] == 2) e->afly[p] = 0;
+    nact += a;
     e->pint[p] = e->it[p];
     e->pint[P + p] = first && e->bmode == BRO_BROYDEN ? BRO_LINEAR : e->bmode;
-    e->pint[2 * P + p] = e->act32[p];
+    e->pint[2 * P + p] = a && e->act32[p];
     e->pint[3 * P + p] = a && e->mixed && e->anchor[p];
-    e->pint[4 * P + p] = zero;
+    e->pint[4 * P + p] = first && !e->x0[p];
     e->pint[5 * P + p] = a && e->fresh[p];
     nanch += e->pint[3 * P + p]; nfresh += e->pint[5 * P + p];
     any_bro |= a && e->pint[P + p] == BRO_BROYDEN;
-    e->fresh[p] = 0;
+    if (a) e->fresh[p] = 0;
   }
-  if (nact == 0) return PNFAM_OK;
+  if (nact == 0 && batch.empty()) return PNFAM_OK;
   c->pit32 += n32; c->pit64 += n64;
-  const bool timed = e->timed;
+  // the completed batches (already complete: ordering only) before their slots step
+  for (int r : resumed_ev) CK(cudaStreamWaitEvent(c->stream, e->aev[r], 0));
   auto tic = [&]() { if (timed) cudaEventRecord(c->ev[0], c->stream); };
   auto toc = [&](int k) {
     if (!timed) return;
@@ -1634,7 +1907,7 @@ static int engine_launch(pnfam_engine* e) {
   // is in flight: engine_finish waited for it)
   int* pi_ = e->pin_i.p;
   double* pd_ = e->pin_d.p;
-  std::memcpy(pi_, e->active.data(), sizeof(int) * P);
+  std::memcpy(pi_, e->stepped.data(), sizeof(int) * P);
   std::memcpy(pi_ + P, e->pint.data(), sizeof(int) * 6 * P);
   CK(cudaMemcpyAsync(c->d_active.p, pi_, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d_pint.p, pi_ + P, sizeof(int) * 6 * P, cudaMemcpyHostToDevice, c->stream));
@@ -1666,18 +1939,35 @@ static int engine_launch(pnfam_engine* e) {
   int rc;
   bool split = false;
   if (!e->no_res) {
-    std::memcpy(pi_ + 7 * P, e->act64.data(), sizeof(int) * P);
-    CK(cudaMemcpyAsync(c->d_act64.p, pi_ + 7 * P, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
-    // FP64 (anchor) evaluations of some points and FP32 increment evaluations of the
-    // others use disjoint scratch and write disjoint rows of hqp: the FP64 ones run
-    // on the second stream, joined before the Green's function (not when stages are timed)
-    split = n64 && n32 && !timed;
-    if (split) {
+    if (async) {
+      // FP64 (anchor) evaluations of the parked slots and FP32 increment evaluations of
+      // the others use disjoint scratch and write disjoint rows of hqp; the batch runs
+      // on the second stream with its own copy of the slot flags
+      const int r = e->aring;
+      e->aring = (e->aring + 1) % ANCH_RING;
+      int* pa = e->pin_a.p + (size_t)r * P;
+      int* da = c->d_act64r.p + (size_t)r * P;
+      std::memcpy(pa, e->act64.data(), sizeof(int) * P);
       CK(cudaEventRecord(c->evf[0], c->stream));
       CK(cudaStreamWaitEvent(c->stream64, c->evf[0], 0));
+      CK(cudaMemcpyAsync(da, pa, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream64));
+      if ((rc = residual_t<double>(c, P, n64, da, false, c->stream64))) return rc;
+      CK(cudaEventRecord(e->aev[r], c->stream64));
+      for (int p : batch) e->afly[p] = 1;
+      e->abatch.push_back({r, std::move(batch)});
+    } else if (n64) {
+      std::memcpy(pi_ + 7 * P, e->act64.data(), sizeof(int) * P);
+      CK(cudaMemcpyAsync(c->d_act64.p, pi_ + 7 * P, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
+      // beside this launch's FP32 increments (disjoint scratch, disjoint rows of hqp):
+      // on the second stream, joined before the Green's function (not when timed)
+      split = n32 > 0 && !timed;
+      if (split) {
+        CK(cudaEventRecord(c->evf[0], c->stream));
+        CK(cudaStreamWaitEvent(c->stream64, c->evf[0], 0));
+      }
+      if ((rc = residual_t<double>(c, P, n64, c->d_act64.p, timed, split ? c->stream64 : c->stream))) return rc;
+      if (split) CK(cudaEventRecord(c->evf[1], c->stream64));
     }
-    if (n64 && (rc = residual_t<double>(c, P, n64, c->d_act64.p, timed, split ? c->stream64 : c->stream))) return rc;
-    if (split) CK(cudaEventRecord(c->evf[1], c->stream64));
     if (e->mixed) {
       std::memcpy(pi_ + 8 * P, e->act32.data(), sizeof(int) * P);
       CK(cudaMemcpyAsync(c->d_act32.p, pi_ + 8 * P, sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
@@ -1688,7 +1978,9 @@ static int engine_launch(pnfam_engine* e) {
         std::memcpy(pi_ + 9 * P, e->actlist.data(), sizeof(int) * n32);
         CK(cudaMemcpyAsync(c->d_actlist.p, pi_ + 9 * P, sizeof(int) * n32, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemsetAsync(c->d_dmax.p, 0, sizeof(unsigned long long) * P, c->stream));
-        k_to_f32<<<vgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
+        // a few elements per thread and one atomic per block for max|X - X_a|
+        const dim3 cgrid((unsigned)std::min<long long>(256, (N + 255) / 256), P);
+        k_to_f32<<<cgrid, 256, 0, c->stream>>>(c->d_state.p, c->d_state32.p, N, P, N, c->d_act32.p, c->d_xsave.p,
                                                c->d_dmax.p);
         if ((rc = residual_t<float>(c, P, n32, c->d_act32.p, timed, c->stream))) return rc;
         c->launches++;
@@ -1764,7 +2056,7 @@ static int engine_finish(pnfam_engine* e) {
   const int nops = e->nops;
   const double pi = 3.141592653589793238462643;
   for (int p = 0; p < e->P; ++p) {
-    if (!e->active[p]) continue;
+    if (!e->active[p] || !e->stepped[p]) continue;
     const bool was_anchor = !e->mixed || e->anchor[p] || e->it[p] == 0;
     e->si[p] = e->hsi[p];
     if (!std::isfinite(e->si[p])) return fail(PNFAM_ENONFINITE, "non-finite residual");
@@ -1838,7 +2130,8 @@ static int solve_impl(pnfam_ctx_t* c, int P, const double* re_w, const double* i
       if (e.active[p] && (rc = engine_set_state(&e, p, x0 + (size_t)p * e.N))) return rc;
   }
   while (engine_nactive(&e) > 0) {
-    if ((rc = engine_launch(&e)) || (rc = engine_finish(&e))) {
+    if ((rc = engine_launch(&e, true)) || (rc = engine_finish(&e))) {
+      cudaStreamSynchronize(c->stream64);
       cudaStreamSynchronize(c->stream);
       g_err = "pnfam_gpu_solve: " + g_err;
       return rc;
@@ -1914,7 +2207,7 @@ extern "C" int pnfam_gpu_engine_launch(pnfam_engine_t* e) {
   if (!e) return fail(PNFAM_EINVAL, "pnfam_gpu_engine_launch: NULL engine");
   if (!e->c) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: the context was freed");
   if (e->pending) return fail(PNFAM_ESTATE, "pnfam_gpu_engine_launch: an evaluation is in flight");
-  const int rc = engine_launch(e);
+  const int rc = engine_launch(e, false);
   if (rc) {
     // nothing of a failed launch may stay in flight (the FP64 anchors' stream included)
     cudaStreamSynchronize(e->c->stream64);
@@ -1963,6 +2256,7 @@ extern "C" int pnfam_gpu_engine_ready(const pnfam_engine_t* e) {
 extern "C" void pnfam_gpu_engine_free(pnfam_engine_t* e) {
   if (!e) return;
   if (e->c) {
+    cudaStreamSynchronize(e->c->stream64);   // anchor batches still in flight
     if (e->pending) cudaStreamSynchronize(e->c->stream);
     e->c->engine = nullptr;
   }
@@ -2144,6 +2438,10 @@ extern "C" int pnfam_gpu_last_profile(const pnfam_ctx_t* c, double* stage_ms, in
   for (int k = 11; k < nstage && k < 16; ++k) stage_ms[k] = c->stage32_ms[k - 11];
   const double live[4] = {(double)c->live_n[0], c->live_ms[0], (double)c->live_n[1], c->live_ms[1]};
   for (int k = 16; k < nstage && k < 20; ++k) stage_ms[k] = live[k - 16];
+  // the autotuner's choices: pg_min (2^30: the pair-tensor path never), the density
+  // task span, and its host time in ms (0: not run)
+  const double tune[3] = {(double)c->pg_min, (double)c->pg_kspan, c->tune_ms};
+  for (int k = 20; k < nstage && k < 23; ++k) stage_ms[k] = tune[k - 20];
   if (launches) *launches = c->launches;
   return PNFAM_OK;
 }

@@ -49,6 +49,7 @@ struct GemmTask {
   long long coff;
   int cbuf, ldc;
   int tile0, ntn;      // first tile in the flattened grid, tiles along N
+  int tm, pad_;        // tile shape: tm rows x 1024 / tm columns (tm = 8 ... 128)
 };
 
 #define GT 32
@@ -60,20 +61,18 @@ __device__ __forceinline__ const T* bufptr(const BufDescT<T>* b, int id, int p, 
   return d.base + (long long)p * d.sp + (long long)plane * d.spl + off;
 }
 
-// C = sum_t alpha_t op(A_t) op(B_t); blockIdx.y = point*2 + plane; T = compute type
-template <class T>
-__global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks, const int* __restrict__ tile2task,
-                                              const BufDescT<T>* __restrict__ bufs, const int* __restrict__ active) {
-  const int z = blockIdx.y;
-  const int p = z >> 1, plane = z & 1;
-  if (active && !active[p]) return;
-  const int tile = blockIdx.x;
-  const GemmTask& Tk = tasks[tile2task[tile]];
-  const int lt = tile - Tk.tile0;
-  const int m0 = (lt / Tk.ntn) * GT, n0 = (lt % Tk.ntn) * GT;
-  __shared__ T As[GK][GT + 1];
-  __shared__ T Bs[GK][GT + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+// C = sum_t alpha_t op(A_t) op(B_t); blockIdx.y = point*2 + plane; T = compute type.
+// Output tiles of TM x TN = 1024 elements (TM = 8 ... 128, chosen per task from its M
+// and N), 2 x 2 per thread; every element sums over k in the same order whatever the
+// shape.
+template <class T, int TM>
+__device__ __forceinline__ void gemm_tile(const GemmTask& Tk, int lt, const BufDescT<T>* __restrict__ bufs, int p,
+                                          int plane, T* smem) {
+  constexpr int TN = 1024 / TM, TX = TN / 2;
+  T* As = smem;                    // [GK][TM + 1]
+  T* Bs = smem + GK * (TM + 1);    // [GK][TN + 1]
+  const int m0 = (lt / Tk.ntn) * TM, n0 = (lt % Tk.ntn) * TN;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   T acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
   const int M = Tk.M, N = Tk.N, K = Tk.K;
   for (int it = 0; it < Tk.nterm; ++it) {
@@ -82,22 +81,25 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks
     const T* B = bufptr(bufs, tm.bbuf, p, plane, tm.boff);
     const T alpha = (T)tm.alpha[plane];
     for (int k0 = 0; k0 < K; k0 += GK) {
-      for (int e = threadIdx.x; e < GK * GT; e += 256) {
-        const int kk = e / GT, mm = e % GT;
+      for (int e = threadIdx.x; e < GK * TM; e += 256) {
+        const int kk = e / TM, mm = e % TM;
         const int gm = m0 + mm, gk = k0 + kk;
         T v = 0;
         if (gm < M && gk < K) v = tm.tA ? A[gk + (long long)gm * tm.lda] : A[gm + (long long)gk * tm.lda];
-        As[kk][mm] = alpha * v;
-        const int gn = n0 + mm;
+        As[kk * (TM + 1) + mm] = alpha * v;
+      }
+      for (int e = threadIdx.x; e < GK * TN; e += 256) {
+        const int kk = e / TN, nn = e % TN;
+        const int gn = n0 + nn, gk = k0 + kk;
         T w = 0;
         if (gn < N && gk < K) w = tm.tB ? B[gn + (long long)gk * tm.ldb] : B[gk + (long long)gn * tm.ldb];
-        Bs[kk][mm] = w;
+        Bs[kk * (TN + 1) + nn] = w;
       }
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < GK; ++kk) {
-        const T a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
-        const T b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
+        const T a0 = As[kk * (TM + 1) + ty * 2], a1 = As[kk * (TM + 1) + ty * 2 + 1];
+        const T b0 = Bs[kk * (TN + 1) + tx * 2], b1 = Bs[kk * (TN + 1) + tx * 2 + 1];
         acc00 = fma(a0, b0, acc00); acc01 = fma(a0, b1, acc01);
         acc10 = fma(a1, b0, acc10); acc11 = fma(a1, b1, acc11);
       }
@@ -110,6 +112,25 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks
   if (r0 < M && c0 + 1 < N) C[r0 + (long long)(c0 + 1) * Tk.ldc] = acc01;
   if (r0 + 1 < M && c0 < N) C[r0 + 1 + (long long)c0 * Tk.ldc] = acc10;
   if (r0 + 1 < M && c0 + 1 < N) C[r0 + 1 + (long long)(c0 + 1) * Tk.ldc] = acc11;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm(const GemmTask* __restrict__ tasks, const int* __restrict__ tile2task,
+                                              const BufDescT<T>* __restrict__ bufs, const int* __restrict__ active) {
+  const int z = blockIdx.y;
+  const int p = z >> 1, plane = z & 1;
+  if (active && !active[p]) return;
+  const int tile = blockIdx.x;
+  const GemmTask& Tk = tasks[tile2task[tile]];
+  const int lt = tile - Tk.tile0;
+  __shared__ T smem[GK * (128 + 1) + GK * (8 + 1)];
+  switch (Tk.tm) {
+    case 8: gemm_tile<T, 8>(Tk, lt, bufs, p, plane, smem); break;
+    case 16: gemm_tile<T, 16>(Tk, lt, bufs, p, plane, smem); break;
+    case 64: gemm_tile<T, 64>(Tk, lt, bufs, p, plane, smem); break;
+    case 128: gemm_tile<T, 128>(Tk, lt, bufs, p, plane, smem); break;
+    default: gemm_tile<T, 32>(Tk, lt, bufs, p, plane, smem); break;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1544,57 +1565,63 @@ __global__ void __launch_bounds__(128) k_meanfield(DevBasisT<T> B, int G, const 
 // ---------------------------------------------------------------------------
 struct HTask {
   int ix, iy;      // block row / column
-  int a0, na;      // row tile inside block ix (spin-uniform), na <= 32
-  int b0, nbc;     // column tile inside block iy, nbc <= 32
+  int a0, na;      // row tile inside block ix (spin-uniform), na <= 1024 / tn
+  int b0, nbc;     // column tile inside block iy, nbc <= tn
   int sa;          // spin of the rows (+1/-1)
   int mode;        // 0: mean field (5 components), 1: pairing (1 component)
   int call;        // 0: pn, 1: np
   int outq;        // HSP quadrant 0..3 (m11, m12, m21, m22)
+  int tn, pad_;    // tile shape: (1024 / tn) rows x tn columns, tn = 32, 16 or 8
   long long ooff;  // block offset inside the quadrant
 };
 
 #define HRC 16   // mesh points per K chunk
 
-// FP64 field projection: 32 x 32 output tiles (na, nbc <= 32), 2 x 2 outputs per
-// thread; warps whose rows lie beyond the tile's na skip the FMAs (the DFMA rate is
-// the bound).  grid (ntasks, P); 256 threads; dynamic smem hproj_fp64_smem_bytes()
+// FP64 field projection: output tiles of TM = 1024 / TN rows x TN columns (TN = 32, 16
+// or 8, chosen per block pair from the block sizes so that little of the FP64 pipe goes
+// to padding), 2 x 2 outputs per thread; warps whose rows lie beyond the tile's na skip
+// the FMAs (the DFMA rate is the bound).  grid (ntasks, P); 256 threads; dynamic smem
+// hproj_fp64_smem_bytes()
+__host__ __device__ constexpr size_t hproj_fp64_smem_tn(int tn) {
+  return (size_t)(5 * (1024 / tn) * HRC + 5 * tn * HRC + 25 * 4 * HRC + 5 * tn * 2 * HRC) * sizeof(double);
+}
 __host__ __device__ constexpr size_t hproj_fp64_smem_bytes() {
-  return (size_t)(5 * 32 * HRC * 2 + 25 * 4 * HRC + 5 * 32 * 2 * HRC) * sizeof(double);
+  return hproj_fp64_smem_tn(8) > hproj_fp64_smem_tn(32) ? hproj_fp64_smem_tn(8) : hproj_fp64_smem_tn(32);
 }
 
-__global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __restrict__ tasks,
-                                                    const double* __restrict__ mf, double* __restrict__ hsp,
-                                                    long long nxy, const int* __restrict__ active) {
+template <int TN>
+__device__ __forceinline__ void hproj_fp64_tile(const DevBasis& B, const HTask& Th, const double* __restrict__ mfp,
+                                                double* __restrict__ hsp, long long nxy, int p,
+                                                unsigned char* smraw, signed char* sns) {
   using T = double;
-  const int p = blockIdx.y;
-  if (!active[p]) return;
-  const HTask Th = tasks[blockIdx.x];
+  constexpr int TM = 1024 / TN, TX = TN / 2;
   const int nghl = B.nghl;
   const long long ps = (long long)B.dqp * nghl;
   const int nc = Th.mode == 0 ? 5 : 1;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  T* sA = reinterpret_cast<T*>(smraw);     // [5][32][HRC]
-  T* sPb = sA + 5 * 32 * HRC;               // [5][32][HRC]
-  T* sMF = sPb + 5 * 32 * HRC;              // [25][2 sb][2 re/im][HRC]
-  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][32][2][HRC]
-  __shared__ signed char sns[32];
+  T* sA = reinterpret_cast<T*>(smraw);     // [5][TM][HRC]
+  T* sPb = sA + 5 * TM * HRC;               // [5][TN][HRC]
+  T* sMF = sPb + 5 * TN * HRC;              // [25][2 sb][2 re/im][HRC]
+  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][TN][2][HRC]
   const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
-  if (threadIdx.x < 32) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
-  const T* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * nghl;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  if (threadIdx.x < TN) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  // rows 2 ty, 2 ty + 1; the rows of warp w start at 64 w / TX
+  const bool rows_live = (64 * (int)(threadIdx.x >> 5)) / TX < Th.na;
   T ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
   for (int r0 = 0; r0 < nghl; r0 += HRC) {
     const int nr = min(HRC, nghl - r0);
     __syncthreads();
-    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
-      const int q = e / (32 * HRC), rem = e % (32 * HRC), aa = rem / HRC, rr = rem % HRC;
-      T va = 0, vb = 0;
-      if (rr < nr) {
-        if (aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
-        if (aa < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + aa) * nghl + r0 + rr];
-      }
-      sA[(q * 32 + aa) * HRC + rr] = va;
-      sPb[(q * 32 + aa) * HRC + rr] = vb;
+    for (int e = threadIdx.x; e < nc * TM * HRC; e += 256) {
+      const int q = e / (TM * HRC), rem = e % (TM * HRC), aa = rem / HRC, rr = rem % HRC;
+      T va = 0;
+      if (rr < nr && aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
+      sA[(q * TM + aa) * HRC + rr] = va;
+    }
+    for (int e = threadIdx.x; e < nc * TN * HRC; e += 256) {
+      const int q = e / (TN * HRC), rem = e % (TN * HRC), bb = rem / HRC, rr = rem % HRC;
+      T vb = 0;
+      if (rr < nr && bb < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + bb) * nghl + r0 + rr];
+      sPb[(q * TN + bb) * HRC + rr] = vb;
     }
     if (Th.mode == 0) {
       for (int e = threadIdx.x; e < 25 * 2 * 2 * HRC; e += 256) {
@@ -1613,33 +1640,34 @@ __global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __r
       }
     }
     __syncthreads();
-    // hpsi(iy, b, r) = sum_iz mf(iy, iz, sa, s_b)(r) phi_iz(b, r)
-    for (int e = threadIdx.x; e < nc * 32 * HRC; e += 256) {
-      const int iy = e / (32 * HRC), rem = e % (32 * HRC), bb = rem / HRC, rr = rem % HRC;
-      const int sb = sns[bb] > 0 ? 0 : 1;
+    // hpsi(iy, b, r) = sum_iz mf(iy, iz, sa, s_b)(r) phi_iz(b, r), for the tile's live columns
+    for (int e = threadIdx.x; e < nc * TN * HRC; e += 256) {
+      const int iy = e / (TN * HRC), rem = e % (TN * HRC), bb = rem / HRC, rr = rem % HRC;
       T hr = 0, hi = 0;
-      if (Th.mode == 0) {
+      if (bb < Th.nbc) {
+        const int sb = sns[bb] > 0 ? 0 : 1;
+        if (Th.mode == 0) {
 #pragma unroll
-        for (int iz = 0; iz < 5; ++iz) {
-          const T f = sPb[(iz * 32 + bb) * HRC + rr];
-          const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
-          hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
+          for (int iz = 0; iz < 5; ++iz) {
+            const T f = sPb[(iz * TN + bb) * HRC + rr];
+            const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
+            hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
+          }
+        } else {
+          const T f = sPb[bb * HRC + rr];
+          hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
         }
-      } else {
-        const T f = sPb[bb * HRC + rr];
-        hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
       }
-      sH[((iy * 32 + bb) * 2) * HRC + rr] = hr;
-      sH[((iy * 32 + bb) * 2 + 1) * HRC + rr] = hi;
+      sH[((iy * TN + bb) * 2) * HRC + rr] = hr;
+      sH[((iy * TN + bb) * 2 + 1) * HRC + rr] = hi;
     }
     __syncthreads();
-    // rows 4w..4w+3 of warp w: nothing to do when they are all beyond na
-    if (4 * (threadIdx.x >> 5) < Th.na)
+    if (rows_live)
     for (int q = 0; q < nc; ++q) {
       for (int rr = 0; rr < HRC; ++rr) {
-        const T a0 = sA[(q * 32 + ty * 2) * HRC + rr], a1 = sA[(q * 32 + ty * 2 + 1) * HRC + rr];
-        const T h0r = sH[((q * 32 + tx * 2) * 2) * HRC + rr], h0i = sH[((q * 32 + tx * 2) * 2 + 1) * HRC + rr];
-        const T h1r = sH[((q * 32 + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * 32 + tx * 2 + 1) * 2 + 1) * HRC + rr];
+        const T a0 = sA[(q * TM + ty * 2) * HRC + rr], a1 = sA[(q * TM + ty * 2 + 1) * HRC + rr];
+        const T h0r = sH[((q * TN + tx * 2) * 2) * HRC + rr], h0i = sH[((q * TN + tx * 2) * 2 + 1) * HRC + rr];
+        const T h1r = sH[((q * TN + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * TN + tx * 2 + 1) * 2 + 1) * HRC + rr];
         ar[0][0] = fma(a0, h0r, ar[0][0]); ai[0][0] = fma(a0, h0i, ai[0][0]);
         ar[0][1] = fma(a0, h1r, ar[0][1]); ai[0][1] = fma(a0, h1i, ai[0][1]);
         ar[1][0] = fma(a1, h0r, ar[1][0]); ai[1][0] = fma(a1, h0i, ai[1][0]);
@@ -1661,6 +1689,20 @@ __global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __r
         oim[e] = (T)2 * ai[i][j];
       }
     }
+}
+
+__global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __restrict__ tasks,
+                                                    const double* __restrict__ mf, double* __restrict__ hsp,
+                                                    long long nxy, const int* __restrict__ active) {
+  const int p = blockIdx.y;
+  if (!active[p]) return;
+  const HTask Th = tasks[blockIdx.x];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ signed char sns[32];
+  const double* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * B.nghl;
+  if (Th.tn == 8) hproj_fp64_tile<8>(B, Th, mfp, hsp, nxy, p, smraw, sns);
+  else if (Th.tn == 16) hproj_fp64_tile<16>(B, Th, mfp, hsp, nxy, p, smraw, sns);
+  else hproj_fp64_tile<32>(B, Th, mfp, hsp, nxy, p, smraw, sns);
 }
 
 // ---------------------------------------------------------------------------
@@ -2484,8 +2526,17 @@ __global__ void __launch_bounds__(256) k_to_f32(const double* __restrict__ in, f
     out[p * ld + e] = (float)v;
   }
   if (dmax) {
+    // one atomic per block: warp maxima, then the block's (a non-negative double orders
+    // like its bit pattern)
+    __shared__ double wm[32];
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(dmax + p, (unsigned long long)__double_as_longlong(m));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = fmax(b, wm[w]);
+      atomicMax(dmax + p, (unsigned long long)__double_as_longlong(b));
+    }
   }
 }
 __global__ void k_to_f64(const float* __restrict__ in, double* __restrict__ out, long long n, long long ld,

@@ -102,7 +102,7 @@ class GPUSolver:
 
     @staticmethod
     def options(max_iter=300, eps=1e-7, broyden_m=50, quench=1.0, alpha_mix=None, timed=False, precision=0,
-                switch_exp=0, live=False, settle=0, near_exp=0):
+                switch_exp=0, live=False, settle=0, near_exp=0, async_anchors=False):
         if alpha_mix is None:
             from .pnfam_setup import ALPHA_MIX as alpha_mix
         o = _lib.SolverOpts()
@@ -114,6 +114,7 @@ class GPUSolver:
         o.reserved[2] = 1 if live else 0
         o.reserved[3] = int(settle)
         o.reserved[4] = int(near_exp)
+        o.reserved[5] = 1 if async_anchors else 0
         return o
 
     def engine(self, slots, owns_solver=False, **opts) -> "Engine":
@@ -171,12 +172,13 @@ class GPUSolver:
     def last_profile(self):
         """Per-stage device ms of the last solve (or of this context's engine so far);
         the *_fp32 entries are the FP32 evaluations of the mixed form."""
-        ms = np.zeros(20); n = C.c_longlong()
-        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 20, C.byref(n)))
+        ms = np.zeros(23); n = C.c_longlong()
+        _lib.check(self.lib.pnfam_gpu_last_profile(self.ctx, _lib.dptr(ms), 23, C.byref(n)))
         names = ("k1_blockgemm", "density", "meanfield", "field_projection", "k2_blockgemm", "green", "broyden",
                  "strength", "total", "point_iterations_fp64", "point_iterations_fp32", "k1_blockgemm_fp32",
                  "density_fp32", "meanfield_fp32", "field_projection_fp32", "k2_blockgemm_fp32",
-                 "live_density_launches", "live_density_ms", "live_projection_launches", "live_projection_ms")
+                 "live_density_launches", "live_density_ms", "live_projection_launches", "live_projection_ms",
+                 "tuned_pair_min_points", "tuned_density_kspan", "autotune_ms")
         return dict(zip(names, ms.tolist())), int(n.value)
 
     def calc_hamiltonian(self, rho_pn, kp, rho_np, km, mixed=False):

@@ -112,6 +112,45 @@ def test_served_mix_matches_each_point_alone(precision):
           f"p99 {st.percentile(99) * 1e3:.1f} ms")
 
 
+def test_asynchronous_anchors_give_each_point_its_result():
+    """Mixed form with asynchronous anchors (opts.reserved[5]): points whose FP64 anchor
+    runs beside other points' FP32 increments are parked until it completes, while the
+    engine keeps stepping the others.  Every point converges to the result of the
+    synchronous batch solve within 1e-6 per Re/Im value of the strength and each cross
+    term (both within 1e-9 of the same fixed point)."""
+    from pynfam_gb300.solver import GPUSolver
+    c, _ = case_for("S40", "RS1-K1", 0)
+    w = _omegas("S40", "RS1-K1")
+    gpu = GPUSolver(c.hfb, c.couplings)
+    gpu.set_operator(c.F, c.G)
+    kw = _kw(c)
+    kw.update(eps=1e-9, precision=1, settle=8, max_iter=300)
+    ref = gpu.solve(w, **kw)
+    eng = gpu.engine(9, async_anchors=True, **kw)
+    todo = list(range(len(w)))
+    got = {}
+    while todo or eng.active:
+        free = eng.slots - eng.active
+        if todo and free:
+            take, todo = todo[:free], todo[free:]
+            assert eng.admit(w[take], take) == len(take)
+        eng.launch()
+        for r in eng.finish():
+            got[r.tag] = r
+    prof, _ = gpu.last_profile()
+    eng.close()
+    gpu.close()
+    assert sorted(got) == list(range(len(w)))
+    scale = np.max(np.abs(ref.re_S[:, 0] + 1j * ref.im_S[:, 0]))
+    for i in range(len(w)):
+        assert got[i].iters >= 0 and ref.iters[i] >= 0, i
+        want = ref.re_S[i] + 1j * ref.im_S[i]
+        for g_, w_ in zip(got[i].S, want):
+            for a, b in ((g_.real, w_.real), (g_.imag, w_.imag)):
+                assert abs(a - b) <= REL * abs(b) + 1e-12 * scale, (i, a, b)
+    assert prof["point_iterations_fp64"] > 0 and prof["point_iterations_fp32"] > 0
+
+
 def test_engine_misuse_is_refused():
     from pynfam_gb300 import _lib
     from pynfam_gb300.solver import GPUSolver
@@ -134,3 +173,27 @@ def test_engine_misuse_is_refused():
         eng.launch()
     assert ei.value.code == 5
     eng.close()
+
+
+def test_autotuner_choices_are_reported_and_cached():
+    """The first mixed-form engine of an operator tunes the pair-tensor GEMMs (the density
+    task span, the point count from which the pair-tensor path is taken) from timed trial
+    evaluations; a second context of the same operator takes the same choices from the
+    process's cache without trials."""
+    from pynfam_gb300.solver import GPUSolver
+    c, _ = case_for("Gd162", "GT-K1", 0)
+    kw = _kw(c)
+    kw.update(precision=1, eps=1e-9)
+    choices = []
+    for _ in range(2):
+        gpu = GPUSolver(c.hfb, c.couplings)
+        gpu.set_operator(c.F, c.G)
+        eng = gpu.engine(16, **kw)
+        prof, _ = gpu.last_profile()
+        choices.append((int(prof["tuned_density_kspan"]), int(prof["tuned_pair_min_points"]), prof["autotune_ms"]))
+        eng.close()
+        gpu.close()
+    (k0, m0, t0), (k1, m1, t1) = choices
+    assert k0 in (96, 192, 384, 768) and (m0 in (1, 2, 4, 8, 16) or m0 == 1 << 30)
+    assert t0 > 0.0 and (k1, m1) == (k0, m0) and t1 == 0.0
+    print(f"Gd162 GT-K1: density task span {k0} K chunks, pair-tensor path from {m0} points, tuning {t0:.0f} ms")

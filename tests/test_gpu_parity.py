@@ -467,12 +467,44 @@ def test_statistical_fam_zero_occupations_is_ground_state_form(solvers):
     assert np.array_equal(r0.iters, r1.iters)
     np.testing.assert_allclose(r1.re_S, r0.re_S, rtol=1e-11, atol=1e-15)
     np.testing.assert_allclose(r1.im_S, r0.im_S, rtol=1e-11, atol=1e-15)
-    # the statistical form is FP64 only; clearing the occupations needs the operator again
-    with pytest.raises(_lib.PnfamGPUError) as e:
-        _solve(gpu, c, omegas[:1], precision=1)
-    assert e.value.code == 1
+    # clearing the occupations needs the operator again
     gpu.set_occupations(None, None)
     with pytest.raises(_lib.PnfamGPUError) as e:
         gpu.solve(omegas[:1])
     assert e.value.code == 5
     gpu.close()
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_statistical_mixed_form_matches_fp64_fixed_point(idx):
+    """The statistical FAM in the mixed form (P and Q quadrants in the FP32 increment
+    evaluations, the 8-part state in pair-arithmetic Broyden, FP64 anchors): every
+    converged point of a contour within 1e-6 of the FP64 statistical fixed point
+    (converged to 1e-12), per Re/Im value of the strength and each cross term."""
+    from pynfam_gb300.solver import GPUSolver
+    name, c, occ = _stat_cases()[idx]
+    case, op = name.split()[:2]
+    pts = golden(case)["operators"][op][:12]
+    omegas = [complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"]) for p in pts]
+    s = c.nml["solver"]
+    gpu = GPUSolver(c.hfb, c.couplings, occupations=occ)
+    gpu.set_operator(c.F, c.G)
+    kw = dict(max_iter=300, broyden_m=s["broyden_history_size"], quench=c.quench)
+    ref = gpu.solve(omegas, eps=TIGHT, **kw)
+    mix = gpu.solve(omegas, eps=MIXED_EPS, precision=1, settle=SETTLE, **kw)
+    gpu.close()
+    worst, n = 0.0, 0
+    for i in range(len(omegas)):
+        assert ref.iters[i] > 0, (name, i)
+        if mix.iters[i] < 0:
+            continue
+        n += 1
+        for k in range(ref.re_S.shape[1]):
+            for got, want in ((mix.re_S[i, k], ref.re_S[i, k]), (mix.im_S[i, k], ref.im_S[i, k])):
+                err = abs(got - want)
+                assert err <= REL * abs(want) + 1e-12 * np.max(np.abs(ref.re_S[:, 0])), (name, i, k, got, want)
+                if abs(want) > 1e-9:
+                    worst = max(worst, err / abs(want))
+    assert n >= len(omegas) - 1, (name, n)
+    print(f"{name}: statistical mixed form, {n} of {len(omegas)} points converged, worst rel err vs FP64 "
+          f"fixed point {worst:.2e}")
