@@ -579,12 +579,21 @@ def run_gpu(args):
                                           f"settings)"}
     if rank == 0 and world == 1 and not args.no_config4:
         line["config4"] = run_config4(args, emit=False)
+    if rank == 0 and world == 1 and not args.no_stream:
+        sl = run_serve_stream(args, emit=False)
+        line["serving_stream"] = {
+            "config": f"{args.nuclei} nuclei drawn from the recorded 40S, 116Kr, 162Gd ground states re-diagonalised "
+                      f"in N_sh from {{{args.nsh}}}; GT- K=0,1 requests of 40-200 CIRCLE points x {args.stream_scale}; "
+                      f"Poisson arrivals; {args.budget_gb:g} GB budget; {args.stream_slots} slots per engine",
+            "nuclei": sl[0]["nuclei"] if sl else [], "form": sl[0]["form"] if sl else None,
+            "rates": [{k: x[k] for k in ("rate_req_per_s", "requests", "points", "converged", "wall_s",
+                                         "converged_per_s", "latency_ms", "peak_engines", "peak_gb")} for x in sl]}
     if rank == 0:
         print(json.dumps(line, default=_plain), flush=True)
     replicas.finish()
 
 
-def run_serve_stream(args):
+def run_serve_stream(args, emit=True):
     """Serving stream (the serving configuration of many nuclei and bases, scaled by --stream-scale):
     nuclei drawn (seeded) from the three recorded ground states (40S, 116Kr, 162Gd)
     re-diagonalised in a basis of N_sh drawn from --nsh, each requesting GT- K = 0
@@ -636,23 +645,45 @@ def run_serve_stream(args):
 
     keys = list(cases)
     npts = {key: max(4, int(round(rng.integers(40, 201) * args.stream_scale))) for key in keys}
+    lines = []
+    # with several ranks (one GPU each) whole nuclei go to ranks by estimated work
+    from pynfam_gb300 import replicas
+    world, rank, local = replicas.env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        replicas.init("nccl")
     for rate in [float(x) for x in args.rates.split(",")]:
         arr = poisson_arrivals(len(keys), rate, seed=args.stream_seed)
         order = rng.permutation(len(keys))
         reqs = [Request(i, keys[j], circle(-15.0, 35.0, 2 * npts[keys[j]]), float(arr[i]))
                 for i, j in enumerate(order)]
+        if world > 1:
+            reqs = replicas.partition(reqs, world, cost=lambda r: len(r.omegas) * cases[r.key].F.mat.nelem)[rank]
         torch.cuda.synchronize()
+        replicas.barrier("cuda")
         server = Server(factory, engine_bytes, slots=slots, budget_bytes=int(args.budget_gb * 1e9))
         out, st = server.run(reqs)
         torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([float(st.points), float(st.converged)], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t)
+            st.points, st.converged = int(t[0].item()), int(t[1].item())
+            st.wall = replicas.max_over_ranks(st.wall, "cuda")
+        if rank != 0:
+            continue
         line = {"serve_stream": True, "rate_req_per_s": rate, "requests": len(reqs),
                 "nuclei": [f"{n} N_sh={s_}" for n, s_ in nuclei], "points": st.points, "converged": st.converged,
                 "wall_s": st.wall, "points_per_s": st.points / st.wall, "converged_per_s": st.converged / st.wall,
                 "latency_ms": {"p50": st.percentile(50) * 1e3, "p99": st.percentile(99) * 1e3},
                 "peak_engines": st.peak_engines, "peak_gb": st.peak_bytes / 1e9, "slots_per_engine": slots,
                 "setup_s": setup_s, "form": f"mixed, epsilon {MIXED_EPS}, settled to 1e-{SETTLE}",
-                "data": "recorded ground states re-diagonalised in larger bases"}
-        print(json.dumps(line, default=_plain), flush=True)
+                "data": "recorded ground states re-diagonalised in larger bases", "ranks": world,
+                "latency_note": "p50/p99 over rank 0's points" if world > 1 else "all points"}
+        lines.append(line)
+        if emit:
+            print(json.dumps(line, default=_plain), flush=True)
+    return lines
 
 
 def config4_cases(nsh=20, seed=3):
@@ -816,7 +847,7 @@ def main():
     ap.add_argument("--serve-stream", action="store_true",
                     help="serving stream of several nuclei and bases with Poisson arrivals (one JSON line per rate)")
     ap.add_argument("--nuclei", type=int, default=6, help="serve-stream: nuclei drawn (with repeats)")
-    ap.add_argument("--nsh", default="8,12,16", help="serve-stream: N_sh values to draw from")
+    ap.add_argument("--nsh", default="8,12,16,20", help="serve-stream: N_sh values to draw from")
     ap.add_argument("--rates", default="5,50,200", help="serve-stream: request arrival rates (1/s)")
     ap.add_argument("--stream-scale", type=float, default=0.25, help="serve-stream: points per request x scale")
     ap.add_argument("--stream-slots", type=int, default=32, help="serve-stream: slots per engine")
@@ -833,6 +864,7 @@ def main():
     ap.add_argument("--c4-slots", type=int, default=16, help="config 4: slots per engine")
     ap.add_argument("--c4-fp64-points", type=int, default=32, help="config 4: points per operator, FP64 form")
     ap.add_argument("--no-config4", action="store_true", help="leave the config 4 object out of the line")
+    ap.add_argument("--no-stream", action="store_true", help="leave the serving-stream object out of the line")
     ap.add_argument("--async-anchors", action="store_true",
                     help="mixed form: FP64 anchors beside FP32 increments run asynchronously")
     ap.add_argument("--solve-only", action="store_true",

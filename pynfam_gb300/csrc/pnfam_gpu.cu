@@ -133,10 +133,11 @@ struct TaskList {
 struct TaskListTC {
   std::vector<GemmTaskTC> tasks;
   DBuf<GemmTaskTC> d_tasks;
-  int maxrows = 0;
+  int maxrows = 0, maxnp = 16;
   void build(const TaskList& tl) {
     tasks.clear();
     maxrows = 0;
+    maxnp = 16;
     for (const GemmTask& g : tl.tasks) {
       GemmTaskTC t;
       memset(&t, 0, sizeof(t));
@@ -148,6 +149,7 @@ struct TaskListTC {
       t.npad = std::max(16, (t.ncols + 15) / 16 * 16);
       t.coff = g.coff; t.cbuf = g.cbuf; t.ldc = g.ldc;
       maxrows = std::max(maxrows, t.mrows);
+      maxnp = std::max(maxnp, t.npad);
       tasks.push_back(t);
     }
   }
@@ -281,6 +283,10 @@ struct pnfam_ctx {
   // chunks per density task (pg_kspan) and, unless PNFAM_GB300_PAIR_MIN fixes it,
   // pg_min, the point count from which the pair-tensor path is the faster one
   int pg_kspan = 384;
+  int pg_kspan_env = 0;   // PNFAM_GB300_PAIR_KSPAN: a fixed span (no span trials)
+  // shared memory of a pair-GEMM CTA (its ring of stages): 128 KB leaves an SM room for a
+  // CTA of the FP64 anchor kernels; PNFAM_GB300_PAIR_SMEM_KB (<= 224) changes it
+  int pg_smem = 128 * 1024;
   bool pg_tuned = false, pg_min_env = false, autotune = true;
   double tune_ms = 0.0;
   std::vector<PGProb> pg_probs;
@@ -702,15 +708,16 @@ static void live_collect(pnfam_ctx* c) {
 // ---------------------------------------------------------------------------
 // pair-tensor GEMMs (pair_gemm.cuh): problems, element lists, tasks
 // ---------------------------------------------------------------------------
-// dynamic shared memory of k_pg_gemm: 128 KB, so that one of its CTAs leaves room on
-// the SM (100 KB) for a CTA of the FP64 anchor kernels or the block GEMMs of other
-// points or engines, whose FP64 and FP32 pipes it does not use
-static constexpr int PG_SMEM = 128 * 1024;
+// dynamic shared memory of k_pg_gemm: by default 128 KB (pnfam_ctx::pg_smem), so that
+// one of its CTAs leaves room on the SM (100 KB) for a CTA of the FP64 anchor kernels or
+// the block GEMMs of other points or engines, whose FP64 and FP32 pipes it does not use;
+// at most PG_SMEM_MAX
+static constexpr int PG_SMEM_MAX = 224 * 1024;
 
 // stages of k_pg_gemm for B slots of bslot floats
-static int pg_stages(int bslot) {
+static int pg_stages(int bslot, int smem) {
   const int per = (int)((PG_ACHUNK + bslot) * sizeof(float));
-  return std::max(2, std::min((int)PG_MAXSTAGE, PG_SMEM / per));
+  return std::max(2, std::min((int)PG_MAXSTAGE, smem / per));
 }
 
 // K chunks per density task the autotuner tries (the finest first)
@@ -804,7 +811,7 @@ static void pg_setup(pnfam_ctx* c) {
   c->pg_nachunk = a0;
   c->pg_nbchunk = b0;
   c->pg_tuned = false;
-  c->pg_kspan = 384;
+  c->pg_kspan = c->pg_kspan_env > 0 ? c->pg_kspan_env : 384;
   pg_density_tasks(c, c->pg_kspan);
   // the largest tasks first: the long projection tiles
   std::stable_sort(c->pg_tproj.begin(), c->pg_tproj.end(),
@@ -862,7 +869,7 @@ static int pg_density(pnfam_ctx* c, int nact, const float* rsp, float* dpart, cu
     const int na = std::min((int)PG_MAXPTS, nact - g0);
     const int* al = c->d_actlist.p + g0;
     const int bslot = ((4 * na + 15) / 16 * 16) * PG_K * 2;
-    const int ns = pg_stages(bslot);
+    const int ns = pg_stages(bslot, c->pg_smem);
     k_pg_pack_rho<<<(unsigned)c->pg_bdens.size(), 256, 0, st>>>(c->d_pg_probs.p, c->d_pg_elems.p, c->d_pg_bdens.p,
                                                                  al, na, rsp, c->nxy, c->d_pg_b.p);
     const int lv = live_begin(c, st);
@@ -884,7 +891,7 @@ static int pg_projection(pnfam_ctx* c, int nact, const float* mf, float* hsp, cu
     const int na = std::min((int)PG_MAXPTS, nact - g0);
     const int* al = c->d_actlist.p + g0;
     const int bslot = ((4 * na + 15) / 16 * 16) * PG_K * 2;
-    const int ns = pg_stages(bslot);
+    const int ns = pg_stages(bslot, c->pg_smem);
     k_pg_pack_field<<<(unsigned)c->pg_bproj.size(), 256, 0, st>>>(c->d_pg_probs.p, c->d_pg_bproj.p, al, na, mf,
                                                                    c->nghl, c->d_pg_b.p);
     const int lv = live_begin(c, st);
@@ -961,8 +968,8 @@ static int launch_gemm(pnfam_ctx* c, TaskList& tl, int P, const int* active, con
 static int launch_gemm_tc(pnfam_ctx* c, TaskListTC& tl, int nact, cudaStream_t st) {
   if (tl.tasks.empty() || nact <= 0) return PNFAM_OK;
   dim3 grid((unsigned)tl.tasks.size(), (unsigned)((2 * nact * tl.maxrows + 127) / 128));
-  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(), st>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_gsplit.p,
-                                                               c->d_actlist.p, nact, c->d_err.p);
+  k_gemm_tc<<<grid, GTC_THREADS, gemm_tc_smem_bytes(tl.maxnp), st>>>(tl.d_tasks.p, c->d_bufs32.p, c->d_gsplit.p,
+                                                                      c->d_actlist.p, nact, tl.maxnp, c->d_err.p);
   c->launches++;
   CK(cudaGetLastError());
   return PNFAM_OK;
@@ -1132,6 +1139,7 @@ static unsigned long long pg_tune_key(const pnfam_ctx* c, int nmax) {
     for (int b = 0; b < 8; ++b) { h ^= (unsigned long long)((v >> (8 * b)) & 0xff); h *= 1099511628211ULL; }
   };
   mix(c->nghl); mix(c->nq); mix(nmax); mix(c->nsm); mix(c->dev); mix(c->pg_min_env ? c->pg_min : -1);
+  mix(c->pg_kspan_env); mix(c->pg_smem);
   for (const PGProb& pr : c->pg_probs) { mix(pr.kind); mix(pr.ntile); mix(pr.nkc); mix(pr.ncol); }
   return h;
 }
@@ -1183,8 +1191,8 @@ static int pg_autotune(pnfam_ctx* c, int P) {
     return PNFAM_OK;
   };
   int rc;
-  // 1. density task span
-  {
+  // 1. density task span (unless PNFAM_GB300_PAIR_KSPAN fixes it)
+  if (c->pg_kspan_env <= 0) {
     std::vector<int> cand;
     for (int span : PG_KSPANS) {
       long long tasks = 0;
@@ -1380,6 +1388,10 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
     if (v && std::atoi(v) > 0) { c->pg_min = std::atoi(v); c->pg_min_env = true; }
     v = std::getenv("PNFAM_GB300_AUTOTUNE");
     c->autotune = !(v && v[0] == '0');
+    v = std::getenv("PNFAM_GB300_PAIR_KSPAN");
+    if (v && std::atoi(v) > 0) c->pg_kspan_env = std::atoi(v);
+    v = std::getenv("PNFAM_GB300_PAIR_SMEM_KB");
+    if (v && std::atoi(v) >= 64) c->pg_smem = std::min(std::atoi(v), PG_SMEM_MAX / 1024) * 1024;
   }
   const int s = c->dqp;
   const long long mo = c->uoff.back() + (long long)c->db.back() * c->db.back();
@@ -1428,7 +1440,7 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
                            (int)density_tc2_smem_bytes()) != cudaSuccess ||
       cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)gemm_tc_smem_bytes()) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pg_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, PG_SMEM) != cudaSuccess) {
+      cudaFuncSetAttribute(k_pg_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, PG_SMEM_MAX) != cudaSuccess) {
     delete c;
     return fail(PNFAM_ECUDA, "pnfam_gpu_init: cannot configure shared memory");
   }

@@ -154,8 +154,10 @@ struct GemmTaskTC {
 };
 enum { GTC_K = 16, GTC_PROD = 256, GTC_THREADS = GTC_PROD + 32 };
 
-__host__ __device__ constexpr size_t gemm_tc_smem_bytes() {
-  return (size_t)2 * (2 * 128 * GTC_K + 2 * 256 * GTC_K) * sizeof(float);
+// two stages sized for the widest padded block (npmax <= 256) of the launch's tasks:
+// narrower task lists leave room for more CTAs per SM, so more loads are in flight
+__host__ __device__ constexpr size_t gemm_tc_smem_bytes(int npmax = 256) {
+  return (size_t)2 * (2 * 128 * GTC_K + 2 * npmax * GTC_K) * sizeof(float);
 }
 
 // the B tile of chunk c of a task: B[n][k] = op(S)[k0 + k][n] (case 0) or
@@ -200,19 +202,20 @@ __global__ void __launch_bounds__(256) k_gemm_bsplit(const GemmTaskTC* __restric
   }
 }
 
-// grid (ntasks, row tiles of 128); HTC_THREADS threads; dynamic smem gemm_tc_smem_bytes()
+// grid (ntasks, row tiles of 128); GTC_THREADS threads; dynamic smem gemm_tc_smem_bytes(npmax),
+// npmax >= every task's npad
 __global__ void __launch_bounds__(GTC_THREADS, 2) k_gemm_tc(const GemmTaskTC* __restrict__ tasks,
                                                             const BufDescT<float>* __restrict__ bufs,
                                                             const float* __restrict__ gsplit,
                                                             const int* __restrict__ actlist, int nact,
-                                                            int* __restrict__ err) {
+                                                            int npmax, int* __restrict__ err) {
   const GemmTaskTC& Tk = tasks[blockIdx.x];
   const int rows_total = 2 * nact * Tk.mrows;
   const int R0 = blockIdx.y * 128;
   if (R0 >= rows_total) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   float* stage_base = reinterpret_cast<float*>(smraw);
-  const int stage_floats = 2 * 128 * GTC_K + 2 * 256 * GTC_K;
+  const int stage_floats = 2 * 128 * GTC_K + 2 * npmax * GTC_K;
   __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -1582,14 +1585,18 @@ struct HTask {
 // to padding), 2 x 2 outputs per thread; warps whose rows lie beyond the tile's na skip
 // the FMAs (the DFMA rate is the bound).  grid (ntasks, P); 256 threads; dynamic smem
 // hproj_fp64_smem_bytes()
+// mesh points per K chunk of a shape: 16, or 8 for the 128-row tiles, so that every
+// shape stays within the 94.7 KB of the 32 x 32 tiles and a CTA of the FP32 kernels
+// (pair-tensor GEMM: 128 KB) still fits beside one on an SM
+__host__ __device__ constexpr int hproj_fp64_hr(int tn) { return tn == 8 ? 8 : HRC; }
 __host__ __device__ constexpr size_t hproj_fp64_smem_tn(int tn) {
-  return (size_t)(5 * (1024 / tn) * HRC + 5 * tn * HRC + 25 * 4 * HRC + 5 * tn * 2 * HRC) * sizeof(double);
+  return (size_t)(5 * (1024 / tn) + 5 * tn + 25 * 4 + 5 * tn * 2) * hproj_fp64_hr(tn) * sizeof(double);
 }
 __host__ __device__ constexpr size_t hproj_fp64_smem_bytes() {
   return hproj_fp64_smem_tn(8) > hproj_fp64_smem_tn(32) ? hproj_fp64_smem_tn(8) : hproj_fp64_smem_tn(32);
 }
 
-template <int TN>
+template <int TN, int HR>
 __device__ __forceinline__ void hproj_fp64_tile(const DevBasis& B, const HTask& Th, const double* __restrict__ mfp,
                                                 double* __restrict__ hsp, long long nxy, int p,
                                                 unsigned char* smraw, signed char* sns) {
@@ -1598,76 +1605,76 @@ __device__ __forceinline__ void hproj_fp64_tile(const DevBasis& B, const HTask& 
   const int nghl = B.nghl;
   const long long ps = (long long)B.dqp * nghl;
   const int nc = Th.mode == 0 ? 5 : 1;
-  T* sA = reinterpret_cast<T*>(smraw);     // [5][TM][HRC]
-  T* sPb = sA + 5 * TM * HRC;               // [5][TN][HRC]
-  T* sMF = sPb + 5 * TN * HRC;              // [25][2 sb][2 re/im][HRC]
-  T* sH = sMF + 25 * 2 * 2 * HRC;           // [5][TN][2][HRC]
+  T* sA = reinterpret_cast<T*>(smraw);     // [5][TM][HR]
+  T* sPb = sA + 5 * TM * HR;               // [5][TN][HR]
+  T* sMF = sPb + 5 * TN * HR;              // [25][2 sb][2 re/im][HR]
+  T* sH = sMF + 25 * 2 * 2 * HR;           // [5][TN][2][HR]
   const int ja0 = B.st[Th.ix] + Th.a0, jb0 = B.st[Th.iy] + Th.b0;
   if (threadIdx.x < TN) sns[threadIdx.x] = threadIdx.x < Th.nbc ? B.ns[jb0 + threadIdx.x] : (signed char)1;
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   // rows 2 ty, 2 ty + 1; the rows of warp w start at 64 w / TX
   const bool rows_live = (64 * (int)(threadIdx.x >> 5)) / TX < Th.na;
   T ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
-  for (int r0 = 0; r0 < nghl; r0 += HRC) {
-    const int nr = min(HRC, nghl - r0);
+  for (int r0 = 0; r0 < nghl; r0 += HR) {
+    const int nr = min(HR, nghl - r0);
     __syncthreads();
-    for (int e = threadIdx.x; e < nc * TM * HRC; e += 256) {
-      const int q = e / (TM * HRC), rem = e % (TM * HRC), aa = rem / HRC, rr = rem % HRC;
+    for (int e = threadIdx.x; e < nc * TM * HR; e += 256) {
+      const int q = e / (TM * HR), rem = e % (TM * HR), aa = rem / HR, rr = rem % HR;
       T va = 0;
       if (rr < nr && aa < Th.na) va = B.phi[q * ps + (long long)(ja0 + aa) * nghl + r0 + rr];
-      sA[(q * TM + aa) * HRC + rr] = va;
+      sA[(q * TM + aa) * HR + rr] = va;
     }
-    for (int e = threadIdx.x; e < nc * TN * HRC; e += 256) {
-      const int q = e / (TN * HRC), rem = e % (TN * HRC), bb = rem / HRC, rr = rem % HRC;
+    for (int e = threadIdx.x; e < nc * TN * HR; e += 256) {
+      const int q = e / (TN * HR), rem = e % (TN * HR), bb = rem / HR, rr = rem % HR;
       T vb = 0;
       if (rr < nr && bb < Th.nbc) vb = B.phi[q * ps + (long long)(jb0 + bb) * nghl + r0 + rr];
-      sPb[(q * TN + bb) * HRC + rr] = vb;
+      sPb[(q * TN + bb) * HR + rr] = vb;
     }
     if (Th.mode == 0) {
-      for (int e = threadIdx.x; e < 25 * 2 * 2 * HRC; e += 256) {
-        const int pair = e / (4 * HRC), rem = e % (4 * HRC), sb = rem / (2 * HRC), rem2 = rem % (2 * HRC);
-        const int ri = rem2 / HRC, rr = rem2 % HRC;
+      for (int e = threadIdx.x; e < 25 * 2 * 2 * HR; e += 256) {
+        const int pair = e / (4 * HR), rem = e % (4 * HR), sb = rem / (2 * HR), rem2 = rem % (2 * HR);
+        const int ri = rem2 / HR, rr = rem2 % HR;
         const int iy = pair / 5, iz = pair % 5;
         T v = 0;
         if (rr < nr) v = mfp[((long long)mfslot(iy, iz, Th.sa, sb == 0 ? 1 : -1) * 2 + ri) * nghl + r0 + rr];
         sMF[e] = v;
       }
     } else {
-      for (int e = threadIdx.x; e < 2 * 2 * HRC; e += 256) {
-        const int sb = e / (2 * HRC), rem = e % (2 * HRC), ri = rem / HRC, rr = rem % HRC;
+      for (int e = threadIdx.x; e < 2 * 2 * HR; e += 256) {
+        const int sb = e / (2 * HR), rem = e % (2 * HR), ri = rem / HR, rr = rem % HR;
         const int slot = 100 + (Th.sa < 0 ? 2 : 0) + sb;
         sMF[e] = rr < nr ? mfp[((long long)slot * 2 + ri) * nghl + r0 + rr] : (T)0;
       }
     }
     __syncthreads();
     // hpsi(iy, b, r) = sum_iz mf(iy, iz, sa, s_b)(r) phi_iz(b, r), for the tile's live columns
-    for (int e = threadIdx.x; e < nc * TN * HRC; e += 256) {
-      const int iy = e / (TN * HRC), rem = e % (TN * HRC), bb = rem / HRC, rr = rem % HRC;
+    for (int e = threadIdx.x; e < nc * TN * HR; e += 256) {
+      const int iy = e / (TN * HR), rem = e % (TN * HR), bb = rem / HR, rr = rem % HR;
       T hr = 0, hi = 0;
       if (bb < Th.nbc) {
         const int sb = sns[bb] > 0 ? 0 : 1;
         if (Th.mode == 0) {
 #pragma unroll
           for (int iz = 0; iz < 5; ++iz) {
-            const T f = sPb[(iz * TN + bb) * HRC + rr];
-            const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HRC];
-            hr = fma(m[rr], f, hr); hi = fma(m[HRC + rr], f, hi);
+            const T f = sPb[(iz * TN + bb) * HR + rr];
+            const T* m = &sMF[((iy * 5 + iz) * 4 + sb * 2) * HR];
+            hr = fma(m[rr], f, hr); hi = fma(m[HR + rr], f, hi);
           }
         } else {
-          const T f = sPb[bb * HRC + rr];
-          hr = sMF[(sb * 2) * HRC + rr] * f; hi = sMF[(sb * 2 + 1) * HRC + rr] * f;
+          const T f = sPb[bb * HR + rr];
+          hr = sMF[(sb * 2) * HR + rr] * f; hi = sMF[(sb * 2 + 1) * HR + rr] * f;
         }
       }
-      sH[((iy * TN + bb) * 2) * HRC + rr] = hr;
-      sH[((iy * TN + bb) * 2 + 1) * HRC + rr] = hi;
+      sH[((iy * TN + bb) * 2) * HR + rr] = hr;
+      sH[((iy * TN + bb) * 2 + 1) * HR + rr] = hi;
     }
     __syncthreads();
     if (rows_live)
     for (int q = 0; q < nc; ++q) {
-      for (int rr = 0; rr < HRC; ++rr) {
-        const T a0 = sA[(q * TM + ty * 2) * HRC + rr], a1 = sA[(q * TM + ty * 2 + 1) * HRC + rr];
-        const T h0r = sH[((q * TN + tx * 2) * 2) * HRC + rr], h0i = sH[((q * TN + tx * 2) * 2 + 1) * HRC + rr];
-        const T h1r = sH[((q * TN + tx * 2 + 1) * 2) * HRC + rr], h1i = sH[((q * TN + tx * 2 + 1) * 2 + 1) * HRC + rr];
+      for (int rr = 0; rr < HR; ++rr) {
+        const T a0 = sA[(q * TM + ty * 2) * HR + rr], a1 = sA[(q * TM + ty * 2 + 1) * HR + rr];
+        const T h0r = sH[((q * TN + tx * 2) * 2) * HR + rr], h0i = sH[((q * TN + tx * 2) * 2 + 1) * HR + rr];
+        const T h1r = sH[((q * TN + tx * 2 + 1) * 2) * HR + rr], h1i = sH[((q * TN + tx * 2 + 1) * 2 + 1) * HR + rr];
         ar[0][0] = fma(a0, h0r, ar[0][0]); ai[0][0] = fma(a0, h0i, ai[0][0]);
         ar[0][1] = fma(a0, h1r, ar[0][1]); ai[0][1] = fma(a0, h1i, ai[0][1]);
         ar[1][0] = fma(a1, h0r, ar[1][0]); ai[1][0] = fma(a1, h0i, ai[1][0]);
@@ -1700,9 +1707,9 @@ __global__ void __launch_bounds__(256) k_hproj_fp64(DevBasis B, const HTask* __r
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ signed char sns[32];
   const double* mfp = mf + ((long long)p * 2 + Th.call) * NMF * 2 * B.nghl;
-  if (Th.tn == 8) hproj_fp64_tile<8>(B, Th, mfp, hsp, nxy, p, smraw, sns);
-  else if (Th.tn == 16) hproj_fp64_tile<16>(B, Th, mfp, hsp, nxy, p, smraw, sns);
-  else hproj_fp64_tile<32>(B, Th, mfp, hsp, nxy, p, smraw, sns);
+  if (Th.tn == 8) hproj_fp64_tile<8, hproj_fp64_hr(8)>(B, Th, mfp, hsp, nxy, p, smraw, sns);
+  else if (Th.tn == 16) hproj_fp64_tile<16, hproj_fp64_hr(16)>(B, Th, mfp, hsp, nxy, p, smraw, sns);
+  else hproj_fp64_tile<32, hproj_fp64_hr(32)>(B, Th, mfp, hsp, nxy, p, smraw, sns);
 }
 
 // ---------------------------------------------------------------------------
