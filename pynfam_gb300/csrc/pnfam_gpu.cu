@@ -284,9 +284,11 @@ struct pnfam_ctx {
   // pg_min, the point count from which the pair-tensor path is the faster one
   int pg_kspan = 384;
   int pg_kspan_env = 0;   // PNFAM_GB300_PAIR_KSPAN: a fixed span (no span trials)
-  // shared memory of a pair-GEMM CTA (its ring of stages): 128 KB leaves an SM room for a
-  // CTA of the FP64 anchor kernels; PNFAM_GB300_PAIR_SMEM_KB (<= 224) changes it
-  int pg_smem = 128 * 1024;
+  // shared memory of a pair-GEMM CTA (its ring of stages): 104 KB puts two CTAs on an SM,
+  // so that one streams the pair tensor while the other starts or drains a task (measured:
+  // 73.4 points/s on the benchmark against 72.6 with one 128 KB CTA and 69.5 with 208 KB);
+  // PNFAM_GB300_PAIR_SMEM_KB (<= 224) changes it
+  int pg_smem = 104 * 1024;
   bool pg_tuned = false, pg_min_env = false, autotune = true;
   double tune_ms = 0.0;
   std::vector<PGProb> pg_probs;
@@ -708,9 +710,8 @@ static void live_collect(pnfam_ctx* c) {
 // ---------------------------------------------------------------------------
 // pair-tensor GEMMs (pair_gemm.cuh): problems, element lists, tasks
 // ---------------------------------------------------------------------------
-// dynamic shared memory of k_pg_gemm: by default 128 KB (pnfam_ctx::pg_smem), so that
-// one of its CTAs leaves room on the SM (100 KB) for a CTA of the FP64 anchor kernels or
-// the block GEMMs of other points or engines, whose FP64 and FP32 pipes it does not use;
+// dynamic shared memory of k_pg_gemm: by default 104 KB (pnfam_ctx::pg_smem), so that
+// two of its CTAs share an SM and one streams while the other starts or drains a task;
 // at most PG_SMEM_MAX
 static constexpr int PG_SMEM_MAX = 224 * 1024;
 
