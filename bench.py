@@ -75,7 +75,7 @@ TIGHT = 1e-12
 NEAR_EXP = 4
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) over the algorithmic bytes of
 # one pair-tensor GEMM launch, from one ncu capture (N_sh = 12, 16 points)
-TRAFFIC_RATIO = {"density_fp32": 1.646e9 / 1.578e9, "field_projection_fp32": 1.790e9 / 1.739e9}
+TRAFFIC_RATIO = {"density_fp32": 1.662e9 / 1.578e9, "field_projection_fp32": 1.773e9 / 1.739e9}
 TRAFFIC_SOURCE = "profiles/k_pg_gemm_nsh12.md"
 REL = 1e-6
 # mixed form: FP64 anchors beside FP32 increments run asynchronously (--async-anchors)

@@ -342,6 +342,19 @@ def test_large_basis_pair_gemm_field_matches_fp64(large_case, monkeypatch):
     assert worst <= 1e-5
 
 
+@pytest.mark.parametrize("kspan", [96, 192, 768])
+def test_pair_gemm_density_task_spans_match_fp64(large_case, kspan, monkeypatch):
+    """Every density task span the autotuner may choose (K chunks per CTA task, hence the
+    number of partial sums the fold adds) gives the FP64 field within the FP32 tolerance
+    (PNFAM_GB300_PAIR_KSPAN fixes the span when the context is created)."""
+    monkeypatch.setenv("PNFAM_GB300_PAIR_GEMM", "1")
+    monkeypatch.setenv("PNFAM_GB300_PAIR_MIN", "1")
+    monkeypatch.setenv("PNFAM_GB300_PAIR_KSPAN", str(kspan))
+    worst = _mixed_vs_fp64(large_case, 8)
+    print(f"N_sh=12 162Gd GT-K1, density span {kspan}: pair-tensor GEMM field worst relative error {worst:.2e}")
+    assert worst <= 1e-5
+
+
 def test_pair_gemm_and_kernel_paths_agree_in_a_batch(monkeypatch):
     """A contour solved in the mixed form with the pair-tensor GEMMs (the default for
     evaluations of 4 or more points) and with the projection and density kernels
