@@ -27,7 +27,20 @@ within 1e-6 (relative) of the FP64 fixed point of the same equations (the FP64
 form converged to 1e-12, computed once and kept in
 tests/golden/bench_fixed_point_nsh16.json).  The plain FP64 form (the drop-in:
 the reference's arithmetic and trajectory, epsilon 1e-7) is measured on the
-same stream and reported beside it.
+same stream and reported beside it.  The pair-tensor GEMMs are tuned once per
+operator when the contexts are set up (outside the timed steps; the choices are
+in the line's "autotune" object).
+
+The same line also carries, unless --no-config4 / --no-stream:
+  config4         the large-basis stress configuration: a synthetic Bogoliubov
+                  state (seed 3) in the full N_sh = 20 basis (blocks up to 231),
+                  GT- K = 0, 1 at 256 CIRCLE points each, a fixed number of FAM
+                  iterations per point (the random state does not converge):
+                  point-iterations/s of both forms and per-stage rates
+  serving_stream  a stream of requests for several nuclei and bases (the three
+                  recorded ground states in N_sh from {8, 12, 16, 20}), Poisson
+                  arrivals at several rates, engines admitted within 150 GB:
+                  converged points/s and p50/p99 latency per rate
 
 Arms:
   default           this repository's GB300 solver through its C ABI
