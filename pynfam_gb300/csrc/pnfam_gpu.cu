@@ -1421,8 +1421,13 @@ extern "C" int pnfam_gpu_init(const pnfam_basis_t* basis, const double* Ep, cons
   // to the tensor-core and bandwidth-bound kernels first and fills what they leave (an
   // SM running one pair-GEMM CTA keeps 100 KB of shared memory and most registers free)
   // with CTAs of the FP64-pipe-bound anchor kernels
+  // (PNFAM_GB300_ANCHOR_PRIORITY=high swaps the two)
   int prio_lo = 0, prio_hi = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  {
+    const char* v = std::getenv("PNFAM_GB300_ANCHOR_PRIORITY");
+    if (v && std::string(v) == "high") std::swap(prio_lo, prio_hi);
+  }
   if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
       cudaEventCreate(&c->evt[0]) != cudaSuccess || cudaEventCreate(&c->evt[1]) != cudaSuccess ||
