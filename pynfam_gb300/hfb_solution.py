@@ -452,6 +452,35 @@ class HFBSolution:
         half = self.nb // 2
         return ib + half if ib < half else ib - half
 
+    def density_matrices(self, it: str) -> list:
+        """HFBTHO's oscillator-basis density matrix ``rk`` (twice rho) of isospin
+        ``it`` ('n' or 'p') per HFBTHO block, in HFBTHO's state order
+        (hfbdiag, hfbtho_solver.f90:1819-1856): rk = 2 sum_k V_ik V_jk over the
+        pairing-window quasiparticles, at temperature T the sum of
+        V (1 - f_k) V + U f_k U."""
+        U, V = (self.Un, self.Vn) if it == "n" else (self.Up, self.Vp)
+        f = self.occupations[1 if it == "n" else 0] if self.occupations is not None else None
+        h = self.hel
+        half = self.nb // 2
+        out = []
+        for ib in range(half):
+            s0, d = int(self.isstart[ib]), int(self.db[ib])
+            v = V[ib]
+            if f is None:
+                rk = 2.0 * (v @ v.T)
+            else:
+                fu = f[s0:s0 + d]
+                pr = int(self.isstart[ib + half])
+                fv = f[pr:pr + d]
+                rk = 2.0 * ((v * (1.0 - fv)) @ v.T + (U[ib] * fu) @ U[ib].T)
+            # undo the spin sort: sorted position i holds HFBTHO state perm[i]
+            ns = np.asarray(h.ns[s0:s0 + d])
+            perm = np.concatenate([np.nonzero(ns > 0)[0], np.nonzero(ns < 0)[0]])
+            r = np.empty_like(rk)
+            r[np.ix_(perm, perm)] = rk
+            out.append(r)
+        return out
+
 
 def load_hfb_solution(path) -> HFBSolution:
     """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file
