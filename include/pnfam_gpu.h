@@ -322,6 +322,49 @@ int pnfam_gpu_last_profile(const pnfam_ctx_t* ctx, double* stage_ms, int nstage,
 
 void pnfam_gpu_free(pnfam_ctx_t* ctx);
 
+/*
+ * Finite-range two-body-current field: the contraction of the Yukawa part of
+ * the axial two-body current with the ground-state density matrices, computed on
+ * the GPU.  Replaces effective_2bc_extfield (pnfam_extfield_2bc.f90:26-915, the
+ * production branch :128-465 and the final basis reorder :901-913), which the
+ * reference calls from setup_extfield (pnfam_solver.f90:620-633) when no .tbc
+ * file exists; its output is what write_tbc stores (pnfam_storage.f90:488-560).
+ *
+ *   ntx, nbx        basis states and blocks of HFBTHO (Omega > 0 half)
+ *   block_size      [nbx] states per block
+ *   nz, nr, nl, ns  [ntx] oscillator quantum numbers in HFBTHO's order
+ *   bz, bp          oscillator lengths (fm)
+ *   rk_n, rk_p      HFBTHO's density matrices rk (twice rho) per block,
+ *                   column-major [size x size], blocks concatenated
+ *   K               projection of the operator's angular momentum (-1, 0, 1)
+ *   beta_minus      1 for beta-, 0 for beta+
+ *   use_p           1: add the pion-pole (momentum-dependent) pieces
+ *   op_cols         [2 nbx] block column (0-based, -1 empty) of each block row of
+ *                   the operator on the time-reversal-doubled basis
+ *   op_offsets      [2 nbx] start of each block row's block in the flat storage
+ *   nxy             elements of the operator's flat storage
+ * Output: pieces [6][nxy] (host) = c3 direct, c3 exchange, c4 direct, c4
+ * exchange, pion-pole direct, pion-pole exchange, in the operator's flat layout
+ * on the spin-sorted basis, with the LECs stripped (c3 = 1, c4 + 1/4 = 1): the
+ * field for given LECs is c3 (c3d + c3e) + (c4 + 1/4) (c4d + c4e) + cpd + cpe.
+ * stats (may be NULL) [6]: host set-up ms, stage-1 ms, stage-2 ms (CUDA events),
+ * radial terms, radial groups, (z_b, z_d) pairs.
+ */
+typedef struct {
+  int ntx, nbx;
+  const int* block_size;
+  const int *nz, *nr, *nl, *ns;
+  double bz, bp;
+  const double* rk_n;
+  const double* rk_p;
+  int K, beta_minus, use_p;
+  const int* op_cols;
+  const long long* op_offsets;
+  long long nxy;
+} pnfam_2bc_input_t;
+
+int pnfam_gpu_2bc_field(const pnfam_2bc_input_t* in, double* pieces, double* stats);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* pnfam_gpu_last_error(void);
 

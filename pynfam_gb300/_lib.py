@@ -18,7 +18,7 @@ EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam
            "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
            "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_ready", "pnfam_gpu_engine_free",
            "pnfam_gpu_calc_hamiltonian_mixed", "pnfam_gpu_set_occupations", "pnfam_gpu_task_tables",
-           "pnfam_gpu_solve_state", "pnfam_gpu_state_size")
+           "pnfam_gpu_solve_state", "pnfam_gpu_state_size", "pnfam_gpu_2bc_field")
 
 TASK_TERMS = 4
 TASK_RECORD = 7 + 10 * TASK_TERMS
@@ -41,6 +41,16 @@ class Coupl(C.Structure):
     _fields_ = [("crho", C.POINTER(C.c_double)), ("cs", C.POINTER(C.c_double)),
                 ("cpair", C.POINTER(C.c_double)), ("cspair", C.POINTER(C.c_double)),
                 ("scalars", C.c_double * 12)]
+
+
+class TwoBodyInput(C.Structure):
+    """pnfam_2bc_input_t"""
+    _fields_ = [("ntx", C.c_int), ("nbx", C.c_int), ("block_size", C.POINTER(C.c_int)),
+                ("nz", C.POINTER(C.c_int)), ("nr", C.POINTER(C.c_int)), ("nl", C.POINTER(C.c_int)),
+                ("ns", C.POINTER(C.c_int)), ("bz", C.c_double), ("bp", C.c_double),
+                ("rk_n", C.POINTER(C.c_double)), ("rk_p", C.POINTER(C.c_double)),
+                ("K", C.c_int), ("beta_minus", C.c_int), ("use_p", C.c_int),
+                ("op_cols", C.POINTER(C.c_int)), ("op_offsets", C.POINTER(C.c_longlong)), ("nxy", C.c_longlong)]
 
 
 class SolverOpts(C.Structure):
@@ -105,6 +115,8 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_set_occupations.restype = C.c_int
     lib.pnfam_gpu_task_tables.argtypes = [C.c_int, ip, ip, C.c_int, ip, C.c_int, C.c_int, dp, C.c_int, ip, lp, lp]
     lib.pnfam_gpu_task_tables.restype = C.c_int
+    lib.pnfam_gpu_2bc_field.argtypes = [C.POINTER(TwoBodyInput), dp, dp]
+    lib.pnfam_gpu_2bc_field.restype = C.c_int
     _lib = lib
     return lib
 

@@ -8,6 +8,7 @@
 #include "../../include/pnfam_gpu.h"
 #include "pnfam_kernels.cuh"
 #include "pair_gemm.cuh"
+#include "tbc.cuh"
 
 #include <cuda_runtime.h>
 
@@ -2662,5 +2663,84 @@ extern "C" int pnfam_gpu_calc_hamiltonian_noalloc(
   for (int k = 0; k < 8; ++k)
     CK(cudaMemcpyAsync(d_out[k], hsp + (k & 1) * 4 * nf + qout[k] * nf, nbytes, cudaMemcpyDeviceToDevice, st));
   CK(cudaStreamSynchronize(st));
+  return PNFAM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Finite-range two-body-current field (effective_2bc_extfield on the GPU)
+// ---------------------------------------------------------------------------
+namespace {
+struct TbcDevice {      // device copies of the prepared tables, freed on scope exit
+  DBuf<double> jz, xr, cp, prho, zbuf, acc;
+  DBuf<int> tq, poff, pz, gq, goff, el;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  ~TbcDevice() {
+    jz.release(); xr.release(); cp.release(); prho.release(); zbuf.release(); acc.release();
+    tq.release(); poff.release(); pz.release(); gq.release(); goff.release(); el.release();
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+}  // namespace
+
+extern "C" int pnfam_gpu_2bc_field(const pnfam_2bc_input_t* in, double* pieces, double* stats) {
+  g_err.clear();
+  if (!in || !pieces || !in->block_size || !in->nz || !in->nr || !in->nl || !in->ns || !in->rk_n || !in->rk_p ||
+      !in->op_cols || !in->op_offsets || in->nxy <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_2bc_field: missing input");
+  const auto h0 = std::chrono::steady_clock::now();
+  tbc::Input ti{in->ntx, in->nbx, in->block_size, in->nz, in->nr, in->nl, in->ns, in->bz, in->bp, in->rk_n, in->rk_p,
+                in->K, in->beta_minus ? 1 : 0, in->use_p ? 1 : 0, in->op_cols, in->op_offsets, in->nxy};
+  tbc::Prepared P;
+  const std::string why = tbc::prepare(ti, P);
+  if (!why.empty()) return fail(PNFAM_EINVAL, "pnfam_gpu_2bc_field: " + why);
+  if ((long long)P.out_index.size() != in->nxy)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_2bc_field: operator block structure does not match nxy");
+  const double prep_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+
+  TbcDevice d;
+  CK(upload(d.jz, P.jz.data(), P.jz.size()));
+  CK(upload(d.xr, P.xr.data(), P.xr.size()));
+  CK(upload(d.cp, P.cp.data(), P.cp.size()));
+  CK(upload(d.tq, P.tq.data(), P.tq.size()));
+  CK(upload(d.poff, P.poff.data(), P.poff.size()));
+  CK(upload(d.pz, P.pz.data(), P.pz.size()));
+  CK(upload(d.prho, P.prho.data(), P.prho.size()));
+  CK(upload(d.gq, P.gq.data(), P.gq.size()));
+  CK(upload(d.goff, P.goff.data(), P.goff.size()));
+  CK(upload(d.el, P.el.data(), P.el.size()));
+  tbc::View v = tbc::view_of(ti, P);
+  v.jz = d.jz.p; v.xr = d.xr.p; v.cp = d.cp.p; v.tq = d.tq.p; v.poff = d.poff.p; v.pz = d.pz.p; v.prho = d.prho.p;
+  v.gq = d.gq.p; v.goff = d.goff.p; v.el = d.el.p;
+  const int NZ = P.nzx + 1;
+  const long long nzt = (long long)NZ * NZ * v.nt;
+  CK(dalloc(d.zbuf, (size_t)nzt * tbc::NQ * tbc::NCG));
+  CK(dalloc(d.acc, (size_t)in->nxy * 6));
+  CK(cudaMemset(d.acc.p, 0, (size_t)in->nxy * 6 * sizeof(double)));
+  v.zbuf = d.zbuf.p; v.acc = d.acc.p;
+  for (auto& e : d.ev) CK(cudaEventCreate(&e));
+
+  CK(cudaEventRecord(d.ev[0], 0));
+  const long long total = nzt * tbc::NCG;
+  const int zgrid = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+  tbc::k_tbc_z<<<zgrid, 256>>>(v, total);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(d.ev[1], 0));
+  CK(cudaFuncSetAttribute(tbc::k_tbc_field, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tbc::TBC_SMEM));
+  if (v.ngroups > 0) tbc::k_tbc_field<<<v.ngroups, tbc::TBC_THREADS, tbc::TBC_SMEM>>>(v);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(d.ev[2], 0));
+  std::vector<double> acc((size_t)in->nxy * 6);
+  CK(cudaMemcpy(acc.data(), d.acc.p, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  float ms1 = 0.f, ms2 = 0.f;
+  CK(cudaEventElapsedTime(&ms1, d.ev[0], d.ev[1]));
+  CK(cudaEventElapsedTime(&ms2, d.ev[1], d.ev[2]));
+  tbc::scatter(P, acc.data(), in->nxy, pieces);
+  for (long long i = 0; i < 6 * in->nxy; ++i)
+    if (!std::isfinite(pieces[i])) return fail(PNFAM_ENONFINITE, "pnfam_gpu_2bc_field: non-finite field element");
+  if (stats) {
+    stats[0] = prep_ms; stats[1] = ms1; stats[2] = ms2;
+    stats[3] = v.nt; stats[4] = v.ngroups; stats[5] = (double)(P.pz.size() / 2);
+  }
   return PNFAM_OK;
 }

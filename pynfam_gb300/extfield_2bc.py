@@ -14,14 +14,16 @@ The reference folds the axial two-body current into the one-body operators
   contracted once with the ground-state densities, which the reference caches
   in ``<fam_output_filename>.tbc`` with the LECs stripped (pnfam_storage.f90:
   488-727) and recomputes from two-body matrix elements when the file is
-  absent (pnfam_extfield_2bc.f90:26, O(N^10) in the oscillator shells);
+  absent (pnfam_extfield_2bc.f90:26, O(N^10) in the oscillator shells); here
+  that contraction runs on the GPU (``finite_range.gamma_pieces``);
 * P, PS0 and the spin-dipole operators RS0/RS1/RS2 (and their I-function
   variants) multiply the one-body integrand by 1 + c(r) (or c(r) alone for
   2 body only), c(r) from nuclear matter at a fixed pair momentum or from the
   DME (pnfam_extfield.f90:1152-1719).
 
-Every function here is a mesh function of the ground-state densities rho,
-tau and Laplacian rho (``HFBSolution``) and runs once per set-up, on the host.
+Every function here but the finite-range contraction is a mesh function of the
+ground-state densities rho, tau and Laplacian rho (``HFBSolution``) and runs
+once per set-up, on the host.
 """
 from __future__ import annotations
 
@@ -456,23 +458,57 @@ def write_tbc(path: str, t: TBCField) -> None:
         fh.write(b"".join(out))
 
 
-def finite_range_field(path: str, hfb, F, lec: LECs, usep_requested: bool, direct_only: bool) -> np.ndarray:
-    """The finite-range GT field of ``path`` with the namelist LECs applied
-    (``read_tbc``, pnfam_storage.f90:562-727): sum of the direct and exchange
-    c3, c4 (and pion-pole) parts, c3 -> c3, c4 -> c4 + 1/4.  A missing or
-    incompatible file is an error: the contraction of the two-body matrix
-    elements that would rebuild it is not part of this solver."""
-    if not os.path.exists(path):
-        raise TwoBodyCurrentError(
-            f"two-body current mode needs the finite-range field file '{path}' (.tbc); computing it from the "
-            "two-body matrix elements is not supported")
-    t = read_tbc(path)
+def _tbc_compatible(t: TBCField, hfb, F, usep_requested: bool) -> bool:
+    """read_tbc's compatibility checks (pnfam_storage.f90:601-628)."""
+    return not (t.use_hblas != 1 or (t.usep == 0 and usep_requested) or t.nb != hfb.nb or t.dqp != hfb.dqp
+                or t.nxy != F.mat.nelem or t.nxy12 != -1 or t.label != F.label or t.k != F.k
+                or t.rank != F.rank or t.beta_minus != int(F.beta_minus) or t.parity_even != int(F.parity_even))
+
+
+def compute_tbc(hfb, F, lec: LECs, usep: bool, mode: int = 0, nxterms: int = 0, compute=None) -> TBCField:
+    """The finite-range field of the operator ``F`` computed from the two-body matrix
+    elements (``effective_2bc_extfield``, on the GPU: ``finite_range.gamma_pieces``), as
+    the ``.tbc`` record write_tbc stores (pnfam_storage.f90:488-560): LECs stripped,
+    Gamma only.  ``compute`` replaces the GPU contraction (tests of the host logic)."""
+    if compute is None:
+        from .finite_range import gamma_pieces as compute
+    try:
+        pieces = compute(hfb, F, usep)
+    except (OSError, RuntimeError) as e:
+        raise TwoBodyCurrentError(f"computing the finite-range two-body-current field (.tbc) needs the CUDA "
+                                  f"library and a GPU: {e}")
+    names = ["c3d", "c3e", "c4d", "c4e"] + (["cpd", "cpe"] if usep else [])
+    lecs = np.array([lec.c3, lec.c4, lec.cd / -0.25])
+    return TBCField(1, int(mode), int(bool(usep)), lecs, int(hfb.nb), int(hfb.dqp), int(F.mat.nelem), -1,
+                    str(F.label), int(F.k), int(F.rank), int(bool(F.beta_minus)), int(bool(F.parity_even)),
+                    np.asarray(parse_mode(mode) if mode else (0,) * 6, dtype=np.int32),
+                    {nm: np.asarray(pieces[nm], dtype=np.float64) for nm in names}, None, int(nxterms))
+
+
+def finite_range_field(path: str, hfb, F, lec: LECs, usep_requested: bool, direct_only: bool, mode: int = 0,
+                       nxterms: int = 0, log=None, compute=None) -> np.ndarray:
+    """The finite-range GT field with the namelist LECs applied: sum of the direct
+    and exchange c3, c4 (and pion-pole) parts, c3 -> c3, c4 -> c4 + 1/4
+    (calc_totgamdel, pnfam_type_gamdel_2bc.f90:85-116).  The pieces come from the
+    ``.tbc`` file at ``path`` (``read_tbc``, pnfam_storage.f90:562-727); a missing,
+    incompatible or corrupted file is recomputed from the two-body matrix elements
+    and stored there, as setup_extfield does (pnfam_solver.f90:617-633)."""
+    say = log or (lambda msg: None)
+    t = None
+    if os.path.exists(path):
+        say(f"  * Reading from extfield file: {path}")
+        try:
+            t = read_tbc(path)
+        except TwoBodyCurrentError as e:
+            say(f"  * The file '{path}' is corrupted! ({e})")
+        if t is not None and not _tbc_compatible(t, hfb, F, usep_requested):
+            say(f"  * The file '{path}' is incompatible with the current calculation!")
+            t = None
+    if t is None:
+        say("  * Calculating 2BC matrix elements...")
+        t = compute_tbc(hfb, F, lec, usep_requested, mode, nxterms, compute)
+        write_tbc(path, t)
     nxy = F.mat.nelem
-    bad = (t.use_hblas != 1 or (t.usep == 0 and usep_requested) or t.nb != hfb.nb or t.dqp != hfb.dqp
-           or t.nxy != nxy or t.nxy12 != -1 or t.label != F.label or t.k != F.k or t.rank != F.rank
-           or t.beta_minus != int(F.beta_minus) or t.parity_even != int(F.parity_even))
-    if bad:
-        raise TwoBodyCurrentError(f"The file '{path}' is incompatible with the current calculation")
     c3, c4 = lec.c3, lec.c4 + 0.25
     g = t.gam
     zero = np.zeros(nxy)

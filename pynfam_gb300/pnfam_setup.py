@@ -88,7 +88,8 @@ def _external_field(hfb, e, use_2bc, lecs, out_name, tbc_dir):
         return F, G
     # ... + the finite-range part (direct only with the DME exchange form)
     path = os.path.join(tbc_dir, f"{str(out_name).strip()}.tbc")
-    fr = finite_range_field(path, hfb, F, lecs, lecs.use_p, use_2bc[1] == 5)
+    mode = int(e.get("two_body_current_mode", 0) or 0)
+    fr = finite_range_field(path, hfb, F, lecs, lecs.use_p, use_2bc[1] == 5, mode, len(G))
     F.mat.set_flat(fr + tmp)
     return F, G
 

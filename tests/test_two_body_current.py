@@ -64,22 +64,52 @@ def test_tbc_round_trip_and_compatibility(tmp_path):
     for k in src.gam:
         assert np.array_equal(src.gam[k], back.gam[k])
     assert p.read_bytes() == open(os.path.join(GOLDEN, "S40_2bc_fam", "GT-K1.tbc"), "rb").read()
-    # a field for another operator is refused, as is a missing file
+    # a field for another operator, and a missing or corrupted file, are recomputed
+    # (here by a stand-in for the GPU contraction that returns the reference's own
+    # GT-K0 pieces) and stored, as setup_extfield does
     c, _ = case_for("S40_2bc_fam", "GT-K0", 0)
     lec = t2.LECs.from_namelist([-3.1962, 3.1962, 0.0])
-    with pytest.raises(t2.TwoBodyCurrentError):
-        t2.finite_range_field(str(p), c.hfb, c.F, lec, False, False)
-    with pytest.raises(t2.TwoBodyCurrentError):
-        t2.finite_range_field(str(tmp_path / "absent.tbc"), c.hfb, c.F, lec, False, False)
+    k0_path = os.path.join(GOLDEN, "S40_2bc_fam", "GT-K0.tbc")
+    k0 = t2.read_tbc(k0_path)
+    calls = []
+
+    def stand_in(h, F, usep):
+        calls.append((F.label, F.k, usep))
+        return dict(k0.gam, cpd=np.zeros(k0.nxy), cpe=np.zeros(k0.nxy))
+    from_file = t2.finite_range_field(k0_path, c.hfb, c.F, lec, False, False)
+    absent = tmp_path / "absent.tbc"
+    bad = tmp_path / "bad.tbc"
+    bad.write_bytes(b"\x00" * 12)
+    for path in (p, absent, bad):
+        calls.clear()
+        got = t2.finite_range_field(str(path), c.hfb, c.F, lec, False, False, 111100, 0, compute=stand_in)
+        assert calls == [("GT", 0, False)]
+        assert path.read_bytes() == open(k0_path, "rb").read()
+        assert np.array_equal(got, from_file)
+    # a compatible file is read, not recomputed
+    calls.clear()
+    t2.finite_range_field(str(absent), c.hfb, c.F, lec, False, False, 111100, 0, compute=stand_in)
+    assert calls == []
+    # a field without the pion-pole pieces is recomputed when they are requested
+    t2.finite_range_field(str(absent), c.hfb, c.F, lec, True, False, 111100, 0, compute=stand_in)
+    assert calls == [("GT", 0, True)]
 
 
-def test_missing_tbc_fails_setup(tmp_path):
+def test_missing_tbc_is_computed_by_setup(tmp_path, monkeypatch):
+    """setup_case computes a missing .tbc (stand-in contraction: the reference's
+    pieces) and composes the same operator as from the reference's file."""
     from golden_cases import namelist_for
-    from pynfam_gb300.pnfam_setup import SetupError, setup_case
+    from pynfam_gb300 import finite_range
+    from pynfam_gb300.pnfam_setup import setup_case
     g = golden("S40_2bc_fam")
     nml = namelist_for("S40_2bc_fam", g["operators"]["GT-K0"][0])
-    with pytest.raises(SetupError, match="tbc"):
-        setup_case(nml, None, hfb=hfb("S40_2bc_fam"), tbc_dir=str(tmp_path))
+    k0_path = os.path.join(GOLDEN, "S40_2bc_fam", "GT-K0.tbc")
+    k0 = t2.read_tbc(k0_path)
+    monkeypatch.setattr(finite_range, "gamma_pieces", lambda h, F, usep: dict(k0.gam))
+    c = setup_case(nml, None, hfb=hfb("S40_2bc_fam"), tbc_dir=str(tmp_path))
+    ref, _ = case_for("S40_2bc_fam", "GT-K0", 0)
+    assert np.array_equal(c.F.mat.flatten(), ref.F.mat.flatten())
+    assert (tmp_path / "GT-K0.tbc").read_bytes() == open(k0_path, "rb").read()
 
 
 @pytest.mark.parametrize("mode,ok", [(0, True), (111100, True), (141100, True), (111001, True), (211100, True),
