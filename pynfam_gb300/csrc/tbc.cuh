@@ -777,34 +777,164 @@ __global__ void k_tbc_z(View v, long long total) {
 }
 
 constexpr int TBC_TCH = 32;         // terms per chunk
-constexpr int TBC_THREADS = 128;    // = TBC_TCH * 2 branches * 2 (direct, exchange)
+constexpr int TBC_THREADS = 256;    // 8 warps
 constexpr size_t TBC_SMEM = sizeof(double) * TBC_TCH * 4 * NCG;
 
+__device__ __forceinline__ void warp_sum6(double* s) {
+#pragma unroll
+  for (int g = 0; g < NG; ++g)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s[g] += __shfl_xor_sync(0xffffffffu, s[g], o);
+}
+
+// radx6 with the 32 lanes of a warp splitting the (ny_i, ny_j, ny_k) combinations;
+// every lane returns the full sums.  Called by all lanes with the same arguments.
+__device__ void radx6_warp(const View& v, int lane, int tab, int ni, int li, int nj, int lj, int nk, int lk, int nl,
+                           int ll, double* s) {
+  const int n1 = v.nrl + 1;
+  const double* X = v.xr + (size_t)tab * n1 * n1 * n1 * n1 * NG;
+  const double* Y = v.xr + (size_t)X00 * n1 * n1 * n1 * n1 * NG;
+  const int Ai = 2 * ni + abs(li), Aj = 2 * nj + abs(lj), Ak = 2 * nk + abs(lk), Al = 2 * nl + abs(ll);
+  const int n3 = (Ai + 1) * (Aj + 1) * (Ak + 1);
+  for (int g = 0; g < NG; ++g) s[g] = 0.0;
+  for (int c = lane; c < n3; c += 32) {
+    const int yk = c % (Ak + 1), r = c / (Ak + 1), yj = r % (Aj + 1), yi = r / (Aj + 1);
+    const double cijk = cp2c_at(v, ni, li, yi) * cp2c_at(v, nj, lj, yj) * cp2c_at(v, nk, lk, yk);
+    for (int yl = (yi + yj + yk) & 1; yl <= Al; yl += 2) {
+      const int sgn = (yi + yj + ((yi + yj + yk + yl) >> 1)) & 1;
+      const double w = (sgn ? -cijk : cijk) * cp2c_at(v, nl, ll, yl);
+      const double* x = X + idx4(n1, Ai - yi, Aj - yj, Ak - yk, Al - yl) * NG;
+      const double* y = Y + idx4(n1, yi, yj, yk, yl) * NG;
+#pragma unroll
+      for (int g = 0; g < NG; ++g) s[g] += w * x[g] * y[g];
+    }
+  }
+  warp_sum6(s);
+}
+
+// radc6_imag with the lanes of a warp splitting the (ny_i, ny_j, ny_k) combinations
+__device__ void radc6_imag_warp(const View& v, int lane, int dip, int ni, int li, int nj, int lj, int nk, int lk,
+                                int nl, int ll, double* s) {
+  const int n1 = v.nrl + 1;
+  const double* X = v.xr + (size_t)X10 * n1 * n1 * n1 * n1 * NG;
+  const double* Y = v.xr + (size_t)(dip == 1 ? X01 : X02) * n1 * n1 * n1 * n1 * NG;
+  const int Ai = 2 * ni + abs(li), Aj = 2 * nj + abs(lj), Ak = 2 * nk + abs(lk), Al = 2 * nl + abs(ll);
+  const int n3 = (Ai + 1) * (Aj + 1) * (Ak + 1);
+  for (int g = 0; g < NG; ++g) s[g] = 0.0;
+  for (int c = lane; c < n3; c += 32) {
+    const int yk = c % (Ak + 1), r = c / (Ak + 1), yj = r % (Aj + 1), yi = r / (Aj + 1);
+    const double cijk = cp2c_at(v, ni, li, yi) * cp2c_at(v, nj, lj, yj) * cp2c_at(v, nk, lk, yk);
+    for (int yl = 0; yl <= Al; ++yl) {
+      const int e = ((yi + yj - yk - yl) % 4 + 4) % 4;
+      if (!(e & 1)) continue;
+      const double w = (e == 1 ? cijk : -cijk) * cp2c_at(v, nl, ll, yl);
+      const double* x = X + idx4(n1, Ai - yi, Aj - yj, Ak - yk, Al - yl) * NG;
+      const double* y = Y + idx4(n1, yi, yj, yk, yl) * NG;
+      for (int g = 0; g < NG; ++g) s[g] += w * x[g] * y[g];
+    }
+  }
+  warp_sum6(s);
+}
+
+// ddgr6 by a warp: lane 0 writes out[g]
+__device__ void ddgr6_warp(const View& v, int lane, int ni, int li, int nj, int lj, int nk, int lk, int nl, int ll,
+                           int di, int dj, int dip, double* out) {
+  if (-li - lj + lk + ll + di + dj != 0) return;          // out stays 0
+  const double r2 = 1.4142135623730951;
+  const int p = dip ? 1 : 0, sm = di + dj;
+  auto tab = [&](int d, int pp) {
+    if (pp == 0) return d == 0 ? (int)X00 : d == 1 ? (int)X10 : (int)X20;
+    if (d == 1) return pp == 1 ? (int)X11 : (int)X12;
+    return pp == 1 ? (int)X01 : (int)X02;
+  };
+  double s[NG], sc;
+  int tb;
+  if (di == 0 && dj == 0) { tb = X00; sc = 1.0; }
+  else if (sm == 2 || sm == -2) { tb = tab(2 - p, dip); sc = 2.0; }
+  else if (sm == 1 || sm == -1) { tb = dj == 0 ? tab(1 - p, dip) : (int)X10; sc = -sm * r2; }
+  else { tb = tab(2 - p, dip); sc = -1.0; }
+  radx6_warp(v, lane, tb, ni, li, nj, lj, nk, lk, nl, ll, s);
+  if (lane == 0)
+    for (int g = 0; g < NG; ++g) out[g] = sc * s[g];
+  if (sm == 0 && !(di == 0 && dj == 0) && dip) {
+    radc6_imag_warp(v, lane, dip, ni, li, nj, lj, nk, lk, nl, ll, s);
+    if (lane == 0)
+      for (int g = 0; g < NG; ++g) out[g] += s[g];
+  }
+}
+
+// jr_vec by a warp into J [NCG] (shared memory)
+__device__ void jr_vec_warp(const View& v, int lane, int na, int la, int nb, int lb, int nc, int lc, int nd, int ld,
+                            double* J) {
+  for (int i = lane; i < NCG; i += 32) J[i] = 0.0;
+  __syncwarp();
+  const int K = v.K;
+#define TBC_RW(piece, di, dj, dip) ddgr6_warp(v, lane, na, la, nb, lb, nc, lc, nd, ld, di, dj, dip, J + (piece) * NG)
+  if (v.use_p) {
+    TBC_RW(R0P, K, -1, 1); TBC_RW(R0Z, K, 0, 1); TBC_RW(R0M, K, +1, 1);
+    TBC_RW(RP0, K, -1, 2); TBC_RW(RZ0, K, 0, 2); TBC_RW(RM0, K, +1, 2);
+  }
+  if (K == 1) {
+    TBC_RW(RKP, +1, -1, 0); TBC_RW(RKZ, +1, 0, 0); TBC_RW(RKM, +1, +1, 0); TBC_RW(RPZ, 0, 0, 0);
+  } else if (K == 0) {
+    TBC_RW(RKP, 0, -1, 0); TBC_RW(RKZ, 0, 0, 0); TBC_RW(RKM, +1, 0, 0); TBC_RW(RPM, +1, -1, 0);
+  } else {
+    TBC_RW(RKP, -1, -1, 0); TBC_RW(RKZ, 0, -1, 0); TBC_RW(RKM, +1, -1, 0); TBC_RW(RZM, 0, 0, 0);
+  }
+#undef TBC_RW
+  __syncwarp();
+  if (lane < NG) {
+    const int g = lane;
+    if (K == 1) {
+      J[RPM * NG + g] = J[RKZ * NG + g]; J[RZM * NG + g] = J[RKM * NG + g]; J[RPZ2 * NG + g] = J[RKP * NG + g];
+    } else if (K == 0) {
+      J[RPZ * NG + g] = J[RKP * NG + g]; J[RZM * NG + g] = J[RKM * NG + g];
+    } else {
+      J[RPZ * NG + g] = J[RKP * NG + g]; J[RPM * NG + g] = J[RKZ * NG + g]; J[RZM2 * NG + g] = J[RKM * NG + g];
+    }
+  }
+  __syncwarp();
+}
+
 // stage 2: one CTA per radial group.  Phase A: the chunk's currents, one (term,
-// branch, direct/exchange) per thread, into shared memory; phase B: every element of
-// the group (thread-owned, no two threads share one) accumulates the chunk's terms.
+// branch, direct/exchange) per warp, the lanes splitting each Cartesian sum, into
+// shared memory; phase B: one element per warp, the lanes splitting the chunk's
+// (term, branch) pairs, reduced across the warp into the element's sums.
 __global__ void __launch_bounds__(TBC_THREADS) k_tbc_field(View v) {
   extern __shared__ double sj[];                 // [TBC_TCH][2][2][NCG]
   __shared__ int ok[TBC_TCH][2];
-  const int grp = blockIdx.x;
+  const int grp = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int e0 = v.goff[grp], e1 = v.goff[grp + 1];
+  const int* q = v.gq + 4 * grp;
+  const int ra = q[0], la = q[1], rc = q[2], lc = q[3];
   for (int t0 = 0; t0 < v.nt; t0 += TBC_TCH) {
-    for (int it = threadIdx.x; it < TBC_TCH * 4; it += blockDim.x) {
+    for (int it = warp; it < TBC_TCH * 4; it += nw) {
       const int tt = it >> 2, br = (it >> 1) & 1, de = it & 1, t = t0 + tt;
-      const int r = t < v.nt ? (int)stage2_jr(v, grp, t, br, de, sj + (size_t)it * NCG) : 0;
-      if (de == 0) ok[tt][br] = r;
+      int lb = 0, ld = 0, sd, sb;
+      double sign;
+      const bool valid = t < v.nt && term_branch(v, t, br, la, lc, &lb, &ld, &sd, &sb, &sign);
+      if (lane == 0 && de == 0) ok[tt][br] = valid ? 1 : 0;
+      if (!valid) continue;
+      const int rb = v.tq[5 * t + 3], rd = v.tq[5 * t + 4];
+      double* J = sj + (size_t)it * NCG;
+      if (de == 0) jr_vec_warp(v, lane, ra, la, rb, lb, rc, lc, rd, ld, J);
+      else jr_vec_warp(v, lane, ra, la, rb, lb, rd, ld, rc, lc, J);
     }
     __syncthreads();
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    for (int e = e0 + warp; e < e1; e += nw) {
       double gam[6] = {0, 0, 0, 0, 0, 0};
-      for (int tt = 0; tt < TBC_TCH; ++tt)
-        for (int br = 0; br < 2; ++br)
-          if (ok[tt][br]) {
-            const double* jd = sj + (size_t)((tt * 2 + br) * 2) * NCG;
-            stage2_elem(v, grp, e, t0 + tt, br, jd, jd + NCG, gam);
-          }
-      double* a = v.acc + (size_t)e * 6;
-      for (int k = 0; k < 6; ++k) a[k] += gam[k];
+      for (int it = lane; it < TBC_TCH * 2; it += 32) {
+        const int tt = it >> 1, br = it & 1;
+        if (ok[tt][br]) {
+          const double* jd = sj + (size_t)((tt * 2 + br) * 2) * NCG;
+          stage2_elem(v, grp, e, t0 + tt, br, jd, jd + NCG, gam);
+        }
+      }
+      warp_sum6(gam);
+      if (lane == 0) {
+        double* a = v.acc + (size_t)e * 6;
+        for (int k = 0; k < 6; ++k) a[k] += gam[k];
+      }
     }
     __syncthreads();
   }
