@@ -41,6 +41,10 @@ The same line also carries, unless --no-config4 / --no-stream:
                   recorded ground states in N_sh from {8, 12, 16, 20}), Poisson
                   arrivals at several rates, engines admitted within 150 GB:
                   converged points/s and p50/p99 latency per rate
+  finite_range_2bc  (unless --no-2bc) the set-up contraction of the finite-range
+                  two-body current for GT- K = 0, 1 of the same ground state
+                  (what the reference caches in .tbc files), wall and kernel
+                  times, and the 40S N_sh = 6 field against the reference's file
 
 Arms:
   default           this repository's GB300 solver through its C ABI
@@ -592,6 +596,8 @@ def run_gpu(args):
                                           f"settings)"}
     if rank == 0 and world == 1 and not args.no_config4:
         line["config4"] = run_config4(args, emit=False)
+    if rank == 0 and world == 1 and not args.no_2bc:
+        line["finite_range_2bc"] = run_tbc(args, emit=False)
     if rank == 0 and world == 1 and not args.no_stream:
         sl = run_serve_stream(args, emit=False)
         line["serving_stream"] = {
@@ -604,6 +610,70 @@ def run_gpu(args):
     if rank == 0:
         print(json.dumps(line, default=_plain), flush=True)
     replicas.finish()
+
+
+def run_tbc(args, emit=True):
+    """Finite-range two-body-current field: the contraction of the Yukawa part of the
+    axial two-body current with the ground-state density matrices, which the
+    reference computes once per operator on the CPU and caches in a .tbc file
+    (pnfam_extfield_2bc.f90; 1.5-2.5 h per K component at 16 shells with OpenMP,
+    per its README_2bc.md).  On the GPU (host table set-up + two kernels): GT- K = 0
+    and K = 1 of the benchmark ground state in the N_sh = --tbc-nsh basis, and the
+    40S N_sh = 6 GT- K = 0 field of the reference's own runs, checked against the
+    reference's .tbc file, beside the CPU oracle's time for that field (unless
+    --no-cpu).  Wall times include the host set-up; the kernels' times are CUDA
+    events."""
+    from pynfam_gb300.extfield import init_external_field
+    from pynfam_gb300.extfield_2bc import read_tbc
+    from pynfam_gb300.finite_range import gamma_pieces
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    from pynfam_gb300.synthetic import ground_state
+    gold = os.path.join(ROOT, "tests", "golden")
+    s40 = load_hfb_solution(os.path.join(gold, "S40_2bc_fam.hel"))
+    F6 = init_external_field(s40, "-", "GT", 0)
+    gamma_pieces(s40, F6)                       # CUDA context and module load
+    st6 = {}
+    t0 = time.perf_counter()
+    g6 = gamma_pieces(s40, F6, stats=st6)
+    wall6 = time.perf_counter() - t0
+    ref = read_tbc(os.path.join(gold, "S40_2bc_fam", "GT-K0.tbc"))
+    scale = max(np.abs(v).max() for v in ref.gam.values())
+    err6 = max(float(np.abs(g6[k] - ref.gam[k]).max()) for k in ref.gam) / scale
+    small = {"workload": "40S (recorded SkO' ground state, N_sh = 6) GT- K=0, 1,640 elements",
+             "wall_ms": 1e3 * wall6, "stage1_ms": st6["stage1_ms"], "stage2_ms": st6["stage2_ms"],
+             "max_err_vs_reference_tbc": err6}
+    if not args.no_cpu:
+        from oracle.tbc_oracle import two_body_gamma
+        h = s40.hel
+        t0 = time.perf_counter()
+        two_body_gamma(h.nz, h.nr, h.nl, h.ns, h.ID, h.bz, h.bp, s40.density_matrices("n"),
+                       s40.density_matrices("p"), F6.mat.cols, F6.mat.offsets(), F6.mat.nelem, 0, True)
+        small["cpu_oracle_s"] = time.perf_counter() - t0
+        small["cpu_oracle"] = "numpy restatement of the reference's loops, memoised elements, 1 host core"
+    hfb = ground_state(HEL, args.tbc_nsh)
+    per_k = []
+    for K in (0, 1):
+        F = init_external_field(hfb, "-", "GT", K)
+        st = {}
+        t0 = time.perf_counter()
+        gamma_pieces(hfb, F, stats=st)
+        wall = time.perf_counter() - t0
+        per_k.append({"K": K, "elements": int(F.mat.nelem), "wall_s": wall, "host_ms": st["host_ms"],
+                      "stage1_ms": st["stage1_ms"], "stage2_ms": st["stage2_ms"], "radial_groups": st["groups"],
+                      "radial_terms": st["terms"], "zpairs": st["pairs"]})
+    total_el = sum(x["elements"] for x in per_k)
+    total_s = sum(x["wall_s"] for x in per_k)
+    obj = {"workload": f"finite-range 2BC field, GT- K=0 and K=1, 162Gd SkO' fields in the full N_sh = "
+                       f"{args.tbc_nsh} basis", "per_K": per_k, "elements_per_s": total_el / total_s,
+           "s40_nsh6": small,
+           "reference_published": "1.5-2.5 h per K component at 16 shells, OpenMP CPU (README_2bc.md)",
+           "bound": "FP64 pipe (the Cartesian sums of the radial elements; k_tbc_field)"}
+    if emit:
+        print(json.dumps({"metric": "finite-range 2BC field elements per second", "value": obj["elements_per_s"],
+                          "unit": "elements/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+                          "data": "recorded ground state re-diagonalised", "config": {"workload": obj["workload"]},
+                          "finite_range_2bc": obj}, default=_plain), flush=True)
+    return obj
 
 
 def run_serve_stream(args, emit=True):
@@ -878,6 +948,10 @@ def main():
     ap.add_argument("--c4-fp64-points", type=int, default=32, help="config 4: points per operator, FP64 form")
     ap.add_argument("--no-config4", action="store_true", help="leave the config 4 object out of the line")
     ap.add_argument("--no-stream", action="store_true", help="leave the serving-stream object out of the line")
+    ap.add_argument("--no-2bc", action="store_true", help="leave the finite-range 2BC field object out of the line")
+    ap.add_argument("--tbc-only", action="store_true", help="only the finite-range 2BC field timing (own line)")
+    ap.add_argument("--tbc-nsh", type=int, default=NSH, help="finite-range 2BC field: N_sh of the basis")
+    ap.add_argument("--no-cpu", action="store_true", help="finite-range 2BC field: skip the CPU oracle timing")
     ap.add_argument("--async-anchors", action="store_true",
                     help="mixed form: FP64 anchors beside FP32 increments run asynchronously")
     ap.add_argument("--solve-only", action="store_true",
@@ -885,7 +959,9 @@ def main():
     args = ap.parse_args()
     global ASYNC_ANCHORS
     ASYNC_ANCHORS = args.async_anchors
-    if args.config4:
+    if args.tbc_only:
+        run_tbc(args)
+    elif args.config4:
         run_config4(args)
     elif args.solve_only:
         run_solve_only(args)

@@ -506,7 +506,10 @@ def finite_range_field(path: str, hfb, F, lec: LECs, usep_requested: bool, direc
             t = None
     if t is None:
         say("  * Calculating 2BC matrix elements...")
-        t = compute_tbc(hfb, F, lec, usep_requested, mode, nxterms, compute)
+        try:
+            t = compute_tbc(hfb, F, lec, usep_requested, mode, nxterms, compute)
+        except TwoBodyCurrentError as e:
+            raise TwoBodyCurrentError(f"no usable finite-range field file '{path}': {e}")
         write_tbc(path, t)
     nxy = F.mat.nelem
     c3, c4 = lec.c3, lec.c4 + 0.25

@@ -74,9 +74,20 @@ def test_cli_reports_missing_ground_state(tmp_path):
     assert "ERROR" in out and "Strength" not in out
 
 
-def test_cli_two_body_current_needs_its_tbc_file(tmp_path):
-    """Mode 111100 reads the finite-range field from <fam_output_filename>.tbc;
-    without it the run fails with a message and no result table."""
+def _gpu_present():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_cli_two_body_current_without_tbc_and_gpu(tmp_path):
+    """Mode 111100 reads the finite-range field from <fam_output_filename>.tbc and
+    computes it on the GPU when the file is missing; with neither, the run fails with
+    a message naming the file and writes no result table."""
+    if _gpu_present():
+        pytest.skip("a GPU is present: the field is computed (see the GPU test below)")
     g = golden("S40_2bc_fam")
     write_in(tmp_path / "GT-K0.in", g["operators"]["GT-K0"][0], g["interaction"], "GT-K0")
     shutil.copyfile(os.path.join(GOLDEN, "S40_2bc_fam.hel"), tmp_path / "hfbtho_output.hel")
@@ -85,6 +96,25 @@ def test_cli_two_body_current_needs_its_tbc_file(tmp_path):
     assert p.returncode == 1 and "GT-K0.tbc" in p.stderr
     out = open(tmp_path / "GT-K0.dat").read()
     assert "GT-K0.tbc" in out and "Strength" not in out
+    assert not (tmp_path / "GT-K0.tbc").exists()
+
+
+@pytest.mark.gpu
+def test_cli_two_body_current_computes_its_tbc_file(tmp_path):
+    """Mode 111100 without a .tbc file: the finite-range field is computed on the GPU
+    and stored, and the run reproduces the recorded 2BC strength."""
+    g = golden("S40_2bc_fam")
+    pt = g["operators"]["GT-K0"][0]
+    write_in(tmp_path / "GT-K0.in", pt, g["interaction"], "GT-K0")
+    shutil.copyfile(os.path.join(GOLDEN, "S40_2bc_fam.hel"), tmp_path / "hfbtho_output.hel")
+    env = dict(os.environ, PNFAM_GB300_CACHE="off")
+    p = subprocess.run([sys.executable, EXE, "GT-K0.in"], cwd=tmp_path, capture_output=True, text=True, env=env)
+    assert p.returncode == 0, p.stderr
+    assert (tmp_path / "GT-K0.tbc").exists()
+    version, conv, t, rows = parse_dat(tmp_path / "GT-K0.dat")
+    re_, im_ = pt["result"]["Strength"]
+    got = rows["Strength"]
+    assert abs(got[0] - re_) <= 1e-6 * abs(re_) and abs(got[1] - im_) <= 1e-6 * abs(im_)
 
 
 def test_cli_rejects_two_arguments(tmp_path):
