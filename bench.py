@@ -676,6 +676,41 @@ def run_tbc(args, emit=True):
     return obj
 
 
+def run_hfb(args, emit=True):
+    """HFB reconstruction of the benchmark ground state (162Gd SkO' fields in the full
+    N_sh = 16 and 20 bases): the host (numpy + LAPACK) form against the form with the
+    basis functions, HFB matrices, eigensolves (batched Jacobi) and densities on the
+    GPU, wall time of each (after one warm-up of each), and the largest differences
+    of the quasiparticle energies (MeV) and of the local density (relative)."""
+    from pynfam_gb300.hel import read_hel
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    from pynfam_gb300.synthetic import extend_basis
+    rows = []
+    load_hfb_solution(read_hel(HEL), device=True)
+    for nsh in (16, 20):
+        h = extend_basis(read_hel(HEL), nsh)
+        t = {}
+        sol = {}
+        for dev in (False, True):
+            t0 = time.perf_counter()
+            sol[dev] = load_hfb_solution(h, device=dev)
+            t[dev] = time.perf_counter() - t0
+        a, b = sol[False], sol[True]
+        rows.append({"nsh": nsh, "states": int(len(h.nr)), "blocks": int(len(h.ID)), "host_s": t[False],
+                     "device_s": t[True],
+                     "max_dE_MeV": float(max(np.abs(a.En - b.En).max(), np.abs(a.Ep - b.Ep).max())),
+                     "max_drho_rel": float(max(np.abs(a.rho_n - b.rho_n).max() / np.abs(a.rho_n).max(),
+                                               np.abs(a.rho_p - b.rho_p).max() / np.abs(a.rho_p).max()))})
+    obj = {"workload": "HFB reconstruction of the 162Gd SkO' ground state in the full N_sh = 16 and 20 bases",
+           "rows": rows}
+    if emit:
+        print(json.dumps({"metric": "HFB reconstruction wall time", "value": rows[0]["device_s"], "unit": "s",
+                          "n_gpus": 1, "higher_is_better": False, "dtype": "f64", "data": "recorded fields",
+                          "config": {"workload": obj["workload"]}, "hfb_reconstruction": obj}, default=_plain),
+              flush=True)
+    return obj
+
+
 def run_serve_stream(args, emit=True):
     """Serving stream (the serving configuration of many nuclei and bases, scaled by --stream-scale):
     nuclei drawn (seeded) from the three recorded ground states (40S, 116Kr, 162Gd)
@@ -950,6 +985,7 @@ def main():
     ap.add_argument("--no-stream", action="store_true", help="leave the serving-stream object out of the line")
     ap.add_argument("--no-2bc", action="store_true", help="leave the finite-range 2BC field object out of the line")
     ap.add_argument("--tbc-only", action="store_true", help="only the finite-range 2BC field timing (own line)")
+    ap.add_argument("--hfb-only", action="store_true", help="only the HFB reconstruction timing, host and GPU")
     ap.add_argument("--tbc-nsh", type=int, default=NSH, help="finite-range 2BC field: N_sh of the basis")
     ap.add_argument("--no-cpu", action="store_true", help="finite-range 2BC field: skip the CPU oracle timing")
     ap.add_argument("--async-anchors", action="store_true",
@@ -959,7 +995,9 @@ def main():
     args = ap.parse_args()
     global ASYNC_ANCHORS
     ASYNC_ANCHORS = args.async_anchors
-    if args.tbc_only:
+    if args.hfb_only:
+        run_hfb(args)
+    elif args.tbc_only:
         run_tbc(args)
     elif args.config4:
         run_config4(args)

@@ -365,6 +365,40 @@ typedef struct {
 
 int pnfam_gpu_2bc_field(const pnfam_2bc_input_t* in, double* pieces, double* stats);
 
+/*
+ * HFB reconstruction on the GPU (the arithmetic of rebuilding an HFBTHO ground
+ * state from its .hel fields; the particle-number loop stays with the caller).
+ * Host arrays in and out; mesh index ih + il*ngh; states in HFBTHO order.
+ *
+ * pnfam_gpu_hfb_basis: oscillator basis functions on the mesh with the square
+ *   roots of the quadrature weights (gaupol, hfbtho_solver.f90:3463-3671):
+ *   out [4][nt][ngh*ngl] = function, d/dr, d/dz, (r, z) Laplacian part.
+ * pnfam_gpu_hfb_matrices: the HFB matrices h and Delta of every block and isospin
+ *   from the fields (gamdel, hfbtho_solver.f90:5190-5302).  fields [2][11][nghl]:
+ *   per isospin (n, p) v, vhb, vr, vz, vd, vs, vSFIZ, vSZFI, vSFIR, vSRFI, dv;
+ *   y [nghl] = 1/r; xlam, xlap [nb] = Omega -/+ 1/2 of the block; out: per block,
+ *   per isospin, h then Delta, nd x nd row-major.
+ * pnfam_gpu_sym_eigen: eigenvalues (ascending) and eigenvectors (columns) of a
+ *   batch of real symmetric matrices (sizes 1..512, concatenated row-major), by
+ *   cyclic Jacobi on the GPU (one CTA per matrix); replaces hfbdiag's DSYEVR.
+ *   sweeps (may be NULL) [nmat]: Jacobi sweeps used.
+ * pnfam_gpu_hfb_densities: sums of DENSIT (hfbtho_solver.f90:4318-4734) over the
+ *   quasiparticles of each block: W [per block nd x nd row-major] the V matrix with
+ *   the columns of quasiparticles outside the pairing window zero; at finite
+ *   temperature also U (same layout) and f [nt] (thermal occupation per column);
+ *   out [3][nghl] = rho, tau, Laplacian-rho sums before normalisation.
+ */
+int pnfam_gpu_hfb_basis(int ngh, int ngl, const double* xh, const double* wh, const double* xl,
+                        const double* wl, double bz, double bp, int nt, const int* nr, const int* nz,
+                        const int* nl, double* out);
+int pnfam_gpu_hfb_matrices(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
+                           const double* y, const double* xlam, const double* xlap, const double* fields,
+                           double* out);
+int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, double* w, double* v, int* sweeps);
+int pnfam_gpu_hfb_densities(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
+                            const double* y, const double* xlam, const double* xlap, const double* W,
+                            const double* U, const double* f, double* out);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* pnfam_gpu_last_error(void);
 

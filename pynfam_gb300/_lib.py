@@ -18,7 +18,8 @@ EXPORTS = ("pnfam_gpu_init", "pnfam_gpu_set_operator", "pnfam_gpu_solve", "pnfam
            "pnfam_gpu_engine_create", "pnfam_gpu_engine_admit", "pnfam_gpu_engine_launch",
            "pnfam_gpu_engine_finish", "pnfam_gpu_engine_active", "pnfam_gpu_engine_ready", "pnfam_gpu_engine_free",
            "pnfam_gpu_calc_hamiltonian_mixed", "pnfam_gpu_set_occupations", "pnfam_gpu_task_tables",
-           "pnfam_gpu_solve_state", "pnfam_gpu_state_size", "pnfam_gpu_2bc_field")
+           "pnfam_gpu_solve_state", "pnfam_gpu_state_size", "pnfam_gpu_2bc_field", "pnfam_gpu_hfb_basis",
+           "pnfam_gpu_hfb_matrices", "pnfam_gpu_sym_eigen", "pnfam_gpu_hfb_densities")
 
 TASK_TERMS = 4
 TASK_RECORD = 7 + 10 * TASK_TERMS
@@ -117,6 +118,15 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_task_tables.restype = C.c_int
     lib.pnfam_gpu_2bc_field.argtypes = [C.POINTER(TwoBodyInput), dp, dp]
     lib.pnfam_gpu_2bc_field.restype = C.c_int
+    lib.pnfam_gpu_hfb_basis.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, C.c_int, ip, ip, ip,
+                                        dp]
+    lib.pnfam_gpu_hfb_basis.restype = C.c_int
+    lib.pnfam_gpu_hfb_matrices.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp]
+    lib.pnfam_gpu_hfb_matrices.restype = C.c_int
+    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, ip]
+    lib.pnfam_gpu_sym_eigen.restype = C.c_int
+    lib.pnfam_gpu_hfb_densities.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp, dp, dp]
+    lib.pnfam_gpu_hfb_densities.restype = C.c_int
     _lib = lib
     return lib
 

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libpnfam_gb300.so")
 SOURCES = ["pnfam_gpu.cu"]
-DEPS = SOURCES + ["pnfam_kernels.cuh", "tc.cuh", "pair_gemm.cuh", "tbc.cuh"]
+DEPS = SOURCES + ["pnfam_kernels.cuh", "tc.cuh", "pair_gemm.cuh", "tbc.cuh", "hfb.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -9,6 +9,7 @@
 #include "pnfam_kernels.cuh"
 #include "pair_gemm.cuh"
 #include "tbc.cuh"
+#include "hfb.cuh"
 
 #include <cuda_runtime.h>
 
@@ -2742,5 +2743,165 @@ extern "C" int pnfam_gpu_2bc_field(const pnfam_2bc_input_t* in, double* pieces, 
     stats[0] = prep_ms; stats[1] = ms1; stats[2] = ms2;
     stats[3] = v.nt; stats[4] = v.ngroups; stats[5] = (double)(P.pz.size() / 2);
   }
+  return PNFAM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// HFB reconstruction kernels (basis functions, HFB matrices, batched symmetric
+// eigensolver, local densities)
+// ---------------------------------------------------------------------------
+namespace {
+struct HfbBufs {
+  DBuf<double> d[8];
+  DBuf<int> i[4];
+  DBuf<size_t> z[2];
+  DBuf<long long> l[1];
+  ~HfbBufs() {
+    for (auto& b : d) b.release();
+    for (auto& b : i) b.release();
+    for (auto& b : z) b.release();
+    for (auto& b : l) b.release();
+  }
+};
+int grid_for(long long n, int threads) { return (int)std::min<long long>((n + threads - 1) / threads, 152LL * 32); }
+}  // namespace
+
+extern "C" int pnfam_gpu_hfb_basis(int ngh, int ngl, const double* xh, const double* wh, const double* xl,
+                                   const double* wl, double bz, double bp, int nt, const int* nr, const int* nz,
+                                   const int* nl, double* out) {
+  g_err.clear();
+  if (ngh <= 0 || ngl <= 0 || nt <= 0 || !xh || !wh || !xl || !wl || !nr || !nz || !nl || !out || bz <= 0 || bp <= 0)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_hfb_basis: bad arguments");
+  HfbBufs B;
+  const size_t nghl = (size_t)ngh * ngl;
+  CK(upload(B.d[0], xh, ngh)); CK(upload(B.d[1], wh, ngh)); CK(upload(B.d[2], xl, ngl)); CK(upload(B.d[3], wl, ngl));
+  CK(upload(B.i[0], nr, nt)); CK(upload(B.i[1], nz, nt)); CK(upload(B.i[2], nl, nt));
+  CK(dalloc(B.d[4], 4 * nghl * nt));
+  hfbk::BasisView b{ngh, ngl, nt, B.d[0].p, B.d[1].p, B.d[2].p, B.d[3].p, bz, bp, B.i[0].p, B.i[1].p, B.i[2].p, B.d[4].p};
+  hfbk::k_hfb_basis<<<grid_for((long long)nt * nghl, 256), 256>>>(b);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, B.d[4].p, 4 * nghl * nt * sizeof(double), cudaMemcpyDeviceToHost));
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_hfb_matrices(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
+                                      const double* y, const double* xlam, const double* xlap, const double* fields,
+                                      double* out) {
+  g_err.clear();
+  if (nb <= 0 || nghl <= 0 || !block_size || !ns || !basis || !y || !xlam || !xlap || !fields || !out)
+    return fail(PNFAM_EINVAL, "pnfam_gpu_hfb_matrices: bad arguments");
+  std::vector<int> bstart(nb + 1, 0);
+  for (int ib = 0; ib < nb; ++ib) {
+    if (block_size[ib] <= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_hfb_matrices: empty block");
+    bstart[ib + 1] = bstart[ib] + block_size[ib];
+  }
+  const int nt = bstart[nb];
+  std::vector<size_t> moff(2 * (size_t)nb);
+  std::vector<int> items;
+  size_t tot = 0;
+  for (int ib = 0; ib < nb; ++ib) {
+    const int nd = block_size[ib];
+    for (int it = 0; it < 2; ++it) {
+      moff[2 * ib + it] = tot;
+      tot += 2 * (size_t)nd * nd;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j <= i; ++j) items.insert(items.end(), {it, ib, i, j});
+    }
+  }
+  HfbBufs B;
+  CK(upload(B.i[0], bstart.data(), bstart.size()));
+  CK(upload(B.i[1], ns, nt));
+  CK(upload(B.i[2], items.data(), items.size()));
+  CK(upload(B.d[0], basis, 4 * (size_t)nt * nghl));
+  CK(upload(B.d[1], y, nghl));
+  CK(upload(B.d[2], xlam, nb));
+  CK(upload(B.d[3], xlap, nb));
+  CK(upload(B.d[4], fields, 2 * (size_t)hfbk::NFIELD * nghl));
+  CK(upload(B.z[0], moff.data(), moff.size()));
+  CK(dalloc(B.d[5], tot));
+  hfbk::MatView m{nb, nt, nghl, B.i[0].p, B.i[1].p, B.d[0].p, B.d[1].p, B.d[2].p, B.d[3].p, B.d[4].p, B.z[0].p,
+                  B.d[5].p};
+  const int nitems = (int)(items.size() / 4);
+  hfbk::k_hfb_matrices<<<grid_for(nitems, 128), 128>>>(m, B.i[2].p, nitems);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, B.d[5].p, tot * sizeof(double), cudaMemcpyDeviceToHost));
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, double* w, double* v, int* sweeps) {
+  g_err.clear();
+  if (nmat <= 0 || !dims || !a || !w || !v) return fail(PNFAM_EINVAL, "pnfam_gpu_sym_eigen: bad arguments");
+  std::vector<long long> off(nmat + 1, 0);
+  for (int k = 0; k < nmat; ++k) {
+    if (dims[k] <= 0 || dims[k] > hfbk::JAC_MAXN)
+      return fail(PNFAM_EINVAL, "pnfam_gpu_sym_eigen: matrix size outside 1.." + std::to_string(hfbk::JAC_MAXN));
+    off[k + 1] = off[k] + (long long)dims[k] * dims[k];
+  }
+  HfbBufs B;
+  CK(upload(B.d[0], a, (size_t)off[nmat]));
+  CK(dalloc(B.d[1], (size_t)off[nmat]));
+  CK(upload(B.l[0], off.data(), off.size()));
+  CK(upload(B.i[0], dims, nmat));
+  CK(dalloc(B.i[1], nmat));
+  hfbk::k_jacobi<<<nmat, hfbk::JAC_THREADS>>>(B.d[0].p, B.d[1].p, B.l[0].p, B.i[0].p, B.i[1].p);
+  CK(cudaGetLastError());
+  std::vector<double> ha((size_t)off[nmat]), hv((size_t)off[nmat]);
+  std::vector<int> st(nmat);
+  CK(cudaMemcpy(ha.data(), B.d[0].p, ha.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hv.data(), B.d[1].p, hv.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(st.data(), B.i[1].p, nmat * sizeof(int), cudaMemcpyDeviceToHost));
+  // eigenvalues ascending, eigenvectors as columns in the same order
+  long long wo = 0;
+  for (int k = 0; k < nmat; ++k) {
+    const int n = dims[k];
+    if (st[k] < 0) return fail(PNFAM_ENONFINITE, "pnfam_gpu_sym_eigen: Jacobi did not converge for matrix " +
+                                                 std::to_string(k));
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    const double* A = ha.data() + off[k];
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A[(size_t)x * n + x] < A[(size_t)y * n + y]; });
+    for (int c = 0; c < n; ++c) {
+      w[wo + c] = A[(size_t)ord[c] * n + ord[c]];
+      for (int i = 0; i < n; ++i) v[off[k] + (size_t)i * n + c] = hv[off[k] + (size_t)i * n + ord[c]];
+    }
+    wo += n;
+    if (sweeps) sweeps[k] = st[k];
+  }
+  return PNFAM_OK;
+}
+
+extern "C" int pnfam_gpu_hfb_densities(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
+                                       const double* y, const double* xlam, const double* xlap, const double* W,
+                                       const double* U, const double* f, double* out) {
+  g_err.clear();
+  if (nb <= 0 || nghl <= 0 || !block_size || !ns || !basis || !y || !xlam || !xlap || !W || !out || (!U) != (!f))
+    return fail(PNFAM_EINVAL, "pnfam_gpu_hfb_densities: bad arguments");
+  std::vector<int> bstart(nb + 1, 0);
+  std::vector<size_t> woff(nb);
+  size_t tot = 0;
+  for (int ib = 0; ib < nb; ++ib) {
+    if (block_size[ib] <= 0) return fail(PNFAM_EINVAL, "pnfam_gpu_hfb_densities: empty block");
+    bstart[ib + 1] = bstart[ib] + block_size[ib];
+    woff[ib] = tot;
+    tot += (size_t)block_size[ib] * block_size[ib];
+  }
+  const int nt = bstart[nb];
+  HfbBufs B;
+  CK(upload(B.i[0], bstart.data(), bstart.size()));
+  CK(upload(B.i[1], ns, nt));
+  CK(upload(B.d[0], basis, 4 * (size_t)nt * nghl));
+  CK(upload(B.d[1], y, nghl));
+  CK(upload(B.d[2], xlam, nb));
+  CK(upload(B.d[3], xlap, nb));
+  CK(upload(B.d[4], W, tot));
+  if (U) { CK(upload(B.d[5], U, tot)); CK(upload(B.d[6], f, nt)); }
+  CK(upload(B.z[0], woff.data(), woff.size()));
+  CK(dalloc(B.d[7], 3 * (size_t)nghl));
+  CK(cudaMemset(B.d[7].p, 0, 3 * (size_t)nghl * sizeof(double)));
+  hfbk::DensView d{nb, nt, nghl, B.i[0].p, B.i[1].p, B.d[0].p, B.d[1].p, B.d[2].p, B.d[3].p, B.z[0].p, B.d[4].p,
+                   U ? B.d[5].p : nullptr, U ? B.d[6].p : nullptr, B.d[7].p};
+  hfbk::k_hfb_densities<<<grid_for((long long)nb * nghl, 128), 128>>>(d);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, B.d[7].p, 3 * (size_t)nghl * sizeof(double), cudaMemcpyDeviceToHost));
   return PNFAM_OK;
 }

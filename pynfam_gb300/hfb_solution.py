@@ -1,6 +1,7 @@
 """HFB ground state for pnFAM, rebuilt from an HFBTHO ``.hel`` file.
 
-This is the input side of the solver (it runs once per nucleus, on the host).
+This is the input side of the solver (it runs once per nucleus, on the host, or
+with the arithmetic of steps 1-4 on the GPU: ``hfb_device``).
 It reproduces what the reference obtains by re-running HFBTHO for zero
 iterations (pnfam: hfbtho_interface.f90:20-226 -> HFBTHO_DFT_SOLVER) and then
 reshaping the result for the FAM (pnfam: hfbtho_solution.f90:137-459):
@@ -99,7 +100,12 @@ class MeshBasis:
     xlap: np.ndarray   # per block: Lambda of spin-down states (Omega+1/2)
 
 
-def build_mesh_basis(h: HelData) -> MeshBasis:
+def build_mesh_basis(h: HelData, device: bool = False) -> MeshBasis:
+    """The basis on the mesh; ``device``: the functions by the GPU kernel."""
+    if device:
+        from . import hfb_device
+        qhla, fi1r, fi1z, fi2d = hfb_device.basis_functions(h)
+        return _mesh_basis_from(h, qhla, fi1r, fi1z, fi2d)
     ngh, ngl = h.ngh, h.ngl
     nzm, nrm, nlm = int(h.nz.max()), int(h.nr.max()), int(h.nl.max())
     qh, qh1 = _hermite_functions(h.xh, h.wh, nzm)
@@ -130,6 +136,19 @@ def build_mesh_basis(h: HelData) -> MeshBasis:
         cnraa = nra + nra + nla + 1
         fi2d[ja] = ((xh * xh - cnzaa) / (bz * bz)
                     + 4.0 * (0.25 - cnraa * v2 + nla * nla * v4) * xl / (bp * bp)) * q
+    return _mesh_basis_from(h, qhla, fi1r, fi1z, fi2d)
+
+
+def _mesh_basis_from(h: HelData, qhla, fi1r, fi1z, fi2d) -> MeshBasis:
+    """MeshBasis of the basis functions with 1/r, z, the inverse weights and the
+    blocks' Lambda values."""
+    ngh, ngl = h.ngh, h.ngl
+    bz, bp = h.bz, h.bp
+    xh = np.tile(h.xh, ngl)
+    xl = np.repeat(h.xl, ngh)
+    wh = np.tile(h.wh, ngl)
+    wl = np.repeat(h.wl, ngh)
+    y = 1.0 / (np.sqrt(xl) * bp)
     wdcor = np.pi * wh * wl * bz * bp * bp
     # Lambda of the spin-up / spin-down members of each block, from Omega
     nb = len(h.ID)
@@ -274,7 +293,11 @@ class QPSolution:
     fwin: list = None   # finite temperature: per block, f of the active quasiparticles (DENSIT)
 
 
-def diagonalise(h: HelData, hd, it: str, tz: float, temper: float = 0.0) -> QPSolution:
+def _eigh_host(mats):
+    return [np.linalg.eigh(m) for m in mats]
+
+
+def diagonalise(h: HelData, hd, it: str, tz: float, temper: float = 0.0, eigh=None) -> QPSolution:
     """hfbdiag(it, icanon) restricted to what pnFAM reads (no blocking); at
     temperature T the particle number of each pairing-window state is
     2 v^2 + 2 (1 - 2 v^2) f(E) (hfbtho_solver.f90:1750-1774)."""
@@ -296,6 +319,7 @@ def diagonalise(h: HelData, hd, it: str, tz: float, temper: float = 0.0) -> QPSo
         erhfb, drhfb = [], []
         eig = []
         nsum = 0.0
+        mats = []
         for (hm, dm) in blocks:
             nd = hm.shape[0]
             M = np.empty((2 * nd, 2 * nd))
@@ -303,7 +327,9 @@ def diagonalise(h: HelData, hd, it: str, tz: float, temper: float = 0.0) -> QPSo
             M[nd:, nd:] = -hm + al * np.eye(nd)
             M[nd:, :nd] = dm
             M[:nd, nd:] = dm
-            w, vec = np.linalg.eigh(M)
+            mats.append(M)
+        for (hm, dm), (w, vec) in zip(blocks, (eigh or _eigh_host)(mats)):
+            nd = hm.shape[0]
             Eq = w[nd:]
             Ub = vec[:nd, nd:]
             Vb = vec[nd:, nd:]
@@ -482,11 +508,16 @@ class HFBSolution:
         return out
 
 
-def load_hfb_solution(path) -> HFBSolution:
+def load_hfb_solution(path, device: bool = None) -> HFBSolution:
     """get_raw_hfb_solution (hfbtho_solution.f90:137-395) from a ``.hel`` file
     (a path, or an already decoded :class:`HelData`).  A finite-temperature
     solution is rebuilt with HFBTHO's thermal particle number and densities and
-    carries the quasiparticle occupations of the statistical FAM."""
+    carries the quasiparticle occupations of the statistical FAM.  ``device``: the
+    basis functions, HFB matrices, eigensolves and densities on the GPU
+    (``hfb_device``); default from PNFAM_GB300_HFB_DEVICE=1, else the host."""
+    if device is None:
+        import os
+        device = os.environ.get("PNFAM_GB300_HFB_DEVICE", "0") == "1"
     h = path if isinstance(path, HelData) else read_hel(path)
     if int(h.N) % 2 or int(h.Z) % 2:
         # an odd nucleus is an HFBTHO solution with a blocked quasiparticle, whose
@@ -495,11 +526,18 @@ def load_hfb_solution(path) -> HFBSolution:
                          "is not supported (pass EFA occupations from pynfam_gb300.statistics to GPUSolver to run "
                          "the statistical FAM on an even-even basis)")
     temper = h.temperature if h.set_temperature else 0.0
-    mb = build_mesh_basis(h)
-    hd = hfb_matrices(h, mb)
-    qpn = diagonalise(h, hd, "n", float(h.N), temper)
-    qpp = diagonalise(h, hd, "p", float(h.Z), temper)
-    hfb = assemble(h, mb, qpn, qpp)
+    if device:
+        from . import hfb_device as dv
+        mb = build_mesh_basis(h, device=True)
+        hd = dv.hfb_matrices(h, mb)
+        eigh, dens = dv.eigh_batch, dv.local_densities
+    else:
+        mb = build_mesh_basis(h)
+        hd = hfb_matrices(h, mb)
+        eigh, dens = None, None
+    qpn = diagonalise(h, hd, "n", float(h.N), temper, eigh)
+    qpp = diagonalise(h, hd, "p", float(h.Z), temper, eigh)
+    hfb = assemble(h, mb, qpn, qpp, dens)
     if temper > 1e-12:
         # the statistical FAM's occupations from the final quasiparticle energies,
         # 0 above the pairing window (hfbtho_solution.f90:376-389, 426, 446)
@@ -509,11 +547,12 @@ def load_hfb_solution(path) -> HFBSolution:
     return hfb
 
 
-def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution) -> HFBSolution:
+def assemble(h: HelData, mb: MeshBasis, qpn: QPSolution, qpp: QPSolution, densities=None) -> HFBSolution:
     """The pnFAM view of Omega>0 quasiparticles (hfbtho_solution.f90:164-459): TR
     doubling, spin sort inside each block, pairing window."""
-    rho_n, tau_n, d2rho_n = local_densities(h, mb, qpn, float(h.N))
-    rho_p, tau_p, d2rho_p = local_densities(h, mb, qpp, float(h.Z))
+    dens = densities or local_densities
+    rho_n, tau_n, d2rho_n = dens(h, mb, qpn, float(h.N))
+    rho_p, tau_p, d2rho_p = dens(h, mb, qpp, float(h.Z))
 
     nbh = len(h.ID)
     nb = 2 * nbh

@@ -1,0 +1,170 @@
+"""The HFB reconstruction with its arithmetic on the GPU (basis functions, HFB
+matrices, batched Jacobi eigensolves inside the particle-number loop, DENSIT).
+
+CPU: the kernels' per-item functions, run serially on the host by a test harness
+built from the same header (tests/hfb_host_check.cpp) behind the library's entry
+points, against the host (numpy) reconstruction, which is pinned to HFBTHO's
+recorded output and to the reference's recorded FAM runs; and the FAM oracle on
+the rebuilt ground state against a recorded point.  GPU: the same through the
+library.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+@pytest.fixture(scope="module")
+def harness_so(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    so = str(tmp_path_factory.mktemp("hfb") / "hfb_host.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                    os.path.join(ROOT, "tests", "hfb_host_check.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    dp, ip, C = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes
+    lib.pnfam_gpu_hfb_basis.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, C.c_int, ip, ip,
+                                        ip, dp]
+    lib.pnfam_gpu_hfb_matrices.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp]
+    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, ip]
+    lib.pnfam_gpu_hfb_densities.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp, dp, dp]
+    lib.pnfam_gpu_last_error.restype = C.c_char_p
+    return lib
+
+
+@pytest.fixture
+def harness(harness_so, monkeypatch):
+    from pynfam_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", harness_so)
+    monkeypatch.setattr(_lib, "load", lambda *a: harness_so)
+    return harness_so
+
+
+def _hel(case, nsh=None):
+    from pynfam_gb300.hel import read_hel
+    from pynfam_gb300.synthetic import extend_basis
+    h = read_hel(os.path.join(GOLD, f"{case}.hel"))
+    return extend_basis(h, nsh) if nsh else h
+
+
+def _compare(a, b):
+    """The device-path solution b against the host one a: quasiparticle energies,
+    local densities, the density matrices rk (invariant under the eigenvector phases
+    and rotations inside degenerate subspaces), basis functions."""
+    assert np.abs(a.En - b.En).max() < 1e-10 and np.abs(a.Ep - b.Ep).max() < 1e-10
+    for x, y in ((a.rho_n, b.rho_n), (a.rho_p, b.rho_p), (a.tau_n, b.tau_n), (a.tau_p, b.tau_p),
+                 (a.d2rho_n, b.d2rho_n), (a.d2rho_p, b.d2rho_p)):
+        assert np.abs(x - y).max() <= 1e-11 * np.abs(x).max()
+    for it in ("n", "p"):
+        for x, y in zip(a.density_matrices(it), b.density_matrices(it)):
+            assert np.abs(x - y).max() < 1e-11
+    assert np.abs(a.wf - b.wf).max() < 1e-13 and np.abs(a.wfd2_all - b.wfd2_all).max() < 1e-11
+
+
+@pytest.mark.parametrize("case,nsh", [("S40", None), ("Gd162", None), ("Kr116", None), ("Gd162", 10)])
+def test_kernel_arithmetic_rebuilds_the_ground_state(case, nsh, harness):
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    h = _hel(case, nsh)
+    _compare(load_hfb_solution(h, device=False), load_hfb_solution(h, device=True))
+
+
+def test_kernel_arithmetic_ground_state_reproduces_recorded_fam_point(harness):
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_cases import golden, namelist_for
+    from oracle.fam_oracle import FAMOracle
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    from pynfam_gb300.pnfam_setup import setup_case
+    pt = golden("S40")["operators"]["GT-K0"][0]
+    c = setup_case(namelist_for("S40", pt), None, hfb=load_hfb_solution(os.path.join(GOLD, "S40.hel"), device=True))
+    s = c.nml["solver"]
+    r = FAMOracle(c.hfb, c.couplings, c.F, c.G, quench=c.quench).solve(
+        c.omega, max_iter=s["max_iter"], eps=s["convergence_epsilon"], broyden_m=s["broyden_history_size"])
+    want = pt["result"]["Strength"]
+    assert r.iter_conv == pt["converged"]
+    assert abs(r.re_str[0] - want[0]) <= 1e-12 * abs(want[0]) and abs(r.im_str[0] - want[1]) <= 1e-11 * abs(want[1])
+
+
+def _eigen_cases(rng):
+    mats = []
+    for n in (1, 2, 3, 7, 40, 81):
+        a = rng.standard_normal((n, n))
+        mats.append(a + a.T)
+    # repeated eigenvalues (the time-reversal and spin degeneracies of HFB blocks)
+    q, _ = np.linalg.qr(rng.standard_normal((30, 30)))
+    d = np.repeat(rng.standard_normal(10), 3)
+    mats.append((q * d) @ q.T)
+    return mats
+
+
+def _check_eigen(mats, res):
+    for a, (w, v) in zip(mats, res):
+        n = a.shape[0]
+        assert np.all(np.diff(w) >= 0)
+        np.testing.assert_allclose(w, np.linalg.eigvalsh(a), atol=1e-12 * max(1.0, np.abs(a).max()) * n)
+        assert np.abs(v.T @ v - np.eye(n)).max() < 1e-12
+        assert np.abs(a @ v - v * w).max() < 1e-12 * max(1.0, np.abs(a).max()) * n
+
+
+def test_jacobi_arithmetic(harness):
+    from pynfam_gb300 import hfb_device
+    mats = _eigen_cases(np.random.default_rng(5))
+    _check_eigen(mats, hfb_device.eigh_batch(mats))
+
+
+# ---------------------------------------------------------------------------------
+# the GPU
+# ---------------------------------------------------------------------------------
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,nsh", [("S40", None), ("Gd162", None), ("Kr116", None), ("Gd162", 10), ("Gd162", 16)])
+def test_gpu_rebuilds_the_ground_state(case, nsh):
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    h = _hel(case, nsh)
+    _compare(load_hfb_solution(h, device=False), load_hfb_solution(h, device=True))
+
+
+@pytest.mark.gpu
+def test_gpu_jacobi():
+    from pynfam_gb300 import hfb_device
+    rng = np.random.default_rng(7)
+    mats = _eigen_cases(rng)
+    for n in (162, 242, 512):
+        a = rng.standard_normal((n, n))
+        mats.append(a + a.T)
+    _check_eigen(mats, hfb_device.eigh_batch(mats))
+
+
+@pytest.mark.gpu
+def test_gpu_ground_state_reproduces_recorded_contour():
+    """The 40S GT K=0 contour on the GPU solver from the ground state rebuilt on the
+    GPU: every recorded strength within 1e-6, the iteration counts within 2."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_cases import golden, namelist_for
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    from pynfam_gb300.pnfam_setup import setup_case
+    from pynfam_gb300.solver import GPUSolver
+    pts = golden("S40")["operators"]["GT-K0"]
+    c = setup_case(namelist_for("S40", pts[0]), None,
+                   hfb=load_hfb_solution(os.path.join(GOLD, "S40.hel"), device=True))
+    s = c.nml["solver"]
+    gpu = GPUSolver(c.hfb, c.couplings)
+    try:
+        gpu.set_operator(c.F, c.G)
+        omegas = [complex(p["namelist"]["real_eqrpa"], p["namelist"]["imag_eqrpa"]) for p in pts]
+        r = gpu.solve(omegas, max_iter=s["max_iter"], eps=s["convergence_epsilon"],
+                      broyden_m=s["broyden_history_size"], quench=c.quench)
+    finally:
+        gpu.close()
+    for i, p in enumerate(pts):
+        want = p["result"]["Strength"]
+        assert abs(r.re_S[i, 0] - want[0]) <= 1e-6 * abs(want[0]), i
+        assert abs(r.im_S[i, 0] - want[1]) <= 1e-6 * abs(want[1]), i
+        assert abs(int(r.iters[i]) - int(p["converged"])) <= 2, (i, r.iters[i], p["converged"])
