@@ -144,10 +144,12 @@ def test_gpu_jacobi():
 @pytest.mark.gpu
 def test_gpu_ground_state_reproduces_recorded_contour():
     """The 40S GT K=0 contour on the GPU solver from the ground state rebuilt on the
-    GPU: every recorded strength within 1e-6, the iteration counts within 2."""
+    GPU: every recorded strength within 1e-6, the iteration counts within the window
+    of the recorded step (exact where si falls through epsilon decisively, wider
+    where it lingers near the threshold, as in the GPU parity tests)."""
     import sys
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from golden_cases import golden, namelist_for
+    from golden_cases import count_window, golden, namelist_for, oracle_counts
     from pynfam_gb300.hfb_solution import load_hfb_solution
     from pynfam_gb300.pnfam_setup import setup_case
     from pynfam_gb300.solver import GPUSolver
@@ -163,8 +165,10 @@ def test_gpu_ground_state_reproduces_recorded_contour():
                       broyden_m=s["broyden_history_size"], quench=c.quench)
     finally:
         gpu.close()
+    counts = oracle_counts()
     for i, p in enumerate(pts):
         want = p["result"]["Strength"]
         assert abs(r.re_S[i, 0] - want[0]) <= 1e-6 * abs(want[0]), i
         assert abs(r.im_S[i, 0] - want[1]) <= 1e-6 * abs(want[1]), i
-        assert abs(int(r.iters[i]) - int(p["converged"])) <= 2, (i, r.iters[i], p["converged"])
+        n, slack = count_window(p, {"near": counts["near"], "point": counts["counts"]["S40"]["GT-K0"][i]})
+        assert abs(int(r.iters[i]) - n) <= slack, (i, r.iters[i], n, p["converged"], slack)
