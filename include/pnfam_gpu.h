@@ -381,7 +381,10 @@ int pnfam_gpu_2bc_field(const pnfam_2bc_input_t* in, double* pieces, double* sta
  * pnfam_gpu_sym_eigen: eigenvalues (ascending) and eigenvectors (columns) of a
  *   batch of real symmetric matrices (sizes 1..512, concatenated row-major), by
  *   cyclic Jacobi on the GPU (one CTA per matrix); replaces hfbdiag's DSYEVR.
- *   sweeps (may be NULL) [nmat]: Jacobi sweeps used.
+ *   v0 (may be NULL): starting orthogonal matrices, same layout (the eigenvectors
+ *   of nearby matrices, e.g. the previous step of the particle-number loop): the
+ *   rotations then start from v0^T a v0.  sweeps (may be NULL) [nmat]: Jacobi
+ *   sweeps used.
  * pnfam_gpu_hfb_densities: sums of DENSIT (hfbtho_solver.f90:4318-4734) over the
  *   quasiparticles of each block: W [per block nd x nd row-major] the V matrix with
  *   the columns of quasiparticles outside the pairing window zero; at finite
@@ -394,7 +397,8 @@ int pnfam_gpu_hfb_basis(int ngh, int ngl, const double* xh, const double* wh, co
 int pnfam_gpu_hfb_matrices(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
                            const double* y, const double* xlam, const double* xlap, const double* fields,
                            double* out);
-int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, double* w, double* v, int* sweeps);
+int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, const double* v0, double* w, double* v,
+                        int* sweeps);
 int pnfam_gpu_hfb_densities(int nb, const int* block_size, int nghl, const int* ns, const double* basis,
                             const double* y, const double* xlam, const double* xlap, const double* W,
                             const double* U, const double* f, double* out);

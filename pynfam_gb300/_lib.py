@@ -123,7 +123,7 @@ def load(path: str = LIBPATH):
     lib.pnfam_gpu_hfb_basis.restype = C.c_int
     lib.pnfam_gpu_hfb_matrices.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp]
     lib.pnfam_gpu_hfb_matrices.restype = C.c_int
-    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, ip]
+    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, dp, ip]
     lib.pnfam_gpu_sym_eigen.restype = C.c_int
     lib.pnfam_gpu_hfb_densities.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp, dp, dp]
     lib.pnfam_gpu_hfb_densities.restype = C.c_int

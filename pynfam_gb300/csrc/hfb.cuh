@@ -200,6 +200,7 @@ constexpr double JAC_TOL = 1e-15;   // off-diagonal Frobenius norm / Frobenius n
 #ifdef __CUDACC__
 constexpr int JAC_THREADS = 256;
 constexpr int JAC_MAXN = 512;
+constexpr int JAC_SMEM_N = 164;     // matrices up to this size are rotated in shared memory (+8 KB static)
 
 __global__ void k_hfb_basis(BasisView b) {
   const long long total = (long long)b.nt * b.ngh * b.ngl;
@@ -213,20 +214,56 @@ __global__ void k_hfb_matrices(MatView m, const int* items, int nitems) {
     matrix_item(m, items[4 * i], items[4 * i + 1], items[4 * i + 2], items[4 * i + 3]);
 }
 
-// one CTA per matrix: A (row-major, overwritten by its eigenvalues on the diagonal),
-// V <- eigenvectors (columns); status[mat] = sweeps used, or -1 if not converged
-__global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double* A, double* V, const long long* off, const int* dim,
-                                                       int* status) {
+// one CTA per matrix: A (row-major; its diagonal ends as the eigenvalues), V <- the
+// eigenvectors (columns); status[mat] = sweeps used, or -1 if not converged.
+// V0 (optional): starting vectors (the previous eigenvectors of a matrix that has
+// changed a little): the rotations start from V0^T A V0 with V = V0.  smem_n > 0: the
+// matrices (all of size <= smem_n) are worked on in dynamic shared memory.
+__global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double* A, double* V, const double* V0, const long long* off,
+                                                       const int* dim, int* status, int smem_n) {
+  extern __shared__ double sA[];
   __shared__ double cs_c[JAC_MAXN / 2], cs_s[JAC_MAXN / 2];
   __shared__ int pp[JAC_MAXN / 2], qq[JAC_MAXN / 2];
   __shared__ double red[JAC_THREADS];
   __shared__ double s_norm;
   __shared__ int s_done;
   const int mat = blockIdx.x, n = dim[mat];
-  double* a = A + off[mat];
+  double* ag = A + off[mat];
+  double* a = smem_n > 0 ? sA : ag;
   double* v = V + off[mat];
   const int m = n + (n & 1);
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x) v[i] = (i / n == i % n) ? 1.0 : 0.0;
+  if (smem_n > 0)
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) a[i] = ag[i];
+  __syncthreads();
+  if (V0) {
+    const double* v0 = V0 + off[mat];
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {      // T = A V0 (in V)
+      const int i = idx / n, j = idx % n;
+      double t = 0.0;
+      for (int k = 0; k < n; ++k) t += a[(size_t)i * n + k] * v0[(size_t)k * n + j];
+      v[idx] = t;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {      // A = V0^T T
+      const int i = idx / n, j = idx % n;
+      double t = 0.0;
+      for (int k = 0; k < n; ++k) t += v0[(size_t)k * n + i] * v[(size_t)k * n + j];
+      a[idx] = t;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int i = idx / n, j = idx % n;
+      if (i < j) {
+        const double x = 0.5 * (a[(size_t)i * n + j] + a[(size_t)j * n + i]);
+        a[(size_t)i * n + j] = x;
+        a[(size_t)j * n + i] = x;
+      }
+    }
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) v[i] = v0[i];
+  } else {
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) v[i] = (i / n == i % n) ? 1.0 : 0.0;
+  }
+  __syncthreads();
   // Frobenius norm of A (unchanged by the rotations)
   double s = 0.0;
   for (int i = threadIdx.x; i < n * n; i += blockDim.x) s += a[i] * a[i];
@@ -278,6 +315,8 @@ __global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double* A, double* V, co
       __syncthreads();
     }
   }
+  if (smem_n > 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) ag[(size_t)i * n + i] = a[(size_t)i * n + i];
   if (threadIdx.x == 0) status[mat] = (n <= 1 || s_done) ? sweep : -1;
 }
 #endif

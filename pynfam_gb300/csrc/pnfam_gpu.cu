@@ -2828,22 +2828,30 @@ extern "C" int pnfam_gpu_hfb_matrices(int nb, const int* block_size, int nghl, c
   return PNFAM_OK;
 }
 
-extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, double* w, double* v, int* sweeps) {
+extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, const double* v0, double* w, double* v,
+                                   int* sweeps) {
   g_err.clear();
   if (nmat <= 0 || !dims || !a || !w || !v) return fail(PNFAM_EINVAL, "pnfam_gpu_sym_eigen: bad arguments");
   std::vector<long long> off(nmat + 1, 0);
+  int maxn = 0;
   for (int k = 0; k < nmat; ++k) {
     if (dims[k] <= 0 || dims[k] > hfbk::JAC_MAXN)
       return fail(PNFAM_EINVAL, "pnfam_gpu_sym_eigen: matrix size outside 1.." + std::to_string(hfbk::JAC_MAXN));
     off[k + 1] = off[k] + (long long)dims[k] * dims[k];
+    maxn = std::max(maxn, dims[k]);
   }
   HfbBufs B;
   CK(upload(B.d[0], a, (size_t)off[nmat]));
   CK(dalloc(B.d[1], (size_t)off[nmat]));
+  if (v0) CK(upload(B.d[2], v0, (size_t)off[nmat]));
   CK(upload(B.l[0], off.data(), off.size()));
   CK(upload(B.i[0], dims, nmat));
   CK(dalloc(B.i[1], nmat));
-  hfbk::k_jacobi<<<nmat, hfbk::JAC_THREADS>>>(B.d[0].p, B.d[1].p, B.l[0].p, B.i[0].p, B.i[1].p);
+  const int smem_n = maxn <= hfbk::JAC_SMEM_N ? maxn : 0;
+  const size_t smem = (size_t)smem_n * smem_n * sizeof(double);
+  CK(cudaFuncSetAttribute(hfbk::k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  hfbk::k_jacobi<<<nmat, hfbk::JAC_THREADS, smem>>>(B.d[0].p, B.d[1].p, v0 ? B.d[2].p : nullptr, B.l[0].p, B.i[0].p,
+                                                   B.i[1].p, smem_n);
   CK(cudaGetLastError());
   std::vector<double> ha((size_t)off[nmat]), hv((size_t)off[nmat]);
   std::vector<int> st(nmat);

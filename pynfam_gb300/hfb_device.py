@@ -69,17 +69,21 @@ def hfb_matrices(h, mb):
     return res
 
 
-def eigh_batch(mats):
+def eigh_batch(mats, start=None, sweeps=None):
     """[(w ascending, eigenvectors as columns)] of real symmetric matrices, one GPU
-    launch (cyclic Jacobi)."""
+    launch (cyclic Jacobi).  ``start``: orthogonal starting matrices (eigenvectors of
+    nearby matrices); ``sweeps``: a list that receives the Jacobi sweeps used."""
     lib = _lib.load()
     dims = _i32([m.shape[0] for m in mats])
     a = _f64(np.concatenate([np.asarray(m, dtype=np.float64).reshape(-1) for m in mats]))
+    v0 = _f64(np.concatenate([np.asarray(m, dtype=np.float64).reshape(-1) for m in start])) if start else None
     w = np.empty(int(dims.sum()))
     v = np.empty(a.size)
     sw = np.zeros(len(mats), dtype=np.int32)
-    _lib.check(lib.pnfam_gpu_sym_eigen(len(mats), _lib.iptr(dims), _lib.dptr(a), _lib.dptr(w), _lib.dptr(v),
-                                       _lib.iptr(sw)))
+    _lib.check(lib.pnfam_gpu_sym_eigen(len(mats), _lib.iptr(dims), _lib.dptr(a), _lib.dptr(v0) if start else None,
+                                       _lib.dptr(w), _lib.dptr(v), _lib.iptr(sw)))
+    if sweeps is not None:
+        sweeps.extend(int(x) for x in sw)
     out, ow, ov = [], 0, 0
     for n in dims:
         n = int(n)
@@ -87,6 +91,20 @@ def eigh_batch(mats):
         ow += n
         ov += n * n
     return out
+
+
+def eigh_chain():
+    """An eigensolver for the steps of one particle-number loop: every call after the
+    first starts from the eigenvectors of the previous call (the matrices change only
+    by the shift of the Fermi energy), which cuts the Jacobi sweeps."""
+    prev = {}
+
+    def eigh(mats):
+        key = tuple(m.shape[0] for m in mats)
+        res = eigh_batch(mats, prev.get(key))
+        prev[key] = [v for _, v in res]
+        return res
+    return eigh
 
 
 def local_densities(h, mb, qp, tz):

@@ -535,8 +535,8 @@ def load_hfb_solution(path, device: bool = None) -> HFBSolution:
         mb = build_mesh_basis(h)
         hd = hfb_matrices(h, mb)
         eigh, dens = None, None
-    qpn = diagonalise(h, hd, "n", float(h.N), temper, eigh)
-    qpp = diagonalise(h, hd, "p", float(h.Z), temper, eigh)
+    qpn = diagonalise(h, hd, "n", float(h.N), temper, eigh and dv.eigh_chain())
+    qpp = diagonalise(h, hd, "p", float(h.Z), temper, eigh and dv.eigh_chain())
     hfb = assemble(h, mb, qpn, qpp, dens)
     if temper > 1e-12:
         # the statistical FAM's occupations from the final quasiparticle energies,

@@ -34,12 +34,37 @@ extern "C" int pnfam_gpu_hfb_matrices(int nb, const int* block_size, int nghl, c
   return 0;
 }
 
-extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, double* w, double* v, int* sweeps) {
+extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, const double* v0, double* w, double* v,
+                                   int* sweeps) {
   long long off = 0, wo = 0;
   for (int k = 0; k < nmat; ++k) {
     const int n = dims[k], m = n + (n & 1);
     std::vector<double> A(a + off, a + off + (size_t)n * n), V((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+    if (v0) {
+      // the kernel's start: T = A V0, A = V0^T T, symmetrised, V = V0
+      const double* q0 = v0 + off;
+      std::vector<double> T((size_t)n * n);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0.0;
+          for (int kk = 0; kk < n; ++kk) t += A[(size_t)i * n + kk] * q0[(size_t)kk * n + j];
+          T[(size_t)i * n + j] = t;
+        }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0.0;
+          for (int kk = 0; kk < n; ++kk) t += q0[(size_t)kk * n + i] * T[(size_t)kk * n + j];
+          A[(size_t)i * n + j] = t;
+        }
+      for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+          const double x = 0.5 * (A[(size_t)i * n + j] + A[(size_t)j * n + i]);
+          A[(size_t)i * n + j] = A[(size_t)j * n + i] = x;
+        }
+      for (size_t i = 0; i < (size_t)n * n; ++i) V[i] = q0[i];
+    } else {
+      for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+    }
     double nrm = 0.0;
     for (double x : A) nrm += x * x;
     nrm = std::sqrt(nrm);

@@ -33,7 +33,7 @@ def harness_so(tmp_path_factory):
     lib.pnfam_gpu_hfb_basis.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, C.c_int, ip, ip,
                                         ip, dp]
     lib.pnfam_gpu_hfb_matrices.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp]
-    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, ip]
+    lib.pnfam_gpu_sym_eigen.argtypes = [C.c_int, ip, dp, dp, dp, dp, ip]
     lib.pnfam_gpu_hfb_densities.argtypes = [C.c_int, ip, C.c_int, ip, dp, dp, dp, dp, dp, dp, dp, dp]
     lib.pnfam_gpu_last_error.restype = C.c_char_p
     return lib
