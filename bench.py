@@ -689,15 +689,19 @@ def run_hfb(args, emit=True):
     load_hfb_solution(read_hel(HEL), device=True)
     for nsh in (16, 20):
         h = extend_basis(read_hel(HEL), nsh)
+        from pynfam_gb300 import hfb_device
         t = {}
         sol = {}
         for dev in (False, True):
+            for k in hfb_device.TIMES:
+                hfb_device.TIMES[k] = 0
             t0 = time.perf_counter()
             sol[dev] = load_hfb_solution(h, device=dev)
             t[dev] = time.perf_counter() - t0
+        steps = dict(hfb_device.TIMES)
         a, b = sol[False], sol[True]
         rows.append({"nsh": nsh, "states": int(len(h.nr)), "blocks": int(len(h.ID)), "host_s": t[False],
-                     "device_s": t[True],
+                     "device_s": t[True], "device_calls_s": steps,
                      "max_dE_MeV": float(max(np.abs(a.En - b.En).max(), np.abs(a.Ep - b.Ep).max())),
                      "max_drho_rel": float(max(np.abs(a.rho_n - b.rho_n).max() / np.abs(a.rho_n).max(),
                                                np.abs(a.rho_p - b.rho_p).max() / np.abs(a.rho_p).max()))})

@@ -2840,7 +2840,13 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
     off[k + 1] = off[k] + (long long)dims[k] * dims[k];
     maxn = std::max(maxn, dims[k]);
   }
-  HfbBufs B;
+  // device buffers kept for the process (grow-only): the particle-number loop calls
+  // this tens of times per ground state
+  static std::mutex mu;
+  static HfbBufs* pool = new HfbBufs;
+  static int smem_set = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  HfbBufs& B = *pool;
   CK(upload(B.d[0], a, (size_t)off[nmat]));
   CK(dalloc(B.d[1], (size_t)off[nmat]));
   if (v0) CK(upload(B.d[2], v0, (size_t)off[nmat]));
@@ -2849,7 +2855,11 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
   CK(dalloc(B.i[1], nmat));
   const int smem_n = maxn <= hfbk::JAC_SMEM_N ? maxn : 0;
   const size_t smem = (size_t)smem_n * smem_n * sizeof(double);
-  CK(cudaFuncSetAttribute(hfbk::k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (!smem_set) {
+    CK(cudaFuncSetAttribute(hfbk::k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)((size_t)hfbk::JAC_SMEM_N * hfbk::JAC_SMEM_N * sizeof(double))));
+    smem_set = 1;
+  }
   hfbk::k_jacobi<<<nmat, hfbk::JAC_THREADS, smem>>>(B.d[0].p, B.d[1].p, v0 ? B.d[2].p : nullptr, B.l[0].p, B.i[0].p,
                                                    B.i[1].p, smem_n);
   CK(cudaGetLastError());

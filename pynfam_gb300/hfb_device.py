@@ -12,10 +12,21 @@ library or a GPU the calls raise.
 from __future__ import annotations
 
 import ctypes as C
+import time
 
 import numpy as np
 
 from . import _lib
+
+# wall seconds spent in each step's library call (read by the benchmark)
+TIMES = {"basis": 0.0, "matrices": 0.0, "eigen": 0.0, "eigen_calls": 0, "densities": 0.0}
+
+
+def _timed(key, fn, *args):
+    t0 = time.perf_counter()
+    rc = fn(*args)
+    TIMES[key] += time.perf_counter() - t0
+    return rc
 
 FIELDS = ("v", "vhb", "vr", "vz", "vd", "vs", "vSFIZ", "vSZFI", "vSFIR", "vSRFI", "dv")
 
@@ -35,7 +46,7 @@ def basis_functions(h):
     out = np.empty(4 * nt * nghl)
     xh, wh, xl, wl = _f64(h.xh), _f64(h.wh), _f64(h.xl), _f64(h.wl)
     nr, nz, nl = _i32(h.nr), _i32(h.nz), _i32(h.nl)
-    _lib.check(lib.pnfam_gpu_hfb_basis(h.ngh, h.ngl, _lib.dptr(xh), _lib.dptr(wh), _lib.dptr(xl), _lib.dptr(wl),
+    _lib.check(_timed("basis", lib.pnfam_gpu_hfb_basis, h.ngh, h.ngl, _lib.dptr(xh), _lib.dptr(wh), _lib.dptr(xl), _lib.dptr(wl),
                                        float(h.bz), float(h.bp), nt, _lib.iptr(nr), _lib.iptr(nz), _lib.iptr(nl),
                                        _lib.dptr(out)))
     q = out.reshape(4, nt, nghl)
@@ -55,7 +66,7 @@ def hfb_matrices(h, mb):
     tot = int(4 * np.sum(np.asarray(h.ID, dtype=np.int64) ** 2))
     out = np.empty(tot)
     basis = _basis_stack(mb)
-    _lib.check(lib.pnfam_gpu_hfb_matrices(len(bs), _lib.iptr(bs), nghl, _lib.iptr(_i32(h.ns)), _lib.dptr(basis),
+    _lib.check(_timed("matrices", lib.pnfam_gpu_hfb_matrices, len(bs), _lib.iptr(bs), nghl, _lib.iptr(_i32(h.ns)), _lib.dptr(basis),
                                           _lib.dptr(_f64(mb.y)), _lib.dptr(_f64(mb.xlam)), _lib.dptr(_f64(mb.xlap)),
                                           _lib.dptr(fields), _lib.dptr(out)))
     res = {"n": [], "p": []}
@@ -80,7 +91,8 @@ def eigh_batch(mats, start=None, sweeps=None):
     w = np.empty(int(dims.sum()))
     v = np.empty(a.size)
     sw = np.zeros(len(mats), dtype=np.int32)
-    _lib.check(lib.pnfam_gpu_sym_eigen(len(mats), _lib.iptr(dims), _lib.dptr(a), _lib.dptr(v0) if start else None,
+    TIMES["eigen_calls"] += 1
+    _lib.check(_timed("eigen", lib.pnfam_gpu_sym_eigen, len(mats), _lib.iptr(dims), _lib.dptr(a), _lib.dptr(v0) if start else None,
                                        _lib.dptr(w), _lib.dptr(v), _lib.iptr(sw)))
     if sweeps is not None:
         sweeps.extend(int(x) for x in sw)
@@ -126,7 +138,7 @@ def local_densities(h, mb, qp, tz):
     U = _f64(np.concatenate(Us)) if thermal else None
     f = _f64(np.concatenate(fs)) if thermal else None
     out = np.empty(3 * nghl)
-    _lib.check(lib.pnfam_gpu_hfb_densities(len(bs), _lib.iptr(bs), nghl, _lib.iptr(_i32(h.ns)),
+    _lib.check(_timed("densities", lib.pnfam_gpu_hfb_densities, len(bs), _lib.iptr(bs), nghl, _lib.iptr(_i32(h.ns)),
                                            _lib.dptr(_basis_stack(mb)), _lib.dptr(_f64(mb.y)),
                                            _lib.dptr(_f64(mb.xlam)), _lib.dptr(_f64(mb.xlap)), _lib.dptr(W),
                                            _lib.dptr(U) if thermal else None, _lib.dptr(f) if thermal else None,
