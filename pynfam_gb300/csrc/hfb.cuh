@@ -179,14 +179,19 @@ HFB_HD inline void jacobi_row(double* A, int n, int p, int q, double c, double s
   A[(size_t)q * n + j] = s * ap + c * aq;
 }
 
-// column step of a round: columns p and q of A and V for row i
-HFB_HD inline void jacobi_col(double* A, double* V, int n, int p, int q, double c, double s, int i) {
+// column step of a round: columns p and q of A for row i
+HFB_HD inline void jacobi_col(double* A, int n, int p, int q, double c, double s, int i) {
   const double ap = A[(size_t)i * n + p], aq = A[(size_t)i * n + q];
   A[(size_t)i * n + p] = c * ap - s * aq;
   A[(size_t)i * n + q] = s * ap + c * aq;
-  const double vp = V[(size_t)i * n + p], vq = V[(size_t)i * n + q];
-  V[(size_t)i * n + p] = c * vp - s * vq;
-  V[(size_t)i * n + q] = s * vp + c * vq;
+}
+
+// the same rotation of the eigenvectors, kept transposed (VT[c][i] = V[i][c]: the
+// rotated columns p and q are contiguous rows of VT)
+HFB_HD inline void jacobi_vt(double* VT, int n, int p, int q, double c, double s, int i) {
+  const double vp = VT[(size_t)p * n + i], vq = VT[(size_t)q * n + i];
+  VT[(size_t)p * n + i] = c * vp - s * vq;
+  VT[(size_t)q * n + i] = s * vp + c * vq;
 }
 
 HFB_HD inline void jacobi_zero(double* A, int n, int p, int q) {
@@ -198,7 +203,7 @@ constexpr int JAC_MAX_SWEEPS = 60;
 constexpr double JAC_TOL = 1e-15;   // off-diagonal Frobenius norm / Frobenius norm at convergence
 
 #ifdef __CUDACC__
-constexpr int JAC_THREADS = 256;
+constexpr int JAC_THREADS = 1024;
 constexpr int JAC_MAXN = 512;
 constexpr int JAC_SMEM_N = 164;     // matrices up to this size are rotated in shared memory (+8 KB static)
 
@@ -215,7 +220,8 @@ __global__ void k_hfb_matrices(MatView m, const int* items, int nitems) {
 }
 
 // one CTA per matrix: A (row-major; its diagonal ends as the eigenvalues), V <- the
-// eigenvectors (columns); status[mat] = sweeps used, or -1 if not converged.
+// eigenvectors, transposed (row c of V holds eigenvector c); status[mat] = sweeps
+// used, or -1 if not converged.
 // V0 (optional): starting vectors (the previous eigenvectors of a matrix that has
 // changed a little): the rotations start from V0^T A V0 with V = V0.  smem_n > 0: the
 // matrices (all of size <= smem_n) are worked on in dynamic shared memory.
@@ -259,7 +265,10 @@ __global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double* A, double* V, co
         a[(size_t)j * n + i] = x;
       }
     }
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) v[i] = v0[i];
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {   // VT = V0^T
+      const int c = idx / n, i = idx % n;
+      v[idx] = v0[(size_t)i * n + c];
+    }
   } else {
     for (int i = threadIdx.x; i < n * n; i += blockDim.x) v[i] = (i / n == i % n) ? 1.0 : 0.0;
   }
@@ -299,14 +308,19 @@ __global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double* A, double* V, co
         pp[k] = p; qq[k] = q < n ? q : -1; cs_c[k] = c; cs_s[k] = sn;
       }
       __syncthreads();
+#pragma unroll 4
       for (int it = threadIdx.x; it < (m / 2) * n; it += blockDim.x) {
         const int k = it / n, j = it % n;
         if (qq[k] >= 0 && cs_s[k] != 0.0) jacobi_row(a, n, pp[k], qq[k], cs_c[k], cs_s[k], j);
       }
       __syncthreads();
+#pragma unroll 4
       for (int it = threadIdx.x; it < (m / 2) * n; it += blockDim.x) {
         const int k = it / n, i = it % n;
-        if (qq[k] >= 0 && cs_s[k] != 0.0) jacobi_col(a, v, n, pp[k], qq[k], cs_c[k], cs_s[k], i);
+        if (qq[k] >= 0 && cs_s[k] != 0.0) {
+          jacobi_col(a, n, pp[k], qq[k], cs_c[k], cs_s[k], i);
+          jacobi_vt(v, n, pp[k], qq[k], cs_c[k], cs_s[k], i);
+        }
       }
       __syncthreads();
       // the rotated element is zero in exact arithmetic

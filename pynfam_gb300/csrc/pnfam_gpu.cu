@@ -2880,7 +2880,7 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
     std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A[(size_t)x * n + x] < A[(size_t)y * n + y]; });
     for (int c = 0; c < n; ++c) {
       w[wo + c] = A[(size_t)ord[c] * n + ord[c]];
-      for (int i = 0; i < n; ++i) v[off[k] + (size_t)i * n + c] = hv[off[k] + (size_t)i * n + ord[c]];
+      for (int i = 0; i < n; ++i) v[off[k] + (size_t)i * n + c] = hv[off[k] + (size_t)ord[c] * n + i];
     }
     wo += n;
     if (sweeps) sweeps[k] = st[k];

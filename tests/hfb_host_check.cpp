@@ -61,7 +61,8 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
           const double x = 0.5 * (A[(size_t)i * n + j] + A[(size_t)j * n + i]);
           A[(size_t)i * n + j] = A[(size_t)j * n + i] = x;
         }
-      for (size_t i = 0; i < (size_t)n * n; ++i) V[i] = q0[i];
+      for (int c = 0; c < n; ++c)
+        for (int i = 0; i < n; ++i) V[(size_t)c * n + i] = q0[(size_t)i * n + c];   // transposed
     } else {
       for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
     }
@@ -91,7 +92,10 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
             for (int j = 0; j < n; ++j) hfbk::jacobi_row(A.data(), n, pp[kk], qq[kk], cc[kk], ss[kk], j);
         for (int kk = 0; kk < m / 2; ++kk)
           if (qq[kk] >= 0 && ss[kk] != 0.0)
-            for (int i = 0; i < n; ++i) hfbk::jacobi_col(A.data(), V.data(), n, pp[kk], qq[kk], cc[kk], ss[kk], i);
+            for (int i = 0; i < n; ++i) {
+              hfbk::jacobi_col(A.data(), n, pp[kk], qq[kk], cc[kk], ss[kk], i);
+              hfbk::jacobi_vt(V.data(), n, pp[kk], qq[kk], cc[kk], ss[kk], i);
+            }
         for (int kk = 0; kk < m / 2; ++kk)
           if (qq[kk] >= 0 && ss[kk] != 0.0) hfbk::jacobi_zero(A.data(), n, pp[kk], qq[kk]);
       }
@@ -102,7 +106,7 @@ extern "C" int pnfam_gpu_sym_eigen(int nmat, const int* dims, const double* a, c
     std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A[(size_t)x * n + x] < A[(size_t)y * n + y]; });
     for (int c = 0; c < n; ++c) {
       w[wo + c] = A[(size_t)ord[c] * n + ord[c]];
-      for (int i = 0; i < n; ++i) v[off + (size_t)i * n + c] = V[(size_t)i * n + ord[c]];
+      for (int i = 0; i < n; ++i) v[off + (size_t)i * n + c] = V[(size_t)ord[c] * n + i];
     }
     if (sweeps) sweeps[k] = sweep;
     off += (long long)n * n;
