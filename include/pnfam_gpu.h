@@ -268,7 +268,8 @@ int pnfam_gpu_calc_hamiltonian_mixed(pnfam_ctx_t* ctx,
  * Limits: nxy <= 32768, nghl <= 1600, dqp <= 1024, nb <= 64 (every operator
  * up to N_sh = 12 on a 40 x 40 mesh); larger sizes return PNFAM_EINVAL.
  * The first call on a device looks up the array's device address and sets a
- * kernel attribute; make that first call before any stream capture.  All
+ * kernel attribute.  No call can be captured into a CUDA graph: each copies
+ * host tables to the device and synchronises the stream before returning.  All
  * calls share the array: calls that overlap on the GPU (from several threads
  * or streams) race and must be serialised by the caller.
  */
