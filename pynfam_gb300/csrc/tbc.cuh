@@ -38,6 +38,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -366,11 +367,20 @@ struct Prepared {
 };
 
 struct Math1D {
-  std::vector<double> fact;
+  static constexpr int GMAX = 200;     // Gamma(m / 2) for |m| <= GMAX, m odd
+  std::vector<double> fact, ghalf;
   Math1D() {
     fact.resize(171);
     fact[0] = 1.0;
     for (int i = 1; i <= 170; ++i) fact[i] = i * fact[i - 1];
+    ghalf.assign(2 * GMAX + 1, 0.0);
+    for (int m = -GMAX; m <= GMAX; ++m)
+      if (m & 1) ghalf[m + GMAX] = std::tgamma(0.5 * m);
+  }
+  // Gamma(x) of a half-integer x (the arguments of the axial element)
+  double gamma_half(double x) const {
+    const int m = (int)std::lround(2.0 * x);
+    return (m & 1) && m >= -GMAX && m <= GMAX ? ghalf[m + GMAX] : std::tgamma(x);
   }
   double binom(int m, int n) const {
     if (n < 0 || n > m) return 0.0;
@@ -381,11 +391,11 @@ struct Math1D {
   // 2F1(a, b; c; x) for non-positive integers a, b: a terminating series
   double hyp2f1(int a, int b, double c, double x) const {
     const int d = std::abs(std::max(a, b)), e = std::abs(std::min(a, b));
-    double s = 0.0;
+    double s = 0.0, xi = 1.0, up = 1.0;         // x^i and the rising factorial (c)_i
     for (int i = 0; i <= d; ++i) {
-      double up = 1.0;
-      for (int j = 0; j < i; ++j) up *= c + j;
-      s += binom(d, i) * binom(e, i) * std::pow(x, i) * fact[i] / up;
+      s += binom(d, i) * binom(e, i) * xi * fact[i] / up;
+      xi *= x;
+      up *= c + i;
     }
     return s;
   }
@@ -408,7 +418,7 @@ struct Math1D {
     for (int n = std::abs(j - l); n <= j + l; n += 2) {
       if ((i + k + n) & 1) break;
       const double xi = (i + k + n + 1) * 0.5;
-      const double fbar = std::tgamma(xi - i) * std::tgamma(xi - k) * std::tgamma(xi - n) /
+      const double fbar = gamma_half(xi - i) * gamma_half(xi - k) * gamma_half(xi - n) /
                           (std::pow(z, xi) * std::sqrt(fact[i] * fact[k] * fact[n])) *
                           hyp2f1(-i, -k, n + 1 - xi, 1 - z);
       v += tz(j, l, n) * fbar;
@@ -493,23 +503,38 @@ struct Dir1D {
   }
 };
 
+// run f(i) for i in [0, n) on the host's cores (each i written by one thread)
+template <class F>
+inline void host_parallel(int n, F f) {
+  const int nt = std::max(1, std::min(n, (int)std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (int w = 0; w < nt; ++w)
+    th.emplace_back([=]() {
+      for (int i = w; i < n; i += nt) f(i);
+    });
+  for (auto& t : th) t.join();
+}
+
 inline Dir1D make_dir(const Math1D& m, int nmax, double b, const double* mu, const double* pf) {
   Dir1D d;
   d.n1 = nmax + 1;
   d.pd1 = 1.0 / (b * 1.4142135623730951);
   d.pd2 = 1.0 / (b * b * 2.0);
   d.t.assign((size_t)d.n1 * d.n1 * d.n1 * d.n1 * NG, 0.0);
-  for (int a = 0; a < d.n1; ++a)
-    for (int bb = 0; bb < d.n1; ++bb)
-      for (int c = 0; c < d.n1; ++c)
-        for (int dd = 0; dd < d.n1; ++dd) {
-          if ((a + bb + c + dd) & 1) continue;
-          for (int g = 0; g < NG; ++g) {
-            double v = m.me(a, bb, c, dd, mu[g], b);
-            if (pf) v *= pf[g];
-            d.t[idx4(d.n1, a, bb, c, dd) * NG + g] = v;
-          }
+  const int n1 = d.n1;
+  double* t = d.t.data();
+  host_parallel(n1 * n1, [&](int ab) {
+    const int a = ab / n1, bb = ab % n1;
+    for (int c = 0; c < n1; ++c)
+      for (int dd = 0; dd < n1; ++dd) {
+        if ((a + bb + c + dd) & 1) continue;
+        for (int g = 0; g < NG; ++g) {
+          double v = m.me(a, bb, c, dd, mu[g], b);
+          if (pf) v *= pf[g];
+          t[idx4(n1, a, bb, c, dd) * NG + g] = v;
         }
+      }
+  });
   return d;
 }
 
@@ -593,21 +618,25 @@ inline std::string prepare(const Input& in, Prepared& P) {
 
   // z parts of the current for every (z_a, z_b, z_c, z_d)
   P.jz.assign((size_t)NZ * NZ * NZ * NZ * NCG, 0.0);
-  for (int a = 0; a < NZ; ++a)
-    for (int b = 0; b < NZ; ++b)
-      for (int c = 0; c < NZ; ++c)
-        for (int d = 0; d < NZ; ++d) jz_vec(dz, in.K, in.use_p, a, b, c, d, &P.jz[idx4(NZ, a, b, c, d) * NCG]);
+  double* jzp = P.jz.data();
+  host_parallel(NZ * NZ, [&](int ab) {
+    const int a = ab / NZ, b = ab % NZ;
+    for (int c = 0; c < NZ; ++c)
+      for (int d = 0; d < NZ; ++d) jz_vec(dz, in.K, in.use_p, a, b, c, d, jzp + idx4(NZ, a, b, c, d) * NCG);
+  });
   // r tables with derivatives, indices 0..nrl
   const int n1 = P.nrl + 1;
   const size_t tsz = (size_t)n1 * n1 * n1 * n1 * NG;
   P.xr.assign(NXTAB * tsz, 0.0);
   const int dtab[NXTAB][2] = {{0, 0}, {1, 0}, {2, 0}, {1, 1}, {1, 2}, {0, 1}, {0, 2}};
+  double* xrp = P.xr.data();
   for (int k = 0; k < NXTAB; ++k) {
     if (k >= X11 && !in.use_p) break;
-    for (int a = 0; a < n1; ++a)
-      for (int b = 0; b < n1; ++b)
-        for (int c = 0; c < n1; ++c)
-          for (int d = 0; d < n1; ++d) dr.me_dp(a, b, c, d, dtab[k][0], dtab[k][1], &P.xr[k * tsz + idx4(n1, a, b, c, d) * NG]);
+    host_parallel(n1 * n1, [&](int ab) {
+      const int a = ab / n1, b = ab % n1;
+      for (int c = 0; c < n1; ++c)
+        for (int d = 0; d < n1; ++d) dr.me_dp(a, b, c, d, dtab[k][0], dtab[k][1], xrp + k * tsz + idx4(n1, a, b, c, d) * NG);
+    });
   }
   // polar -> Cartesian coefficients, n <= nrl/2, |l| <= nrl, ny <= nrl
   const int L = P.nrl;

@@ -58,7 +58,7 @@ def host_harness(tmp_path_factory):
     if cxx is None:
         pytest.skip("no C++ compiler")
     so = str(tmp_path_factory.mktemp("tbc") / "tbc_host.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-pthread", "-o", so,
                     os.path.join(ROOT, "tests", "tbc_host_check.cpp")], check=True)
     return ctypes.CDLL(so)
 
