@@ -119,6 +119,25 @@ def test_jacobi_arithmetic(harness):
     _check_eigen(mats, hfb_device.eigh_batch(mats))
 
 
+def test_jacobi_warm_start(harness):
+    """A matrix shifted the way the particle-number loop shifts it (lambda times
+    diag(1, -1)), started from the previous eigenvectors: the same eigenpairs in
+    fewer sweeps."""
+    from pynfam_gb300 import hfb_device
+    rng = np.random.default_rng(11)
+    n = 60
+    a = rng.standard_normal((n, n))
+    a = a + a.T
+    s = np.diag(np.r_[np.ones(n // 2), -np.ones(n // 2)])
+    cold = []
+    first = hfb_device.eigh_batch([a], sweeps=cold)
+    b = a - 1e-3 * s
+    warm = []
+    res = hfb_device.eigh_batch([b], start=[first[0][1]], sweeps=warm)
+    _check_eigen([b], res)
+    assert warm[0] < cold[0], (warm, cold)
+
+
 # ---------------------------------------------------------------------------------
 # the GPU
 # ---------------------------------------------------------------------------------
