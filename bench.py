@@ -45,6 +45,9 @@ The same line also carries, unless --no-config4 / --no-stream:
                   two-body current for GT- K = 0, 1 of the same ground state
                   (what the reference caches in .tbc files), wall and kernel
                   times, and the 40S N_sh = 6 field against the reference's file
+  hfb_reconstruction  (unless --no-hfb) the ground state rebuilt from the .hel
+                  fields at N_sh = 16 and 20, on the host and with its arithmetic
+                  on the GPU, wall times and the largest differences
 
 Arms:
   default           this repository's GB300 solver through its C ABI
@@ -598,6 +601,8 @@ def run_gpu(args):
         line["config4"] = run_config4(args, emit=False)
     if rank == 0 and world == 1 and not args.no_2bc:
         line["finite_range_2bc"] = run_tbc(args, emit=False)
+    if rank == 0 and world == 1 and not args.no_hfb:
+        line["hfb_reconstruction"] = run_hfb(args, emit=False)
     if rank == 0 and world == 1 and not args.no_stream:
         sl = run_serve_stream(args, emit=False)
         line["serving_stream"] = {
@@ -990,6 +995,7 @@ def main():
     ap.add_argument("--no-2bc", action="store_true", help="leave the finite-range 2BC field object out of the line")
     ap.add_argument("--tbc-only", action="store_true", help="only the finite-range 2BC field timing (own line)")
     ap.add_argument("--hfb-only", action="store_true", help="only the HFB reconstruction timing, host and GPU")
+    ap.add_argument("--no-hfb", action="store_true", help="leave the HFB reconstruction object out of the line")
     ap.add_argument("--tbc-nsh", type=int, default=NSH, help="finite-range 2BC field: N_sh of the basis")
     ap.add_argument("--no-cpu", action="store_true", help="finite-range 2BC field: skip the CPU oracle timing")
     ap.add_argument("--async-anchors", action="store_true",
