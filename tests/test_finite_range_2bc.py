@@ -102,6 +102,23 @@ def test_kernel_arithmetic_matches_oracle_with_pion_pole(host_harness):
         assert np.abs(got[nm] - w).max() <= 1e-12 * scale, nm
 
 
+def test_kernel_arithmetic_matches_oracle_on_deformed_ground_state(host_harness):
+    """The recorded 162Gd ground state (prolate; no recorded two-body-current run):
+    the kernels' arithmetic against the oracle, GT K = 1."""
+    from oracle.tbc_oracle import two_body_gamma
+    from pynfam_gb300.extfield import init_external_field
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    hfb = load_hfb_solution(os.path.join(GOLD, "Gd162.hel"))
+    F = init_external_field(hfb, "-", "GT", 1)
+    h = hfb.hel
+    want = two_body_gamma(h.nz, h.nr, h.nl, h.ns, h.ID, h.bz, h.bp, hfb.density_matrices("n"),
+                          hfb.density_matrices("p"), F.mat.cols, F.mat.offsets(), F.mat.nelem, 1, True)
+    got = _harness(host_harness, hfb, F, False)
+    scale = max(np.abs(w).max() for w in want.values())
+    for nm in PIECES:
+        assert np.abs(got[nm] - want[nm]).max() <= 1e-12 * scale, nm
+
+
 # ---------------------------------------------------------------------------------
 # the GPU
 # ---------------------------------------------------------------------------------
