@@ -75,6 +75,22 @@ def test_kernel_arithmetic_rebuilds_the_ground_state(case, nsh, harness):
     _compare(load_hfb_solution(h, device=False), load_hfb_solution(h, device=True))
 
 
+@pytest.mark.parametrize("case", ["S40", "Kr116"])
+def test_kernel_arithmetic_rebuilds_a_thermal_state(case, harness):
+    """The finite-temperature reconstruction (HFBTHO's thermal hfbdiag/ALambda/DENSIT:
+    the densities take U f + V (1 - f) per quasiparticle): a recorded ground state
+    rebuilt at T = 0.5 MeV (no recorded thermal run exists), both forms, with the
+    thermal occupations."""
+    import copy
+    from pynfam_gb300.hfb_solution import load_hfb_solution
+    h = copy.copy(_hel(case))
+    h.set_temperature, h.temperature = True, 0.5
+    a, b = load_hfb_solution(h, device=False), load_hfb_solution(h, device=True)
+    _compare(a, b)
+    assert a.temperature == b.temperature == 0.5
+    assert np.abs(a.fn - b.fn).max() < 1e-12 and np.abs(a.fp - b.fp).max() < 1e-12
+
+
 def test_kernel_arithmetic_ground_state_reproduces_recorded_fam_point(harness):
     import sys
     sys.path.insert(0, os.path.join(ROOT, "tests"))
