@@ -510,7 +510,11 @@ def finite_range_field(path: str, hfb, F, lec: LECs, usep_requested: bool, direc
             t = compute_tbc(hfb, F, lec, usep_requested, mode, nxterms, compute)
         except TwoBodyCurrentError as e:
             raise TwoBodyCurrentError(f"no usable finite-range field file '{path}': {e}")
-        write_tbc(path, t)
+        try:
+            write_tbc(path, t)
+        except OSError as e:
+            # the file only caches the field for later runs; this run goes on without it
+            say(f"  * Could not store the field in '{path}': {e}")
     nxy = F.mat.nelem
     c3, c4 = lec.c3, lec.c4 + 0.25
     g = t.gam

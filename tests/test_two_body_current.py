@@ -95,6 +95,19 @@ def test_tbc_round_trip_and_compatibility(tmp_path):
     assert calls == [("GT", 0, True)]
 
 
+def test_unwritable_tbc_location_keeps_the_computed_field(tmp_path):
+    """A field computed where its .tbc cannot be stored is still used."""
+    c, _ = case_for("S40_2bc_fam", "GT-K0", 0)
+    lec = t2.LECs.from_namelist([-3.1962, 3.1962, 0.0])
+    k0_path = os.path.join(GOLDEN, "S40_2bc_fam", "GT-K0.tbc")
+    k0 = t2.read_tbc(k0_path)
+    msgs = []
+    got = t2.finite_range_field(str(tmp_path / "no_such_dir" / "GT-K0.tbc"), c.hfb, c.F, lec, False, False, 111100, 0,
+                                log=msgs.append, compute=lambda h, F, usep: dict(k0.gam))
+    assert np.array_equal(got, t2.finite_range_field(k0_path, c.hfb, c.F, lec, False, False))
+    assert any("Could not store" in m for m in msgs)
+
+
 def test_missing_tbc_is_computed_by_setup(tmp_path, monkeypatch):
     """setup_case computes a missing .tbc (stand-in contraction: the reference's
     pieces) and composes the same operator as from the reference's file."""
